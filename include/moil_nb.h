@@ -1,0 +1,197 @@
+/*
+ * moil_nb.h -- C ABI of the GB300 nonbonded energy/force library.
+ *
+ * Drop-in for the nonbonded Ewald block of MOIL's eforce() (pot/eforce.f:122-204):
+ * real-space LJ + erfc-Coulomb over the pair lists (pot/cdie_ewald.f,
+ * pot/watwat_ewald.f, symm/symcdie_ewald.f, symm/symwat_ewald.f), the exclusion
+ * erf corrections (pot/cdie_ewald.f:117-199), the 1-4 terms (pot/ener14.f), the
+ * PME reciprocal sum (pot/ewald_receip.f) and the self energy
+ * (symm/ewald_init.f:131-150), plus the list rebuild that MOIL does in
+ * squeeze()/nbondm()/syminit() (symm/squeeze.f, pot/nbondm.f, symm/syminit.f).
+ *
+ * Conventions follow MOIL's COMMON blocks:
+ *   - coordinates coor(3,npt) and gradients dpot(3,npt) are interleaved x,y,z
+ *     per atom (Fortran column-major), Å and kcal/mol/Å; dpot = dE/dx (-force);
+ *   - atom numbers inside index arrays (exc2, spec1/2, poipt) are 1-based as
+ *     MOIL stores them;
+ *   - energies are kcal/mol and fill the same names as /ENERGY/ and /EWALD3/.
+ *
+ * Every call returns an int status (MOIL_NB_OK == 0) and never aborts: MOIL's
+ * alert(...,1) is the caller's decision (pot/nbond.f:164-173).  A handle is
+ * not thread safe; use one handle per host thread.
+ */
+#ifndef MOIL_NB_H
+#define MOIL_NB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    MOIL_NB_OK = 0,
+    MOIL_NB_ERR_ARG = 1,          /* bad pointer / size / handle */
+    MOIL_NB_ERR_CUDA = 2,         /* CUDA runtime error (message via moil_nb_last_error) */
+    MOIL_NB_ERR_NONNEUTRAL = 3,   /* |sum q| > 1e-7: symm/ewald_init.f:62-72 */
+    MOIL_NB_ERR_GRID = 4,         /* PME grid not 2/3/5-smooth, > 128 per side, or order != 4 */
+    MOIL_NB_ERR_BOX = 5,          /* cutoff + water extent does not fit half the box */
+    MOIL_NB_ERR_OVERFLOW = 6,     /* device list capacity exceeded (retry grows it) */
+    MOIL_NB_ERR_NAN = 7,          /* non-finite coordinate or result */
+    MOIL_NB_ERR_TOPOLOGY = 8,     /* water monomer not O,H,H with full intramolecular exclusions */
+    MOIL_NB_ERR_TIMEOUT = 9,      /* a bounded device wait expired */
+    MOIL_NB_ERR_NOMEM = 10,
+    MOIL_NB_ERR_STATE = 11        /* call order (e.g. eval before init) */
+};
+
+/* precision of the device path */
+enum {
+    MOIL_NB_MIXED = 0,            /* FP32 pair/spline/FFT math, int64 fixed-point force accumulation,
+                                     FP64 energies, exclusion/1-4 corrections and self energy */
+    MOIL_NB_FP64 = 1              /* plain FP64 throughout, one system per launch (baseline path) */
+};
+
+/* monomer kinds (moname in MOIL) */
+enum {
+    MOIL_MON_OTHER = 0,           /* solute residue: never squeezed */
+    MOIL_MON_WATER = 1,           /* 'TIP3' / 'SPC*': O,H,H; O-O group cutoff (pot/nbondm.f:189-199) */
+    MOIL_MON_ION = 2              /* squeezed single-molecule monomer (symm/squeeze.f:82-86) */
+};
+
+/* Run parameters: the keywords pot/energy.f:188-253 reads, plus device knobs. */
+typedef struct moil_nb_params {
+    double rvmx;        /* LJ cutoff (Å)                     'rvmx' */
+    double relx;        /* Coulomb cutoff (Å)                'relx' */
+    double eps;         /* dielectric                         'epsi' */
+    double a, b, c;     /* orthorhombic box (Å)              'symm xtra ytra ztra' */
+    double dtol;        /* Ewald direct-sum tolerance         'ewald dtol' (used when alpha <= 0) */
+    double alpha;       /* Ewald coefficient (Å^-1); > 0 overrides dtol */
+    int nfft1, nfft2, nfft3;  /* PME grid                    'grdx grdy grdz' */
+    int order;          /* B-spline order                     'iord' (4 only) */
+    int arith;          /* 1: Lorentz-Berthelot combination ('arith'), 0: geometric */
+    int hvdw0;          /* 1 (MOIL default): geometric pairs with epsgm12 < 1e-3 are Coulomb-only */
+    int lj_switch;      /* extension, not in MOIL (default 0): CHARMM LJ switch on [r_on, rvmx] */
+    double r_on;
+    double skin;        /* device pair-list skin (Å); lists rebuild automatically when an atom
+                           moved more than skin/2 since the last build */
+    int list_period;    /* > 0: also rebuild every list_period evaluations ('#lis') */
+    int precision;      /* MOIL_NB_MIXED or MOIL_NB_FP64 */
+} moil_nb_params;
+
+/* Topology: the COMMON arrays of one system (borrowed; copied at init). */
+typedef struct moil_topology {
+    int npt;
+    const double *ptchg;      /* /CONNDBL/ ptchg(npt) */
+    const double *epsgm6;     /* /CONNDBL/ epsgm6(npt)  (connect/fillpt.f:136-184 encoding) */
+    const double *epsgm12;    /* /CONNDBL/ epsgm12(npt) */
+    const int *exc1;          /* exc1(0:npt): CSR end pointers */
+    const int *exc2;          /* exc2(exc1(npt)): partner atoms, 1-based, listed under the lower atom */
+    int totspe;               /* 1-4 pairs (pot/ener14.f) */
+    const int *spec1, *spec2; /* 1-based */
+    const double *p14;        /* p14(3,totspe): A, B, qq*kofdie*el14 */
+    int totmon;
+    const int *poipt;         /* poipt(totmon): last atom (1-based) of each monomer */
+    const int *montype;       /* MOIL_MON_* per monomer */
+} moil_topology;
+
+/* Energies (kcal/mol), the /ENERGY/ and /EWALD3/ names eforce() fills. */
+typedef struct moil_energies {
+    double e_vdw, e_el;       /* primary-box LJ and real-space Coulomb */
+    double e_vsym, e_lsym;    /* image (translated) LJ and real-space Coulomb */
+    double e_el14, e_vdw14;   /* 1-4 */
+    double e_corr;            /* exclusion erf corrections */
+    double e_self;            /* Ewald self energy */
+    double e_ew_receip;       /* PME reciprocal */
+    double e_total;           /* sum of the above (nonbonded part of e_total) */
+    double e_dir;             /* e_el + e_lsym */
+} moil_energies;
+
+/* One replica of a batch: its own parameters and topology. */
+typedef struct moil_replica {
+    const moil_nb_params *params;
+    const moil_topology *topo;
+} moil_replica;
+
+/* Per-stage device times of the last timed evaluation (ms, CUDA events). */
+typedef struct moil_nb_timing {
+    float prepare_ms, list_ms, water_ms, atom_ms, excl_ms;
+    float pme_spread_fft_ms, pme_conv_ms, pme_gather_ms, finalize_ms, total_ms;
+    int list_rebuilt;
+    int launches;             /* kernels launched by the evaluation */
+} moil_nb_timing;
+
+typedef struct moil_nb_ctx moil_nb_ctx;
+
+/* ---- lifecycle --------------------------------------------------------- */
+/* Create a handle on CUDA device `device`.  Replaces the state ewald_init()
+ * and the first calls of nbondm()/syminit() set up (symm/ewald_init.f:8). */
+int moil_nb_create(moil_nb_ctx **h, int device);
+void moil_nb_destroy(moil_nb_ctx *h);
+const char *moil_nb_strerror(int status);
+const char *moil_nb_last_error(const moil_nb_ctx *h);
+
+/* Single system: ewald_init() equivalent -- alpha (from dtol by bisection,
+ * symm/ewald_init.f:298-335, unless params->alpha > 0), neutrality check,
+ * self energy, B-spline moduli (pot/ewald_receip.f:413-481), topology upload. */
+int moil_nb_init(moil_nb_ctx *h, const moil_nb_params *p, const moil_topology *t);
+
+/* Batch of independent replicas (chain/path images, milestoning swarm):
+ * each replica keeps its own box, cutoffs, grid and topology. */
+int moil_nb_init_batch(moil_nb_ctx *h, int nrep, const moil_replica *reps);
+
+/* Ewald coefficient the handle uses for replica r. */
+int moil_nb_get_alpha(const moil_nb_ctx *h, int r, double *alpha);
+
+/* ---- evaluation -------------------------------------------------------- */
+/* Nonbonded energy + gradient of all replicas, host buffers (replica-major,
+ * MOIL atom order within a replica).  dpot is overwritten with this block's
+ * gradient; energies[r] per replica.  Lists rebuild as params->skin and
+ * list_period require (replaces squeeze/nbondm/syminit + eforce nonbonded). */
+int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *energies);
+
+/* The same with coordinates and gradient already in device memory
+ * (device pointers, same layout); energies still go to host memory. */
+int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *energies);
+
+/* Force a list rebuild at the next evaluation (MOIL: nbondm() + syminit()). */
+int moil_nb_request_rebuild(moil_nb_ctx *h);
+
+/* MOIL's squeeze() on host coordinates: water and ion monomers whose first
+ * atom left [-L/2, L/2] move back by one box length (symm/squeeze.f:66-145). */
+int moil_nb_squeeze(const moil_nb_params *p, const moil_topology *t, double *coor);
+
+/* Total number of atoms over all replicas. */
+int moil_nb_natoms(const moil_nb_ctx *h, int64_t *natoms);
+
+/* CUDA stream the handle launches on (cudaStream_t as void*). */
+void *moil_nb_stream(const moil_nb_ctx *h);
+
+/* ---- instrumentation --------------------------------------------------- */
+int moil_nb_set_timing(moil_nb_ctx *h, int on);
+int moil_nb_get_timing(const moil_nb_ctx *h, moil_nb_timing *t);
+/* In-cutoff site pairs of the last list build (for roofline accounting). */
+int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *water_pairs, int64_t *atom_pairs);
+/* Capture the device part of an evaluation into a CUDA graph (1) or launch
+ * kernel by kernel (0, default).  Graph replays are used when on. */
+int moil_nb_set_graph(moil_nb_ctx *h, int on);
+
+/* ---- Fortran entry points (gfortran naming, all arguments by reference) --
+ * A maintainer replaces the nonbonded block of pot/eforce.f:122-204 with
+ *     call eforce_nb_gpu(npt, coor, dpot, enb, status)
+ * where enb(11) receives the moil_energies fields in declaration order.
+ * The handle lives in a library-held slot set up by ewald_init_gpu; eforce_nb_gpu ADDS
+ * the nonbonded gradient to dpot (MOIL's terms accumulate after eforce zeroes dpot).
+ * params11 = (rvmx, relx, eps, a, b, c, dtol, alpha, r_on, skin, list_period)
+ * iparams8 = (nfft1, nfft2, nfft3, order, arith, hvdw0, lj_switch, precision) */
+void ewald_init_gpu_(const int *npt, const double *ptchg, const double *epsgm6, const double *epsgm12,
+                     const int *exc1, const int *exc2, const int *totspe, const int *spec1, const int *spec2,
+                     const double *p14, const int *totmon, const int *poipt, const int *montype,
+                     const double *params11, const int *iparams8, int *status);
+void nblist_gpu_(int *status);
+void eforce_nb_gpu_(const int *npt, const double *coor, double *dpot, double *enb, int *status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOIL_NB_H */

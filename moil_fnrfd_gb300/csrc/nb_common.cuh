@@ -1,0 +1,133 @@
+// nb_common.cuh -- data layout and device helpers shared by the nonbonded kernels.
+//
+// Device layout (one handle, any number of replicas):
+//   caller order : atoms in MOIL order, replica-major (coor(3,npt) of each replica back to back)
+//   site order   : atoms regrouped for the pair kernels, rebuilt at every list build:
+//                  [0, 3*nW)        water sites, molecule m -> sites 3m (O), 3m+1, 3m+2 (H, H)
+//                  [3*nW, nsite)    non-water atoms
+//                  waters and non-water atoms are each ordered by (replica, cell, unit id)
+//   units        : one per water molecule (anchor = O) and one per non-water atom
+//
+// Fixed point: pair-kernel gradients are accumulated per lane in FP32 over short chunks
+// and flushed to int64 at 2^32 units per kcal/mol/Å; integer addition makes the total
+// independent of summation order, so forces are bit-identical run to run.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "erfcx_coef.h"
+
+#define NB_KOFDIE 332.0716            // COMMON/CONVERT.BLOCK:13
+#define NB_FIX_SCALE 4294967296.0     // 2^32
+#define NB_FIX_SCALE_F 4294967296.0f
+#define NB_FIX_INV (1.0 / 4294967296.0)
+#define NB_PLANE_SCALE 1099511627776.0  // 2^40: PME plane accumulation
+#define NB_MAX_FFT 128
+#define NB_TWO_OVER_SQRTPI 1.1283791670955126
+
+// per-replica constants (read by every kernel)
+struct RepDev {
+    int atom0, natom;        // caller atoms
+    int wat0, nwat;          // sorted water molecules [wat0, wat0+nwat)
+    int oth0, noth;          // sorted non-water atoms (index into the non-water block)
+    int cell0, nc[3];        // cell grid
+    float L[3], invL[3];
+    float Llo[3];            // Ld - (double)L: the box shift is applied as L + Llo so FP32
+                             // image displacements carry no box-rounding bias
+    double Ld[3], invLd[3];
+    float rv2, re2, rmax2;   // LJ cutoff^2, Coulomb cutoff^2, max of both
+    float rlist2;            // (rmax + skin)^2 : list radius between anchors of like units
+    float rlistw2;           // (rmax + skin + 2*rwat)^2 : list radius anchor-to-anchor, mixed units
+    float alpha, ex2c;       // alpha, alpha^2 * log2(e)
+    float c2a;               // 2 alpha / sqrt(pi)
+    double alphad;
+    float ron2, swden;       // LJ switch (extension)
+    float qq[3];             // water qO*qO, qO*qH, qH*qH times kofdie/eps (pot/watwat_ewald.f:70-79)
+    float w12, w6;           // water O-O LJ A, B (pot/watwat_ewald.f:62-68)
+    double qqd[3], w12d, w6d;
+    double epstmp;           // kofdie / eps
+    int n1, n2, n3, n1h;     // PME grid, n1h = n1/2 + 1
+    long long g0;            // first complex element of this replica's half-complex grid
+    int zb0;                 // first z-bin of this replica
+    int bsp0;                // bsp moduli: [bsp0, +n1) x, [+n1, +n2) y, [+n2, +n3) z
+    float fc;                // sqrt(kofdie/eps)
+    double fcd;
+    double pme_fac;          // pi^2 / alpha^2
+    double pivol;            // pi * volume
+    int arith, hvdw0, lj_switch, has_water;
+    double e_self;
+};
+
+// site flags
+#define SF_CHARGED 1u        // |q| > 1e-6 (connect/chsort.f:17-24)
+#define SF_WATER 2u
+#define SF_HTINY 4u          // geometric rule: epsgm12 < 1e-3 (pot/nbond.f:115-126)
+
+// work descriptors for the PME plane / column kernels
+struct PlaneWork { int rep, z; };
+struct ColWork { int rep, ky, kx0; };
+
+// ---------------------------------------------------------------------------------
+// precision traits
+
+template <typename T> struct vec4;
+template <> struct vec4<float> { typedef float4 type; };
+template <> struct vec4<double> { typedef double4 type; };
+template <typename T> struct cplx;
+template <> struct cplx<float> { typedef float2 type; };
+template <> struct cplx<double> { typedef double2 type; };
+
+__device__ __forceinline__ float nb_rint(float x) { return rintf(x); }
+__device__ __forceinline__ double nb_rint(double x) { return rint(x); }
+__device__ __forceinline__ float nb_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double nb_rsqrt(double x) { return rsqrt(x); }
+
+template <typename T> __device__ __forceinline__ T rep_L(const RepDev &r, int k);
+template <> __device__ __forceinline__ float rep_L<float>(const RepDev &r, int k) { return r.L[k]; }
+template <> __device__ __forceinline__ double rep_L<double>(const RepDev &r, int k) { return r.Ld[k]; }
+template <typename T> __device__ __forceinline__ T rep_invL(const RepDev &r, int k);
+template <> __device__ __forceinline__ float rep_invL<float>(const RepDev &r, int k) { return r.invL[k]; }
+template <> __device__ __forceinline__ double rep_invL<double>(const RepDev &r, int k) { return r.invLd[k]; }
+
+// t - n*L for the image shift n, with the box length split in two FP32 parts (FP32) or
+// exact (FP64)
+__device__ __forceinline__ float nb_shift(const RepDev &R, int k, float t, float n)
+{
+    return fmaf(-n, R.Llo[k], fmaf(-n, R.L[k], t));
+}
+__device__ __forceinline__ double nb_shift(const RepDev &R, int k, double t, double n) { return t - n * R.Ld[k]; }
+
+// erfc(x) and the derivative factor for the Ewald real-space term.
+//   FP32: erfc(x) = exp(-x^2) * erfcx(x); erfcx from the fitted form in erfcx_coef.h,
+//         exp(-x^2) = exp2(-x^2 log2 e).
+//   FP64: libdevice erfc / exp.
+// Returns erfc(x); *ex = exp(-x^2).
+__device__ __forceinline__ float nb_erfc_ex(float x, float x2log2e, float *ex)
+{
+    const float C[ERFCX_NC] = ERFCX_COEFS;
+    float xc = fminf(x, 4.5f);
+    float t = __frcp_rn(fmaf(ERFCX_P, xc, 1.0f));
+    float u = fmaf(ERFCX_A, t, ERFCX_B);
+    float p = C[ERFCX_NC - 1];
+#pragma unroll
+    for (int k = ERFCX_NC - 2; k >= 0; --k) p = fmaf(p, u, C[k]);
+    float e = exp2f(-x2log2e);
+    *ex = e;
+    return e * (t * p);
+}
+
+__device__ __forceinline__ double nb_erfc_ex(double x, double /*unused*/, double *ex)
+{
+    *ex = exp(-x * x);
+    return erfc(x);
+}
+
+// 64-bit fixed-point flush of an FP32 partial gradient
+__device__ __forceinline__ long long nb_fix(float v) { return __float2ll_rn(v * NB_FIX_SCALE_F); }
+__device__ __forceinline__ long long nb_fix(double v) { return __double2ll_rn(v * NB_FIX_SCALE); }
+
+// bounded-status helpers
+#define NB_DEV_ERR_OVERFLOW 1
+#define NB_DEV_ERR_NAN 2
+#define NB_DEV_ERR_BIGFORCE 4
+#define NB_DEV_ERR_RWAT 8

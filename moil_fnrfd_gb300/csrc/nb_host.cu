@@ -1,0 +1,761 @@
+// nb_host.cu -- C ABI: handle lifecycle, ewald_init equivalent, evaluation driver.
+//
+// An evaluation is one stream-ordered sequence with no host round trip until the final
+// copy of energies and status:
+//   prepare     caller FP64 coordinates -> site-ordered FP32 (or FP64) copies; sets the
+//               device rebuild flag when any site moved more than skin/2 since the build
+//   lists       (device-gated) unit sort + W1/W2/X list count/scan/fill
+//   real space  water-molecule kernel and non-water-atom kernel
+//   excl/1-4    FP64 corrections
+//   PME         bin, spread+FFT(x,y), FFT(z)+convolution, FFT(y,x)+gather
+//   finalize    gradient assembly in MOIL order, per-replica energies
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "nb_internal.h"
+
+namespace {
+
+const char *kStatusText[] = {
+    "ok", "bad argument", "CUDA error", "system not neutral", "unsupported PME grid",
+    "cutoff does not fit half the box", "pair-list capacity exceeded", "non-finite coordinate or result",
+    "unsupported water topology", "bounded device wait expired", "out of memory", "call order"};
+
+// symm/ewald_init.f:298-335 (find_ewaldcof): doubling, then 60+i bisection steps
+double find_ewaldcof(double cutoff, double dtol)
+{
+    double x = 0.5, xlo, xhi;
+    int i = 0;
+    do {
+        x *= 2.0;
+        ++i;
+    } while (erfc(x * cutoff) / cutoff >= dtol);
+    int n = i + 60;
+    xlo = 0.0;
+    xhi = x;
+    for (i = 1; i <= n; ++i) {
+        x = 0.5 * (xlo + xhi);
+        if (erfc(x * cutoff) / cutoff >= dtol) xlo = x; else xhi = x;
+    }
+    return x;
+}
+
+// pot/ewald_receip.f:413-481 (load_bsp_moduli / DFTMOD) for order 4
+void bsp_moduli(int n, double *mod)
+{
+    // B-spline values at w = 0 (fill_bspline): 1/6, 2/3, 1/6, 0 in slots 2..5
+    std::vector<double> arr(n + 8, 0.0);
+    const double th[4] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 0.0};
+    for (int j = 2; j <= 5 && j <= n; ++j) arr[j - 1] = th[j - 2];
+    for (int k = 1; k <= n; ++k) {
+        double s1 = 0, s2 = 0;
+        for (int j = 1; j <= n; ++j) {
+            double arg = 2.0 * M_PI * (k - 1) * (j - 1) / n;
+            s1 += arr[j - 1] * cos(arg);
+            s2 += arr[j - 1] * sin(arg);
+        }
+        mod[k - 1] = s1 * s1 + s2 * s2;
+    }
+    for (int k = 1; k <= n; ++k)
+        if (mod[k - 1] < 1e-7) mod[k - 1] = 0.5 * (mod[(k - 2 + n) % n] + mod[k % n]);
+}
+
+template <typename T> void free_ptr(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+void release_device(NbCtx *c)
+{
+    free_ptr(c->d_reps); free_ptr(c->d_q); free_ptr(c->d_lj_f); free_ptr(c->d_lj_d); free_ptr(c->d_aflags);
+    free_ptr(c->d_atom_rep); free_ptr(c->d_unit_atom); free_ptr(c->d_unit_rep); free_ptr(c->d_unit_key);
+    free_ptr(c->d_unit_slot); free_ptr(c->d_bin_count); free_ptr(c->d_bin_start); free_ptr(c->d_sorted_unit);
+    free_ptr(c->d_site_orig); free_ptr(c->d_site_of); free_ptr(c->d_site_rep); free_ptr(c->d_site_flags);
+    free_ptr(c->d_pos); free_ptr(c->d_posb); free_ptr(c->d_woff); free_ptr(c->d_site_lj); free_ptr(c->d_site_q);
+    free_ptr(c->d_wl1_off); free_ptr(c->d_wl1); free_ptr(c->d_wl2_off); free_ptr(c->d_wl2); free_ptr(c->d_xl_off);
+    free_ptr(c->d_xl); free_ptr(c->d_count_tmp); free_ptr(c->d_ex_off); free_ptr(c->d_ex_j); free_ptr(c->d_p14_off);
+    free_ptr(c->d_p14_j); free_ptr(c->d_p14_par); free_ptr(c->d_grad_site); free_ptr(c->d_e_unit);
+    free_ptr(c->d_grad_ex); free_ptr(c->d_e_ex); free_ptr(c->d_plans); free_ptr(c->d_rep_plan); free_ptr(c->d_tw);
+    free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
+    free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
+    free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
+    c->inited = 0;
+}
+
+int validate_replica(NbCtx *c, const moil_nb_params *p, const moil_topology *t, int r)
+{
+    char buf[256];
+    if (!p || !t || t->npt <= 0 || !t->ptchg || !t->epsgm6 || !t->epsgm12 || !t->exc1 || !t->poipt ||
+        !t->montype || t->totmon <= 0) {
+        snprintf(buf, sizeof buf, "replica %d: missing topology arrays", r);
+        c->err = buf;
+        return MOIL_NB_ERR_ARG;
+    }
+    if (t->poipt[t->totmon - 1] != t->npt) {
+        snprintf(buf, sizeof buf, "replica %d: poipt(totmon) != npt", r);
+        c->err = buf;
+        return MOIL_NB_ERR_ARG;
+    }
+    double tot = 0;
+    for (int i = 0; i < t->npt; ++i) tot += t->ptchg[i];
+    if (fabs(tot) > 1e-7) {   // symm/ewald_init.f:62-72
+        snprintf(buf, sizeof buf, "replica %d: total charge %.3e (add counterions)", r, tot);
+        c->err = buf;
+        return MOIL_NB_ERR_NONNEUTRAL;
+    }
+    if (p->order != 4) { c->err = "only spline order 4 is implemented"; return MOIL_NB_ERR_GRID; }
+    double rmax = std::max(p->rvmx, p->relx);
+    double lmin = std::min(p->a, std::min(p->b, p->c));
+    if (!(rmax > 0) || !(lmin > 0) || rmax > 0.5 * lmin) {
+        snprintf(buf, sizeof buf, "replica %d: cutoff %.3f exceeds half the box %.3f", r, rmax, 0.5 * lmin);
+        c->err = buf;
+        return MOIL_NB_ERR_BOX;
+    }
+    return MOIL_NB_OK;
+}
+
+// exclusion partner lookup in MOIL's CSR (1-based)
+bool excl_has(const moil_topology *t, int l, int m)
+{
+    for (int k = t->exc1[l - 1] + 1; k <= t->exc1[l]; ++k)
+        if (t->exc2[k - 1] == m) return true;
+    return false;
+}
+
+template <typename V> int upload(NbCtx *c, V *&dst, const std::vector<V> &src)
+{
+    size_t n = std::max<size_t>(src.size(), 1);
+    NB_CUDA_OK(c, cudaMalloc((void **)&dst, sizeof(V) * n));
+    if (!src.empty()) NB_CUDA_OK(c, cudaMemcpy(dst, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice));
+    return MOIL_NB_OK;
+}
+
+#define NB_TRY(x)                      \
+    do {                               \
+        int rc_ = (x);                 \
+        if (rc_ != MOIL_NB_OK) return rc_; \
+    } while (0)
+
+int alloc_lists(NbCtx *c)
+{
+    free_ptr(c->d_wl1);
+    free_ptr(c->d_wl2);
+    free_ptr(c->d_xl);
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1, sizeof(int) * std::max<int64_t>(c->cap_wl1, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl2, sizeof(int) * std::max<int64_t>(c->cap_wl2, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_xl, sizeof(int) * std::max<int64_t>(c->cap_xl, 1)));
+    return MOIL_NB_OK;
+}
+
+int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
+{
+    if (c->inited) release_device(c);
+    c->err.clear();
+    if (nrep <= 0 || !reps) { c->err = "no replicas"; return MOIL_NB_ERR_ARG; }
+    const moil_nb_params &p0 = *reps[0].params;
+    c->precision = p0.precision == MOIL_NB_FP64 ? MOIL_NB_FP64 : MOIL_NB_MIXED;
+    c->skin = (float)(p0.skin > 0 ? p0.skin : 0.0);
+    c->list_period = p0.list_period;
+    c->nrep = nrep;
+    c->rh.assign(nrep, RepHost());
+    c->rd.assign(nrep, RepDev());
+    c->bsp_h.clear();
+    // host staging
+    std::vector<double> q, lj_e12, lj_e6;
+    std::vector<unsigned> aflags;
+    std::vector<int> atom_rep, unit_atom_w, unit_atom_o, unit_rep_w, unit_rep_o;
+    std::vector<std::vector<int>> exn, p14n;
+    std::vector<std::vector<double>> p14p;
+    int64_t atom0 = 0, wat0 = 0, oth0 = 0, zb0 = 0, g0 = 0;
+    int cell0 = 0;
+    for (int r = 0; r < nrep; ++r) {
+        const moil_nb_params *p = reps[r].params;
+        const moil_topology *t = reps[r].topo;
+        NB_TRY(validate_replica(c, p, t, r));
+        if ((p->precision == MOIL_NB_FP64) != (c->precision == MOIL_NB_FP64)) {
+            c->err = "all replicas of a handle must use one precision";
+            return MOIL_NB_ERR_ARG;
+        }
+        RepHost &H = c->rh[r];
+        RepDev &R = c->rd[r];
+        memset(&R, 0, sizeof(R));
+        H.p = *p;
+        H.npt = t->npt;
+        double alpha = p->alpha > 0 ? p->alpha : find_ewaldcof(p->relx, p->dtol > 0 ? p->dtol : 1e-6);
+        H.alpha = alpha;
+        double epstmp = NB_KOFDIE / p->eps;
+        // water monomers: O,H,H with all intramolecular pairs excluded
+        int nwat = 0, last_o = -1;
+        std::vector<char> is_w(t->npt + 1, 0);
+        for (int m = 0; m < t->totmon; ++m) {
+            int first = m == 0 ? 1 : t->poipt[m - 1] + 1, last = t->poipt[m];
+            if (t->montype[m] == MOIL_MON_WATER) {
+                if (last - first != 2 || !excl_has(t, first, first + 1) || !excl_has(t, first, first + 2) ||
+                    !excl_has(t, first + 1, first + 2)) {
+                    char buf[160];
+                    snprintf(buf, sizeof buf, "replica %d monomer %d: water must be O,H,H with its three pairs excluded", r, m + 1);
+                    c->err = buf;
+                    return MOIL_NB_ERR_TOPOLOGY;
+                }
+                for (int k = first; k <= last; ++k) is_w[k] = 1;
+                ++nwat;
+                last_o = first;
+            }
+        }
+        // exclusions: water atoms only with their own molecule
+        for (int l = 1; l <= t->npt; ++l)
+            for (int k = t->exc1[l - 1] + 1; k <= t->exc1[l]; ++k) {
+                int m = t->exc2[k - 1];
+                if (m < 1 || m > t->npt) { c->err = "exclusion partner out of range"; return MOIL_NB_ERR_ARG; }
+                if ((is_w[l] || is_w[m])) {
+                    bool same = is_w[l] && is_w[m] && std::abs(l - m) <= 2;
+                    if (same) {
+                        // same molecule iff they share the monomer (O index <= both <= O+2)
+                    }
+                    if (!(is_w[l] && is_w[m]) || !same) {
+                        c->err = "exclusions between a water and another monomer are not supported";
+                        return MOIL_NB_ERR_TOPOLOGY;
+                    }
+                }
+            }
+        // replica geometry and constants
+        R.atom0 = (int)atom0; R.natom = t->npt;
+        R.L[0] = (float)p->a; R.L[1] = (float)p->b; R.L[2] = (float)p->c;
+        R.Ld[0] = p->a; R.Ld[1] = p->b; R.Ld[2] = p->c;
+        for (int d = 0; d < 3; ++d) {
+            R.invL[d] = (float)(1.0 / R.Ld[d]);
+            R.invLd[d] = 1.0 / R.Ld[d];
+            R.Llo[d] = (float)(R.Ld[d] - (double)R.L[d]);
+        }
+        double rmax = std::max(p->rvmx, p->relx);
+        R.rv2 = (float)(p->rvmx * p->rvmx);
+        R.re2 = (float)(p->relx * p->relx);
+        R.rmax2 = (float)(rmax * rmax);
+        double rl = rmax + c->skin, rlw = rl + c->rwat;
+        R.rlist2 = (float)(rl * rl);
+        R.rlistw2 = (float)(rlw * rlw);
+        R.alpha = (float)alpha;
+        R.alphad = alpha;
+        R.ex2c = (float)(alpha * alpha * 1.4426950408889634);
+        R.c2a = (float)(alpha * NB_TWO_OVER_SQRTPI);
+        R.lj_switch = p->lj_switch ? 1 : 0;
+        R.ron2 = (float)(p->r_on * p->r_on);
+        if (p->lj_switch) {
+            double d = p->rvmx * p->rvmx - p->r_on * p->r_on;
+            R.swden = (float)(1.0 / (d * d * d));
+        }
+        R.arith = p->arith ? 1 : 0;
+        R.hvdw0 = p->hvdw0 ? 1 : 0;
+        R.epstmp = epstmp;
+        R.has_water = nwat > 0;
+        if (last_o > 0) {   // pot/watwat_ewald.f:40-79: constants from the last water
+            int io = last_o - 1, ih = last_o;
+            double qo = t->ptchg[io], qh = t->ptchg[ih];
+            R.qqd[0] = epstmp * qo * qo; R.qqd[1] = epstmp * qo * qh; R.qqd[2] = epstmp * qh * qh;
+            if (!p->arith) {
+                R.w6d = t->epsgm6[io] * t->epsgm6[io];
+                R.w12d = t->epsgm12[io] * t->epsgm12[io];
+            } else {
+                R.w6d = pow(t->epsgm12[io], 2) * pow(t->epsgm6[io], 6);
+                R.w12d = pow(t->epsgm12[io], 2) * pow(t->epsgm6[io], 12);
+            }
+            for (int k = 0; k < 3; ++k) R.qq[k] = (float)R.qqd[k];
+            R.w12 = (float)R.w12d; R.w6 = (float)R.w6d;
+        }
+        double s2 = 0;
+        for (int i = 0; i < t->npt; ++i) s2 += t->ptchg[i] * t->ptchg[i];
+        R.e_self = -alpha * sqrt(1.0 / M_PI) * epstmp * s2;   // symm/ewald_init.f:131-150
+        // cells
+        for (int d = 0; d < 3; ++d) R.nc[d] = std::max(1, (int)floor(R.Ld[d] / rlw));
+        R.cell0 = cell0;
+        cell0 += R.nc[0] * R.nc[1] * R.nc[2];
+        // PME
+        R.n1 = p->nfft1; R.n2 = p->nfft2; R.n3 = p->nfft3;
+        if (R.n1 < 4 || R.n2 < 4 || R.n3 < 4) { c->err = "PME grid below 4 points"; return MOIL_NB_ERR_GRID; }
+        R.n1h = R.n1 / 2 + 1;
+        R.g0 = g0;
+        g0 += (int64_t)R.n1h * R.n2 * R.n3;
+        R.zb0 = (int)zb0;
+        zb0 += R.n3;
+        R.bsp0 = (int)c->bsp_h.size();
+        {
+            int ns[3] = {R.n1, R.n2, R.n3};
+            for (int d = 0; d < 3; ++d) {
+                std::vector<double> m(ns[d]);
+                bsp_moduli(ns[d], m.data());
+                c->bsp_h.insert(c->bsp_h.end(), m.begin(), m.end());
+            }
+        }
+        R.fcd = sqrt(epstmp);
+        R.fc = (float)R.fcd;
+        R.pme_fac = M_PI * M_PI / (alpha * alpha);
+        R.pivol = M_PI * p->a * p->b * p->c;
+        // atoms and units
+        R.wat0 = (int)wat0; R.oth0 = (int)oth0;
+        int noth = 0;
+        for (int m = 0; m < t->totmon; ++m) {
+            int first = m == 0 ? 1 : t->poipt[m - 1] + 1, last = t->poipt[m];
+            if (t->montype[m] == MOIL_MON_WATER) {
+                unit_atom_w.push_back((int)(atom0 + first - 1));
+                unit_rep_w.push_back(r);
+            } else {
+                for (int k = first; k <= last; ++k) {
+                    unit_atom_o.push_back((int)(atom0 + k - 1));
+                    unit_rep_o.push_back(r);
+                    ++noth;
+                }
+            }
+        }
+        R.nwat = nwat; R.noth = noth;
+        wat0 += nwat; oth0 += noth;
+        for (int i = 0; i < t->npt; ++i) {
+            q.push_back(t->ptchg[i]);
+            lj_e12.push_back(t->epsgm12[i]);
+            lj_e6.push_back(t->epsgm6[i]);
+            unsigned f = 0;
+            if (fabs(t->ptchg[i]) > 1e-6) f |= SF_CHARGED;
+            if (is_w[i + 1]) f |= SF_WATER;
+            if (t->epsgm12[i] < 1e-3) f |= SF_HTINY;
+            aflags.push_back(f);
+            atom_rep.push_back(r);
+        }
+        // exclusion and 1-4 partners, both directions, caller indices
+        size_t base = exn.size();
+        exn.resize(base + t->npt);
+        p14n.resize(base + t->npt);
+        p14p.resize(base + t->npt);
+        for (int l = 1; l <= t->npt; ++l)
+            for (int k = t->exc1[l - 1] + 1; k <= t->exc1[l]; ++k) {
+                int m = t->exc2[k - 1];
+                exn[base + l - 1].push_back((int)(atom0 + m - 1));
+                exn[base + m - 1].push_back((int)(atom0 + l - 1));
+            }
+        for (int k = 0; k < t->totspe; ++k) {
+            int j = t->spec1[k], l = t->spec2[k];
+            if (j < 1 || j > t->npt || l < 1 || l > t->npt) { c->err = "1-4 partner out of range"; return MOIL_NB_ERR_ARG; }
+            for (int side = 0; side < 2; ++side) {
+                int a = side ? l : j, b = side ? j : l;
+                p14n[base + a - 1].push_back((int)(atom0 + b - 1));
+                for (int d = 0; d < 3; ++d) p14p[base + a - 1].push_back(t->p14[3 * k + d]);
+            }
+        }
+        atom0 += t->npt;
+    }
+    c->natom = atom0;
+    c->nW = wat0;
+    c->nA = oth0;
+    c->nsite = 3 * c->nW + c->nA;
+    c->nunit = c->nW + c->nA;
+    c->ncell = cell0;
+    c->grid_elems = g0;
+    c->nzbin = (int)zb0;
+    if (c->nsite != c->natom) { c->err = "internal: site count"; return MOIL_NB_ERR_ARG; }
+    for (int r = 0; r < nrep; ++r) c->rd[r].oth0 = c->rd[r].oth0;   // already set
+
+    // device uploads
+    NB_TRY(upload(c, c->d_q, q));
+    {
+        std::vector<float2> ljf(q.size());
+        std::vector<double2> ljd(q.size());
+        for (size_t i = 0; i < q.size(); ++i) {
+            ljf[i] = make_float2((float)lj_e12[i], (float)lj_e6[i]);
+            ljd[i] = make_double2(lj_e12[i], lj_e6[i]);
+        }
+        NB_TRY(upload(c, c->d_lj_f, ljf));
+        NB_TRY(upload(c, c->d_lj_d, ljd));
+    }
+    NB_TRY(upload(c, c->d_aflags, aflags));
+    NB_TRY(upload(c, c->d_atom_rep, atom_rep));
+    {
+        std::vector<int> ua(unit_atom_w), ur(unit_rep_w);
+        ua.insert(ua.end(), unit_atom_o.begin(), unit_atom_o.end());
+        ur.insert(ur.end(), unit_rep_o.begin(), unit_rep_o.end());
+        NB_TRY(upload(c, c->d_unit_atom, ua));
+        NB_TRY(upload(c, c->d_unit_rep, ur));
+    }
+    {
+        std::vector<int> off(c->natom + 1, 0), js, poff(c->natom + 1, 0), pj;
+        std::vector<double> pp;
+        for (int64_t a = 0; a < c->natom; ++a) {
+            off[a + 1] = off[a] + (int)exn[a].size();
+            js.insert(js.end(), exn[a].begin(), exn[a].end());
+            poff[a + 1] = poff[a] + (int)p14n[a].size();
+            pj.insert(pj.end(), p14n[a].begin(), p14n[a].end());
+            pp.insert(pp.end(), p14p[a].begin(), p14p[a].end());
+        }
+        NB_TRY(upload(c, c->d_ex_off, off));
+        NB_TRY(upload(c, c->d_ex_j, js));
+        NB_TRY(upload(c, c->d_p14_off, poff));
+        NB_TRY(upload(c, c->d_p14_j, pj));
+        NB_TRY(upload(c, c->d_p14_par, pp));
+    }
+    NB_TRY(upload(c, c->d_reps, c->rd));
+    const size_t ts = c->precision == MOIL_NB_FP64 ? 8 : 4;
+    int64_t nu = c->nunit, ns = c->nsite;
+    NB_CUDA_OK(c, cudaMalloc(&c->d_unit_key, sizeof(int) * nu));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_unit_slot, sizeof(int) * nu));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_bin_count, sizeof(int) * (2 * c->ncell + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_bin_start, sizeof(int) * (2 * c->ncell + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_sorted_unit, sizeof(int) * nu));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_site_orig, sizeof(int) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_site_of, sizeof(int) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_site_rep, sizeof(int) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_site_flags, sizeof(unsigned) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_pos, 4 * ts * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_posb, sizeof(float4) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_woff, 4 * ts * 2 * std::max<int64_t>(c->nW, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_site_lj, 2 * ts * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_site_q, ts * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1_off, sizeof(int) * (c->nW + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl2_off, sizeof(int) * (c->nW + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_xl_off, sizeof(int) * (c->nA + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_count_tmp, sizeof(int) * (2 * std::max(c->nW, c->nA) + 2)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_grad_site, sizeof(long long) * 3 * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_unit, sizeof(double) * 4 * std::max<int64_t>(nu, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_grad_ex, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_ex, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_zcount, sizeof(int) * (c->nzbin + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_zstart, sizeof(int) * (c->nzbin + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_zslot, sizeof(int) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_zatoms, sizeof(int) * ns));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_rep, sizeof(double) * 16 * nrep));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_coor, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_dpot, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMemset(c->d_grad_site, 0, sizeof(long long) * 3 * ns));
+    NB_CUDA_OK(c, cudaMemset(c->d_e_unit, 0, sizeof(double) * 4 * std::max<int64_t>(nu, 1)));
+    // list capacities from densities (grown on overflow)
+    c->cap_wl1 = c->cap_wl2 = c->cap_xl = 64;
+    for (int r = 0; r < nrep; ++r) {
+        const RepDev &R = c->rd[r];
+        double vol = R.Ld[0] * R.Ld[1] * R.Ld[2];
+        double rl = sqrt((double)R.rlist2), rlw = sqrt((double)R.rlistw2);
+        double sph = 4.0 / 3.0 * M_PI, vl = std::min(sph * rl * rl * rl, vol), vw = std::min(sph * rlw * rlw * rlw, vol);
+        c->cap_wl1 += (int64_t)(R.nwat * (vl * R.nwat / vol) * 1.3) + 32;
+        c->cap_wl2 += (int64_t)(R.nwat * (vw * R.noth / vol) * 1.5) + 32;
+        c->cap_xl += (int64_t)(R.noth * (vw * (3.0 * R.nwat + R.noth) / vol) * 1.5) + 32;
+    }
+    NB_TRY(alloc_lists(c));
+    c->h_e_rep.assign(16 * nrep, 0.0);
+    NB_TRY(nb_pme_configure(c));
+    NB_CUDA_OK(c, cudaDeviceSynchronize());
+    c->need_rebuild = 1;
+    c->evals_since_build = 0;
+    c->inited = 1;
+    return MOIL_NB_OK;
+}
+
+int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
+{
+    cudaStream_t s = c->stream;
+    c->launches = 0;
+    bool forced = c->need_rebuild || (c->list_period > 0 && c->evals_since_build >= c->list_period);
+    if (c->timing) cudaEventRecord(c->ev[0], s);
+    int init_status[2] = {forced ? 1 : 0, 0};
+    cudaMemcpyAsync(c->d_status, init_status, sizeof(init_status), cudaMemcpyHostToDevice, s);
+    if (!forced) nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
+    nb_launch_build_lists(c, d_coor);               // every kernel here is gated by the flag
+    if (c->timing) cudaEventRecord(c->ev[1], s);
+    nb_launch_realspace(c);
+    nb_launch_excl14(c, d_coor);
+    if (c->timing) cudaEventRecord(c->ev[5], s);
+    nb_launch_pme(c);
+    nb_launch_finalize(c, d_dpot);
+    if (c->timing) cudaEventRecord(c->ev[10], s);
+    cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(c->h_e_rep.data(), c->d_e_rep, sizeof(double) * 16 * c->nrep, cudaMemcpyDeviceToHost, s);
+    NB_CUDA_OK(c, cudaStreamSynchronize(s));
+    NB_CUDA_OK(c, cudaGetLastError());
+    int rebuilt = c->h_status[0] != 0;
+    if (rebuilt) {
+        c->evals_since_build = 0;
+        c->last_water_pairs = c->h_status[2];
+        c->last_atom_pairs = c->h_status[4];
+        c->last_list_entries = (int64_t)c->h_status[2] + c->h_status[3] + c->h_status[4];
+    }
+    c->evals_since_build++;
+    c->need_rebuild = 0;
+    if (c->timing) {
+        moil_nb_timing &t = c->last_timing;
+        auto el = [&](int a, int b) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]);
+            return ms;
+        };
+        t.list_ms = el(0, 1);
+        t.prepare_ms = 0;
+        t.water_ms = el(2, 3);
+        t.atom_ms = el(3, 4);
+        t.excl_ms = el(4, 5);
+        t.pme_spread_fft_ms = el(6, 7);
+        t.pme_conv_ms = el(7, 8);
+        t.pme_gather_ms = el(8, 9);
+        t.finalize_ms = el(9, 10);
+        t.total_ms = el(0, 10);
+        t.list_rebuilt = rebuilt;
+        t.launches = c->launches;
+    }
+    int err = c->h_status[1];
+    if (err & NB_DEV_ERR_OVERFLOW) return MOIL_NB_ERR_OVERFLOW;
+    if (err & NB_DEV_ERR_NAN) { c->err = "non-finite coordinate or gradient"; return MOIL_NB_ERR_NAN; }
+    if (err & NB_DEV_ERR_RWAT) { c->err = "a water hydrogen moved more than 1.1 A from its oxygen"; return MOIL_NB_ERR_TOPOLOGY; }
+    return MOIL_NB_OK;
+}
+
+int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
+{
+    int rc = MOIL_NB_OK;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        rc = eval_once(c, d_coor, d_dpot);
+        if (rc != MOIL_NB_ERR_OVERFLOW) break;
+        // grow from the exact totals the count pass produced, then redo with a fresh build
+        int64_t need1 = c->h_status[2], need2 = c->h_status[3], need3 = c->h_status[4];
+        c->cap_wl1 = std::max<int64_t>(c->cap_wl1, need1 + need1 / 8 + 64);
+        c->cap_wl2 = std::max<int64_t>(c->cap_wl2, need2 + need2 / 8 + 64);
+        c->cap_xl = std::max<int64_t>(c->cap_xl, need3 + need3 / 8 + 64);
+        int a = alloc_lists(c);
+        if (a != MOIL_NB_OK) return a;
+        c->need_rebuild = 1;
+    }
+    if (rc != MOIL_NB_OK) return rc;
+    if (e) {
+        for (int r = 0; r < c->nrep; ++r) {
+            const double *o = c->h_e_rep.data() + 16 * r;
+            moil_energies &E = e[r];
+            E.e_vdw = o[0]; E.e_el = o[1]; E.e_vsym = o[2]; E.e_lsym = o[3];
+            E.e_el14 = o[4]; E.e_vdw14 = o[5]; E.e_corr = o[6]; E.e_self = o[7];
+            E.e_ew_receip = o[8]; E.e_total = o[9]; E.e_dir = o[10];
+        }
+    }
+    return MOIL_NB_OK;
+}
+
+std::mutex g_fortran_mu;
+moil_nb_ctx *g_fortran_ctx = nullptr;
+std::vector<double> g_fortran_buf;
+
+}  // namespace
+
+struct moil_nb_ctx : NbCtx {};
+
+extern "C" {
+
+const char *moil_nb_strerror(int s)
+{
+    if (s < 0 || s >= (int)(sizeof(kStatusText) / sizeof(kStatusText[0]))) return "unknown status";
+    return kStatusText[s];
+}
+
+const char *moil_nb_last_error(const moil_nb_ctx *h) { return h ? h->err.c_str() : "null handle"; }
+
+int moil_nb_create(moil_nb_ctx **out, int device)
+{
+    if (!out) return MOIL_NB_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return MOIL_NB_ERR_CUDA;
+    if (device < 0 || device >= ndev) return MOIL_NB_ERR_ARG;
+    moil_nb_ctx *h = new moil_nb_ctx();
+    h->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return MOIL_NB_ERR_CUDA;
+    }
+    for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
+    if (cudaMallocHost(&h->h_status, sizeof(int) * 8) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
+        moil_nb_destroy(h);
+        return MOIL_NB_ERR_CUDA;
+    }
+    cudaMemset(h->d_status, 0, sizeof(int) * 8);
+    *out = h;
+    return MOIL_NB_OK;
+}
+
+void moil_nb_destroy(moil_nb_ctx *h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    release_device(h);
+    for (int k = 0; k < 12; ++k)
+        if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+    if (h->h_status) cudaFreeHost(h->h_status);
+    if (h->d_status) cudaFree(h->d_status);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int moil_nb_init(moil_nb_ctx *h, const moil_nb_params *p, const moil_topology *t)
+{
+    if (!h || !p || !t) return MOIL_NB_ERR_ARG;
+    moil_replica r = {p, t};
+    cudaSetDevice(h->device);
+    return init_impl(h, 1, &r);
+}
+
+int moil_nb_init_batch(moil_nb_ctx *h, int nrep, const moil_replica *reps)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    cudaSetDevice(h->device);
+    return init_impl(h, nrep, reps);
+}
+
+int moil_nb_get_alpha(const moil_nb_ctx *h, int r, double *alpha)
+{
+    if (!h || !alpha || !h->inited || r < 0 || r >= h->nrep) return MOIL_NB_ERR_ARG;
+    *alpha = h->rh[r].alpha;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *e)
+{
+    if (!h || !coor || !dpot) return MOIL_NB_ERR_ARG;
+    if (!h->inited) return MOIL_NB_ERR_STATE;
+    cudaSetDevice(h->device);
+    size_t bytes = sizeof(double) * 3 * h->natom;
+    NB_CUDA_OK(h, cudaMemcpyAsync(h->d_coor, coor, bytes, cudaMemcpyHostToDevice, h->stream));
+    int rc = eval_impl(h, h->d_coor, h->d_dpot, e);
+    if (rc != MOIL_NB_OK) return rc;
+    NB_CUDA_OK(h, cudaMemcpyAsync(dpot, h->d_dpot, bytes, cudaMemcpyDeviceToHost, h->stream));
+    NB_CUDA_OK(h, cudaStreamSynchronize(h->stream));
+    return MOIL_NB_OK;
+}
+
+int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *e)
+{
+    if (!h || !d_coor || !d_dpot) return MOIL_NB_ERR_ARG;
+    if (!h->inited) return MOIL_NB_ERR_STATE;
+    cudaSetDevice(h->device);
+    return eval_impl(h, d_coor, d_dpot, e);
+}
+
+int moil_nb_request_rebuild(moil_nb_ctx *h)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    h->need_rebuild = 1;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_squeeze(const moil_nb_params *p, const moil_topology *t, double *coor)
+{
+    // symm/squeeze.f:66-145: water and ion monomers move by one box length when their first
+    // atom is outside [-L/2, L/2]; y first, then x, then z (the order MOIL tests them)
+    if (!p || !t || !coor) return MOIL_NB_ERR_ARG;
+    double ha = 0.5 * p->a, hb = 0.5 * p->b, hc = 0.5 * p->c;
+    for (int m = 0; m < t->totmon; ++m) {
+        if (t->montype[m] == MOIL_MON_OTHER) continue;
+        int is = m == 0 ? 0 : t->poipt[m - 1], ie = t->poipt[m];
+        double xc = coor[3 * is], yc = coor[3 * is + 1], zc = coor[3 * is + 2];
+        for (int k = is; k < ie; ++k) {
+            if (yc < -hb) coor[3 * k + 1] += p->b;
+            if (yc > hb) coor[3 * k + 1] -= p->b;
+            if (xc < -ha) coor[3 * k] += p->a;
+            if (zc < -hc) coor[3 * k + 2] += p->c;
+            if (xc > ha) coor[3 * k] -= p->a;
+            if (zc > hc) coor[3 * k + 2] -= p->c;
+        }
+    }
+    return MOIL_NB_OK;
+}
+
+int moil_nb_natoms(const moil_nb_ctx *h, int64_t *n)
+{
+    if (!h || !n) return MOIL_NB_ERR_ARG;
+    *n = h->natom;
+    return MOIL_NB_OK;
+}
+
+void *moil_nb_stream(const moil_nb_ctx *h) { return h ? (void *)h->stream : nullptr; }
+
+int moil_nb_set_timing(moil_nb_ctx *h, int on)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    h->timing = on ? 1 : 0;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_get_timing(const moil_nb_ctx *h, moil_nb_timing *t)
+{
+    if (!h || !t) return MOIL_NB_ERR_ARG;
+    *t = h->last_timing;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *water_pairs, int64_t *atom_pairs)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    if (list_entries) *list_entries = h->last_list_entries;
+    if (water_pairs) *water_pairs = h->last_water_pairs;
+    if (atom_pairs) *atom_pairs = h->last_atom_pairs;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_set_graph(moil_nb_ctx *h, int on)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    h->use_graph = on ? 1 : 0;
+    return MOIL_NB_OK;
+}
+
+// ---- Fortran entry points --------------------------------------------------------
+void ewald_init_gpu_(const int *npt, const double *ptchg, const double *epsgm6, const double *epsgm12,
+                     const int *exc1, const int *exc2, const int *totspe, const int *spec1, const int *spec2,
+                     const double *p14, const int *totmon, const int *poipt, const int *montype,
+                     const double *params11, const int *iparams8, int *status)
+{
+    std::lock_guard<std::mutex> lk(g_fortran_mu);
+    if (!status) return;
+    if (!npt || !params11 || !iparams8) { *status = MOIL_NB_ERR_ARG; return; }
+    if (!g_fortran_ctx) {
+        int rc = moil_nb_create(&g_fortran_ctx, 0);
+        if (rc != MOIL_NB_OK) { *status = rc; return; }
+    }
+    moil_nb_params p;
+    memset(&p, 0, sizeof p);
+    p.rvmx = params11[0]; p.relx = params11[1]; p.eps = params11[2];
+    p.a = params11[3]; p.b = params11[4]; p.c = params11[5];
+    p.dtol = params11[6]; p.alpha = params11[7]; p.r_on = params11[8]; p.skin = params11[9];
+    p.nfft1 = iparams8[0]; p.nfft2 = iparams8[1]; p.nfft3 = iparams8[2]; p.order = iparams8[3];
+    p.arith = iparams8[4]; p.hvdw0 = iparams8[5]; p.lj_switch = iparams8[6]; p.precision = iparams8[7];
+    p.list_period = (int)params11[10];
+    moil_topology t;
+    t.npt = *npt; t.ptchg = ptchg; t.epsgm6 = epsgm6; t.epsgm12 = epsgm12; t.exc1 = exc1; t.exc2 = exc2;
+    t.totspe = totspe ? *totspe : 0; t.spec1 = spec1; t.spec2 = spec2; t.p14 = p14;
+    t.totmon = totmon ? *totmon : 0; t.poipt = poipt; t.montype = montype;
+    *status = moil_nb_init(g_fortran_ctx, &p, &t);
+}
+
+void nblist_gpu_(int *status)
+{
+    std::lock_guard<std::mutex> lk(g_fortran_mu);
+    if (!status) return;
+    *status = g_fortran_ctx ? moil_nb_request_rebuild(g_fortran_ctx) : MOIL_NB_ERR_STATE;
+}
+
+void eforce_nb_gpu_(const int *npt, const double *coor, double *dpot, double *enb, int *status)
+{
+    // MOIL's terms accumulate into dpot (pot/eforce.f:64-68 zeroes it first), so this entry
+    // adds the nonbonded gradient to what the caller already holds.
+    std::lock_guard<std::mutex> lk(g_fortran_mu);
+    if (!status) return;
+    if (!g_fortran_ctx || !npt || !coor || !dpot) { *status = g_fortran_ctx ? MOIL_NB_ERR_ARG : MOIL_NB_ERR_STATE; return; }
+    if ((int64_t)*npt != g_fortran_ctx->natom) { *status = MOIL_NB_ERR_ARG; return; }
+    g_fortran_buf.resize(3 * (size_t)*npt);
+    moil_energies e;
+    int rc = moil_nb_eval(g_fortran_ctx, coor, g_fortran_buf.data(), &e);
+    if (rc == MOIL_NB_OK) {
+        for (size_t k = 0; k < g_fortran_buf.size(); ++k) dpot[k] += g_fortran_buf[k];
+        if (enb) {
+            const double v[11] = {e.e_vdw, e.e_el, e.e_vsym, e.e_lsym, e.e_el14, e.e_vdw14,
+                                  e.e_corr, e.e_self, e.e_ew_receip, e.e_total, e.e_dir};
+            memcpy(enb, v, sizeof v);
+        }
+    }
+    *status = rc;
+}
+
+}  // extern "C"

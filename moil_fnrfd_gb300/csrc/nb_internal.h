@@ -1,0 +1,154 @@
+// nb_internal.h -- handle state shared by the host orchestration and the kernel files.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "moil_nb.h"
+#include "nb_common.cuh"
+
+// FFT plan for one length: radices (4, 2, 3, 5 in that order) and twiddles exp(-2 pi i k / n)
+struct FftPlanDev {
+    int n, nst, tw0, pad;
+    int rad[8];
+};
+
+struct RepHost {
+    moil_nb_params p;
+    int npt;
+    double alpha;
+    std::vector<double> q, e6, e12;
+    std::vector<int> exc1, exc2, spec1, spec2, poipt, montype;
+    std::vector<double> p14;
+    int nwat;
+    int nuniq_oth;
+};
+
+struct NbCtx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int precision = MOIL_NB_MIXED;
+    int inited = 0;
+    std::string err;
+
+    // replicas
+    int nrep = 0;
+    std::vector<RepHost> rh;
+    std::vector<RepDev> rd;
+    RepDev *d_reps = nullptr;
+    int64_t natom = 0, nW = 0, nA = 0, nsite = 0, nunit = 0;
+    float skin = 1.0f, rwat = 1.1f;
+    int list_period = 0;
+
+    // static per caller atom
+    double *d_q = nullptr;        // charges
+    float2 *d_lj_f = nullptr;     // (epsgm12, epsgm6) per caller atom, FP32 copy
+    double2 *d_lj_d = nullptr;    // FP64 copy
+    unsigned *d_aflags = nullptr; // SF_* per caller atom
+    int *d_atom_rep = nullptr;
+
+    // units
+    int *d_unit_atom = nullptr;   // first caller atom of each unit (waters first, then others)
+    int *d_unit_rep = nullptr;
+    int ncell = 0;                // total cells over replicas
+    int *d_unit_key = nullptr, *d_unit_slot = nullptr;
+    int *d_bin_count = nullptr, *d_bin_start = nullptr;   // 2*ncell bins (+1)
+    int *d_sorted_unit = nullptr;
+
+    // site arrays
+    int *d_site_orig = nullptr, *d_site_of = nullptr, *d_site_rep = nullptr;
+    unsigned *d_site_flags = nullptr;
+    void *d_pos = nullptr;        // float4 / double4 (x, y, z, q_eff)
+    float4 *d_posb = nullptr;     // positions at the last list build
+    void *d_woff = nullptr;       // float4 / double4: water H offsets from O, 2 per molecule (FP64-computed)
+    void *d_site_lj = nullptr;    // float2 / double2
+    void *d_site_q = nullptr;     // float / double (PME charge)
+
+    // pair lists (CSR)
+    int *d_wl1_off = nullptr, *d_wl1 = nullptr;
+    int *d_wl2_off = nullptr, *d_wl2 = nullptr;
+    int *d_xl_off = nullptr, *d_xl = nullptr;
+    int64_t cap_wl1 = 0, cap_wl2 = 0, cap_xl = 0;
+    int *d_count_tmp = nullptr;   // scratch counts
+
+    // exclusion / 1-4 lists per caller atom (both directions)
+    int *d_ex_off = nullptr, *d_ex_j = nullptr;
+    int *d_p14_off = nullptr, *d_p14_j = nullptr;
+    double *d_p14_par = nullptr;
+
+    // outputs
+    long long *d_grad_site = nullptr;  // nsite*3 fixed point
+    double *d_e_unit = nullptr;        // nunit*4
+    double *d_grad_ex = nullptr;       // natom*3
+    double *d_e_ex = nullptr;          // natom*3
+
+    // PME
+    std::vector<FftPlanDev> plans;
+    FftPlanDev *d_plans = nullptr;
+    std::vector<int> rep_plan;         // 3 plan indices per replica
+    int *d_rep_plan = nullptr;
+    void *d_tw = nullptr;              // float2 / double2 twiddles
+    std::vector<double> bsp_h;
+    void *d_bsp = nullptr;             // float / double moduli
+    int nzbin = 0;
+    int *d_zcount = nullptr, *d_zstart = nullptr, *d_zslot = nullptr, *d_zatoms = nullptr;
+    void *d_fr = nullptr;              // float4 / double4 per site (fr1, fr2, fr3, q*fc)
+    void *d_grid = nullptr;            // half-complex grids, float2 / double2
+    int64_t grid_elems = 0;
+    void *d_part = nullptr;            // per site 4 slots x 3 (float / double)
+    std::vector<PlaneWork> planes;
+    PlaneWork *d_planes = nullptr;
+    std::vector<ColWork> cols;
+    ColWork *d_cols = nullptr;
+    std::vector<int> col_begin;        // per replica, nrep+1
+    int *d_col_begin = nullptr;
+    double *d_e_col = nullptr;         // energy partial per column work item
+    size_t smem_plane_fwd = 0, smem_plane_inv = 0, smem_zconv = 0;
+    int max_n1 = 0, max_n2 = 0, max_n3 = 0;
+
+    // energies
+    double *d_e_rep = nullptr;         // nrep * 16
+    std::vector<double> h_e_rep;
+
+    // caller buffers used by host-pointer evaluations
+    double *d_coor = nullptr, *d_dpot = nullptr;
+
+    // device status: [0] rebuild flag, [1] error bits, [2..4] list totals, [5] rebuilt this eval
+    int *d_status = nullptr;
+    int *h_status = nullptr;           // pinned mirror
+    int need_rebuild = 1;
+    int evals_since_build = 0;
+    int64_t last_list_entries = 0, last_water_pairs = 0, last_atom_pairs = 0;
+
+    // instrumentation
+    int timing = 0;
+    cudaEvent_t ev[12];
+    moil_nb_timing last_timing{};
+    int use_graph = 0;
+    int launches = 0;
+};
+
+// ---- launchers implemented in the kernel files -------------------------------------
+// lists (nb_lists.cu)
+void nb_launch_build_lists(NbCtx *c, const double *d_coor);
+void nb_launch_prepare(NbCtx *c, const double *d_coor, int check);
+void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_total);
+// real space + corrections (nb_realspace.cu)
+void nb_launch_realspace(NbCtx *c);
+void nb_launch_excl14(NbCtx *c, const double *d_coor);
+// PME (nb_pme.cu)
+void nb_launch_pme(NbCtx *c);
+int nb_pme_configure(NbCtx *c);
+// finalize (nb_realspace.cu)
+void nb_launch_finalize(NbCtx *c, double *d_dpot);
+
+#define NB_CUDA_OK(c, call)                                                         \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            (c)->err = std::string(#call) + ": " + cudaGetErrorString(e_);          \
+            return MOIL_NB_ERR_CUDA;                                                \
+        }                                                                           \
+    } while (0)

@@ -1,0 +1,584 @@
+// nb_pme.cu -- PME reciprocal sum (pot/ewald_receip.f:101-1080), GB300 layout.
+//
+// The reference spreads into a padded complex grid, runs two full 3D C2C FFTs
+// (pubz3d / FFTPACK) with the influence function in between (scalar_sum) and gathers.
+// Here the grid never exists as a real-space array in HBM:
+//   k_pme_bin      fractional coordinates fr = n (w - anint(w) + 1/2) (:250-260), atoms
+//                  bucketed by int(fr3) (the z plane their stencil ends on)
+//   k_plane_fwd    one CTA per (replica, z plane): the 4x4 x-y stencils of every atom whose
+//                  z stencil touches the plane are accumulated in shared memory in 64-bit
+//                  fixed point (order independent), then R2C along x and C2C along y in
+//                  shared memory; only the half-complex plane goes to HBM
+//   k_zconv        one CTA per (replica, ky, 16 kx columns): C2C along z, influence function
+//                  exp(-pi^2 m^2 / alpha^2) / (pi V B(m) m^2) with the FP64 energy sum
+//                  (scalar_sum, :723-812), inverse C2C along z, written back in place
+//   k_plane_inv    one CTA per (replica, z plane): inverse C2C along y, C2R along x in shared
+//                  memory, then each atom's gradient share from this plane (grad_sum,
+//                  :815-970) into its own slot -- four planes, four slots, summed at the end
+// FFTs: Stockham autosort, radix 4/2/3/5, one warp per line, twiddles from a table of
+// exp(-2 pi i k / n) computed on the host in FP64.  Inverse = conj(FFT(conj(x))),
+// unnormalised like FFTPACK's cfftb.
+#include "nb_internal.h"
+
+namespace {
+
+template <typename C> __device__ __forceinline__ C cmk(double r, double i);
+template <> __device__ __forceinline__ float2 cmk<float2>(double r, double i) { return make_float2((float)r, (float)i); }
+template <> __device__ __forceinline__ double2 cmk<double2>(double r, double i) { return make_double2(r, i); }
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b)
+{
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+// multiply by -i
+template <typename C> __device__ __forceinline__ C cmi(C a) { C r; r.x = a.y; r.y = -a.x; return r; }
+
+// forward DFT butterflies, W_R = exp(-2 pi i / R)
+template <typename C> __device__ __forceinline__ void bfly2(C *v)
+{
+    C a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+template <typename C> __device__ __forceinline__ void bfly4(C *v)
+{
+    C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]), t2 = cadd(v[1], v[3]), t3 = cmi(csub(v[1], v[3]));
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+}
+template <typename C> __device__ __forceinline__ void bfly3(C *v)
+{
+    typedef decltype(v[0].x) T;
+    const T h = (T)0.86602540378443864676;   // sqrt(3)/2
+    C s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+    C m;
+    m.x = v[0].x - (T)0.5 * s.x;
+    m.y = v[0].y - (T)0.5 * s.y;
+    C r0 = cadd(v[0], s);
+    C r1, r2;
+    r1.x = m.x + h * d.y; r1.y = m.y - h * d.x;
+    r2.x = m.x - h * d.y; r2.y = m.y + h * d.x;
+    v[0] = r0; v[1] = r1; v[2] = r2;
+}
+template <typename C> __device__ __forceinline__ void bfly5(C *v)
+{
+    typedef decltype(v[0].x) T;
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;   // cos(2pi/5), cos(4pi/5)
+    const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;    // sin(2pi/5), sin(4pi/5)
+    C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]), a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    C x0 = v[0];
+    C p1, p2;  // real-combination parts
+    p1.x = x0.x + c1 * a1.x + c2 * a2.x; p1.y = x0.y + c1 * a1.y + c2 * a2.y;
+    p2.x = x0.x + c2 * a1.x + c1 * a2.x; p2.y = x0.y + c2 * a1.y + c1 * a2.y;
+    C q1, q2;  // imaginary parts: q = s.b ; result +- (-i) q
+    q1.x = s1 * b1.x + s2 * b2.x; q1.y = s1 * b1.y + s2 * b2.y;
+    q2.x = s2 * b1.x - s1 * b2.x; q2.y = s2 * b1.y - s1 * b2.y;
+    v[0].x = x0.x + a1.x + a2.x; v[0].y = x0.y + a1.y + a2.y;
+    C mq1 = cmi(q1), mq2 = cmi(q2);
+    v[1] = cadd(p1, mq1);
+    v[4] = csub(p1, mq1);
+    v[2] = cadd(p2, mq2);
+    v[3] = csub(p2, mq2);
+}
+
+// one line of length n in shared memory (x), scratch y; returns the buffer holding the result
+template <typename C>
+__device__ C *warp_fft(C *x, C *y, const FftPlanDev &p, const C *__restrict__ tw, int lane)
+{
+    int n = p.n, Ns = 1;
+    for (int st = 0; st < p.nst; ++st) {
+        int R = p.rad[st], nb = n / R, stride = n / (Ns * R);
+        for (int j = lane; j < nb; j += 32) {
+            C v[5];
+            int jm = j % Ns;
+            for (int r = 0; r < R; ++r) v[r] = x[j + r * nb];
+            int tstep = jm * stride;
+            for (int r = 1; r < R; ++r) {
+                int t = (r * tstep) % n;
+                v[r] = cmul(v[r], tw[t]);
+            }
+            if (R == 4) bfly4(v);
+            else if (R == 2) bfly2(v);
+            else if (R == 3) bfly3(v);
+            else bfly5(v);
+            int idxD = (j / Ns) * Ns * R + jm;
+            for (int r = 0; r < R; ++r) y[idxD + r * Ns] = v[r];
+        }
+        __syncwarp();
+        C *t = x; x = y; y = t;
+        Ns *= R;
+    }
+    return x;
+}
+
+// MOIL fill_bspline for order 4 (ewald_receip.f:1022-1080)
+template <typename T>
+__device__ __forceinline__ void bspline4(T w, T th[4], T dth[4])
+{
+    th[3] = 0;
+    th[1] = w;
+    th[0] = (T)1 - w;
+    th[2] = (T)0.5 * w * th[1];
+    th[1] = (T)0.5 * ((w + (T)1) * th[0] + ((T)2 - w) * th[1]);
+    th[0] = (T)0.5 * ((T)1 - w) * th[0];
+    dth[0] = -th[0];
+    dth[1] = th[0] - th[1];
+    dth[2] = th[1] - th[2];
+    dth[3] = th[2] - th[3];
+    const T d3 = (T)(1.0 / 3.0);
+    th[3] = d3 * w * th[2];
+    th[2] = d3 * ((w + (T)1) * th[1] + ((T)3 - w) * th[2]);
+    th[1] = d3 * ((w + (T)2) * th[0] + ((T)2 - w) * th[1]);
+    th[0] = d3 * ((T)1 - w) * th[0];
+}
+
+__device__ __forceinline__ float nb_round(float x) { return roundf(x); }
+__device__ __forceinline__ double nb_round(double x) { return round(x); }
+
+// ---------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_pme_bin(int nsite, const int *__restrict__ site_rep, const RepDev *__restrict__ reps,
+                          const void *pos_v, const void *q_v, void *fr_v, int *__restrict__ zcount,
+                          int *__restrict__ zslot)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsite) return;
+    typedef typename vec4<T>::type T4;
+    const RepDev &R = reps[site_rep[s]];
+    T4 p = ((const T4 *)pos_v)[s];
+    T w, f1, f2, f3;
+    w = p.x * rep_invL<T>(R, 0); f1 = (T)R.n1 * (w - nb_round(w) + (T)0.5);
+    w = p.y * rep_invL<T>(R, 1); f2 = (T)R.n2 * (w - nb_round(w) + (T)0.5);
+    w = p.z * rep_invL<T>(R, 2); f3 = (T)R.n3 * (w - nb_round(w) + (T)0.5);
+    T4 o;
+    o.x = f1; o.y = f2; o.z = f3;
+    o.w = ((const T *)q_v)[s] * (sizeof(T) == 4 ? (T)R.fc : (T)R.fcd);
+    ((T4 *)fr_v)[s] = o;
+    int zb = (int)f3;
+    zb = zb >= R.n3 ? zb - R.n3 : (zb < 0 ? 0 : zb);
+    zslot[s] = atomicAdd(&zcount[R.zb0 + zb], 1);
+}
+
+__global__ void k_pme_scatter(int nsite, const int *__restrict__ site_rep, const RepDev *__restrict__ reps,
+                              const void *fr_v, int is_double, const int *__restrict__ zstart,
+                              const int *__restrict__ zslot, int *__restrict__ zatoms)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsite) return;
+    const RepDev &R = reps[site_rep[s]];
+    double f3 = is_double ? ((const double4 *)fr_v)[s].z : (double)((const float4 *)fr_v)[s].z;
+    int zb = (int)f3;
+    zb = zb >= R.n3 ? zb - R.n3 : (zb < 0 ? 0 : zb);
+    zatoms[zstart[R.zb0 + zb] + zslot[s]] = s;
+}
+
+template <typename T> struct Acc;
+template <> struct Acc<float> {
+    typedef unsigned long long type;
+    __device__ static void add(type *p, float v) { atomicAdd(p, (unsigned long long)__float2ll_rn(v * 1099511627776.0f)); }
+    __device__ static float get(type v) { return __ll2float_rn((long long)v) * (1.0f / 1099511627776.0f); }
+};
+template <> struct Acc<double> {
+    typedef double type;
+    __device__ static void add(type *p, double v) { atomicAdd(p, v); }
+    __device__ static double get(type v) { return v; }
+};
+
+__device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_plane_fwd(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                   const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                                   const void *tw_v, const int *__restrict__ zstart,
+                                                   const int *__restrict__ zatoms, const void *fr_v, void *grid_v)
+{
+    typedef typename cplx<T>::type C;
+    typedef typename vec4<T>::type T4;
+    typedef typename Acc<T>::type A;
+    extern __shared__ __align__(16) unsigned char smem[];
+    PlaneWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h, pitch = n1h | 1;
+    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
+    const C *tw = (const C *)tw_v;
+    A *acc = (A *)smem;
+    C *P = (C *)(smem + align16(sizeof(A) * n1 * n2));
+    C *scr = P + n2 * pitch;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
+    __syncthreads();
+    const T4 *fr = (const T4 *)fr_v;
+    for (int tp = 0; tp < 4; ++tp) {
+        int zb = w.z + tp;
+        zb = zb >= n3 ? zb - n3 : zb;
+        int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
+        int t3 = 3 - tp;
+        for (int idx = threadIdx.x; idx < (b1 - b0) * 4; idx += blockDim.x) {
+            int s = zatoms[b0 + (idx >> 2)], t2 = idx & 3;
+            T4 f = fr[s];
+            int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
+            bspline4<T>(f.x - (T)i1, th1, dt1);
+            bspline4<T>(f.y - (T)i2, th2, dt2);
+            bspline4<T>(f.z - (T)i3, th3, dt3);
+            int j = i2 - 3 + t2;
+            j = (j + 2 * n2) % n2;
+            T v = th2[t2] * th3[t3] * f.w;
+            A *row = acc + j * n1;
+#pragma unroll
+            for (int t1 = 0; t1 < 4; ++t1) {
+                int i = (i1 - 3 + t1 + 2 * n1) % n1;
+                Acc<T>::add(row + i, v * th1[t1]);
+            }
+        }
+    }
+    __syncthreads();
+    C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
+    // R2C along x (C2C of the real row, first n1/2+1 outputs kept)
+    for (int j = warp; j < n2; j += nwarp) {
+        for (int i = lane; i < n1; i += 32) x[i] = cmk<C>((double)Acc<T>::get(acc[j * n1 + i]), 0.0);
+        __syncwarp();
+        C *res = warp_fft<C>(x, y, p1, tw + p1.tw0, lane);
+        for (int k = lane; k < n1h; k += 32) P[j * pitch + k] = res[k];
+        __syncwarp();
+    }
+    __syncthreads();
+    // C2C along y
+    for (int k = warp; k < n1h; k += nwarp) {
+        for (int j = lane; j < n2; j += 32) x[j] = P[j * pitch + k];
+        __syncwarp();
+        C *res = warp_fft<C>(x, y, p2, tw + p2.tw0, lane);
+        for (int j = lane; j < n2; j += 32) P[j * pitch + k] = res[j];
+        __syncwarp();
+    }
+    __syncthreads();
+    C *g = (C *)grid_v + R.g0 + (size_t)w.z * n2 * n1h;
+    for (int idx = threadIdx.x; idx < n2 * n1h; idx += blockDim.x) {
+        int ky = idx / n1h, kx = idx - ky * n1h;
+        g[idx] = P[ky * pitch + kx];
+    }
+}
+
+#define NB_TK 16
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                               const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                               const void *tw_v, const void *bsp_v, void *grid_v,
+                                               double *__restrict__ e_col)
+{
+    typedef typename cplx<T>::type C;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[256];
+    ColWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
+    const int tk = min(NB_TK, n1h - w.kx0);
+    const int n3p = n3 | 1;
+    const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
+    const C *tw = (const C *)tw_v;
+    const T *bsp = (const T *)bsp_v + R.bsp0;
+    C *tile = (C *)smem;
+    C *scr = tile + NB_TK * n3p;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    C *g = (C *)grid_v + R.g0;
+    for (int idx = threadIdx.x; idx < tk * n3; idx += blockDim.x) {
+        int kz = idx / tk, c = idx - kz * tk;
+        tile[c * n3p + kz] = g[((size_t)kz * n2 + w.ky) * n1h + w.kx0 + c];
+    }
+    __syncthreads();
+    double en = 0;
+    C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
+    const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
+    const int m2 = w.ky < nf2 ? w.ky : w.ky - n2;
+    const T mh2 = (T)m2 * rep_invL<T>(R, 1);
+    const T fac = (T)R.pme_fac, pivol = (T)R.pivol;
+    for (int c = warp; c < tk; c += nwarp) {
+        const int kx = w.kx0 + c;
+        for (int kz = lane; kz < n3; kz += 32) x[kz] = tile[c * n3p + kz];
+        __syncwarp();
+        C *res = warp_fft<C>(x, y, p3, tw + p3.tw0, lane);
+        const T mh1 = (T)kx * rep_invL<T>(R, 0);
+        const T wgt = (kx == 0 || (2 * kx == n1)) ? (T)1 : (T)2;
+        const T b12 = bsp[kx] * bsp[n1 + w.ky];
+        for (int kz = lane; kz < n3; kz += 32) {
+            int m3 = kz < nf3 ? kz : kz - n3;
+            T mh3 = (T)m3 * rep_invL<T>(R, 2);
+            T msq = mh1 * mh1 + mh2 * mh2 + mh3 * mh3;
+            T eterm = (T)0;
+            if (kx != 0 || w.ky != 0 || kz != 0) eterm = exp(-fac * msq) / (pivol * b12 * bsp[n1 + n2 + kz] * msq);
+            C v = res[kz];
+            en += (double)(wgt * eterm * (v.x * v.x + v.y * v.y));
+            v.x *= eterm;
+            v.y *= eterm;
+            res[kz] = cconj(v);      // inverse = conj(FFT(conj(.)))
+        }
+        __syncwarp();
+        C *other = (res == x) ? y : x;
+        C *res2 = warp_fft<C>(res, other, p3, tw + p3.tw0, lane);
+        for (int kz = lane; kz < n3; kz += 32) tile[c * n3p + kz] = cconj(res2[kz]);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < tk * n3; idx += blockDim.x) {
+        int kz = idx / tk, c = idx - kz * tk;
+        g[((size_t)kz * n2 + w.ky) * n1h + w.kx0 + c] = tile[c * n3p + kz];
+    }
+    red[threadIdx.x] = en;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) e_col[blockIdx.x] = red[0];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                   const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                                   const void *tw_v, const int *__restrict__ zstart,
+                                                   const int *__restrict__ zatoms, const void *fr_v,
+                                                   const void *grid_v, T *__restrict__ part)
+{
+    typedef typename cplx<T>::type C;
+    typedef typename vec4<T>::type T4;
+    extern __shared__ __align__(16) unsigned char smem[];
+    PlaneWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h, pitch = n1h | 1;
+    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
+    const C *tw = (const C *)tw_v;
+    T *Rp = (T *)smem;
+    C *P = (C *)(smem + align16(sizeof(T) * n1 * n2));
+    C *scr = P + n2 * pitch;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const C *g = (const C *)grid_v + R.g0 + (size_t)w.z * n2 * n1h;
+    for (int idx = threadIdx.x; idx < n2 * n1h; idx += blockDim.x) {
+        int ky = idx / n1h, kx = idx - ky * n1h;
+        P[ky * pitch + kx] = g[idx];
+    }
+    __syncthreads();
+    C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
+    // inverse C2C along y
+    for (int k = warp; k < n1h; k += nwarp) {
+        for (int j = lane; j < n2; j += 32) x[j] = cconj(P[j * pitch + k]);
+        __syncwarp();
+        C *res = warp_fft<C>(x, y, p2, tw + p2.tw0, lane);
+        for (int j = lane; j < n2; j += 32) P[j * pitch + k] = cconj(res[j]);
+        __syncwarp();
+    }
+    __syncthreads();
+    // C2R along x: Hermitian row, inverse C2C, real part
+    for (int j = warp; j < n2; j += nwarp) {
+        for (int i = lane; i < n1; i += 32) {
+            C v = i < n1h ? P[j * pitch + i] : cconj(P[j * pitch + (n1 - i)]);
+            x[i] = cconj(v);
+        }
+        __syncwarp();
+        C *res = warp_fft<C>(x, y, p1, tw + p1.tw0, lane);
+        for (int i = lane; i < n1; i += 32) Rp[j * n1 + i] = res[i].x;   // real part of conj(.) unchanged
+        __syncwarp();
+    }
+    __syncthreads();
+    // gradient share of this plane for every atom whose z stencil touches it
+    const T4 *fr = (const T4 *)fr_v;
+    for (int tp = 0; tp < 4; ++tp) {
+        int zb = w.z + tp;
+        zb = zb >= n3 ? zb - n3 : zb;
+        int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
+        int t3 = 3 - tp;
+        for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
+            int s = zatoms[idx];
+            T4 f = fr[s];
+            int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
+            bspline4<T>(f.x - (T)i1, th1, dt1);
+            bspline4<T>(f.y - (T)i2, th2, dt2);
+            bspline4<T>(f.z - (T)i3, th3, dt3);
+            T gx = 0, gy = 0, gz = 0;
+#pragma unroll
+            for (int t2 = 0; t2 < 4; ++t2) {
+                int j = (i2 - 3 + t2 + 2 * n2) % n2;
+                const T *row = Rp + j * n1;
+                T sx = 0, sy = 0;
+#pragma unroll
+                for (int t1 = 0; t1 < 4; ++t1) {
+                    int i = (i1 - 3 + t1 + 2 * n1) % n1;
+                    T q = row[i];
+                    sx += q * dt1[t1];
+                    sy += q * th1[t1];
+                }
+                gx += sx * th2[t2];
+                gy += sy * dt2[t2];
+                gz += sy * th2[t2];
+            }
+            T *o = part + 12 * (size_t)s + 3 * t3;
+            o[0] = gx * th3[t3];
+            o[1] = gy * th3[t3];
+            o[2] = gz * dt3[t3];
+        }
+    }
+}
+
+template <typename T>
+void pme_t(NbCtx *c)
+{
+    cudaStream_t s = c->stream;
+    const int B = 256;
+    if (c->timing) cudaEventRecord(c->ev[6], s);
+    cudaMemsetAsync(c->d_zcount, 0, sizeof(int) * (c->nzbin + 1), s);
+    k_pme_bin<T><<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_reps, c->d_pos,
+                                                            c->d_site_q, c->d_fr, c->d_zcount, c->d_zslot);
+    nb_exclusive_scan(c, c->d_zcount, c->d_zstart, c->nzbin, nullptr);
+    k_pme_scatter<<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_reps, c->d_fr,
+                                                             sizeof(T) == 8, c->d_zstart, c->d_zslot, c->d_zatoms);
+    k_plane_fwd<T><<<(int)c->planes.size(), 256, c->smem_plane_fwd, s>>>(
+        c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw, c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid);
+    if (c->timing) cudaEventRecord(c->ev[7], s);
+    k_zconv<T><<<(int)c->cols.size(), 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                                c->d_tw, c->d_bsp, c->d_grid, c->d_e_col);
+    if (c->timing) cudaEventRecord(c->ev[8], s);
+    k_plane_inv<T><<<(int)c->planes.size(), 256, c->smem_plane_inv, s>>>(
+        c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw, c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid,
+        (T *)c->d_part);
+    if (c->timing) cudaEventRecord(c->ev[9], s);
+    c->launches += 6;
+}
+
+// radix plan: 4s first, then 2, 3, 5; returns 0 if n is not 2/3/5-smooth or too long
+int make_plan(int n, FftPlanDev *p)
+{
+    memset(p, 0, sizeof(*p));
+    p->n = n;
+    int m = n, k = 0;
+    if (n < 2 || n > NB_MAX_FFT) return 0;
+    while (m % 4 == 0) { p->rad[k++] = 4; m /= 4; }
+    while (m % 2 == 0) { p->rad[k++] = 2; m /= 2; }
+    while (m % 3 == 0) { p->rad[k++] = 3; m /= 3; }
+    while (m % 5 == 0) { p->rad[k++] = 5; m /= 5; }
+    if (m != 1 || k > 8) return 0;
+    p->nst = k;
+    return 1;
+}
+
+template <typename T>
+size_t plane_fwd_smem(int n1, int n2)
+{
+    typedef typename cplx<T>::type C;
+    size_t acc = (sizeof(typename Acc<T>::type) * n1 * n2 + 15) & ~(size_t)15;
+    return acc + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
+}
+template <typename T>
+size_t plane_inv_smem(int n1, int n2)
+{
+    typedef typename cplx<T>::type C;
+    size_t r = (sizeof(T) * n1 * n2 + 15) & ~(size_t)15;
+    return r + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
+}
+template <typename T>
+size_t zconv_smem(int n3)
+{
+    typedef typename cplx<T>::type C;
+    return sizeof(C) * NB_TK * (n3 | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
+}
+
+template <typename T>
+int configure_t(NbCtx *c)
+{
+    typedef typename cplx<T>::type C;
+    // plans for each distinct length
+    c->plans.clear();
+    c->rep_plan.assign(3 * c->nrep, 0);
+    std::vector<double> twr, twi;
+    for (int r = 0; r < c->nrep; ++r) {
+        int ns[3] = {c->rd[r].n1, c->rd[r].n2, c->rd[r].n3};
+        for (int d = 0; d < 3; ++d) {
+            int found = -1;
+            for (size_t k = 0; k < c->plans.size(); ++k)
+                if (c->plans[k].n == ns[d]) found = (int)k;
+            if (found < 0) {
+                FftPlanDev p;
+                if (!make_plan(ns[d], &p)) return MOIL_NB_ERR_GRID;
+                p.tw0 = (int)twr.size();
+                for (int t = 0; t < ns[d]; ++t) {
+                    double ang = -2.0 * M_PI * (double)t / (double)ns[d];
+                    twr.push_back(cos(ang));
+                    twi.push_back(sin(ang));
+                }
+                c->plans.push_back(p);
+                found = (int)c->plans.size() - 1;
+            }
+            c->rep_plan[3 * r + d] = found;
+        }
+    }
+    std::vector<C> tw(twr.size());
+    for (size_t k = 0; k < twr.size(); ++k) { tw[k].x = (T)twr[k]; tw[k].y = (T)twi[k]; }
+    NB_CUDA_OK(c, cudaMalloc(&c->d_plans, sizeof(FftPlanDev) * c->plans.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_plans, c->plans.data(), sizeof(FftPlanDev) * c->plans.size(), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_rep_plan, sizeof(int) * c->rep_plan.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_rep_plan, c->rep_plan.data(), sizeof(int) * c->rep_plan.size(), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_tw, sizeof(C) * tw.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_tw, tw.data(), sizeof(C) * tw.size(), cudaMemcpyHostToDevice));
+    std::vector<T> bsp(c->bsp_h.size());
+    for (size_t k = 0; k < bsp.size(); ++k) bsp[k] = (T)c->bsp_h[k];
+    NB_CUDA_OK(c, cudaMalloc(&c->d_bsp, sizeof(T) * bsp.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_bsp, bsp.data(), sizeof(T) * bsp.size(), cudaMemcpyHostToDevice));
+    // work lists
+    c->planes.clear();
+    c->cols.clear();
+    c->col_begin.assign(c->nrep + 1, 0);
+    size_t sf = 0, si = 0, sz = 0;
+    for (int r = 0; r < c->nrep; ++r) {
+        const RepDev &R = c->rd[r];
+        for (int z = 0; z < R.n3; ++z) c->planes.push_back(PlaneWork{r, z});
+        c->col_begin[r] = (int)c->cols.size();
+        for (int ky = 0; ky < R.n2; ++ky)
+            for (int kx0 = 0; kx0 < R.n1h; kx0 += NB_TK) c->cols.push_back(ColWork{r, ky, kx0});
+        sf = std::max(sf, plane_fwd_smem<T>(R.n1, R.n2));
+        si = std::max(si, plane_inv_smem<T>(R.n1, R.n2));
+        sz = std::max(sz, zconv_smem<T>(R.n3));
+    }
+    c->col_begin[c->nrep] = (int)c->cols.size();
+    int dev_smem = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    if ((int)sf > dev_smem || (int)si > dev_smem || (int)sz > dev_smem) return MOIL_NB_ERR_GRID;
+    c->smem_plane_fwd = sf;
+    c->smem_plane_inv = si;
+    c->smem_zconv = sz;
+    NB_CUDA_OK(c, cudaFuncSetAttribute(k_plane_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sf));
+    NB_CUDA_OK(c, cudaFuncSetAttribute(k_plane_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si));
+    NB_CUDA_OK(c, cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_planes, sizeof(PlaneWork) * c->planes.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_planes, c->planes.data(), sizeof(PlaneWork) * c->planes.size(), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_cols, sizeof(ColWork) * c->cols.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_cols, c->cols.data(), sizeof(ColWork) * c->cols.size(), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_col_begin, sizeof(int) * (c->nrep + 1)));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_col_begin, c->col_begin.data(), sizeof(int) * (c->nrep + 1), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_col, sizeof(double) * c->cols.size()));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_grid, sizeof(C) * c->grid_elems));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_fr, sizeof(typename vec4<T>::type) * c->nsite));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_part, sizeof(T) * 12 * c->nsite));
+    NB_CUDA_OK(c, cudaMemset(c->d_part, 0, sizeof(T) * 12 * c->nsite));
+    return MOIL_NB_OK;
+}
+
+}  // namespace
+
+void nb_launch_pme(NbCtx *c)
+{
+    if (c->precision == MOIL_NB_FP64) pme_t<double>(c);
+    else pme_t<float>(c);
+}
+
+int nb_pme_configure(NbCtx *c)
+{
+    return c->precision == MOIL_NB_FP64 ? configure_t<double>(c) : configure_t<float>(c);
+}

@@ -1,0 +1,457 @@
+// nb_realspace.cu -- real-space LJ + erfc-Coulomb, exclusion/1-4 corrections, finalize.
+//
+// Pair semantics are MOIL's predicate evaluated at the current coordinates:
+//   water-water   pot/watwat_ewald.f:131-612 (+ images, symm/symwat_ewald.f): the molecule
+//                 pair is in iff O-O r^2 <= max(cutvdw2, cutele2); then all 9 site pairs get
+//                 erfc-Coulomb with the O-O image shift and no per-site cutoff, O-O LJ if
+//                 r^2 <= cutvdw2.
+//   other pairs   pot/cdie_ewald.f:313-671 (+ symm/symcdie_ewald.f) with the lists of
+//                 pot/nbond.f:115-149: LJ iff r^2 < cutvdw2 (and not the geometric hydrogen
+//                 rule inside cutele2), Coulomb iff both charged and r^2 < max(cutvdw2, cutele2).
+//   primary vs image: a pair whose minimum-image shift is zero is a primary-box pair
+//                 (e_vdw/e_el); any other shift is one of MOIL's translated images
+//                 (e_vsym/e_lsym).
+// Lists are full (each pair appears under both atoms); every lane owns its own gradient,
+// so nothing is written twice and no atomics are needed.  Energies are halved at the end.
+#include "nb_internal.h"
+
+namespace {
+
+#define CHUNK 8
+
+template <typename T>
+__device__ __forceinline__ void lj_switch_apply(const RepDev &R, T r2, T &e1, T &df1)
+{
+    if (R.lj_switch && r2 > (T)R.ron2) {
+        T d = (T)R.rv2 - r2;
+        T sw = d * d * ((T)R.rv2 + (T)2 * r2 - (T)3 * (T)R.ron2) * (T)R.swden;
+        T dsw = (T)12 * d * ((T)R.ron2 - r2) * (T)R.swden;
+        df1 = df1 * sw + e1 * dsw;
+        e1 *= sw;
+    }
+}
+
+template <typename T> struct Consts;
+template <> struct Consts<float> {
+    __device__ static float qq(const RepDev &R, int k) { return R.qq[k]; }
+    __device__ static float w12(const RepDev &R) { return R.w12; }
+    __device__ static float w6(const RepDev &R) { return R.w6; }
+    __device__ static float alpha(const RepDev &R) { return R.alpha; }
+    __device__ static float epstmp(const RepDev &R) { return (float)R.epstmp; }
+};
+template <> struct Consts<double> {
+    __device__ static double qq(const RepDev &R, int k) { return R.qqd[k]; }
+    __device__ static double w12(const RepDev &R) { return R.w12d; }
+    __device__ static double w6(const RepDev &R) { return R.w6d; }
+    __device__ static double alpha(const RepDev &R) { return R.alphad; }
+    __device__ static double epstmp(const RepDev &R) { return R.epstmp; }
+};
+
+// one non-water-type pair (cdie_ewald list1/2/3 semantics); d already minimum-imaged
+template <typename T>
+__device__ __forceinline__ T atom_pair(const RepDev &R, T r2, T qi, T qj, T e12i, T e6i, T e12j, T e6j,
+                                       unsigned fi, unsigned fj, T &eel, T &elj)
+{
+    bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < (T)R.re2;
+    bool lj = r2 < (T)R.rv2 && !hr;
+    T qq = qi * qj;
+    bool el = r2 < (T)R.rmax2 && qq != (T)0;
+    if (!lj && !el) return (T)0;
+    T rinv = nb_rsqrt(r2);
+    T s2 = rinv * rinv;
+    T df = 0;
+    if (el) {
+        T x = Consts<T>::alpha(R) * r2 * rinv;
+        T ex;
+        T erfcv = nb_erfc_ex(x, r2 * (T)R.ex2c, &ex);
+        qq *= Consts<T>::epstmp(R);
+        T e = qq * erfcv * rinv;
+        df = -(e + qq * (T)R.c2a * ex) * s2;
+        eel += e;
+    }
+    if (lj) {
+        T s6 = s2 * s2 * s2, A, B;
+        if (!R.arith) {
+            A = e12i * e12j * s6 * s6;
+            B = e6i * e6j * s6;
+        } else {
+            T aa = e12i * e12j, sg = (T)0.5 * (e6i + e6j);
+            T b1 = sg * sg * sg;
+            b1 = b1 * b1;
+            B = aa * b1 * s6;
+            A = aa * b1 * b1 * s6 * s6;
+        }
+        T e1 = A - B;
+        T df1 = (T)-6 * s2 * (A + e1);
+        lj_switch_apply<T>(R, r2, e1, df1);
+        elj += e1;
+        df += df1;
+    }
+    return df;
+}
+
+template <typename T>
+__device__ __forceinline__ void min_image(const RepDev &R, T &dx, T &dy, T &dz, bool &img)
+{
+    T nx = nb_rint(dx * rep_invL<T>(R, 0)), ny = nb_rint(dy * rep_invL<T>(R, 1)), nz = nb_rint(dz * rep_invL<T>(R, 2));
+    dx = nb_shift(R, 0, dx, nx);
+    dy = nb_shift(R, 1, dy, ny);
+    dz = nb_shift(R, 2, dz, nz);
+    img = (nx != (T)0) | (ny != (T)0) | (nz != (T)0);
+}
+
+__device__ __forceinline__ void flush(float g[], long long G[], int n)
+{
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (k < n) { G[k] += nb_fix(g[k]); g[k] = 0.f; }
+    }
+}
+__device__ __forceinline__ void flush(double g[], long long G[], int n)
+{
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (k < n) { G[k] += nb_fix(g[k]); g[k] = 0.0; }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// water molecule per thread: W1 (water-water, 9 site pairs) then W2 (water-site x other)
+template <typename T>
+__global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                                               const void *pos_v, const void *woff_v, const void *lj_v,
+                                               const unsigned *__restrict__ sflags,
+                                               const int *__restrict__ wl1_off, const int *__restrict__ wl1,
+                                               const int *__restrict__ wl2_off, const int *__restrict__ wl2,
+                                               long long *__restrict__ grad, double *__restrict__ e_unit)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nW) return;
+    typedef typename vec4<T>::type T4;
+    typedef typename cplx<T>::type T2;
+    const T4 *pos = (const T4 *)pos_v;
+    const T4 *woff = (const T4 *)woff_v;
+    const RepDev &R = reps[site_rep[3 * i]];
+    T4 si[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    // i-site offsets from O (a = 0 is O itself)
+    const T4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
+    const T oi[3][3] = {{(T)0, (T)0, (T)0}, {oi1.x, oi1.y, oi1.z}, {oi2.x, oi2.y, oi2.z}};
+    T g[9];
+    long long G[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { g[k] = 0; G[k] = 0; }
+    double elp = 0, eli = 0, eep = 0, eei = 0;
+    const T iL0 = rep_invL<T>(R, 0), iL1 = rep_invL<T>(R, 1), iL2 = rep_invL<T>(R, 2);
+    const T rmax2 = (T)R.rmax2, rv2 = (T)R.rv2, alpha = Consts<T>::alpha(R), ex2c = (T)R.ex2c, c2a = (T)R.c2a;
+    const T qOO = Consts<T>::qq(R, 0), qOH = Consts<T>::qq(R, 1), qHH = Consts<T>::qq(R, 2);
+    const T w12 = Consts<T>::w12(R), w6 = Consts<T>::w6(R);
+    int k0 = wl1_off[i], k1 = wl1_off[i + 1], cnt = 0;
+    for (int k = k0; k < k1; ++k) {
+        int j = wl1[k];
+        T4 oj = pos[3 * j];
+        T dx = si[0].x - oj.x, dy = si[0].y - oj.y, dz = si[0].z - oj.z;
+        T nx = nb_rint(dx * iL0), ny = nb_rint(dy * iL1), nz = nb_rint(dz * iL2);
+        dx = nb_shift(R, 0, dx, nx);
+        dy = nb_shift(R, 1, dy, ny);
+        dz = nb_shift(R, 2, dz, nz);
+        T r2oo = dx * dx + dy * dy + dz * dz;
+        if (r2oo <= rmax2) {
+            T4 oj1 = woff[2 * j], oj2 = woff[2 * j + 1];
+            // q[b] = (O_i - O_j - nL) - offset_j[b]; site displacement = offset_i[a] + q[b]
+            const T q[3][3] = {{dx, dy, dz}, {dx - oj1.x, dy - oj1.y, dz - oj1.z}, {dx - oj2.x, dy - oj2.y, dz - oj2.z}};
+            T e_el = 0, e_lj = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    T ddx = a ? oi[a][0] + q[b][0] : q[b][0];
+                    T ddy = a ? oi[a][1] + q[b][1] : q[b][1];
+                    T ddz = a ? oi[a][2] + q[b][2] : q[b][2];
+                    T rr2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                    T rinv = nb_rsqrt(rr2);
+                    T s2 = rinv * rinv;
+                    T x = alpha * rr2 * rinv;
+                    T ex;
+                    T erfcv = nb_erfc_ex(x, rr2 * ex2c, &ex);
+                    const T qq = (a == 0 && b == 0) ? qOO : ((a == 0 || b == 0) ? qOH : qHH);
+                    T e = qq * erfcv * rinv;
+                    T df = -(e + qq * c2a * ex) * s2;
+                    if (a == 0 && b == 0) {
+                        if (rr2 <= rv2) {
+                            T s6 = s2 * s2 * s2, A = w12 * s6 * s6, B = w6 * s6;
+                            T e1 = A - B, df1 = (T)-6 * s2 * (A + e1);
+                            lj_switch_apply<T>(R, rr2, e1, df1);
+                            e_lj += e1;
+                            df += df1;
+                        }
+                    }
+                    e_el += e;
+                    g[3 * a] += df * ddx;
+                    g[3 * a + 1] += df * ddy;
+                    g[3 * a + 2] += df * ddz;
+                }
+            }
+            bool img = (nx != (T)0) | (ny != (T)0) | (nz != (T)0);
+            if (img) { eei += (double)e_el; eli += (double)e_lj; }
+            else { eep += (double)e_el; elp += (double)e_lj; }
+        }
+        if (++cnt == CHUNK) { flush(g, G, 9); cnt = 0; }
+    }
+    flush(g, G, 9);
+    // water sites against non-water atoms: atom semantics per site pair
+    {
+        const T2 *lj = (const T2 *)lj_v;
+        T2 lji[3] = {lj[3 * i], lj[3 * i + 1], lj[3 * i + 2]};
+        unsigned fi[3] = {sflags[3 * i], sflags[3 * i + 1], sflags[3 * i + 2]};
+        int q0 = wl2_off[i], q1 = wl2_off[i + 1];
+        cnt = 0;
+        for (int k = q0; k < q1; ++k) {
+            int s = wl2[k];
+            T4 xj = pos[s];
+            T2 ljj = lj[s];
+            unsigned fj = sflags[s];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                T dx = si[a].x - xj.x, dy = si[a].y - xj.y, dz = si[a].z - xj.z;
+                bool img;
+                min_image<T>(R, dx, dy, dz, img);
+                T r2 = dx * dx + dy * dy + dz * dz;
+                T eel = 0, elj = 0;
+                T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj);
+                g[3 * a] += df * dx;
+                g[3 * a + 1] += df * dy;
+                g[3 * a + 2] += df * dz;
+                if (img) { eei += (double)eel; eli += (double)elj; }
+                else { eep += (double)eel; elp += (double)elj; }
+            }
+            if (++cnt == CHUNK) { flush(g, G, 9); cnt = 0; }
+        }
+        flush(g, G, 9);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = G[k];
+    double *eu = e_unit + 4 * (size_t)i;
+    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei;
+}
+
+// non-water atom per thread over its full site list
+template <typename T>
+__global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                                              const void *pos_v, const void *lj_v, const unsigned *__restrict__ sflags,
+                                              const int *__restrict__ xl_off, const int *__restrict__ xl,
+                                              long long *__restrict__ grad, double *__restrict__ e_unit)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nA) return;
+    typedef typename vec4<T>::type T4;
+    typedef typename cplx<T>::type T2;
+    const T4 *pos = (const T4 *)pos_v;
+    const T2 *lj = (const T2 *)lj_v;
+    int si = 3 * nW + k;
+    const RepDev &R = reps[site_rep[si]];
+    T4 xi = pos[si];
+    T2 lji = lj[si];
+    unsigned fi = sflags[si];
+    T g[3] = {0, 0, 0};
+    long long G[3] = {0, 0, 0};
+    double elp = 0, eli = 0, eep = 0, eei = 0;
+    int cnt = 0;
+    for (int q = xl_off[k]; q < xl_off[k + 1]; ++q) {
+        int s = xl[q];
+        T4 xj = pos[s];
+        T2 ljj = lj[s];
+        T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        bool img;
+        min_image<T>(R, dx, dy, dz, img);
+        T r2 = dx * dx + dy * dy + dz * dz;
+        T eel = 0, elj = 0;
+        T df = atom_pair<T>(R, r2, xi.w, xj.w, lji.x, lji.y, ljj.x, ljj.y, fi, sflags[s], eel, elj);
+        g[0] += df * dx; g[1] += df * dy; g[2] += df * dz;
+        if (img) { eei += (double)eel; eli += (double)elj; }
+        else { eep += (double)eel; elp += (double)elj; }
+        if (++cnt == CHUNK) { flush(g, G, 3); cnt = 0; }
+    }
+    flush(g, G, 3);
+    grad[(size_t)3 * si] = G[0];
+    grad[(size_t)3 * si + 1] = G[1];
+    grad[(size_t)3 * si + 2] = G[2];
+    double *eu = e_unit + 4 * (size_t)(nW + k);
+    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei;
+}
+
+// ---------------------------------------------------------------------------------
+// exclusion erf corrections (cdie_ewald.f:117-199) and 1-4 terms (ener14.f:38-95), FP64,
+// gathered per atom over both directions; raw (unimaged) displacements as MOIL uses.
+__global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
+                         const double *__restrict__ coor, const double *__restrict__ q, const int *__restrict__ ex_off,
+                         const int *__restrict__ ex_j, const int *__restrict__ p_off, const int *__restrict__ p_j,
+                         const double *__restrict__ p_par, double *__restrict__ grad, double *__restrict__ e_out)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natom) return;
+    const RepDev &R = reps[atom_rep[a]];
+    double xa = coor[3 * (size_t)a], ya = coor[3 * (size_t)a + 1], za = coor[3 * (size_t)a + 2];
+    double gx = 0, gy = 0, gz = 0, ecorr = 0, eel14 = 0, evdw14 = 0;
+    double qa = q[a] * R.epstmp, al = R.alphad;
+    for (int k = ex_off[a]; k < ex_off[a + 1]; ++k) {
+        int b = ex_j[k];
+        double rx = xa - coor[3 * (size_t)b], ry = ya - coor[3 * (size_t)b + 1], rz = za - coor[3 * (size_t)b + 2];
+        double r2 = rx * rx + ry * ry + rz * rz, s2 = 1.0 / r2, rij = sqrt(r2), s = 1.0 / rij;
+        double qq = qa * q[b], x = al * rij;
+        double erfv = erf(x), derfc = NB_TWO_OVER_SQRTPI * exp(-x * x);
+        double e2 = -qq * s * erfv;
+        double df = qq * s * (s2 * erfv - s * al * derfc);
+        gx += df * rx; gy += df * ry; gz += df * rz;
+        ecorr += 0.5 * e2;
+    }
+    for (int k = p_off[a]; k < p_off[a + 1]; ++k) {
+        int b = p_j[k];
+        const double *p = p_par + 3 * (size_t)k;
+        double rx = xa - coor[3 * (size_t)b], ry = ya - coor[3 * (size_t)b + 1], rz = za - coor[3 * (size_t)b + 2];
+        double r2 = rx * rx + ry * ry + rz * rz, s2 = 1.0 / r2, e1 = 0, df1 = 0, e2 = 0, df2 = 0;
+        if (p[0] > 1e-12) {
+            double s6 = s2 * s2 * s2, A = p[0] * s6 * s6, B = p[1] * s6;
+            e1 = A - B;
+            df1 = -6.0 * s2 * (A + e1);
+        }
+        if (fabs(p[2]) > 1e-12) {
+            double s = sqrt(s2);
+            e2 = p[2] * s;
+            df2 = -e2 * s2;
+        }
+        double df = df1 + df2;
+        gx += df * rx; gy += df * ry; gz += df * rz;
+        evdw14 += 0.5 * e1;
+        eel14 += 0.5 * e2;
+    }
+    grad[3 * (size_t)a] = gx; grad[3 * (size_t)a + 1] = gy; grad[3 * (size_t)a + 2] = gz;
+    e_out[3 * (size_t)a] = ecorr; e_out[3 * (size_t)a + 1] = eel14; e_out[3 * (size_t)a + 2] = evdw14;
+}
+
+// ---------------------------------------------------------------------------------
+// gradient assembly in MOIL order: fixed-point real space + FP64 corrections + PME
+template <typename T>
+__global__ void k_final_grad(int natom, const int *__restrict__ site_of, const int *__restrict__ atom_rep,
+                             const RepDev *__restrict__ reps, const long long *__restrict__ grad_site,
+                             const double *__restrict__ grad_ex, const T *__restrict__ part,
+                             const double *__restrict__ q, double *__restrict__ dpot, int *st)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natom) return;
+    const RepDev &R = reps[atom_rep[a]];
+    int s = site_of[a];
+    double pg[3] = {0, 0, 0};
+    const T *p = part + 12 * (size_t)s;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        pg[0] += (double)p[3 * t];
+        pg[1] += (double)p[3 * t + 1];
+        pg[2] += (double)p[3 * t + 2];
+    }
+    double qf = q[a] * R.fcd;
+    double sc[3] = {qf * R.n1 * R.invLd[0], qf * R.n2 * R.invLd[1], qf * R.n3 * R.invLd[2]};
+    bool bad = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double v = (double)grad_site[3 * (size_t)s + d] * NB_FIX_INV + grad_ex[3 * (size_t)a + d] + sc[d] * pg[d];
+        bad |= !(v == v);
+        dpot[3 * (size_t)a + d] = v;
+    }
+    if (bad) atomicOr(&st[1], NB_DEV_ERR_NAN);
+}
+
+// per-replica energies: fixed-order block reductions (deterministic)
+__device__ double block_sum(double v, double *sh)
+{
+    int t = threadIdx.x;
+    sh[t] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (t < o) sh[t] += sh[t + o];
+        __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_final_energy(int nW, const RepDev *__restrict__ reps, const double *__restrict__ e_unit,
+                               const double *__restrict__ e_ex, const double *__restrict__ e_col,
+                               const int *__restrict__ col_begin, double *__restrict__ e_rep)
+{
+    __shared__ double sh[256];
+    int r = blockIdx.x;
+    const RepDev &R = reps[r];
+    double acc[4] = {0, 0, 0, 0}, ex[3] = {0, 0, 0}, ec = 0;
+    for (int u = R.wat0 + threadIdx.x; u < R.wat0 + R.nwat; u += blockDim.x)
+        for (int k = 0; k < 4; ++k) acc[k] += e_unit[4 * (size_t)u + k];
+    for (int u = nW + R.oth0 + threadIdx.x; u < nW + R.oth0 + R.noth; u += blockDim.x)
+        for (int k = 0; k < 4; ++k) acc[k] += e_unit[4 * (size_t)u + k];
+    for (int a = R.atom0 + threadIdx.x; a < R.atom0 + R.natom; a += blockDim.x)
+        for (int k = 0; k < 3; ++k) ex[k] += e_ex[3 * (size_t)a + k];
+    for (int w = col_begin[r] + threadIdx.x; w < col_begin[r + 1]; w += blockDim.x) ec += e_col[w];
+    double elp = 0.5 * block_sum(acc[0], sh), eli = 0.5 * block_sum(acc[1], sh);
+    double eep = 0.5 * block_sum(acc[2], sh), eei = 0.5 * block_sum(acc[3], sh);
+    double ecorr = block_sum(ex[0], sh), eel14 = block_sum(ex[1], sh), evdw14 = block_sum(ex[2], sh);
+    double erec = 0.5 * block_sum(ec, sh);
+    if (threadIdx.x == 0) {
+        double *o = e_rep + 16 * (size_t)r;
+        o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym
+        o[4] = eel14; o[5] = evdw14; o[6] = ecorr; o[7] = R.e_self; o[8] = erec;
+        o[9] = elp + eep + eli + eei + eel14 + evdw14 + ecorr + R.e_self + erec;
+        o[10] = eep + eei;
+    }
+}
+
+template <typename T>
+void realspace_t(NbCtx *c)
+{
+    cudaStream_t s = c->stream;
+    if (c->timing) cudaEventRecord(c->ev[2], s);
+    if (c->nW > 0) {
+        k_water<T><<<(int)((c->nW + 127) / 128), 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos,
+                                                              c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_off, c->d_wl1,
+                                                              c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
+        c->launches++;
+    }
+    if (c->timing) cudaEventRecord(c->ev[3], s);
+    if (c->nA > 0) {
+        k_atom<T><<<(int)((c->nA + 127) / 128), 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep,
+                                                             c->d_pos, c->d_site_lj, c->d_site_flags, c->d_xl_off,
+                                                             c->d_xl, c->d_grad_site, c->d_e_unit);
+        c->launches++;
+    }
+    if (c->timing) cudaEventRecord(c->ev[4], s);
+}
+
+}  // namespace
+
+void nb_launch_realspace(NbCtx *c)
+{
+    if (c->precision == MOIL_NB_FP64) realspace_t<double>(c);
+    else realspace_t<float>(c);
+}
+
+void nb_launch_excl14(NbCtx *c, const double *d_coor)
+{
+    k_excl14<<<(int)((c->natom + 127) / 128), 128, 0, c->stream>>>(
+        (int)c->natom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_ex_off, c->d_ex_j, c->d_p14_off, c->d_p14_j,
+        c->d_p14_par, c->d_grad_ex, c->d_e_ex);
+    c->launches++;
+}
+
+void nb_launch_finalize(NbCtx *c, double *d_dpot)
+{
+    cudaStream_t s = c->stream;
+    if (c->precision == MOIL_NB_FP64)
+        k_final_grad<double><<<(int)((c->natom + 255) / 256), 256, 0, s>>>(
+            (int)c->natom, c->d_site_of, c->d_atom_rep, c->d_reps, c->d_grad_site, c->d_grad_ex,
+            (const double *)c->d_part, c->d_q, d_dpot, c->d_status);
+    else
+        k_final_grad<float><<<(int)((c->natom + 255) / 256), 256, 0, s>>>(
+            (int)c->natom, c->d_site_of, c->d_atom_rep, c->d_reps, c->d_grad_site, c->d_grad_ex,
+            (const float *)c->d_part, c->d_q, d_dpot, c->d_status);
+    k_final_energy<<<c->nrep, 256, 0, s>>>((int)c->nW, c->d_reps, c->d_e_unit, c->d_e_ex, c->d_e_col, c->d_col_begin,
+                                           c->d_e_rep);
+    c->launches += 2;
+}

@@ -1,0 +1,270 @@
+"""Python front end of the GPU library, mirroring MOIL's energy-routine interface.
+
+MOIL's callers do ``call ewald_init()`` once, ``call squeeze(); call nbondm();
+call syminit()`` when lists are due, then ``call eforce()`` which fills
+``dpot`` and the ``/ENERGY/`` scalars (pot/energy.f:410-436,
+dynamics/dyna.f:130-144).  :class:`Nonbonded` offers the same steps over the
+C ABI of ``include/moil_nb.h``:
+
+    nb = Nonbonded(system)            # ewald_init()
+    nb.nblist()                        # nbondm() + syminit() at the next call
+    dpot, e = nb.eforce(coor)          # nonbonded block of eforce()
+
+There is no CPU fallback: if the CUDA library cannot be loaded or no GPU is
+visible, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+MOIL_NB_MIXED, MOIL_NB_FP64 = 0, 1
+ENERGY_KEYS = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_el14", "e_vdw14", "e_corr", "e_self",
+               "e_ew_receip", "e_total", "e_dir")
+
+EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_last_error", "moil_nb_init",
+            "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device",
+            "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
+            "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
+            "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("rvmx", ctypes.c_double), ("relx", ctypes.c_double), ("eps", ctypes.c_double),
+                ("a", ctypes.c_double), ("b", ctypes.c_double), ("c", ctypes.c_double),
+                ("dtol", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("nfft1", ctypes.c_int), ("nfft2", ctypes.c_int), ("nfft3", ctypes.c_int), ("order", ctypes.c_int),
+                ("arith", ctypes.c_int), ("hvdw0", ctypes.c_int), ("lj_switch", ctypes.c_int),
+                ("r_on", ctypes.c_double), ("skin", ctypes.c_double), ("list_period", ctypes.c_int),
+                ("precision", ctypes.c_int)]
+
+
+class Topology(ctypes.Structure):
+    _fields_ = [("npt", ctypes.c_int), ("ptchg", _dp), ("epsgm6", _dp), ("epsgm12", _dp),
+                ("exc1", _ip), ("exc2", _ip), ("totspe", ctypes.c_int), ("spec1", _ip), ("spec2", _ip),
+                ("p14", _dp), ("totmon", ctypes.c_int), ("poipt", _ip), ("montype", _ip)]
+
+
+class Energies(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ENERGY_KEYS]
+
+
+class Replica(ctypes.Structure):
+    _fields_ = [("params", ctypes.POINTER(Params)), ("topo", ctypes.POINTER(Topology))]
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_float) for k in ("prepare_ms", "list_ms", "water_ms", "atom_ms", "excl_ms",
+                                               "pme_spread_fft_ms", "pme_conv_ms", "pme_gather_ms",
+                                               "finalize_ms", "total_ms")] + [
+        ("list_rebuilt", ctypes.c_int), ("launches", ctypes.c_int)]
+
+
+class MoilNbError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"moil_nb status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load ``libmoil_nb.so`` (building it with nvcc when missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build_if_missing else _build.LIB
+    if not os.path.exists(path):
+        raise MoilNbError(-1, f"CUDA library not built: {path}")
+    L = ctypes.CDLL(path)
+    L.moil_nb_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
+    L.moil_nb_destroy.argtypes = [ctypes.c_void_p]
+    L.moil_nb_destroy.restype = None
+    L.moil_nb_strerror.restype = ctypes.c_char_p
+    L.moil_nb_strerror.argtypes = [ctypes.c_int]
+    L.moil_nb_last_error.restype = ctypes.c_char_p
+    L.moil_nb_last_error.argtypes = [ctypes.c_void_p]
+    L.moil_nb_init.argtypes = [ctypes.c_void_p, ctypes.POINTER(Params), ctypes.POINTER(Topology)]
+    L.moil_nb_init_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Replica)]
+    L.moil_nb_get_alpha.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+    L.moil_nb_eval.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(Energies)]
+    L.moil_nb_eval_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Energies)]
+    L.moil_nb_request_rebuild.argtypes = [ctypes.c_void_p]
+    L.moil_nb_squeeze.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Topology), _dp]
+    L.moil_nb_natoms.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+    L.moil_nb_stream.restype = ctypes.c_void_p
+    L.moil_nb_stream.argtypes = [ctypes.c_void_p]
+    L.moil_nb_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.moil_nb_get_timing.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timing)]
+    L.moil_nb_pair_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                     ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.moil_nb_set_graph.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    _lib = L
+    return L
+
+
+def _check(L, h, rc):
+    if rc != 0:
+        detail = L.moil_nb_last_error(h).decode() if h else ""
+        raise MoilNbError(rc, f"{L.moil_nb_strerror(rc).decode()} {detail}".strip())
+
+
+class _Keep:
+    def __init__(self):
+        self.refs = []
+
+    def d(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self.refs.append(a)
+        return a.ctypes.data_as(_dp)
+
+    def i(self, a):
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        if a.size == 0:
+            a = np.zeros(1, dtype=np.int32)
+        self.refs.append(a)
+        return a.ctypes.data_as(_ip)
+
+
+def make_params(s, precision=MOIL_NB_MIXED, skin=1.0, list_period=0, lj_switch=False, alpha=None) -> Params:
+    p = Params()
+    p.rvmx, p.relx, p.eps = float(s.rvmx), float(s.relx), float(s.eps)
+    p.a, p.b, p.c = (float(x) for x in s.box)
+    p.dtol = 0.0
+    p.alpha = float(s.alpha if alpha is None else alpha)
+    p.nfft1, p.nfft2, p.nfft3 = (int(x) for x in s.nfft)
+    p.order = int(s.order)
+    p.arith, p.hvdw0 = int(s.arith), int(s.hvdw0)
+    p.lj_switch = int(lj_switch)
+    p.r_on = float(s.r_on)
+    p.skin = float(skin)
+    p.list_period = int(list_period)
+    p.precision = int(precision)
+    return p
+
+
+def make_topology(s, keep: _Keep) -> Topology:
+    t = Topology()
+    t.npt = s.npt
+    t.ptchg, t.epsgm6, t.epsgm12 = keep.d(s.ptchg), keep.d(s.epsgm6), keep.d(s.epsgm12)
+    t.exc1, t.exc2 = keep.i(s.exc1), keep.i(s.exc2)
+    t.totspe = len(s.spec1)
+    t.spec1, t.spec2 = keep.i(s.spec1), keep.i(s.spec2)
+    t.p14 = keep.d(s.p14 if len(s.p14) else np.zeros(3))
+    t.totmon = s.totmon
+    t.poipt, t.montype = keep.i(s.poipt), keep.i(s.montype)
+    return t
+
+
+class Nonbonded:
+    """One device handle over one system or a batch of independent replicas."""
+
+    def __init__(self, systems, precision=MOIL_NB_MIXED, device=0, skin=1.0, list_period=0,
+                 lj_switch=False, timing=False):
+        self.L = load()
+        h = ctypes.c_void_p()
+        _check(self.L, None, self.L.moil_nb_create(ctypes.byref(h), int(device)))
+        self.h = h
+        self.batch = isinstance(systems, (list, tuple))
+        self.systems = list(systems) if self.batch else [systems]
+        keep = _Keep()
+        self._params = [make_params(s, precision, skin, list_period, lj_switch) for s in self.systems]
+        self._topos = [make_topology(s, keep) for s in self.systems]
+        reps = (Replica * len(self.systems))()
+        for k in range(len(self.systems)):
+            reps[k].params = ctypes.pointer(self._params[k])
+            reps[k].topo = ctypes.pointer(self._topos[k])
+        _check(self.L, self.h, self.L.moil_nb_init_batch(self.h, len(self.systems), reps))
+        del keep
+        self.natom = sum(s.npt for s in self.systems)
+        self.offsets = np.cumsum([0] + [s.npt for s in self.systems])
+        self._e = (Energies * len(self.systems))()
+        if timing:
+            self.set_timing(True)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.moil_nb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def alpha(self, r=0) -> float:
+        a = ctypes.c_double()
+        _check(self.L, self.h, self.L.moil_nb_get_alpha(self.h, int(r), ctypes.byref(a)))
+        return a.value
+
+    def nblist(self):
+        """MOIL's nbondm() + syminit(): rebuild the lists at the next evaluation."""
+        _check(self.L, self.h, self.L.moil_nb_request_rebuild(self.h))
+
+    def eforce_into(self, coor: np.ndarray, dpot: np.ndarray):
+        """Evaluate into caller-owned (natom,3) float64 arrays; returns per-replica energies."""
+        assert coor.dtype == np.float64 and coor.flags.c_contiguous and coor.size == 3 * self.natom
+        assert dpot.dtype == np.float64 and dpot.flags.c_contiguous and dpot.size == 3 * self.natom
+        _check(self.L, self.h, self.L.moil_nb_eval(self.h, coor.ctypes.data_as(_dp), dpot.ctypes.data_as(_dp),
+                                                   self._e))
+        return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+
+    def eforce(self, coor=None):
+        """Nonbonded dpot (dE/dx, kcal/mol/Å) and energies.  Single system: (dpot, dict);
+        batch: (list of dpot, list of dict)."""
+        if coor is None:
+            coor = np.concatenate([s.coor for s in self.systems], axis=0)
+        elif self.batch and isinstance(coor, (list, tuple)):
+            coor = np.concatenate(coor, axis=0)
+        coor = np.ascontiguousarray(coor, dtype=np.float64).reshape(self.natom, 3)
+        dpot = np.empty_like(coor)
+        e = self.eforce_into(coor, dpot)
+        if not self.batch:
+            return dpot, e[0]
+        return [dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))], e
+
+    def eforce_device(self, d_coor_ptr: int, d_dpot_ptr: int):
+        """Evaluate on device-resident buffers (raw CUDA pointers)."""
+        _check(self.L, self.h, self.L.moil_nb_eval_device(self.h, ctypes.c_void_p(d_coor_ptr),
+                                                          ctypes.c_void_p(d_dpot_ptr), self._e))
+        return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+
+    def set_timing(self, on=True):
+        _check(self.L, self.h, self.L.moil_nb_set_timing(self.h, int(on)))
+
+    def timing(self) -> dict:
+        t = Timing()
+        _check(self.L, self.h, self.L.moil_nb_get_timing(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Timing._fields_}
+
+    def pair_stats(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(self.L, self.h, self.L.moil_nb_pair_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"list_entries": a.value, "water_list": b.value, "atom_list": c.value}
+
+    def stream(self) -> int:
+        return self.L.moil_nb_stream(self.h) or 0
+
+
+def squeeze(s, coor: np.ndarray) -> np.ndarray:
+    """MOIL's squeeze() on a copy of coor (symm/squeeze.f:66-145) through the C ABI."""
+    L = load()
+    keep = _Keep()
+    p = make_params(s)
+    t = make_topology(s, keep)
+    out = np.ascontiguousarray(coor, dtype=np.float64).copy()
+    _check(L, None, L.moil_nb_squeeze(ctypes.byref(p), ctypes.byref(t), out.ctypes.data_as(_dp)))
+    return out
