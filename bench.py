@@ -1,0 +1,342 @@
+"""Benchmark: atom-evaluations/s of MOIL's nonbonded energy/force path on one GB300.
+
+Workload (default): 512 independent periodic TIP3P boxes of uneven size (atom counts
+log-uniform in [1500, 12000], whole molecules, 0.997 g/cm^3, rc 9 Å, alpha 0.35,
+PME grid the smallest 2/3/5-smooth n >= 1 point/Å, order 4) evaluated together in one
+batched, mixed-precision pass -- the path-image / milestoning-swarm shape.  A step is
+one full nonbonded evaluation of every replica (real space + exclusion corrections +
+PME + self), with the pair lists rebuilt every 10 steps as MOIL's '#lis 10' does.
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference] [--gpus N]
+
+value      : atom-evals/s, coordinates and gradients resident in device memory
+e2e        : the same through moil_nb_eval with pinned host buffers (copies timed)
+roofline   : the dominant kernel against the FP32 pipe (pair math is FP32-bound)
+cpu_baseline: the oracle (a C restatement of MOIL's FP64 routines, MOIL's own list path
+             and erfc table) on a bounded sample of replicas, one host thread
+plain_fp64 : the plain FP64 GPU path, one replica per launch, on a sample of replicas
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-evals/s mixed+batched vs plain FP64 on 1 GB300 at ≤1e-5 rel RMS force err"
+F_PAIR = 50            # FP32 operations per in-cutoff site pair (FMA = 2, MUFU = 1)
+LIST_PERIOD = 10
+SKIN = 1.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def fp32_peak_tflops(sm_mhz):
+    """FP32 FMA peak of a 152-SM GB300 (128 FP32 lanes/SM, 2 flops per FMA) at sm_mhz."""
+    return 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+        sm = []
+        mx = 0.0
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = max(mx, float(r[1]))
+                for k, nm in enumerate(names):
+                    if r[4 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(rank=0):
+    from moil_fnrfd_gb300 import systems
+    reps = systems.config3(512, seed=3000 + 7919 * rank)
+    return reps
+
+
+def cpu_baseline(reps, budget_s=12.0):
+    """The oracle, MOIL's list path + erfc table, one host thread, lists every 10 evals."""
+    from oracle import oracle
+    done_atoms = 0
+    t0 = time.perf_counter()
+    n = 0
+    for s in reps:
+        oracle.eforce_batch([s], mode="moil", nthreads=1, nevals=LIST_PERIOD, list_period=LIST_PERIOD)
+        done_atoms += s.npt * LIST_PERIOD
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done_atoms / dt, "unit": "atom-evals/s", "cores": 1, "kind": "port",
+            "sample": f"{n} of {len(reps)} replicas x {LIST_PERIOD} evaluations (lists rebuilt once), "
+                      f"oracle in MOIL list-path mode (13 image translations, erfc spline table, +2 Å buffers), "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    """Reference arm: MOIL's algorithm (the oracle restatement; MOIL's Fortran cannot be
+    built here) on all host cores, same workload, metric and units."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle
+    reps = build_workload()
+    threads = os.cpu_count() or 1
+    sample = reps[:max(threads, 1) * 2]
+    atoms = sum(s.npt for s in sample) * LIST_PERIOD
+    times = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle.eforce_batch(sample, mode="moil", nthreads=threads, nevals=LIST_PERIOD, list_period=LIST_PERIOD)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+    value = atoms * len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "512 batched uneven TIP3P boxes (1500-12000 atoms each), rc 9, alpha 0.35",
+                       "sample_per_step": f"{len(sample)} replicas x {LIST_PERIOD} evaluations"},
+            "cpu_baseline": {"value": value, "unit": "atom-evals/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} of {len(reps)} replicas x {LIST_PERIOD} evaluations per step, "
+                                       "OpenMP over replicas, oracle in MOIL list-path mode"},
+            "e2e": {"value": value, "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from moil_fnrfd_gb300.nb import MOIL_NB_FP64, MOIL_NB_MIXED, Nonbonded
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+
+    t0 = time.perf_counter()
+    reps = build_workload(rank)
+    natoms = sum(s.npt for s in reps)
+    log(f"workload: {len(reps)} replicas, {natoms} atoms, generated in {time.perf_counter() - t0:.1f} s")
+    nb = Nonbonded(reps, precision=MOIL_NB_MIXED, device=local, skin=SKIN, list_period=LIST_PERIOD)
+    stream = torch.cuda.ExternalStream(nb.stream())
+    coor = np.ascontiguousarray(np.concatenate([s.coor for s in reps]), dtype=np.float64)
+    d_coor = torch.from_numpy(coor).to(f"cuda:{local}")
+    d_dpot = torch.empty_like(d_coor)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step_device():
+        nb.eforce_device(d_coor.data_ptr(), d_dpot.data_ptr(), want_energies=False)
+
+    for _ in range(args.warmup):
+        step_device()
+    # per-stage times (library events on its own stream), outside the timed region
+    nb.set_timing(True)
+    stages = []
+    for _ in range(LIST_PERIOD):
+        step_device()
+        stages.append(nb.timing())
+    nb.set_timing(False)
+    site_pairs = nb.pair_stats()["site_pairs"]
+    launches = int(statistics.median(t["launches"] for t in stages))
+
+    # timed region: device-resident inputs, L2 flushed between steps (not timed)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+        step_device()
+        b.record(stream)
+        ev.append((a, b))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s])
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t[0])
+    value = natoms * args.steps * world / total_s
+
+    # e2e through the public host-buffer call: H2D + evaluation + D2H every step
+    h_coor = torch.from_numpy(coor).pin_memory()
+    h_dpot = torch.empty_like(h_coor).pin_memory()
+    hc, hd = h_coor.numpy(), h_dpot.numpy()
+    for _ in range(3):
+        nb.eforce_into(hc, hd, want_energies=False)
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        nb.eforce_into(hc, hd, want_energies=False)
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    e2e_value = natoms * args.steps * world / (sum(e2e_ms) / 1e3)
+
+    # dominant kernel and its roofline (FP32 pipe): average over steps without a rebuild
+    no_build = [t for t in stages if not t["list_rebuilt"]] or stages
+    keys = ["water_ms", "atom_ms", "excl_ms", "pme_spread_fft_ms", "pme_conv_ms", "pme_gather_ms", "finalize_ms"]
+    avg = {k: statistics.mean(t[k] for t in no_build) for k in keys}
+    avg["list_ms"] = statistics.mean(t["list_ms"] for t in stages)
+    dom = max(keys, key=lambda k: avg[k])
+    sm_mhz = clk["sm_mhz"] or peaks().get("sm_max_mhz", 2070.0)
+    peak_fp32 = fp32_peak_tflops(peaks().get("sm_max_mhz", 2070.0))
+    roof = None
+    if dom in ("water_ms", "atom_ms"):
+        achieved = site_pairs * F_PAIR / (avg["water_ms"] + avg["atom_ms"]) / 1e9   # TFLOP/s
+        roof = {"kernel": "k_water+k_atom (real space)", "bound": "fp32", "achieved": achieved,
+                "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
+                "peak_source": "nominal FP32 FMA peak at the measured max SM clock (152 SMs x 128 lanes x 2); "
+                               "MEASURED_PEAKS.json has no FP32 figure",
+                "work": f"{site_pairs} unique in-cutoff site pairs x {F_PAIR} FP32 ops per launch"}
+    else:
+        hbm = peaks().get("hbm_gbs", 6800.0)
+        ng = sum(s.nfft[0] * s.nfft[1] * s.nfft[2] for s in reps)
+        b = 56 * natoms + 64 * ng
+        t_pme = (avg["pme_spread_fft_ms"] + avg["pme_conv_ms"] + avg["pme_gather_ms"]) / 1e3
+        achieved = b / t_pme / 1e9
+        roof = {"kernel": "PME (bin+spread+FFT, convolution, gather)", "bound": "hbm", "achieved": achieved,
+                "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                "work": "56 N + 64 Ng bytes per evaluation"}
+
+    out = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "512 batched uneven TIP3P boxes (config 3 shape): 1500-12000 atoms each, "
+                                  "rc 9 Å, alpha 0.35, PME order 4 on 2/3/5-smooth grids >= 1 pt/Å",
+                      "replicas": len(reps), "atoms": natoms, "list_period": LIST_PERIOD, "skin": SKIN,
+                      "l2": "256 MB buffer written between timed steps (untimed)",
+                      "precision": "FP32 pair/spline/FFT math, int64 fixed-point forces, FP64 energies and corrections"},
+           "stage_ms": {k: round(v, 4) for k, v in avg.items()},
+           "site_pairs": site_pairs,
+           "roofline": roof,
+           "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": int(coor.nbytes),
+                   "d2h_bytes_per_step": int(coor.nbytes + 16 * 8 * len(reps))},
+           "clocks": clk, "gpu_launches": launches * args.steps}
+
+    # accuracy and the plain FP64 path on a sample of replicas (denominator of the 20x target)
+    if not args.no_fp64 and rank == 0:
+        sample = reps[:24]
+        d_mixed = d_dpot.cpu().numpy()
+        offs = np.cumsum([0] + [s.npt for s in reps])
+        errs, fp_ms, fp_atoms = [], 0.0, 0
+        for k, s in enumerate(sample):
+            p = Nonbonded(s, precision=MOIL_NB_FP64, device=local, skin=SKIN, list_period=LIST_PERIOD)
+            st = torch.cuda.ExternalStream(p.stream())
+            dc = torch.from_numpy(s.coor).to(f"cuda:{local}")
+            dd = torch.empty_like(dc)
+            for _ in range(2):
+                p.eforce_device(dc.data_ptr(), dd.data_ptr())
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            for _ in range(LIST_PERIOD):
+                p.eforce_device(dc.data_ptr(), dd.data_ptr())
+            b.record(st)
+            torch.cuda.synchronize()
+            fp_ms += a.elapsed_time(b)
+            fp_atoms += s.npt * LIST_PERIOD
+            ref = dd.cpu().numpy()
+            mine = d_mixed[offs[k]:offs[k + 1]]
+            errs.append(float(np.sqrt(((mine - ref) ** 2).sum() / (ref ** 2).sum())))
+            p.close()
+        fp64_value = fp_atoms / (fp_ms / 1e3)
+        out["plain_fp64"] = {"value": fp64_value, "unit": "atom-evals/s",
+                             "sample": f"{len(sample)} replicas, one per handle/launch sequence, "
+                                       f"{LIST_PERIOD} evaluations each (one list build)"}
+        out["speedup_vs_plain_fp64"] = value / fp64_value
+        out["force_err_vs_fp64"] = {"max_rel_rms": max(errs), "replicas": len(errs)}
+    nb.close()
+
+    if not args.no_cpu and rank == 0:
+        out["cpu_baseline"] = cpu_baseline(reps)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

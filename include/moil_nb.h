@@ -170,8 +170,9 @@ void *moil_nb_stream(const moil_nb_ctx *h);
 /* ---- instrumentation --------------------------------------------------- */
 int moil_nb_set_timing(moil_nb_ctx *h, int on);
 int moil_nb_get_timing(const moil_nb_ctx *h, moil_nb_timing *t);
-/* In-cutoff site pairs of the last list build (for roofline accounting). */
-int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *water_pairs, int64_t *atom_pairs);
+/* Pair-list entries of the last build and the unique site pairs inside the cutoff
+ * predicate in the last evaluation (the pairs MOIL's kernels evaluate). */
+int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *site_pairs);
 /* Capture the device part of an evaluation into a CUDA graph (1) or launch
  * kernel by kernel (0, default).  Graph replays are used when on. */
 int moil_nb_set_graph(moil_nb_ctx *h, int on);

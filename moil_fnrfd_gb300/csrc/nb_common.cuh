@@ -24,6 +24,7 @@
 #define NB_PLANE_SCALE 1099511627776.0  // 2^40: PME plane accumulation
 #define NB_MAX_FFT 128
 #define NB_TWO_OVER_SQRTPI 1.1283791670955126
+#define NB_EU 5                       // per-unit outputs: LJ prim, LJ img, Coul prim, Coul img, site pairs
 
 // per-replica constants (read by every kernel)
 struct RepDev {

@@ -416,7 +416,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl_off, sizeof(int) * (c->nA + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_count_tmp, sizeof(int) * (2 * std::max(c->nW, c->nA) + 2)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_grad_site, sizeof(long long) * 3 * ns));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_e_unit, sizeof(double) * 4 * std::max<int64_t>(nu, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_unit, sizeof(double) * NB_EU * std::max<int64_t>(nu, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_grad_ex, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMalloc(&c->d_e_ex, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMalloc(&c->d_zcount, sizeof(int) * (c->nzbin + 1)));
@@ -427,7 +427,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_coor, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMalloc(&c->d_dpot, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMemset(c->d_grad_site, 0, sizeof(long long) * 3 * ns));
-    NB_CUDA_OK(c, cudaMemset(c->d_e_unit, 0, sizeof(double) * 4 * std::max<int64_t>(nu, 1)));
+    NB_CUDA_OK(c, cudaMemset(c->d_e_unit, 0, sizeof(double) * NB_EU * std::max<int64_t>(nu, 1)));
     // list capacities from densities (grown on overflow)
     c->cap_wl1 = c->cap_wl2 = c->cap_xl = 64;
     for (int r = 0; r < nrep; ++r) {
@@ -530,6 +530,11 @@ int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
             E.e_el14 = o[4]; E.e_vdw14 = o[5]; E.e_corr = o[6]; E.e_self = o[7];
             E.e_ew_receip = o[8]; E.e_total = o[9]; E.e_dir = o[10];
         }
+    }
+    {
+        double np = 0;
+        for (int r = 0; r < c->nrep; ++r) np += c->h_e_rep[16 * r + 11];
+        c->last_site_pairs = (int64_t)(np + 0.5);
     }
     return MOIL_NB_OK;
 }
@@ -685,12 +690,11 @@ int moil_nb_get_timing(const moil_nb_ctx *h, moil_nb_timing *t)
     return MOIL_NB_OK;
 }
 
-int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *water_pairs, int64_t *atom_pairs)
+int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *site_pairs)
 {
     if (!h) return MOIL_NB_ERR_ARG;
     if (list_entries) *list_entries = h->last_list_entries;
-    if (water_pairs) *water_pairs = h->last_water_pairs;
-    if (atom_pairs) *atom_pairs = h->last_atom_pairs;
+    if (site_pairs) *site_pairs = h->last_site_pairs;
     return MOIL_NB_OK;
 }
 

@@ -120,7 +120,7 @@ struct NbCtx {
     int *h_status = nullptr;           // pinned mirror
     int need_rebuild = 1;
     int evals_since_build = 0;
-    int64_t last_list_entries = 0, last_water_pairs = 0, last_atom_pairs = 0;
+    int64_t last_list_entries = 0, last_water_pairs = 0, last_atom_pairs = 0, last_site_pairs = 0;
 
     // instrumentation
     int timing = 0;

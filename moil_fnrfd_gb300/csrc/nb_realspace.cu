@@ -50,13 +50,14 @@ template <> struct Consts<double> {
 // one non-water-type pair (cdie_ewald list1/2/3 semantics); d already minimum-imaged
 template <typename T>
 __device__ __forceinline__ T atom_pair(const RepDev &R, T r2, T qi, T qj, T e12i, T e6i, T e12j, T e6j,
-                                       unsigned fi, unsigned fj, T &eel, T &elj)
+                                       unsigned fi, unsigned fj, T &eel, T &elj, int &npair)
 {
     bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < (T)R.re2;
     bool lj = r2 < (T)R.rv2 && !hr;
     T qq = qi * qj;
     bool el = r2 < (T)R.rmax2 && qq != (T)0;
     if (!lj && !el) return (T)0;
+    ++npair;
     T rinv = nb_rsqrt(r2);
     T s2 = rinv * rinv;
     T df = 0;
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
 #pragma unroll
     for (int k = 0; k < 9; ++k) { g[k] = 0; G[k] = 0; }
     double elp = 0, eli = 0, eep = 0, eei = 0;
+    int npair = 0;
     const T iL0 = rep_invL<T>(R, 0), iL1 = rep_invL<T>(R, 1), iL2 = rep_invL<T>(R, 2);
     const T rmax2 = (T)R.rmax2, rv2 = (T)R.rv2, alpha = Consts<T>::alpha(R), ex2c = (T)R.ex2c, c2a = (T)R.c2a;
     const T qOO = Consts<T>::qq(R, 0), qOH = Consts<T>::qq(R, 1), qHH = Consts<T>::qq(R, 2);
@@ -194,6 +196,7 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
             bool img = (nx != (T)0) | (ny != (T)0) | (nz != (T)0);
             if (img) { eei += (double)e_el; eli += (double)e_lj; }
             else { eep += (double)e_el; elp += (double)e_lj; }
+            npair += 9;
         }
         if (++cnt == CHUNK) { flush(g, G, 9); cnt = 0; }
     }
@@ -217,7 +220,8 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
                 min_image<T>(R, dx, dy, dz, img);
                 T r2 = dx * dx + dy * dy + dz * dz;
                 T eel = 0, elj = 0;
-                T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj);
+                T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj,
+                                    npair);
                 g[3 * a] += df * dx;
                 g[3 * a + 1] += df * dy;
                 g[3 * a + 2] += df * dz;
@@ -230,8 +234,8 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = G[k];
-    double *eu = e_unit + 4 * (size_t)i;
-    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei;
+    double *eu = e_unit + NB_EU * (size_t)i;
+    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei; eu[4] = (double)npair;
 }
 
 // non-water atom per thread over its full site list
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     T g[3] = {0, 0, 0};
     long long G[3] = {0, 0, 0};
     double elp = 0, eli = 0, eep = 0, eei = 0;
-    int cnt = 0;
+    int cnt = 0, npair = 0;
     for (int q = xl_off[k]; q < xl_off[k + 1]; ++q) {
         int s = xl[q];
         T4 xj = pos[s];
@@ -265,7 +269,7 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
         min_image<T>(R, dx, dy, dz, img);
         T r2 = dx * dx + dy * dy + dz * dz;
         T eel = 0, elj = 0;
-        T df = atom_pair<T>(R, r2, xi.w, xj.w, lji.x, lji.y, ljj.x, ljj.y, fi, sflags[s], eel, elj);
+        T df = atom_pair<T>(R, r2, xi.w, xj.w, lji.x, lji.y, ljj.x, ljj.y, fi, sflags[s], eel, elj, npair);
         g[0] += df * dx; g[1] += df * dy; g[2] += df * dz;
         if (img) { eei += (double)eel; eli += (double)elj; }
         else { eep += (double)eel; elp += (double)elj; }
@@ -275,8 +279,8 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     grad[(size_t)3 * si] = G[0];
     grad[(size_t)3 * si + 1] = G[1];
     grad[(size_t)3 * si + 2] = G[2];
-    double *eu = e_unit + 4 * (size_t)(nW + k);
-    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei;
+    double *eu = e_unit + NB_EU * (size_t)(nW + k);
+    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei; eu[4] = (double)npair;
 }
 
 // ---------------------------------------------------------------------------------
@@ -382,11 +386,11 @@ __global__ void k_final_energy(int nW, const RepDev *__restrict__ reps, const do
     __shared__ double sh[256];
     int r = blockIdx.x;
     const RepDev &R = reps[r];
-    double acc[4] = {0, 0, 0, 0}, ex[3] = {0, 0, 0}, ec = 0;
+    double acc[NB_EU] = {0, 0, 0, 0, 0}, ex[3] = {0, 0, 0}, ec = 0;
     for (int u = R.wat0 + threadIdx.x; u < R.wat0 + R.nwat; u += blockDim.x)
-        for (int k = 0; k < 4; ++k) acc[k] += e_unit[4 * (size_t)u + k];
+        for (int k = 0; k < NB_EU; ++k) acc[k] += e_unit[NB_EU * (size_t)u + k];
     for (int u = nW + R.oth0 + threadIdx.x; u < nW + R.oth0 + R.noth; u += blockDim.x)
-        for (int k = 0; k < 4; ++k) acc[k] += e_unit[4 * (size_t)u + k];
+        for (int k = 0; k < NB_EU; ++k) acc[k] += e_unit[NB_EU * (size_t)u + k];
     for (int a = R.atom0 + threadIdx.x; a < R.atom0 + R.natom; a += blockDim.x)
         for (int k = 0; k < 3; ++k) ex[k] += e_ex[3 * (size_t)a + k];
     for (int w = col_begin[r] + threadIdx.x; w < col_begin[r + 1]; w += blockDim.x) ec += e_col[w];
@@ -394,12 +398,14 @@ __global__ void k_final_energy(int nW, const RepDev *__restrict__ reps, const do
     double eep = 0.5 * block_sum(acc[2], sh), eei = 0.5 * block_sum(acc[3], sh);
     double ecorr = block_sum(ex[0], sh), eel14 = block_sum(ex[1], sh), evdw14 = block_sum(ex[2], sh);
     double erec = 0.5 * block_sum(ec, sh);
+    double npairs = 0.5 * block_sum(acc[4], sh);
     if (threadIdx.x == 0) {
         double *o = e_rep + 16 * (size_t)r;
         o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym
         o[4] = eel14; o[5] = evdw14; o[6] = ecorr; o[7] = R.e_self; o[8] = erec;
         o[9] = elp + eep + eli + eei + eel14 + evdw14 + ecorr + R.e_self + erec;
         o[10] = eep + eei;
+        o[11] = npairs;                                           // in-cutoff site pairs
     }
 }
 

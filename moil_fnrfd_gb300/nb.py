@@ -108,8 +108,7 @@ def load(build_if_missing: bool = True):
     L.moil_nb_stream.argtypes = [ctypes.c_void_p]
     L.moil_nb_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.moil_nb_get_timing.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timing)]
-    L.moil_nb_pair_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
-                                     ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.moil_nb_pair_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.moil_nb_set_graph.argtypes = [ctypes.c_void_p, ctypes.c_int]
     _lib = L
     return L
@@ -214,13 +213,17 @@ class Nonbonded:
         """MOIL's nbondm() + syminit(): rebuild the lists at the next evaluation."""
         _check(self.L, self.h, self.L.moil_nb_request_rebuild(self.h))
 
-    def eforce_into(self, coor: np.ndarray, dpot: np.ndarray):
+    def energies(self):
+        """Per-replica energies of the last evaluation."""
+        return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+
+    def eforce_into(self, coor: np.ndarray, dpot: np.ndarray, want_energies: bool = True):
         """Evaluate into caller-owned (natom,3) float64 arrays; returns per-replica energies."""
         assert coor.dtype == np.float64 and coor.flags.c_contiguous and coor.size == 3 * self.natom
         assert dpot.dtype == np.float64 and dpot.flags.c_contiguous and dpot.size == 3 * self.natom
         _check(self.L, self.h, self.L.moil_nb_eval(self.h, coor.ctypes.data_as(_dp), dpot.ctypes.data_as(_dp),
                                                    self._e))
-        return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+        return self.energies() if want_energies else None
 
     def eforce(self, coor=None):
         """Nonbonded dpot (dE/dx, kcal/mol/Å) and energies.  Single system: (dpot, dict);
@@ -236,11 +239,11 @@ class Nonbonded:
             return dpot, e[0]
         return [dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))], e
 
-    def eforce_device(self, d_coor_ptr: int, d_dpot_ptr: int):
+    def eforce_device(self, d_coor_ptr: int, d_dpot_ptr: int, want_energies: bool = True):
         """Evaluate on device-resident buffers (raw CUDA pointers)."""
         _check(self.L, self.h, self.L.moil_nb_eval_device(self.h, ctypes.c_void_p(d_coor_ptr),
                                                           ctypes.c_void_p(d_dpot_ptr), self._e))
-        return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+        return self.energies() if want_energies else None
 
     def set_timing(self, on=True):
         _check(self.L, self.h, self.L.moil_nb_set_timing(self.h, int(on)))
@@ -251,9 +254,9 @@ class Nonbonded:
         return {k: getattr(t, k) for k, _ in Timing._fields_}
 
     def pair_stats(self):
-        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        _check(self.L, self.h, self.L.moil_nb_pair_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return {"list_entries": a.value, "water_list": b.value, "atom_list": c.value}
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        _check(self.L, self.h, self.L.moil_nb_pair_stats(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return {"list_entries": a.value, "site_pairs": b.value}
 
     def stream(self) -> int:
         return self.L.moil_nb_stream(self.h) or 0

@@ -1012,15 +1012,41 @@ static void finish(ora_output *out)
     out->e_dir = out->e_el + out->e_lsym;
 }
 
+static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out);
+
 int ora_eforce(const ora_input *in, double *dpot, ora_output *out)
+{
+    return ora_eforce_repeat(in, dpot, out, 1, 1);
+}
+
+/* nevals evaluations at the same coordinates with the lists rebuilt every
+ * list_period evaluations: MOIL's dyna loop (dynamics/dyna.f:106-183) with '#lis'. */
+int ora_eforce_repeat(const ora_input *in, double *dpot, ora_output *out, int nevals, int list_period)
 {
     ctx cc, *c = &cc;
     lists L;
-    int i, k, isym;
-    memset(out, 0, sizeof(*out));
+    int e;
+    if (nevals < 1 || list_period < 1) return -2;
     if (ctx_init(c, in)) return -1;
     if (in->squeeze) squeeze(c);
-    build_lists(c, &L);
+    for (e = 0; e < nevals; e++) {
+        if (e % list_period == 0) {
+            if (e) free_lists(&L);
+            build_lists(c, &L);
+        }
+        memset(out, 0, sizeof(*out));
+        eforce_lists(c, &L, dpot, out);
+    }
+    free_lists(&L);
+    ctx_free(c);
+    return 0;
+}
+
+static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
+{
+    const ora_input *in = c->in;
+    lists L = *LL;
+    int i, k, isym;
     memset(dpot, 0, sizeof(double) * 3 * in->npt);
     out->ewaldcof = c->ewaldcof;
     out->e_self = self_energy(c);
@@ -1123,9 +1149,6 @@ int ora_eforce(const ora_input *in, double *dpot, ora_output *out)
     out->list_sizes[3] = L.listwt1.n; out->list_sizes[4] = L.listwt2.n;
     out->list_sizes[5] = L.nprim1; out->list_sizes[6] = L.nprimw1; out->list_sizes[7] = L.nprimw2;
     finish(out);
-    free_lists(&L);
-    ctx_free(c);
-    return 0;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1302,7 +1325,8 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
     return 0;
 }
 
-int ora_eforce_batch(int nsys, const ora_input *in, double **dpot, ora_output *out, int mi, int nthreads)
+int ora_eforce_batch(int nsys, const ora_input *in, double **dpot, ora_output *out, int mi, int nthreads,
+                     int nevals, int list_period)
 {
     int s, bad = 0;
 #ifdef _OPENMP
@@ -1310,7 +1334,8 @@ int ora_eforce_batch(int nsys, const ora_input *in, double **dpot, ora_output *o
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : bad)
 #endif
     for (s = 0; s < nsys; s++) {
-        int r = mi ? ora_eforce_mi(&in[s], dpot[s], &out[s]) : ora_eforce(&in[s], dpot[s], &out[s]);
+        int r = mi ? ora_eforce_mi(&in[s], dpot[s], &out[s])
+                   : ora_eforce_repeat(&in[s], dpot[s], &out[s], nevals, list_period);
         if (r) bad++;
     }
     (void)nthreads;

@@ -76,8 +76,13 @@ int ora_eforce(const ora_input *in, double *dpot, ora_output *out);
  * at the given coordinates (the parity reference for the GPU path). */
 int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out);
 
-/* Batch of independent systems, OpenMP over systems (CPU baseline). */
-int ora_eforce_batch(int nsys, const ora_input *in, double **dpot, ora_output *out, int mi, int nthreads);
+/* nevals evaluations with lists rebuilt every list_period (MOIL's '#lis'). */
+int ora_eforce_repeat(const ora_input *in, double *dpot, ora_output *out, int nevals, int list_period);
+
+/* Batch of independent systems, OpenMP over systems (CPU baseline); mi selects the
+ * minimum-image evaluator, otherwise nevals/list_period as ora_eforce_repeat. */
+int ora_eforce_batch(int nsys, const ora_input *in, double **dpot, ora_output *out, int mi, int nthreads,
+                     int nevals, int list_period);
 
 double ora_find_ewaldcof(double cutoff, double dtol);
 /* erfc table: returns number of points (4 coefficients each) written to tab (capacity cap). */

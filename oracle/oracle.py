@@ -81,7 +81,8 @@ def lib():
         L.ora_eforce.argtypes = [ctypes.POINTER(OraInput), _dp, ctypes.POINTER(OraOutput)]
         L.ora_eforce_mi.argtypes = [ctypes.POINTER(OraInput), _dp, ctypes.POINTER(OraOutput)]
         L.ora_eforce_batch.argtypes = [ctypes.c_int, ctypes.POINTER(OraInput), ctypes.POINTER(_dp),
-                                       ctypes.POINTER(OraOutput), ctypes.c_int, ctypes.c_int]
+                                       ctypes.POINTER(OraOutput), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int]
         L.ora_find_ewaldcof.restype = ctypes.c_double
         L.ora_find_ewaldcof.argtypes = [ctypes.c_double, ctypes.c_double]
         L.ora_erfc_table.argtypes = [ctypes.c_double, ctypes.c_double, _dp, ctypes.c_int]
@@ -186,8 +187,9 @@ def eforce(s, mode: str = "parity", **kw):
     return dpot, output_dict(out)
 
 
-def eforce_batch(systems, mode: str = "parity", nthreads: int = 0, **kw):
-    """Independent systems evaluated on nthreads host threads (0: OpenMP default)."""
+def eforce_batch(systems, mode: str = "parity", nthreads: int = 0, nevals: int = 1, list_period: int = 1, **kw):
+    """Independent systems on nthreads host threads (0: OpenMP default); each system is
+    evaluated nevals times with its lists rebuilt every list_period evaluations."""
     keep = _Keep()
     n = len(systems)
     ins = (OraInput * n)()
@@ -199,7 +201,8 @@ def eforce_batch(systems, mode: str = "parity", nthreads: int = 0, **kw):
         d = np.zeros((s.npt, 3), dtype=np.float64)
         res.append(d)
         dp[k] = _p(d)
-    rc = lib().ora_eforce_batch(n, ins, dp, outs, 1 if mode == "mi" else 0, int(nthreads))
+    rc = lib().ora_eforce_batch(n, ins, dp, outs, 1 if mode == "mi" else 0, int(nthreads), int(nevals),
+                                int(list_period))
     if rc != 0:
         raise RuntimeError("oracle batch failed")
     return res, [output_dict(outs[k]) for k in range(n)]
