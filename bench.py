@@ -106,10 +106,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(rank=0):
+def build_workload(rank=0, n_rep=512):
+    """The 512-replica batch; a smaller n_rep keeps the first n_rep replicas (profiling)."""
     from moil_fnrfd_gb300 import systems
     reps = systems.config3(512, seed=3000 + 7919 * rank)
-    return reps
+    return reps[:n_rep]
 
 
 def cpu_baseline(reps, budget_s=12.0):
@@ -171,6 +172,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 leg")
+    ap.add_argument("--replicas", type=int, default=512, help="first R replicas only (profiling captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -188,7 +190,7 @@ def main():
     torch.cuda.set_device(local)
 
     t0 = time.perf_counter()
-    reps = build_workload(rank)
+    reps = build_workload(rank, args.replicas)
     natoms = sum(s.npt for s in reps)
     log(f"workload: {len(reps)} replicas, {natoms} atoms, generated in {time.perf_counter() - t0:.1f} s")
     nb = Nonbonded(reps, precision=MOIL_NB_MIXED, device=local, skin=SKIN, list_period=LIST_PERIOD)
