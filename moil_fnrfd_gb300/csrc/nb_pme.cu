@@ -490,6 +490,17 @@ size_t zconv_smem(int n3)
     return sizeof(C) * NB_TK * (n3 | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
 }
 
+// raise a kernel's dynamic shared-memory limit to at least `bytes` (never lower it)
+template <typename K>
+cudaError_t raise_smem_limit(K *kernel, size_t bytes)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 template <typename T>
 int configure_t(NbCtx *c)
 {
@@ -553,9 +564,10 @@ int configure_t(NbCtx *c)
     c->smem_plane_fwd = sf;
     c->smem_plane_inv = si;
     c->smem_zconv = sz;
-    NB_CUDA_OK(c, cudaFuncSetAttribute(k_plane_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sf));
-    NB_CUDA_OK(c, cudaFuncSetAttribute(k_plane_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si));
-    NB_CUDA_OK(c, cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz));
+    // the limit is per kernel, shared by every handle in the process: only ever raise it
+    NB_CUDA_OK(c, raise_smem_limit(k_plane_fwd<T>, sf));
+    NB_CUDA_OK(c, raise_smem_limit(k_plane_inv<T>, si));
+    NB_CUDA_OK(c, raise_smem_limit(k_zconv<T>, sz));
     NB_CUDA_OK(c, cudaMalloc(&c->d_planes, sizeof(PlaneWork) * c->planes.size()));
     NB_CUDA_OK(c, cudaMemcpy(c->d_planes, c->planes.data(), sizeof(PlaneWork) * c->planes.size(), cudaMemcpyHostToDevice));
     NB_CUDA_OK(c, cudaMalloc(&c->d_cols, sizeof(ColWork) * c->cols.size()));
