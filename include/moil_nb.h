@@ -177,6 +177,32 @@ int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *sit
  * kernel by kernel (0, default).  Graph replays are used when on. */
 int moil_nb_set_graph(moil_nb_ctx *h, int on);
 
+/* ---- PME reciprocal sum without device allocation -------------------------
+ * No counterpart in the reference (MOIL's ewald_receip() works on static COMMON
+ * arrays and never allocates).  This entry point is for callers that cannot call
+ * cudaMalloc: a host program whose device memory is already claimed by another
+ * runtime's caching pool, or code that cannot accept the device-wide
+ * synchronisation that cudaMalloc/cudaFree may impose in the middle of its own
+ * stream work.  It computes the PME reciprocal energy and its gradient for one
+ * system with the same kernels as the handle path, taking every scratch buffer
+ * from one file-scope device array of about 7.5 MB that each GPU loading this
+ * library holds until the process exits.
+ *   limits   natom <= 65536; each grid side 4..64 and 2/3/5-smooth; order 4;
+ *            mixed precision (FP32 spline and FFT math, FP64 energy)
+ *   device   d_coor (3*natom, x,y,z per atom), d_q (natom), d_dpot (3*natom,
+ *            OVERWRITTEN with the reciprocal-space gradient dE/dx)
+ *   host     box[3], grid[3] (nfft1..3), *e_recip (energy, kcal/mol)
+ *   stream   cudaStream_t as void* (0: the default stream); the call returns after
+ *            synchronising it
+ * The first call on a device looks up the device address of the array (set-up);
+ * make that first call before any stream capture.  Every call reuses the same array
+ * and leaves the last call's contents in it (the bin counters are cleared each call,
+ * all other regions are rewritten before they are read), so calls that overlap on
+ * the GPU -- from two streams or two host threads -- race: serialise them. */
+int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int natom, const double *box,
+                        const int *grid, double alpha, double eps, double *d_dpot, double *e_recip,
+                        void *stream);
+
 /* ---- Fortran entry points (gfortran naming, all arguments by reference) --
  * A maintainer replaces the nonbonded block of pot/eforce.f:122-204 with
  *     call eforce_nb_gpu(npt, coor, dpot, enb, status)

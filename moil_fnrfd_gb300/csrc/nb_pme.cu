@@ -594,3 +594,237 @@ int nb_pme_configure(NbCtx *c)
 {
     return c->precision == MOIL_NB_FP64 ? configure_t<double>(c) : configure_t<float>(c);
 }
+
+// ---------------------------------------------------------------------------------
+// Allocation-free PME reciprocal sum (moil_nb_pme_noalloc).
+//
+// For callers that cannot allocate device memory: the same bin / spread+FFT / convolution /
+// FFT+gather kernels as the handle path, with every scratch buffer carved out of one
+// file-scope device array.  The array is sized for at most NA_MAX_ATOMS atoms and PME
+// grids of at most NA_MAX_N points per side; every GPU that loads this library holds it
+// (about 7.5 MB) until the process exits.
+#include <mutex>
+
+namespace {
+
+constexpr int NA_MAX_ATOMS = 65536;
+constexpr int NA_MAX_N = 64;
+constexpr int NA_MAX_COLS = NA_MAX_N * ((NA_MAX_N / 2 + 1 + NB_TK - 1) / NB_TK);
+constexpr size_t na_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// arena regions (byte offsets, 256-byte aligned)
+constexpr size_t NA_POS = 0;
+constexpr size_t NA_Q = NA_POS + na_up(sizeof(float4) * NA_MAX_ATOMS);
+constexpr size_t NA_REP = NA_Q + na_up(sizeof(float) * NA_MAX_ATOMS);
+constexpr size_t NA_FR = NA_REP + na_up(sizeof(int) * NA_MAX_ATOMS);
+constexpr size_t NA_ZSLOT = NA_FR + na_up(sizeof(float4) * NA_MAX_ATOMS);
+constexpr size_t NA_ZATOMS = NA_ZSLOT + na_up(sizeof(int) * NA_MAX_ATOMS);
+constexpr size_t NA_PART = NA_ZATOMS + na_up(sizeof(int) * NA_MAX_ATOMS);
+constexpr size_t NA_ZCOUNT = NA_PART + na_up(sizeof(float) * 12 * NA_MAX_ATOMS);
+constexpr size_t NA_ZSTART = NA_ZCOUNT + na_up(sizeof(int) * (NA_MAX_N + 1));
+constexpr size_t NA_GRID = NA_ZSTART + na_up(sizeof(int) * (NA_MAX_N + 1));
+constexpr size_t NA_ECOL = NA_GRID + na_up(sizeof(float2) * (NA_MAX_N / 2 + 1) * NA_MAX_N * NA_MAX_N);
+constexpr size_t NA_PLANES = NA_ECOL + na_up(sizeof(double) * NA_MAX_COLS);
+constexpr size_t NA_COLS = NA_PLANES + na_up(sizeof(PlaneWork) * NA_MAX_N);
+constexpr size_t NA_COLBEG = NA_COLS + na_up(sizeof(ColWork) * NA_MAX_COLS);
+constexpr size_t NA_PLANS = NA_COLBEG + na_up(sizeof(int) * 2);
+constexpr size_t NA_REPPLAN = NA_PLANS + na_up(sizeof(FftPlanDev) * 3);
+constexpr size_t NA_TW = NA_REPPLAN + na_up(sizeof(int) * 3);
+constexpr size_t NA_BSP = NA_TW + na_up(sizeof(float2) * 3 * NA_MAX_N);
+constexpr size_t NA_REPS = NA_BSP + na_up(sizeof(float) * 3 * NA_MAX_N);
+constexpr size_t NA_EOUT = NA_REPS + na_up(sizeof(RepDev));
+constexpr size_t NA_STATUS = NA_EOUT + na_up(sizeof(double));
+constexpr size_t NA_BYTES = NA_STATUS + na_up(sizeof(int) * 8);
+
+static __device__ __align__(256) unsigned char g_pme_scratch[NA_BYTES];
+
+std::mutex g_na_mu;
+constexpr int NA_MAX_DEVICES = 64;
+unsigned char *g_na_base[NA_MAX_DEVICES] = {};
+
+__global__ void k_na_load(int natom, const double *__restrict__ coor, const double *__restrict__ q,
+                          float4 *__restrict__ pos, float *__restrict__ sq, int *__restrict__ srep)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natom) return;
+    pos[a] = make_float4((float)coor[3 * (size_t)a], (float)coor[3 * (size_t)a + 1], (float)coor[3 * (size_t)a + 2], 0.f);
+    sq[a] = (float)q[a];
+    srep[a] = 0;
+}
+
+// gradient from the four per-plane slots (grad_sum, pot/ewald_receip.f:815-970); overwrites dpot
+__global__ void k_na_grad(int natom, const RepDev *__restrict__ reps, const double *__restrict__ q,
+                          const float *__restrict__ part, double *__restrict__ dpot)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natom) return;
+    const RepDev &R = reps[0];
+    double pg[3] = {0, 0, 0};
+    const float *p = part + 12 * (size_t)a;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+        for (int d = 0; d < 3; ++d) pg[d] += (double)p[3 * t + d];
+    double qf = q[a] * R.fcd;
+    dpot[3 * (size_t)a] = qf * R.n1 * R.invLd[0] * pg[0];
+    dpot[3 * (size_t)a + 1] = qf * R.n2 * R.invLd[1] * pg[1];
+    dpot[3 * (size_t)a + 2] = qf * R.n3 * R.invLd[2] * pg[2];
+}
+
+__global__ void k_na_energy(int ncol, const double *__restrict__ e_col, double *__restrict__ out)
+{
+    __shared__ double sh[256];
+    double v = 0;
+    for (int w = threadIdx.x; w < ncol; w += blockDim.x) v += e_col[w];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = 0.5 * sh[0];
+}
+
+// |DFT|^2 of the order-4 B-spline at w = 0 (pot/ewald_receip.f:413-481)
+void na_bsp_moduli(int n, float *mod)
+{
+    const double th[4] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 0.0};
+    std::vector<double> m(n);
+    for (int k = 0; k < n; ++k) {
+        double s1 = 0, s2 = 0;
+        for (int j = 1; j <= 4 && j < n; ++j) {
+            double arg = 2.0 * M_PI * k * j / n;
+            s1 += th[j - 1] * cos(arg);
+            s2 += th[j - 1] * sin(arg);
+        }
+        m[k] = s1 * s1 + s2 * s2;
+    }
+    for (int k = 0; k < n; ++k) {
+        if (m[k] < 1e-7) m[k] = 0.5 * (m[(k - 1 + n) % n] + m[(k + 1) % n]);
+        mod[k] = (float)m[k];
+    }
+}
+
+}  // namespace
+
+extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int natom, const double *box,
+                                   const int *grid, double alpha, double eps, double *d_dpot, double *e_recip,
+                                   void *stream_v)
+{
+    if (!d_coor || !d_q || !box || !grid || !d_dpot || !e_recip) return MOIL_NB_ERR_ARG;
+    if (natom < 1 || natom > NA_MAX_ATOMS || !(alpha > 0) || !(eps > 0)) return MOIL_NB_ERR_ARG;
+    for (int d = 0; d < 3; ++d) {
+        FftPlanDev p;
+        if (!(box[d] > 0) || grid[d] < 4 || grid[d] > NA_MAX_N || !make_plan(grid[d], &p)) return MOIL_NB_ERR_GRID;
+    }
+    cudaStream_t stream = (cudaStream_t)stream_v;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return MOIL_NB_ERR_CUDA;
+    unsigned char *base = nullptr;
+    {
+        // first call on this device: resolve the device address of the scratch array (the
+        // symbol itself is only a host-side stand-in and must not be handed to a kernel)
+        std::lock_guard<std::mutex> lk(g_na_mu);
+        if (!g_na_base[dev]) {
+            void *ptr = nullptr;
+            if (cudaGetSymbolAddress(&ptr, g_pme_scratch) != cudaSuccess || !ptr) return MOIL_NB_ERR_CUDA;
+            g_na_base[dev] = (unsigned char *)ptr;
+        }
+        base = g_na_base[dev];
+    }
+    const int n1 = grid[0], n2 = grid[1], n3 = grid[2];
+    // shared-memory limits for this grid (raise only; other handles may need more)
+    if (raise_smem_limit(k_plane_fwd<float>, plane_fwd_smem<float>(n1, n2)) != cudaSuccess ||
+        raise_smem_limit(k_plane_inv<float>, plane_inv_smem<float>(n1, n2)) != cudaSuccess ||
+        raise_smem_limit(k_zconv<float>, zconv_smem<float>(n3)) != cudaSuccess)
+        return MOIL_NB_ERR_CUDA;
+    // one-replica constants, FFT plans and twiddles, B-spline moduli, work lists (host side)
+    RepDev R;
+    memset(&R, 0, sizeof(R));
+    for (int d = 0; d < 3; ++d) {
+        R.Ld[d] = box[d];
+        R.L[d] = (float)box[d];
+        R.invLd[d] = 1.0 / box[d];
+        R.invL[d] = (float)(1.0 / box[d]);
+        R.Llo[d] = (float)(box[d] - (double)R.L[d]);
+    }
+    R.n1 = n1; R.n2 = n2; R.n3 = n3; R.n1h = n1 / 2 + 1;
+    R.epstmp = NB_KOFDIE / eps;
+    R.fcd = sqrt(R.epstmp);
+    R.fc = (float)R.fcd;
+    R.alpha = (float)alpha;
+    R.alphad = alpha;
+    R.pme_fac = M_PI * M_PI / (alpha * alpha);
+    R.pivol = M_PI * box[0] * box[1] * box[2];
+    R.natom = natom;
+    FftPlanDev plans[3];
+    int rep_plan[3];
+    float2 tw[3 * NA_MAX_N];
+    float bsp[3 * NA_MAX_N];
+    int ntw = 0;
+    for (int d = 0; d < 3; ++d) {
+        make_plan(grid[d], &plans[d]);
+        plans[d].tw0 = ntw;
+        for (int t = 0; t < grid[d]; ++t) {
+            double ang = -2.0 * M_PI * (double)t / (double)grid[d];
+            tw[ntw++] = make_float2((float)cos(ang), (float)sin(ang));
+        }
+        rep_plan[d] = d;
+    }
+    na_bsp_moduli(n1, bsp);
+    na_bsp_moduli(n2, bsp + n1);
+    na_bsp_moduli(n3, bsp + n1 + n2);
+    NbCtx tmp;
+    tmp.stream = stream;
+    tmp.nrep = 1;
+    tmp.nsite = natom;
+    tmp.nzbin = n3;
+    for (int z = 0; z < n3; ++z) tmp.planes.push_back(PlaneWork{0, z});
+    for (int ky = 0; ky < n2; ++ky)
+        for (int kx0 = 0; kx0 < R.n1h; kx0 += NB_TK) tmp.cols.push_back(ColWork{0, ky, kx0});
+    int col_begin[2] = {0, (int)tmp.cols.size()};
+    tmp.smem_plane_fwd = plane_fwd_smem<float>(n1, n2);
+    tmp.smem_plane_inv = plane_inv_smem<float>(n1, n2);
+    tmp.smem_zconv = zconv_smem<float>(n3);
+    tmp.d_pos = base + NA_POS;
+    tmp.d_site_q = base + NA_Q;
+    tmp.d_site_rep = (int *)(base + NA_REP);
+    tmp.d_fr = base + NA_FR;
+    tmp.d_zslot = (int *)(base + NA_ZSLOT);
+    tmp.d_zatoms = (int *)(base + NA_ZATOMS);
+    tmp.d_part = base + NA_PART;
+    tmp.d_zcount = (int *)(base + NA_ZCOUNT);
+    tmp.d_zstart = (int *)(base + NA_ZSTART);
+    tmp.d_grid = base + NA_GRID;
+    tmp.d_e_col = (double *)(base + NA_ECOL);
+    tmp.d_planes = (PlaneWork *)(base + NA_PLANES);
+    tmp.d_cols = (ColWork *)(base + NA_COLS);
+    tmp.d_col_begin = (int *)(base + NA_COLBEG);
+    tmp.d_plans = (FftPlanDev *)(base + NA_PLANS);
+    tmp.d_rep_plan = (int *)(base + NA_REPPLAN);
+    tmp.d_tw = base + NA_TW;
+    tmp.d_bsp = base + NA_BSP;
+    tmp.d_reps = (RepDev *)(base + NA_REPS);
+    tmp.d_status = (int *)(base + NA_STATUS);
+    double *d_eout = (double *)(base + NA_EOUT);
+#define NA_CP(dst, src, bytes)                                                                       \
+    if (cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, stream) != cudaSuccess)      \
+        return MOIL_NB_ERR_CUDA;
+    NA_CP(tmp.d_reps, &R, sizeof(R));
+    NA_CP(tmp.d_plans, plans, sizeof(plans));
+    NA_CP(tmp.d_rep_plan, rep_plan, sizeof(rep_plan));
+    NA_CP(tmp.d_tw, tw, sizeof(float2) * ntw);
+    NA_CP(tmp.d_bsp, bsp, sizeof(float) * (n1 + n2 + n3));
+    NA_CP(tmp.d_planes, tmp.planes.data(), sizeof(PlaneWork) * tmp.planes.size());
+    NA_CP(tmp.d_cols, tmp.cols.data(), sizeof(ColWork) * tmp.cols.size());
+    NA_CP(tmp.d_col_begin, col_begin, sizeof(col_begin));
+#undef NA_CP
+    k_na_load<<<(natom + 255) / 256, 256, 0, stream>>>(natom, d_coor, d_q, (float4 *)tmp.d_pos,
+                                                       (float *)tmp.d_site_q, tmp.d_site_rep);
+    pme_t<float>(&tmp);
+    k_na_grad<<<(natom + 255) / 256, 256, 0, stream>>>(natom, tmp.d_reps, d_q, (const float *)tmp.d_part, d_dpot);
+    k_na_energy<<<1, 256, 0, stream>>>((int)tmp.cols.size(), tmp.d_e_col, d_eout);
+    if (cudaMemcpyAsync(e_recip, d_eout, sizeof(double), cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+        return MOIL_NB_ERR_CUDA;
+    if (cudaStreamSynchronize(stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) return MOIL_NB_ERR_CUDA;
+    return MOIL_NB_OK;
+}
