@@ -66,7 +66,7 @@ struct RepDev {
 
 // work descriptors for the PME plane / column kernels
 struct PlaneWork { int rep, z; };
-struct ColWork { int rep, ky, kx0; };
+struct ColWork { int rep, kx, ky0; };   // z columns at fixed kx for ky in [ky0, ky0 + tile)
 
 // ---------------------------------------------------------------------------------
 // precision traits

@@ -9,10 +9,16 @@
 #include "moil_nb.h"
 #include "nb_common.cuh"
 
-// FFT plan for one length: radices (4, 2, 3, 5 in that order) and twiddles exp(-2 pi i k / n)
+// FFT plan for one length: radices (4, 2, 3, 5 in that order), twiddles exp(-2 pi i k / n)
+// at tw0, and per Stockham stage s: the span Ns, the butterfly count nb = n/R, the magic
+// multiplier for dividing by nb, and nb (twiddle step, destination index) entries at tab0+off[s]
 struct FftPlanDev {
-    int n, nst, tw0, pad;
+    int n, nst, tw0, tab0;
     int rad[8];
+    int ns[8];
+    int nb[8];
+    int off[8];
+    unsigned magic[8];
 };
 
 struct RepHost {
@@ -90,6 +96,7 @@ struct NbCtx {
     std::vector<int> rep_plan;         // 3 plan indices per replica
     int *d_rep_plan = nullptr;
     void *d_tw = nullptr;              // float2 / double2 twiddles
+    int2 *d_tab = nullptr;             // Stockham stage tables (twiddle step, destination index)
     std::vector<double> bsp_h;
     void *d_bsp = nullptr;             // float / double moduli
     int nzbin = 0;

@@ -2,29 +2,36 @@
 //
 // The reference spreads into a padded complex grid, runs two full 3D C2C FFTs
 // (pubz3d / FFTPACK) with the influence function in between (scalar_sum) and gathers.
-// Here the grid never exists as a real-space array in HBM:
+// Here the real-space charge grid never exists in HBM:
 //   k_pme_bin      fractional coordinates fr = n (w - anint(w) + 1/2) (:250-260), atoms
-//                  bucketed by int(fr3) (the z plane their stencil ends on)
-//   k_plane_fwd    one CTA per (replica, z plane): the 4x4 x-y stencils of every atom whose
+//                  bucketed by int(fr3) (the last z plane of their stencil)
+//   plane_fwd      one CTA per (replica, z plane): the 4x4 x-y stencils of every atom whose
 //                  z stencil touches the plane are accumulated in shared memory in 64-bit
-//                  fixed point (order independent), then R2C along x and C2C along y in
-//                  shared memory; only the half-complex plane goes to HBM
-//   k_zconv        one CTA per (replica, ky, 16 kx columns): C2C along z, influence function
+//                  fixed point (order independent, hence deterministic), then R2C along x
+//                  and C2C along y in shared memory; the half-complex plane goes to HBM
+//                  as [z][kx][ky]
+//   zconv          one CTA per (replica, kx, run of ky): C2C along z, the influence function
 //                  exp(-pi^2 m^2 / alpha^2) / (pi V B(m) m^2) with the FP64 energy sum
 //                  (scalar_sum, :723-812), inverse C2C along z, written back in place
-//   k_plane_inv    one CTA per (replica, z plane): inverse C2C along y, C2R along x in shared
-//                  memory, then each atom's gradient share from this plane (grad_sum,
+//   plane_inv      one CTA per (replica, z plane): inverse C2C along y, C2R along x in shared
+//                  memory, then each atom's share of the gradient from this plane (grad_sum,
 //                  :815-970) into its own slot -- four planes, four slots, summed at the end
-// FFTs: Stockham autosort, radix 4/2/3/5, one warp per line, twiddles from a table of
-// exp(-2 pi i k / n) computed on the host in FP64.  Inverse = conj(FFT(conj(x))),
-// unnormalised like FFTPACK's cfftb.
+// FFTs (FP32 path): Stockham autosort with radices 4/2/3/5; every pass transforms all lines
+// of a tile at once, the block's threads spread over (line, butterfly) pairs, with the
+// index arithmetic (twiddle step, destination) read from per-stage tables built on the host
+// and the line number obtained by a multiply-high by a precomputed magic constant.  The
+// last pass of a direction stores transposed, so the next direction reads contiguous lines.
+// The plain FP64 path uses a simpler one-warp-per-line FFT with the same layout.
+// Inverse transforms are conj(FFT(conj(x))), unnormalised like FFTPACK's cfftb.
+#include <mutex>
+
 #include "nb_internal.h"
 
 namespace {
 
-template <typename C> __device__ __forceinline__ C cmk(double r, double i);
-template <> __device__ __forceinline__ float2 cmk<float2>(double r, double i) { return make_float2((float)r, (float)i); }
-template <> __device__ __forceinline__ double2 cmk<double2>(double r, double i) { return make_double2(r, i); }
+template <typename C> __device__ __forceinline__ C cmk(float r, float i);
+template <> __device__ __forceinline__ float2 cmk<float2>(float r, float i) { return make_float2(r, i); }
+template <> __device__ __forceinline__ double2 cmk<double2>(float r, float i) { return make_double2(r, i); }
 
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
@@ -75,10 +82,10 @@ template <typename C> __device__ __forceinline__ void bfly5(C *v)
     const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;    // sin(2pi/5), sin(4pi/5)
     C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]), a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
     C x0 = v[0];
-    C p1, p2;  // real-combination parts
+    C p1, p2;
     p1.x = x0.x + c1 * a1.x + c2 * a2.x; p1.y = x0.y + c1 * a1.y + c2 * a2.y;
     p2.x = x0.x + c2 * a1.x + c1 * a2.x; p2.y = x0.y + c2 * a1.y + c1 * a2.y;
-    C q1, q2;  // imaginary parts: q = s.b ; result +- (-i) q
+    C q1, q2;   // the sine combinations; results are p -/+ i q
     q1.x = s1 * b1.x + s2 * b2.x; q1.y = s1 * b1.y + s2 * b2.y;
     q2.x = s2 * b1.x - s1 * b2.x; q2.y = s2 * b1.y - s1 * b2.y;
     v[0].x = x0.x + a1.x + a2.x; v[0].y = x0.y + a1.y + a2.y;
@@ -87,36 +94,6 @@ template <typename C> __device__ __forceinline__ void bfly5(C *v)
     v[4] = csub(p1, mq1);
     v[2] = cadd(p2, mq2);
     v[3] = csub(p2, mq2);
-}
-
-// one line of length n in shared memory (x), scratch y; returns the buffer holding the result
-template <typename C>
-__device__ C *warp_fft(C *x, C *y, const FftPlanDev &p, const C *__restrict__ tw, int lane)
-{
-    int n = p.n, Ns = 1;
-    for (int st = 0; st < p.nst; ++st) {
-        int R = p.rad[st], nb = n / R, stride = n / (Ns * R);
-        for (int j = lane; j < nb; j += 32) {
-            C v[5];
-            int jm = j % Ns;
-            for (int r = 0; r < R; ++r) v[r] = x[j + r * nb];
-            int tstep = jm * stride;
-            for (int r = 1; r < R; ++r) {
-                int t = (r * tstep) % n;
-                v[r] = cmul(v[r], tw[t]);
-            }
-            if (R == 4) bfly4(v);
-            else if (R == 2) bfly2(v);
-            else if (R == 3) bfly3(v);
-            else bfly5(v);
-            int idxD = (j / Ns) * Ns * R + jm;
-            for (int r = 0; r < R; ++r) y[idxD + r * Ns] = v[r];
-        }
-        __syncwarp();
-        C *t = x; x = y; y = t;
-        Ns *= R;
-    }
-    return x;
 }
 
 // MOIL fill_bspline for order 4 (ewald_receip.f:1022-1080)
@@ -143,7 +120,11 @@ __device__ __forceinline__ void bspline4(T w, T th[4], T dth[4])
 __device__ __forceinline__ float nb_round(float x) { return roundf(x); }
 __device__ __forceinline__ double nb_round(double x) { return round(x); }
 
+__device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
 // ---------------------------------------------------------------------------------
+// binning (both precisions)
+
 template <typename T>
 __global__ void k_pme_bin(int nsite, const int *__restrict__ site_rep, const RepDev *__restrict__ reps,
                           const void *pos_v, const void *q_v, void *fr_v, int *__restrict__ zcount,
@@ -180,6 +161,7 @@ __global__ void k_pme_scatter(int nsite, const int *__restrict__ site_rep, const
     zatoms[zstart[R.zb0 + zb] + zslot[s]] = s;
 }
 
+// plane accumulation: 64-bit fixed point (2^40 per unit) for FP32, FP64 atomics for FP64
 template <typename T> struct Acc;
 template <> struct Acc<float> {
     typedef unsigned long long type;
@@ -192,32 +174,16 @@ template <> struct Acc<double> {
     __device__ static double get(type v) { return v; }
 };
 
-__device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
-
+// the 4x4 x-y stencil of every atom whose z stencil reaches plane z
 template <typename T>
-__global__ void __launch_bounds__(256) k_plane_fwd(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
-                                                   const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
-                                                   const void *tw_v, const int *__restrict__ zstart,
-                                                   const int *__restrict__ zatoms, const void *fr_v, void *grid_v)
+__device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *__restrict__ zstart,
+                                             const int *__restrict__ zatoms, const typename vec4<T>::type *fr,
+                                             typename Acc<T>::type *acc)
 {
-    typedef typename cplx<T>::type C;
     typedef typename vec4<T>::type T4;
-    typedef typename Acc<T>::type A;
-    extern __shared__ __align__(16) unsigned char smem[];
-    PlaneWork w = work[blockIdx.x];
-    const RepDev &R = reps[w.rep];
-    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h, pitch = n1h | 1;
-    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
-    const C *tw = (const C *)tw_v;
-    A *acc = (A *)smem;
-    C *P = (C *)(smem + align16(sizeof(A) * n1 * n2));
-    C *scr = P + n2 * pitch;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
-    __syncthreads();
-    const T4 *fr = (const T4 *)fr_v;
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
     for (int tp = 0; tp < 4; ++tp) {
-        int zb = w.z + tp;
+        int zb = z + tp;
         zb = zb >= n3 ? zb - n3 : zb;
         int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
         int t3 = 3 - tp;
@@ -232,26 +198,324 @@ __global__ void __launch_bounds__(256) k_plane_fwd(const PlaneWork *__restrict__
             int j = i2 - 3 + t2;
             j = (j + 2 * n2) % n2;
             T v = th2[t2] * th3[t3] * f.w;
-            A *row = acc + j * n1;
+            typename Acc<T>::type *row = acc + j * n1;
+            int i0 = i1 - 3 + 2 * n1;
 #pragma unroll
-            for (int t1 = 0; t1 < 4; ++t1) {
-                int i = (i1 - 3 + t1 + 2 * n1) % n1;
-                Acc<T>::add(row + i, v * th1[t1]);
+            for (int t1 = 0; t1 < 4; ++t1) Acc<T>::add(row + (i0 + t1) % n1, v * th1[t1]);
+        }
+    }
+}
+
+// gradient share of plane z (real values Rp[ky][x]) for the atoms whose z stencil reaches it
+template <typename T>
+__device__ __forceinline__ void gather_plane(const RepDev &R, int z, const int *__restrict__ zstart,
+                                             const int *__restrict__ zatoms, const typename vec4<T>::type *fr,
+                                             const T *Rp, T *__restrict__ part)
+{
+    typedef typename vec4<T>::type T4;
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
+    for (int tp = 0; tp < 4; ++tp) {
+        int zb = z + tp;
+        zb = zb >= n3 ? zb - n3 : zb;
+        int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
+        int t3 = 3 - tp;
+        for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
+            int s = zatoms[idx];
+            T4 f = fr[s];
+            int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
+            bspline4<T>(f.x - (T)i1, th1, dt1);
+            bspline4<T>(f.y - (T)i2, th2, dt2);
+            bspline4<T>(f.z - (T)i3, th3, dt3);
+            T gx = 0, gy = 0, gz = 0;
+            int i0 = i1 - 3 + 2 * n1;
+#pragma unroll
+            for (int t2 = 0; t2 < 4; ++t2) {
+                int j = (i2 - 3 + t2 + 2 * n2) % n2;
+                const T *row = Rp + j * n1;
+                T sx = 0, sy = 0;
+#pragma unroll
+                for (int t1 = 0; t1 < 4; ++t1) {
+                    T q = row[(i0 + t1) % n1];
+                    sx += q * dt1[t1];
+                    sy += q * th1[t1];
+                }
+                gx += sx * th2[t2];
+                gy += sy * dt2[t2];
+                gz += sy * th2[t2];
             }
+            T *o = part + 12 * (size_t)s + 3 * t3;
+            o[0] = gx * th3[t3];
+            o[1] = gy * th3[t3];
+            o[2] = gz * dt3[t3];
+        }
+    }
+}
+
+// influence function (scalar_sum): m folded as MOIL does (k > ceil(n/2) - 1 -> k - n)
+template <typename T>
+__device__ __forceinline__ T eterm_of(const RepDev &R, const T *bsp, int kx, int ky, int kz)
+{
+    if (kx == 0 && ky == 0 && kz == 0) return (T)0;
+    const int nf2 = (R.n2 + 1) / 2, nf3 = (R.n3 + 1) / 2;
+    int m2 = ky < nf2 ? ky : ky - R.n2, m3 = kz < nf3 ? kz : kz - R.n3;
+    T mh1 = (T)kx * rep_invL<T>(R, 0), mh2 = (T)m2 * rep_invL<T>(R, 1), mh3 = (T)m3 * rep_invL<T>(R, 2);
+    T msq = mh1 * mh1 + mh2 * mh2 + mh3 * mh3;
+    return exp(-(T)R.pme_fac * msq) /
+           ((T)R.pivol * bsp[kx] * bsp[R.n1 + ky] * bsp[R.n1 + R.n2 + kz] * msq);
+}
+
+// =================================================================================
+// FP32 path: block-cooperative table-driven Stockham passes
+
+#define NB_TKF 32     // z lines per zconv CTA (FP32 path)
+
+// One Stockham stage over L lines of length n.  Source line l at src + l*ss (contiguous).
+// Destination: MODE 0 natural (dst + l*ds), MODE 1 transposed (dst[k*L + l] for k < keep),
+// MODE 2 real part natural (rdst + l*ds).  CONJ_OUT conjugates the stored values.
+template <int RADIX, int MODE, bool CONJ_OUT>
+__device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                           float *__restrict__ rdst, int L, int ss, int ds, int keep,
+                                           int Ns, int nb, unsigned magic, const int2 *__restrict__ tab,
+                                           const float2 *__restrict__ tw)
+{
+    const int total = L * nb;
+    for (int b = threadIdx.x; b < total; b += blockDim.x) {
+        int line = nb == 1 ? b : (int)__umulhi((unsigned)b, magic);
+        int j = b - line * nb;
+        int2 e = __ldg(tab + j);
+        const float2 *s = src + line * ss + j;
+        float2 v[RADIX];
+#pragma unroll
+        for (int r = 0; r < RADIX; ++r) v[r] = s[r * nb];
+#pragma unroll
+        for (int r = 1; r < RADIX; ++r) v[r] = cmul(v[r], __ldg(tw + r * e.x));
+        if (RADIX == 4) bfly4(v);
+        else if (RADIX == 2) bfly2(v);
+        else if (RADIX == 3) bfly3(v);
+        else bfly5(v);
+#pragma unroll
+        for (int r = 0; r < RADIX; ++r) {
+            float2 o = CONJ_OUT ? cconj(v[r]) : v[r];
+            int k = e.y + r * Ns;
+            if (MODE == 0) dst[line * ds + k] = o;
+            else if (MODE == 1) { if (k < keep) dst[k * L + line] = o; }
+            else rdst[line * ds + k] = o.x;
         }
     }
     __syncthreads();
+}
+
+template <int MODE, bool CONJ_OUT>
+__device__ __forceinline__ void fft_pass(int R, const float2 *src, float2 *dst, float *rdst, int L, int ss, int ds,
+                                         int keep, int Ns, int nb, unsigned magic, const int2 *tab, const float2 *tw)
+{
+    switch (R) {
+    case 4: fft_pass_r<4, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    case 2: fft_pass_r<2, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    case 3: fft_pass_r<3, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    default: fft_pass_r<5, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    }
+}
+
+// Full forward FFT of L lines (length p.n, contiguous, line stride n) held in a; b is scratch.
+// The last pass is stored in the mode given; returns the buffer holding the result.
+// conj_last conjugates the final output (second half of an inverse transform).
+template <int LAST_MODE, bool CONJ_LAST>
+__device__ float2 *fft_lines(const FftPlanDev &p, float2 *a, float2 *b, float *rdst, int L, int keep,
+                             const int2 *tab, const float2 *tw)
+{
+    float2 *src = a, *dst = b;
+    const int n = p.n;
+    for (int s = 0; s < p.nst; ++s) {
+        const int2 *t = tab + p.tab0 + p.off[s];
+        if (s + 1 < p.nst) {
+            fft_pass<0, false>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s], t, tw + p.tw0);
+        } else {
+            int ds = LAST_MODE == 1 ? 0 : n;
+            fft_pass<LAST_MODE, CONJ_LAST>(p.rad[s], src, dst, rdst, L, n, ds, keep, p.ns[s], p.nb[s], p.magic[s], t,
+                                           tw + p.tw0);
+        }
+        float2 *x = src; src = dst; dst = x;
+    }
+    return src;
+}
+
+__global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                     const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                                     const float2 *__restrict__ tw, const int2 *__restrict__ tab,
+                                                     const int *__restrict__ zstart, const int *__restrict__ zatoms,
+                                                     const float4 *__restrict__ fr, float2 *__restrict__ grid)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PlaneWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
+    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
+    unsigned long long *acc = (unsigned long long *)smem;
+    float2 *A = (float2 *)smem;                 // the accumulator bytes, reused after conversion
+    float2 *B = A + n1 * n2;
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0ull;
+    __syncthreads();
+    spread_plane<float>(R, w.z, zstart, zatoms, fr, acc);
+    __syncthreads();
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) {
+        float v = Acc<float>::get(acc[k]);
+        A[k] = make_float2(v, 0.f);
+    }
+    __syncthreads();
+    // x: n2 rows of n1 (real input); last pass keeps kx < n1h, transposed to [kx][y]
+    float2 *X = fft_lines<1, false>(p1, A, B, nullptr, n2, n1h, tab, tw);
+    // y: n1h lines of n2
+    float2 *Y = fft_lines<0, false>(p2, X, X == A ? B : A, nullptr, n1h, 0, tab, tw);
+    float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
+    for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) g[k] = Y[k];
+}
+
+__global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                 const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                                 const float2 *__restrict__ tw, const int2 *__restrict__ tab,
+                                                 const float *__restrict__ bsp_all, float2 *__restrict__ grid,
+                                                 double *__restrict__ e_col)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[256];
+    const ColWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
+    const int tk = min(NB_TKF, n2 - w.ky0);
+    const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
+    const float *bsp = bsp_all + R.bsp0;
+    float2 *A = (float2 *)smem, *B = A + NB_TKF * n3;
+    float2 *g = grid + R.g0 + (size_t)w.kx * n2 + w.ky0;
+    const size_t zs = (size_t)n1h * n2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int kz = warp; kz < n3; kz += 8)
+        if (lane < tk) A[lane * n3 + kz] = g[kz * zs + lane];
+    __syncthreads();
+    float2 *F = fft_lines<0, false>(p3, A, B, nullptr, tk, 0, tab, tw);
+    float2 *Fo = F == A ? B : A;
+    const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
+    float en = 0.f;
+    for (int c = warp; c < tk; c += 8) {
+        const int ky = w.ky0 + c;
+        for (int kz = lane; kz < n3; kz += 32) {
+            float et = eterm_of<float>(R, bsp, w.kx, ky, kz);
+            float2 v = F[c * n3 + kz];
+            en += wgt * et * (v.x * v.x + v.y * v.y);
+            F[c * n3 + kz] = make_float2(v.x * et, -v.y * et);    // conj: the inverse runs forward
+        }
+    }
+    __syncthreads();
+    float2 *I = fft_lines<0, true>(p3, F, Fo, nullptr, tk, 0, tab, tw);
+    for (int kz = warp; kz < n3; kz += 8)
+        if (lane < tk) g[kz * zs + lane] = I[lane * n3 + kz];
+    red[threadIdx.x] = (double)en;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) e_col[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                     const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                                     const float2 *__restrict__ tw, const int2 *__restrict__ tab,
+                                                     const int *__restrict__ zstart, const int *__restrict__ zatoms,
+                                                     const float4 *__restrict__ fr, const float2 *__restrict__ grid,
+                                                     float *__restrict__ part)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PlaneWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
+    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
+    float2 *P0 = (float2 *)smem, *P1 = P0 + n1 * n2, *Q = P1 + n1 * n2;
+    float *Rp = (float *)Q;       // the real plane reuses Q once Q has been read
+    const float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
+    // [kx][ky] lines of n2, conjugated (inverse through the forward transform)
+    for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) P0[k] = cconj(g[k]);
+    __syncthreads();
+    // y: n1h lines; last pass conjugates back and stores transposed to Q[ky][kx]
+    fft_lines<1, true>(p2, P0, P1, nullptr, n1h, n2, tab, tw);
+    // which buffer got the transposed result depends on the pass count
+    float2 *Yt = (p2.nst & 1) ? P1 : P0;
+    // expand each ky row to the full Hermitian line of n1, conjugated again for the inverse
+    float2 *Xs = Yt == P0 ? P1 : P0;
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) {
+        int ky = k / n1, i = k - ky * n1;
+        float2 v = i < n1h ? Yt[ky * n1h + i] : cconj(Yt[ky * n1h + (n1 - i)]);
+        Xs[k] = cconj(v);
+    }
+    __syncthreads();
+    // x: n2 lines of n1; the last pass stores real parts into Rp[ky][x]
+    fft_lines<2, false>(p1, Xs, Yt, Rp, n2, 0, tab, tw);
+    gather_plane<float>(R, w.z, zstart, zatoms, fr, Rp, part);
+}
+
+// =================================================================================
+// FP64 (plain) path: one warp per line, same grid layout [z][kx][ky]
+
+template <typename C>
+__device__ C *warp_fft(C *x, C *y, const FftPlanDev &p, const C *__restrict__ tw, int lane)
+{
+    int n = p.n, Ns = 1;
+    for (int st = 0; st < p.nst; ++st) {
+        int R = p.rad[st], nb = n / R, stride = n / (Ns * R);
+        for (int j = lane; j < nb; j += 32) {
+            C v[5];
+            int jm = j % Ns;
+            for (int r = 0; r < R; ++r) v[r] = x[j + r * nb];
+            int tstep = jm * stride;
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * tstep]);
+            if (R == 4) bfly4(v);
+            else if (R == 2) bfly2(v);
+            else if (R == 3) bfly3(v);
+            else bfly5(v);
+            int idxD = (j / Ns) * Ns * R + jm;
+            for (int r = 0; r < R; ++r) y[idxD + r * Ns] = v[r];
+        }
+        __syncwarp();
+        C *t = x; x = y; y = t;
+        Ns *= R;
+    }
+    return x;
+}
+
+#define NB_TK 16
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_plane_fwd(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                   const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
+                                                   const void *tw_v, const int *__restrict__ zstart,
+                                                   const int *__restrict__ zatoms, const void *fr_v, void *grid_v)
+{
+    typedef typename cplx<T>::type C;
+    typedef typename Acc<T>::type A;
+    extern __shared__ __align__(16) unsigned char smem[];
+    PlaneWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h, pitch = n1h | 1;
+    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
+    const C *tw = (const C *)tw_v;
+    A *acc = (A *)smem;
+    C *P = (C *)(smem + align16(sizeof(A) * n1 * n2));
+    C *scr = P + n2 * pitch;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
+    __syncthreads();
+    spread_plane<T>(R, w.z, zstart, zatoms, (const typename vec4<T>::type *)fr_v, acc);
+    __syncthreads();
     C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
-    // R2C along x (C2C of the real row, first n1/2+1 outputs kept)
     for (int j = warp; j < n2; j += nwarp) {
-        for (int i = lane; i < n1; i += 32) x[i] = cmk<C>((double)Acc<T>::get(acc[j * n1 + i]), 0.0);
+        for (int i = lane; i < n1; i += 32) { x[i].x = Acc<T>::get(acc[j * n1 + i]); x[i].y = 0; }
         __syncwarp();
         C *res = warp_fft<C>(x, y, p1, tw + p1.tw0, lane);
         for (int k = lane; k < n1h; k += 32) P[j * pitch + k] = res[k];
         __syncwarp();
     }
     __syncthreads();
-    // C2C along y
     for (int k = warp; k < n1h; k += nwarp) {
         for (int j = lane; j < n2; j += 32) x[j] = P[j * pitch + k];
         __syncwarp();
@@ -262,12 +526,10 @@ __global__ void __launch_bounds__(256) k_plane_fwd(const PlaneWork *__restrict__
     __syncthreads();
     C *g = (C *)grid_v + R.g0 + (size_t)w.z * n2 * n1h;
     for (int idx = threadIdx.x; idx < n2 * n1h; idx += blockDim.x) {
-        int ky = idx / n1h, kx = idx - ky * n1h;
+        int kx = idx / n2, ky = idx - kx * n2;
         g[idx] = P[ky * pitch + kx];
     }
 }
-
-#define NB_TK 16
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
@@ -281,7 +543,7 @@ __global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work,
     ColWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
-    const int tk = min(NB_TK, n1h - w.kx0);
+    const int tk = min(NB_TK, n2 - w.ky0);
     const int n3p = n3 | 1;
     const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
     const C *tw = (const C *)tw_v;
@@ -289,37 +551,28 @@ __global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work,
     C *tile = (C *)smem;
     C *scr = tile + NB_TK * n3p;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    C *g = (C *)grid_v + R.g0;
+    C *g = (C *)grid_v + R.g0 + (size_t)w.kx * n2 + w.ky0;
+    const size_t zs = (size_t)n1h * n2;
     for (int idx = threadIdx.x; idx < tk * n3; idx += blockDim.x) {
         int kz = idx / tk, c = idx - kz * tk;
-        tile[c * n3p + kz] = g[((size_t)kz * n2 + w.ky) * n1h + w.kx0 + c];
+        tile[c * n3p + kz] = g[kz * zs + c];
     }
     __syncthreads();
     double en = 0;
     C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
-    const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
-    const int m2 = w.ky < nf2 ? w.ky : w.ky - n2;
-    const T mh2 = (T)m2 * rep_invL<T>(R, 1);
-    const T fac = (T)R.pme_fac, pivol = (T)R.pivol;
+    const T wgt = (w.kx == 0 || (2 * w.kx == n1)) ? (T)1 : (T)2;
     for (int c = warp; c < tk; c += nwarp) {
-        const int kx = w.kx0 + c;
+        const int ky = w.ky0 + c;
         for (int kz = lane; kz < n3; kz += 32) x[kz] = tile[c * n3p + kz];
         __syncwarp();
         C *res = warp_fft<C>(x, y, p3, tw + p3.tw0, lane);
-        const T mh1 = (T)kx * rep_invL<T>(R, 0);
-        const T wgt = (kx == 0 || (2 * kx == n1)) ? (T)1 : (T)2;
-        const T b12 = bsp[kx] * bsp[n1 + w.ky];
         for (int kz = lane; kz < n3; kz += 32) {
-            int m3 = kz < nf3 ? kz : kz - n3;
-            T mh3 = (T)m3 * rep_invL<T>(R, 2);
-            T msq = mh1 * mh1 + mh2 * mh2 + mh3 * mh3;
-            T eterm = (T)0;
-            if (kx != 0 || w.ky != 0 || kz != 0) eterm = exp(-fac * msq) / (pivol * b12 * bsp[n1 + n2 + kz] * msq);
+            T et = eterm_of<T>(R, bsp, w.kx, ky, kz);
             C v = res[kz];
-            en += (double)(wgt * eterm * (v.x * v.x + v.y * v.y));
-            v.x *= eterm;
-            v.y *= eterm;
-            res[kz] = cconj(v);      // inverse = conj(FFT(conj(.)))
+            en += (double)(wgt * et * (v.x * v.x + v.y * v.y));
+            v.x *= et;
+            v.y *= et;
+            res[kz] = cconj(v);
         }
         __syncwarp();
         C *other = (res == x) ? y : x;
@@ -330,7 +583,7 @@ __global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work,
     __syncthreads();
     for (int idx = threadIdx.x; idx < tk * n3; idx += blockDim.x) {
         int kz = idx / tk, c = idx - kz * tk;
-        g[((size_t)kz * n2 + w.ky) * n1h + w.kx0 + c] = tile[c * n3p + kz];
+        g[kz * zs + c] = tile[c * n3p + kz];
     }
     red[threadIdx.x] = en;
     __syncthreads();
@@ -349,11 +602,10 @@ __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__
                                                    const void *grid_v, T *__restrict__ part)
 {
     typedef typename cplx<T>::type C;
-    typedef typename vec4<T>::type T4;
     extern __shared__ __align__(16) unsigned char smem[];
     PlaneWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
-    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h, pitch = n1h | 1;
+    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h, pitch = n1h | 1;
     const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
     const C *tw = (const C *)tw_v;
     T *Rp = (T *)smem;
@@ -362,12 +614,11 @@ __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const C *g = (const C *)grid_v + R.g0 + (size_t)w.z * n2 * n1h;
     for (int idx = threadIdx.x; idx < n2 * n1h; idx += blockDim.x) {
-        int ky = idx / n1h, kx = idx - ky * n1h;
+        int kx = idx / n2, ky = idx - kx * n2;
         P[ky * pitch + kx] = g[idx];
     }
     __syncthreads();
     C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
-    // inverse C2C along y
     for (int k = warp; k < n1h; k += nwarp) {
         for (int j = lane; j < n2; j += 32) x[j] = cconj(P[j * pitch + k]);
         __syncwarp();
@@ -376,7 +627,6 @@ __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__
         __syncwarp();
     }
     __syncthreads();
-    // C2R along x: Hermitian row, inverse C2C, real part
     for (int j = warp; j < n2; j += nwarp) {
         for (int i = lane; i < n1; i += 32) {
             C v = i < n1h ? P[j * pitch + i] : cconj(P[j * pitch + (n1 - i)]);
@@ -384,49 +634,15 @@ __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__
         }
         __syncwarp();
         C *res = warp_fft<C>(x, y, p1, tw + p1.tw0, lane);
-        for (int i = lane; i < n1; i += 32) Rp[j * n1 + i] = res[i].x;   // real part of conj(.) unchanged
+        for (int i = lane; i < n1; i += 32) Rp[j * n1 + i] = res[i].x;
         __syncwarp();
     }
     __syncthreads();
-    // gradient share of this plane for every atom whose z stencil touches it
-    const T4 *fr = (const T4 *)fr_v;
-    for (int tp = 0; tp < 4; ++tp) {
-        int zb = w.z + tp;
-        zb = zb >= n3 ? zb - n3 : zb;
-        int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
-        int t3 = 3 - tp;
-        for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
-            int s = zatoms[idx];
-            T4 f = fr[s];
-            int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
-            T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
-            bspline4<T>(f.x - (T)i1, th1, dt1);
-            bspline4<T>(f.y - (T)i2, th2, dt2);
-            bspline4<T>(f.z - (T)i3, th3, dt3);
-            T gx = 0, gy = 0, gz = 0;
-#pragma unroll
-            for (int t2 = 0; t2 < 4; ++t2) {
-                int j = (i2 - 3 + t2 + 2 * n2) % n2;
-                const T *row = Rp + j * n1;
-                T sx = 0, sy = 0;
-#pragma unroll
-                for (int t1 = 0; t1 < 4; ++t1) {
-                    int i = (i1 - 3 + t1 + 2 * n1) % n1;
-                    T q = row[i];
-                    sx += q * dt1[t1];
-                    sy += q * th1[t1];
-                }
-                gx += sx * th2[t2];
-                gy += sy * dt2[t2];
-                gz += sy * th2[t2];
-            }
-            T *o = part + 12 * (size_t)s + 3 * t3;
-            o[0] = gx * th3[t3];
-            o[1] = gy * th3[t3];
-            o[2] = gz * dt3[t3];
-        }
-    }
+    gather_plane<T>(R, w.z, zstart, zatoms, (const typename vec4<T>::type *)fr_v, Rp, part);
 }
+
+// ---------------------------------------------------------------------------------
+// launch sequence (both precisions)
 
 template <typename T>
 void pme_t(NbCtx *c)
@@ -440,21 +656,38 @@ void pme_t(NbCtx *c)
     nb_exclusive_scan(c, c->d_zcount, c->d_zstart, c->nzbin, nullptr);
     k_pme_scatter<<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_reps, c->d_fr,
                                                              sizeof(T) == 8, c->d_zstart, c->d_zslot, c->d_zatoms);
-    k_plane_fwd<T><<<(int)c->planes.size(), 256, c->smem_plane_fwd, s>>>(
-        c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw, c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid);
-    if (c->timing) cudaEventRecord(c->ev[7], s);
-    k_zconv<T><<<(int)c->cols.size(), 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan,
-                                                                c->d_tw, c->d_bsp, c->d_grid, c->d_e_col);
-    if (c->timing) cudaEventRecord(c->ev[8], s);
-    k_plane_inv<T><<<(int)c->planes.size(), 256, c->smem_plane_inv, s>>>(
-        c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw, c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid,
-        (T *)c->d_part);
+    const int np = (int)c->planes.size(), nc = (int)c->cols.size();
+    if (sizeof(T) == 4) {
+        k_plane_fwd_f<<<np, 256, c->smem_plane_fwd, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                           (const float2 *)c->d_tw, c->d_tab, c->d_zstart,
+                                                           c->d_zatoms, (const float4 *)c->d_fr, (float2 *)c->d_grid);
+        if (c->timing) cudaEventRecord(c->ev[7], s);
+        k_zconv_f<<<nc, 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                  (const float2 *)c->d_tw, c->d_tab, (const float *)c->d_bsp,
+                                                  (float2 *)c->d_grid, c->d_e_col);
+        if (c->timing) cudaEventRecord(c->ev[8], s);
+        k_plane_inv_f<<<np, 256, c->smem_plane_inv, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                           (const float2 *)c->d_tw, c->d_tab, c->d_zstart,
+                                                           c->d_zatoms, (const float4 *)c->d_fr,
+                                                           (const float2 *)c->d_grid, (float *)c->d_part);
+    } else {
+        k_plane_fwd<T><<<np, 256, c->smem_plane_fwd, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw,
+                                                          c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid);
+        if (c->timing) cudaEventRecord(c->ev[7], s);
+        k_zconv<T><<<nc, 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw,
+                                                   c->d_bsp, c->d_grid, c->d_e_col);
+        if (c->timing) cudaEventRecord(c->ev[8], s);
+        k_plane_inv<T><<<np, 256, c->smem_plane_inv, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw,
+                                                          c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid,
+                                                          (T *)c->d_part);
+    }
     if (c->timing) cudaEventRecord(c->ev[9], s);
     c->launches += 6;
 }
 
-// radix plan: 4s first, then 2, 3, 5; returns 0 if n is not 2/3/5-smooth or too long
-int make_plan(int n, FftPlanDev *p)
+// radix plan and Stockham tables: 4s first, then 2, 3, 5; returns 0 if n is not
+// 2/3/5-smooth or too long.  tab receives (twiddle step, destination index) per butterfly.
+int make_plan(int n, FftPlanDev *p, std::vector<int2> *tab)
 {
     memset(p, 0, sizeof(*p));
     p->n = n;
@@ -466,12 +699,29 @@ int make_plan(int n, FftPlanDev *p)
     while (m % 5 == 0) { p->rad[k++] = 5; m /= 5; }
     if (m != 1 || k > 8) return 0;
     p->nst = k;
+    int Ns = 1, off = 0;
+    for (int s = 0; s < k; ++s) {
+        int R = p->rad[s], nb = n / R, stride = n / (Ns * R);
+        p->ns[s] = Ns;
+        p->nb[s] = nb;
+        p->off[s] = off;
+        p->magic[s] = nb > 1 ? 0xFFFFFFFFu / (unsigned)nb + 1u : 0u;
+        if (tab) {
+            for (int j = 0; j < nb; ++j) {
+                int jm = j % Ns;
+                tab->push_back(make_int2(jm * stride, (j / Ns) * Ns * R + jm));
+            }
+        }
+        off += nb;
+        Ns *= R;
+    }
     return 1;
 }
 
 template <typename T>
 size_t plane_fwd_smem(int n1, int n2)
 {
+    if (sizeof(T) == 4) return (size_t)2 * n1 * n2 * sizeof(float2);
     typedef typename cplx<T>::type C;
     size_t acc = (sizeof(typename Acc<T>::type) * n1 * n2 + 15) & ~(size_t)15;
     return acc + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -479,6 +729,7 @@ size_t plane_fwd_smem(int n1, int n2)
 template <typename T>
 size_t plane_inv_smem(int n1, int n2)
 {
+    if (sizeof(T) == 4) return (size_t)(2 * n1 + (n1 / 2 + 1)) * n2 * sizeof(float2);
     typedef typename cplx<T>::type C;
     size_t r = (sizeof(T) * n1 * n2 + 15) & ~(size_t)15;
     return r + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -486,9 +737,11 @@ size_t plane_inv_smem(int n1, int n2)
 template <typename T>
 size_t zconv_smem(int n3)
 {
+    if (sizeof(T) == 4) return (size_t)2 * NB_TKF * n3 * sizeof(float2);
     typedef typename cplx<T>::type C;
     return sizeof(C) * NB_TK * (n3 | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
 }
+template <typename T> int col_tile() { return sizeof(T) == 4 ? NB_TKF : NB_TK; }
 
 // raise a kernel's dynamic shared-memory limit to at least `bytes` (never lower it)
 template <typename K>
@@ -502,13 +755,27 @@ cudaError_t raise_smem_limit(K *kernel, size_t bytes)
 }
 
 template <typename T>
+cudaError_t raise_pme_limits(size_t sf, size_t sz, size_t si)
+{
+    cudaError_t e;
+    if (sizeof(T) == 4) {
+        if ((e = raise_smem_limit(k_plane_fwd_f, sf)) != cudaSuccess) return e;
+        if ((e = raise_smem_limit(k_zconv_f, sz)) != cudaSuccess) return e;
+        return raise_smem_limit(k_plane_inv_f, si);
+    }
+    if ((e = raise_smem_limit(k_plane_fwd<T>, sf)) != cudaSuccess) return e;
+    if ((e = raise_smem_limit(k_zconv<T>, sz)) != cudaSuccess) return e;
+    return raise_smem_limit(k_plane_inv<T>, si);
+}
+
+template <typename T>
 int configure_t(NbCtx *c)
 {
     typedef typename cplx<T>::type C;
-    // plans for each distinct length
     c->plans.clear();
     c->rep_plan.assign(3 * c->nrep, 0);
     std::vector<double> twr, twi;
+    std::vector<int2> tab;
     for (int r = 0; r < c->nrep; ++r) {
         int ns[3] = {c->rd[r].n1, c->rd[r].n2, c->rd[r].n3};
         for (int d = 0; d < 3; ++d) {
@@ -517,7 +784,9 @@ int configure_t(NbCtx *c)
                 if (c->plans[k].n == ns[d]) found = (int)k;
             if (found < 0) {
                 FftPlanDev p;
-                if (!make_plan(ns[d], &p)) return MOIL_NB_ERR_GRID;
+                int tab0 = (int)tab.size();
+                if (!make_plan(ns[d], &p, &tab)) return MOIL_NB_ERR_GRID;
+                p.tab0 = tab0;
                 p.tw0 = (int)twr.size();
                 for (int t = 0; t < ns[d]; ++t) {
                     double ang = -2.0 * M_PI * (double)t / (double)ns[d];
@@ -538,21 +807,24 @@ int configure_t(NbCtx *c)
     NB_CUDA_OK(c, cudaMemcpy(c->d_rep_plan, c->rep_plan.data(), sizeof(int) * c->rep_plan.size(), cudaMemcpyHostToDevice));
     NB_CUDA_OK(c, cudaMalloc(&c->d_tw, sizeof(C) * tw.size()));
     NB_CUDA_OK(c, cudaMemcpy(c->d_tw, tw.data(), sizeof(C) * tw.size(), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_tab, sizeof(int2) * tab.size()));
+    NB_CUDA_OK(c, cudaMemcpy(c->d_tab, tab.data(), sizeof(int2) * tab.size(), cudaMemcpyHostToDevice));
     std::vector<T> bsp(c->bsp_h.size());
     for (size_t k = 0; k < bsp.size(); ++k) bsp[k] = (T)c->bsp_h[k];
     NB_CUDA_OK(c, cudaMalloc(&c->d_bsp, sizeof(T) * bsp.size()));
     NB_CUDA_OK(c, cudaMemcpy(c->d_bsp, bsp.data(), sizeof(T) * bsp.size(), cudaMemcpyHostToDevice));
-    // work lists
+    // work lists: planes (replica, z) and z columns (replica, kx, ky run)
     c->planes.clear();
     c->cols.clear();
     c->col_begin.assign(c->nrep + 1, 0);
     size_t sf = 0, si = 0, sz = 0;
+    const int tk = col_tile<T>();
     for (int r = 0; r < c->nrep; ++r) {
         const RepDev &R = c->rd[r];
         for (int z = 0; z < R.n3; ++z) c->planes.push_back(PlaneWork{r, z});
         c->col_begin[r] = (int)c->cols.size();
-        for (int ky = 0; ky < R.n2; ++ky)
-            for (int kx0 = 0; kx0 < R.n1h; kx0 += NB_TK) c->cols.push_back(ColWork{r, ky, kx0});
+        for (int kx = 0; kx < R.n1h; ++kx)
+            for (int ky0 = 0; ky0 < R.n2; ky0 += tk) c->cols.push_back(ColWork{r, kx, ky0});
         sf = std::max(sf, plane_fwd_smem<T>(R.n1, R.n2));
         si = std::max(si, plane_inv_smem<T>(R.n1, R.n2));
         sz = std::max(sz, zconv_smem<T>(R.n3));
@@ -560,14 +832,15 @@ int configure_t(NbCtx *c)
     c->col_begin[c->nrep] = (int)c->cols.size();
     int dev_smem = 0;
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-    if ((int)sf > dev_smem || (int)si > dev_smem || (int)sz > dev_smem) return MOIL_NB_ERR_GRID;
+    if ((int)sf > dev_smem || (int)si > dev_smem || (int)sz > dev_smem) {
+        c->err = "PME grid plane does not fit in shared memory";
+        return MOIL_NB_ERR_GRID;
+    }
     c->smem_plane_fwd = sf;
     c->smem_plane_inv = si;
     c->smem_zconv = sz;
     // the limit is per kernel, shared by every handle in the process: only ever raise it
-    NB_CUDA_OK(c, raise_smem_limit(k_plane_fwd<T>, sf));
-    NB_CUDA_OK(c, raise_smem_limit(k_plane_inv<T>, si));
-    NB_CUDA_OK(c, raise_smem_limit(k_zconv<T>, sz));
+    NB_CUDA_OK(c, raise_pme_limits<T>(sf, sz, si));
     NB_CUDA_OK(c, cudaMalloc(&c->d_planes, sizeof(PlaneWork) * c->planes.size()));
     NB_CUDA_OK(c, cudaMemcpy(c->d_planes, c->planes.data(), sizeof(PlaneWork) * c->planes.size(), cudaMemcpyHostToDevice));
     NB_CUDA_OK(c, cudaMalloc(&c->d_cols, sizeof(ColWork) * c->cols.size()));
@@ -599,17 +872,17 @@ int nb_pme_configure(NbCtx *c)
 // Allocation-free PME reciprocal sum (moil_nb_pme_noalloc).
 //
 // For callers that cannot allocate device memory: the same bin / spread+FFT / convolution /
-// FFT+gather kernels as the handle path, with every scratch buffer carved out of one
+// FFT+gather kernels as the handle path (FP32), with every scratch buffer carved out of one
 // file-scope device array.  The array is sized for at most NA_MAX_ATOMS atoms and PME
 // grids of at most NA_MAX_N points per side; every GPU that loads this library holds it
 // (about 7.5 MB) until the process exits.
-#include <mutex>
 
 namespace {
 
 constexpr int NA_MAX_ATOMS = 65536;
 constexpr int NA_MAX_N = 64;
-constexpr int NA_MAX_COLS = NA_MAX_N * ((NA_MAX_N / 2 + 1 + NB_TK - 1) / NB_TK);
+constexpr int NA_MAX_COLS = (NA_MAX_N / 2 + 1) * ((NA_MAX_N + NB_TKF - 1) / NB_TKF);
+constexpr int NA_MAX_TAB = 3 * 8 * NA_MAX_N;
 constexpr size_t na_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // arena regions (byte offsets, 256-byte aligned)
@@ -630,7 +903,8 @@ constexpr size_t NA_COLBEG = NA_COLS + na_up(sizeof(ColWork) * NA_MAX_COLS);
 constexpr size_t NA_PLANS = NA_COLBEG + na_up(sizeof(int) * 2);
 constexpr size_t NA_REPPLAN = NA_PLANS + na_up(sizeof(FftPlanDev) * 3);
 constexpr size_t NA_TW = NA_REPPLAN + na_up(sizeof(int) * 3);
-constexpr size_t NA_BSP = NA_TW + na_up(sizeof(float2) * 3 * NA_MAX_N);
+constexpr size_t NA_TAB = NA_TW + na_up(sizeof(float2) * 3 * NA_MAX_N);
+constexpr size_t NA_BSP = NA_TAB + na_up(sizeof(int2) * NA_MAX_TAB);
 constexpr size_t NA_REPS = NA_BSP + na_up(sizeof(float) * 3 * NA_MAX_N);
 constexpr size_t NA_EOUT = NA_REPS + na_up(sizeof(RepDev));
 constexpr size_t NA_STATUS = NA_EOUT + na_up(sizeof(double));
@@ -714,7 +988,8 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     if (natom < 1 || natom > NA_MAX_ATOMS || !(alpha > 0) || !(eps > 0)) return MOIL_NB_ERR_ARG;
     for (int d = 0; d < 3; ++d) {
         FftPlanDev p;
-        if (!(box[d] > 0) || grid[d] < 4 || grid[d] > NA_MAX_N || !make_plan(grid[d], &p)) return MOIL_NB_ERR_GRID;
+        if (!(box[d] > 0) || grid[d] < 4 || grid[d] > NA_MAX_N || !make_plan(grid[d], &p, nullptr))
+            return MOIL_NB_ERR_GRID;
     }
     cudaStream_t stream = (cudaStream_t)stream_v;
     int dev = 0;
@@ -733,11 +1008,10 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     }
     const int n1 = grid[0], n2 = grid[1], n3 = grid[2];
     // shared-memory limits for this grid (raise only; other handles may need more)
-    if (raise_smem_limit(k_plane_fwd<float>, plane_fwd_smem<float>(n1, n2)) != cudaSuccess ||
-        raise_smem_limit(k_plane_inv<float>, plane_inv_smem<float>(n1, n2)) != cudaSuccess ||
-        raise_smem_limit(k_zconv<float>, zconv_smem<float>(n3)) != cudaSuccess)
+    if (raise_pme_limits<float>(plane_fwd_smem<float>(n1, n2), zconv_smem<float>(n3),
+                                plane_inv_smem<float>(n1, n2)) != cudaSuccess)
         return MOIL_NB_ERR_CUDA;
-    // one-replica constants, FFT plans and twiddles, B-spline moduli, work lists (host side)
+    // one-replica constants, FFT plans and tables, B-spline moduli, work lists (host side)
     RepDev R;
     memset(&R, 0, sizeof(R));
     for (int d = 0; d < 3; ++d) {
@@ -759,10 +1033,13 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     FftPlanDev plans[3];
     int rep_plan[3];
     float2 tw[3 * NA_MAX_N];
+    std::vector<int2> tab;
     float bsp[3 * NA_MAX_N];
     int ntw = 0;
     for (int d = 0; d < 3; ++d) {
-        make_plan(grid[d], &plans[d]);
+        int tab0 = (int)tab.size();
+        make_plan(grid[d], &plans[d], &tab);
+        plans[d].tab0 = tab0;
         plans[d].tw0 = ntw;
         for (int t = 0; t < grid[d]; ++t) {
             double ang = -2.0 * M_PI * (double)t / (double)grid[d];
@@ -770,6 +1047,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
         }
         rep_plan[d] = d;
     }
+    if ((int)tab.size() > NA_MAX_TAB) return MOIL_NB_ERR_GRID;
     na_bsp_moduli(n1, bsp);
     na_bsp_moduli(n2, bsp + n1);
     na_bsp_moduli(n3, bsp + n1 + n2);
@@ -779,8 +1057,8 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     tmp.nsite = natom;
     tmp.nzbin = n3;
     for (int z = 0; z < n3; ++z) tmp.planes.push_back(PlaneWork{0, z});
-    for (int ky = 0; ky < n2; ++ky)
-        for (int kx0 = 0; kx0 < R.n1h; kx0 += NB_TK) tmp.cols.push_back(ColWork{0, ky, kx0});
+    for (int kx = 0; kx < R.n1h; ++kx)
+        for (int ky0 = 0; ky0 < n2; ky0 += NB_TKF) tmp.cols.push_back(ColWork{0, kx, ky0});
     int col_begin[2] = {0, (int)tmp.cols.size()};
     tmp.smem_plane_fwd = plane_fwd_smem<float>(n1, n2);
     tmp.smem_plane_inv = plane_inv_smem<float>(n1, n2);
@@ -802,6 +1080,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     tmp.d_plans = (FftPlanDev *)(base + NA_PLANS);
     tmp.d_rep_plan = (int *)(base + NA_REPPLAN);
     tmp.d_tw = base + NA_TW;
+    tmp.d_tab = (int2 *)(base + NA_TAB);
     tmp.d_bsp = base + NA_BSP;
     tmp.d_reps = (RepDev *)(base + NA_REPS);
     tmp.d_status = (int *)(base + NA_STATUS);
@@ -813,6 +1092,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     NA_CP(tmp.d_plans, plans, sizeof(plans));
     NA_CP(tmp.d_rep_plan, rep_plan, sizeof(rep_plan));
     NA_CP(tmp.d_tw, tw, sizeof(float2) * ntw);
+    NA_CP(tmp.d_tab, tab.data(), sizeof(int2) * tab.size());
     NA_CP(tmp.d_bsp, bsp, sizeof(float) * (n1 + n2 + n3));
     NA_CP(tmp.d_planes, tmp.planes.data(), sizeof(PlaneWork) * tmp.planes.size());
     NA_CP(tmp.d_cols, tmp.cols.data(), sizeof(ColWork) * tmp.cols.size());
