@@ -173,6 +173,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     std::vector<std::vector<int>> exn, p14n;
     std::vector<std::vector<double>> p14p;
     int64_t atom0 = 0, wat0 = 0, oth0 = 0, zb0 = 0, g0 = 0;
+    int water_fast = 1;
     int cell0 = 0;
     for (int r = 0; r < nrep; ++r) {
         const moil_nb_params *p = reps[r].params;
@@ -206,6 +207,10 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
                 for (int k = first; k <= last; ++k) is_w[k] = 1;
                 ++nwat;
                 last_o = first;
+                // the per-molecule correction kernel needs exactly the three pairs, once each
+                if (t->exc1[first] - t->exc1[first - 1] != 2 || t->exc1[first + 1] - t->exc1[first] != 1 ||
+                    t->exc1[first + 2] - t->exc1[first + 1] != 0)
+                    water_fast = 0;
             }
         }
         // exclusions: water atoms only with their own molecule
@@ -339,6 +344,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         for (int k = 0; k < t->totspe; ++k) {
             int j = t->spec1[k], l = t->spec2[k];
             if (j < 1 || j > t->npt || l < 1 || l > t->npt) { c->err = "1-4 partner out of range"; return MOIL_NB_ERR_ARG; }
+            if (is_w[j] || is_w[l]) water_fast = 0;
             for (int side = 0; side < 2; ++side) {
                 int a = side ? l : j, b = side ? j : l;
                 p14n[base + a - 1].push_back((int)(atom0 + b - 1));
@@ -415,7 +421,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl1_off, sizeof(int) * (c->nW + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl2_off, sizeof(int) * (c->nW + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl_off, sizeof(int) * (c->nA + 1)));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_count_tmp, sizeof(int) * (2 * std::max(c->nW, c->nA) + 2)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_count_tmp, sizeof(int) * (3 * std::max(c->nW, c->nA) + 3)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_grad_site, sizeof(long long) * 3 * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_e_unit, sizeof(double) * NB_EU * std::max<int64_t>(nu, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_grad_ex, sizeof(double) * 3 * c->natom));
@@ -446,6 +452,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaDeviceSynchronize());
     c->need_rebuild = 1;
     c->evals_since_build = 0;
+    c->water_excl_fast = water_fast;
     c->inited = 1;
     return MOIL_NB_OK;
 }

@@ -47,6 +47,7 @@ struct NbCtx {
     int64_t natom = 0, nW = 0, nA = 0, nsite = 0, nunit = 0;
     float skin = 1.0f, rwat = 1.1f;
     int list_period = 0;
+    int water_excl_fast = 0;      // every water's exclusions are exactly O-H1, O-H2, H1-H2
 
     // static per caller atom
     double *d_q = nullptr;        // charges

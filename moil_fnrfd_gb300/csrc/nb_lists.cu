@@ -200,10 +200,12 @@ __device__ __forceinline__ bool nb_excluded(const int *__restrict__ ex_off, cons
 template <typename T, int FILL>
 __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep, const void *pos_v,
                         const int *__restrict__ bin_start, int ncell, const int *__restrict__ sorted,
-                        int *__restrict__ cnt1, int *__restrict__ cnt2, const int *__restrict__ off1,
-                        const int *__restrict__ off2, int *__restrict__ l1, int *__restrict__ l2, int64_t cap1,
-                        int64_t cap2, int *st)
+                        int *__restrict__ cnt1, int *__restrict__ cnt2, int *__restrict__ cntn,
+                        const int *__restrict__ off1, const int *__restrict__ off2, int *__restrict__ l1,
+                        int *__restrict__ l2, int64_t cap1, int64_t cap2, int *st)
 {
+    // W1 entries are stored in two groups: molecules already inside the cutoff at build
+    // time first, skin-only molecules after them, so lanes of a warp stay converged
     if (rebuild_off(st)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nW) return;
@@ -215,9 +217,9 @@ __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__re
     cell_of<T>(R, oi.x, oi.y, oi.z, ci);
     int nx = nb_axis_cells(ci[0], R.nc[0], cx), ny = nb_axis_cells(ci[1], R.nc[1], cy),
         nz = nb_axis_cells(ci[2], R.nc[2], cz);
-    int n1 = 0, n2 = 0;
-    int w1 = FILL ? off1[i] : 0, w2 = FILL ? off2[i] : 0;
-    T rl2 = (T)R.rlist2, rw2 = (T)R.rlistw2;
+    int n1 = 0, n2 = 0, nn = 0;
+    int w1 = FILL ? off1[i] : 0, w2 = FILL ? off2[i] : 0, wf = FILL ? off1[i] + cntn[i] : 0;
+    T rl2 = (T)R.rlist2, rw2 = (T)R.rlistw2, rc2 = (T)R.rmax2;
     int nW_i = nW;
     for (int a = 0; a < nz; ++a)
         for (int b = 0; b < ny; ++b)
@@ -227,8 +229,14 @@ __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__re
                 for (int p = bin_start[cell]; p < bin_start[cell + 1]; ++p) {
                     if (p == i) continue;
                     T4 oj = pos[3 * p];
-                    if (mi_r2<T>(R, oi.x - oj.x, oi.y - oj.y, oi.z - oj.z) < rl2) {
-                        if (FILL) { if (w1 + n1 < cap1) l1[w1 + n1] = p; }
+                    T r2 = mi_r2<T>(R, oi.x - oj.x, oi.y - oj.y, oi.z - oj.z);
+                    if (r2 < rl2) {
+                        bool near = r2 <= rc2;
+                        if (FILL) {
+                            int at = near ? w1 + nn : wf + (n1 - nn);
+                            if (at < cap1) l1[at] = p;
+                        }
+                        nn += near;
                         n1++;
                     }
                 }
@@ -242,7 +250,7 @@ __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__re
                     }
                 }
             }
-    if (!FILL) { cnt1[i] = n1; cnt2[i] = n2; }
+    if (!FILL) { cnt1[i] = n1; cnt2[i] = n2; cntn[i] = nn; }
     else if ((int64_t)w1 + n1 > cap1 || (int64_t)w2 + n2 > cap2) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
 }
 
@@ -367,14 +375,16 @@ void build_lists_t(NbCtx *c, const double *d_coor)
     if (c->nW > 0) {
         int nb = (int)((c->nW + 127) / 128);
         k_wlist<T, 0><<<nb, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         c->d_sorted_unit, c->d_count_tmp, c->d_count_tmp + c->nW + 1, nullptr,
-                                         nullptr, nullptr, nullptr, 0, 0, c->d_status);
+                                         c->d_sorted_unit, c->d_count_tmp, c->d_count_tmp + c->nW + 1,
+                                         c->d_count_tmp + 2 * (c->nW + 1), nullptr, nullptr, nullptr, nullptr, 0, 0,
+                                         c->d_status);
         k_scan<<<1, 1024, 0, s>>>(c->d_count_tmp, c->d_wl1_off, (int)c->nW, c->d_status + 2, c->d_status, 1);
         k_scan<<<1, 1024, 0, s>>>(c->d_count_tmp + c->nW + 1, c->d_wl2_off, (int)c->nW, c->d_status + 3,
                                   c->d_status, 1);
         k_wlist<T, 1><<<nb, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         c->d_sorted_unit, nullptr, nullptr, c->d_wl1_off, c->d_wl2_off, c->d_wl1,
-                                         c->d_wl2, c->cap_wl1, c->cap_wl2, c->d_status);
+                                         c->d_sorted_unit, nullptr, nullptr, c->d_count_tmp + 2 * (c->nW + 1),
+                                         c->d_wl1_off, c->d_wl2_off, c->d_wl1, c->d_wl2, c->cap_wl1, c->cap_wl2,
+                                         c->d_status);
         c->launches += 4;
     }
     if (c->nA > 0) {

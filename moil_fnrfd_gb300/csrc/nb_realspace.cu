@@ -117,31 +117,47 @@ __device__ __forceinline__ void flush(double g[], long long G[], int n)
 }
 
 // ---------------------------------------------------------------------------------
-// water molecule per thread: W1 (water-water, 9 site pairs) then W2 (water-site x other)
+// water molecule per thread: W1 (water-water, 9 site pairs) then W2 (water-site x other).
+// Per-lane FP32 partial gradients and energies are flushed every CHUNK list entries into
+// int64 / FP64 accumulators kept in shared memory (one column per thread), which keeps
+// them out of the register file.
+#define WBLOCK 128
 template <typename T>
-__global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
-                                               const void *pos_v, const void *woff_v, const void *lj_v,
-                                               const unsigned *__restrict__ sflags,
-                                               const int *__restrict__ wl1_off, const int *__restrict__ wl1,
-                                               const int *__restrict__ wl2_off, const int *__restrict__ wl2,
-                                               long long *__restrict__ grad, double *__restrict__ e_unit)
+__global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 5 : 2) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                                                     const void *pos_v, const void *woff_v, const void *lj_v,
+                                                     const unsigned *__restrict__ sflags,
+                                                     const int *__restrict__ wl1_off, const int *__restrict__ wl1,
+                                                     const int *__restrict__ wl2_off, const int *__restrict__ wl2,
+                                                     long long *__restrict__ grad, double *__restrict__ e_unit)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ long long sG[9][WBLOCK];
+    __shared__ double sE[4][WBLOCK];
+    const int t = threadIdx.x;
+    int i = blockIdx.x * WBLOCK + t;
     if (i >= nW) return;
     typedef typename vec4<T>::type T4;
     typedef typename cplx<T>::type T2;
     const T4 *pos = (const T4 *)pos_v;
     const T4 *woff = (const T4 *)woff_v;
     const RepDev &R = reps[site_rep[3 * i]];
-    T4 si[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) sG[k][t] = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sE[k][t] = 0.0;
+    const T4 oi0 = pos[3 * i];
     // i-site offsets from O (a = 0 is O itself)
     const T4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
     const T oi[3][3] = {{(T)0, (T)0, (T)0}, {oi1.x, oi1.y, oi1.z}, {oi2.x, oi2.y, oi2.z}};
     T g[9];
-    long long G[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) { g[k] = 0; G[k] = 0; }
-    double elp = 0, eli = 0, eep = 0, eei = 0;
+    for (int k = 0; k < 9; ++k) g[k] = 0;
+    T e4[4] = {0, 0, 0, 0};    // LJ prim, LJ img, Coulomb prim, Coulomb img
+    auto flush_all = [&]() {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) { sG[k][t] += nb_fix(g[k]); g[k] = 0; }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { sE[k][t] += (double)e4[k]; e4[k] = 0; }
+    };
     int npair = 0;
     const T iL0 = rep_invL<T>(R, 0), iL1 = rep_invL<T>(R, 1), iL2 = rep_invL<T>(R, 2);
     const T rmax2 = (T)R.rmax2, rv2 = (T)R.rv2, alpha = Consts<T>::alpha(R), ex2c = (T)R.ex2c, c2a = (T)R.c2a;
@@ -151,7 +167,7 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
     for (int k = k0; k < k1; ++k) {
         int j = wl1[k];
         T4 oj = pos[3 * j];
-        T dx = si[0].x - oj.x, dy = si[0].y - oj.y, dz = si[0].z - oj.z;
+        T dx = oi0.x - oj.x, dy = oi0.y - oj.y, dz = oi0.z - oj.z;
         T nx = nb_rint(dx * iL0), ny = nb_rint(dy * iL1), nz = nb_rint(dz * iL2);
         dx = nb_shift(R, 0, dx, nx);
         dy = nb_shift(R, 1, dy, ny);
@@ -193,20 +209,21 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
                     g[3 * a + 2] += df * ddz;
                 }
             }
-            bool img = (nx != (T)0) | (ny != (T)0) | (nz != (T)0);
-            if (img) { eei += (double)e_el; eli += (double)e_lj; }
-            else { eep += (double)e_el; elp += (double)e_lj; }
+            const bool img = (nx != (T)0) | (ny != (T)0) | (nz != (T)0);
+            e4[img ? 1 : 0] += e_lj;
+            e4[img ? 3 : 2] += e_el;
             npair += 9;
         }
-        if (++cnt == CHUNK) { flush(g, G, 9); cnt = 0; }
+        if (++cnt == CHUNK) { flush_all(); cnt = 0; }
     }
-    flush(g, G, 9);
+    flush_all();
     // water sites against non-water atoms: atom semantics per site pair
-    {
+    int q0 = wl2_off[i], q1 = wl2_off[i + 1];
+    if (q0 < q1) {
         const T2 *lj = (const T2 *)lj_v;
-        T2 lji[3] = {lj[3 * i], lj[3 * i + 1], lj[3 * i + 2]};
-        unsigned fi[3] = {sflags[3 * i], sflags[3 * i + 1], sflags[3 * i + 2]};
-        int q0 = wl2_off[i], q1 = wl2_off[i + 1];
+        const T4 si[3] = {oi0, pos[3 * i + 1], pos[3 * i + 2]};
+        const T2 lji[3] = {lj[3 * i], lj[3 * i + 1], lj[3 * i + 2]};
+        const unsigned fi[3] = {sflags[3 * i], sflags[3 * i + 1], sflags[3 * i + 2]};
         cnt = 0;
         for (int k = q0; k < q1; ++k) {
             int s = wl2[k];
@@ -225,17 +242,17 @@ __global__ void __launch_bounds__(128) k_water(int nW, const RepDev *__restrict_
                 g[3 * a] += df * dx;
                 g[3 * a + 1] += df * dy;
                 g[3 * a + 2] += df * dz;
-                if (img) { eei += (double)eel; eli += (double)elj; }
-                else { eep += (double)eel; elp += (double)elj; }
+                e4[img ? 1 : 0] += elj;
+                e4[img ? 3 : 2] += eel;
             }
-            if (++cnt == CHUNK) { flush(g, G, 9); cnt = 0; }
+            if (++cnt == CHUNK) { flush_all(); cnt = 0; }
         }
-        flush(g, G, 9);
+        flush_all();
     }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = G[k];
+    for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
-    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei; eu[4] = (double)npair;
+    eu[0] = sE[0][t]; eu[1] = sE[1][t]; eu[2] = sE[2][t]; eu[3] = sE[3][t]; eu[4] = (double)npair;
 }
 
 // non-water atom per thread over its full site list
@@ -284,15 +301,89 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
 }
 
 // ---------------------------------------------------------------------------------
+// Water exclusion corrections (cdie_ewald.f:117-199 for the O-H1, O-H2, H1-H2 pairs of each
+// water), one thread per molecule, each pair once.  With u = (alpha r)^2,
+//   e  = -qq erf(alpha r)/r = -qq alpha (2/sqrt(pi)) S(u),   S(u) = sum (-1)^n u^n / (n! (2n+1))
+//   df = (de/dr)/r          = -qq (4 alpha^3/sqrt(pi)) S'(u)
+// (Taylor series of erf, Abramowitz & Stegun 7.1.5), evaluated in FP64 with 16 terms, which
+// is exact to rounding for u <= 0.5 (r <= 2.0 Å at alpha 0.35); larger u uses erf/exp.
+__constant__ double c_erf_s[16] = {
+    1, -0.33333333333333331, 0.10000000000000001, -0.023809523809523808, 0.0046296296296296294,
+    -0.00075757575757575758, 0.00010683760683760684, -1.3227513227513228e-05, 1.4589169000933706e-06,
+    -1.4503852223150468e-07, 1.3122532963802806e-08, -1.0892221037148573e-09, 8.3507027951472397e-11,
+    -5.9477940136376354e-12, 3.9554295164585257e-13, -2.4668270102644571e-14};
+__constant__ double c_erf_ds[15] = {
+    -0.33333333333333331, 0.20000000000000001, -0.071428571428571425, 0.018518518518518517,
+    -0.003787878787878788, 0.00064102564102564103, -9.2592592592592588e-05, 1.1671335200746965e-05,
+    -1.3053467000835422e-06, 1.3122532963802806e-07, -1.1981443140863431e-08, 1.0020843354176688e-09,
+    -7.7321322177289257e-11, 5.537601323041936e-12, -3.7002405153966856e-13};
+
+__device__ __forceinline__ void excl_pair(double qq, double al, double rx, double ry, double rz, double &e, double &df)
+{
+    double r2 = rx * rx + ry * ry + rz * rz, u = al * al * r2;
+    if (u <= 0.5) {
+        double s = c_erf_s[15], ds = c_erf_ds[14];
+#pragma unroll
+        for (int k = 14; k >= 0; --k) s = fma(s, u, c_erf_s[k]);
+#pragma unroll
+        for (int k = 13; k >= 0; --k) ds = fma(ds, u, c_erf_ds[k]);
+        e = -qq * al * NB_TWO_OVER_SQRTPI * s;
+        df = -qq * 2.0 * al * al * al * NB_TWO_OVER_SQRTPI * ds;
+    } else {
+        double rij = sqrt(r2), sinv = 1.0 / rij, x = al * rij;
+        double erfv = erf(x), derfc = NB_TWO_OVER_SQRTPI * exp(-x * x);
+        e = -qq * sinv * erfv;
+        df = qq * sinv * (sinv * sinv * erfv - sinv * al * derfc);
+    }
+}
+
+__global__ void k_excl_water(int nW, const int *__restrict__ unit_atom, const int *__restrict__ atom_rep,
+                             const RepDev *__restrict__ reps, const double *__restrict__ coor,
+                             const double *__restrict__ q, double *__restrict__ grad, double *__restrict__ e_out)
+{
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nW) return;
+    const int a0 = unit_atom[u];
+    const RepDev &R = reps[atom_rep[a0]];
+    double x[3][3], qs[3], g[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, ecorr = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        x[k][0] = coor[3 * (size_t)(a0 + k)];
+        x[k][1] = coor[3 * (size_t)(a0 + k) + 1];
+        x[k][2] = coor[3 * (size_t)(a0 + k) + 2];
+        qs[k] = q[a0 + k];
+    }
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        const int a = pa[p], b = pb[p];
+        double rx = x[a][0] - x[b][0], ry = x[a][1] - x[b][1], rz = x[a][2] - x[b][2];
+        double e, df;
+        excl_pair(qs[a] * qs[b] * R.epstmp, R.alphad, rx, ry, rz, e, df);
+        ecorr += e;
+        g[a][0] += df * rx; g[a][1] += df * ry; g[a][2] += df * rz;
+        g[b][0] -= df * rx; g[b][1] -= df * ry; g[b][2] -= df * rz;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double *gp = grad + 3 * (size_t)(a0 + k), *ep = e_out + 3 * (size_t)(a0 + k);
+        gp[0] = g[k][0]; gp[1] = g[k][1]; gp[2] = g[k][2];
+        ep[0] = k == 0 ? ecorr : 0.0; ep[1] = 0.0; ep[2] = 0.0;
+    }
+}
+
 // exclusion erf corrections (cdie_ewald.f:117-199) and 1-4 terms (ener14.f:38-95), FP64,
 // gathered per atom over both directions; raw (unimaged) displacements as MOIL uses.
+// With skip_water set, water atoms are left to k_excl_water.
 __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
                          const double *__restrict__ coor, const double *__restrict__ q, const int *__restrict__ ex_off,
                          const int *__restrict__ ex_j, const int *__restrict__ p_off, const int *__restrict__ p_j,
-                         const double *__restrict__ p_par, double *__restrict__ grad, double *__restrict__ e_out)
+                         const double *__restrict__ p_par, const unsigned *__restrict__ aflags, int skip_water,
+                         double *__restrict__ grad, double *__restrict__ e_out)
 {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= natom) return;
+    if (skip_water && (aflags[a] & SF_WATER)) return;
     const RepDev &R = reps[atom_rep[a]];
     double xa = coor[3 * (size_t)a], ya = coor[3 * (size_t)a + 1], za = coor[3 * (size_t)a + 2];
     double gx = 0, gy = 0, gz = 0, ecorr = 0, eel14 = 0, evdw14 = 0;
@@ -415,7 +506,7 @@ void realspace_t(NbCtx *c)
     cudaStream_t s = c->stream;
     if (c->timing) cudaEventRecord(c->ev[2], s);
     if (c->nW > 0) {
-        k_water<T><<<(int)((c->nW + 127) / 128), 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos,
+        k_water<T><<<(int)((c->nW + WBLOCK - 1) / WBLOCK), WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos,
                                                               c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_off, c->d_wl1,
                                                               c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
         c->launches++;
@@ -440,10 +531,18 @@ void nb_launch_realspace(NbCtx *c)
 
 void nb_launch_excl14(NbCtx *c, const double *d_coor)
 {
-    k_excl14<<<(int)((c->natom + 127) / 128), 128, 0, c->stream>>>(
-        (int)c->natom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_ex_off, c->d_ex_j, c->d_p14_off, c->d_p14_j,
-        c->d_p14_par, c->d_grad_ex, c->d_e_ex);
-    c->launches++;
+    const int fast = c->water_excl_fast && c->nW > 0;
+    if (fast) {
+        k_excl_water<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
+            (int)c->nW, c->d_unit_atom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_grad_ex, c->d_e_ex);
+        c->launches++;
+    }
+    if (!fast || c->nA > 0) {
+        k_excl14<<<(int)((c->natom + 127) / 128), 128, 0, c->stream>>>(
+            (int)c->natom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_ex_off, c->d_ex_j, c->d_p14_off,
+            c->d_p14_j, c->d_p14_par, c->d_aflags, fast, c->d_grad_ex, c->d_e_ex);
+        c->launches++;
+    }
 }
 
 void nb_launch_finalize(NbCtx *c, double *d_dpot)
