@@ -53,6 +53,8 @@ struct RepDev {
     int bsp0;                // bsp moduli: [bsp0, +n1) x, [+n1, +n2) y, [+n2, +n3) z
     float fc;                // sqrt(kofdie/eps)
     double fcd;
+    float spread_scale;      // FP32 path: plane accumulation in int32 units of 1/spread_scale,
+    float spread_inv;        // a power of two chosen so one atom's contribution stays below 2^21
     double pme_fac;          // pi^2 / alpha^2
     double pivol;            // pi * volume
     int arith, hvdw0, lj_switch, has_water;

@@ -299,6 +299,17 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         }
         R.fcd = sqrt(epstmp);
         R.fc = (float)R.fcd;
+        {
+            // int32 plane accumulation: one atom's largest stencil weight, q fc (2/3)^3, times
+            // the scale stays below 2^21 (so the FP32 rounding trick is exact); power of two
+            double qmax = 0;
+            for (int i = 0; i < t->npt; ++i) qmax = std::max(qmax, fabs(t->ptchg[i]));
+            double contrib = qmax * R.fcd * (8.0 / 27.0);
+            int k = contrib > 0 ? (int)floor(log2(2097152.0 / contrib)) : 24;
+            k = std::min(24, std::max(8, k));
+            R.spread_scale = (float)ldexp(1.0, k);
+            R.spread_inv = (float)ldexp(1.0, -k);
+        }
         R.pme_fac = M_PI * M_PI / (alpha * alpha);
         R.pivol = M_PI * p->a * p->b * p->c;
         // atoms and units

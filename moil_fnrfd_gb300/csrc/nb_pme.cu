@@ -161,24 +161,27 @@ __global__ void k_pme_scatter(int nsite, const int *__restrict__ site_rep, const
     zatoms[zstart[R.zb0 + zb] + zslot[s]] = s;
 }
 
-// plane accumulation: 64-bit fixed point (2^40 per unit) for FP32, FP64 atomics for FP64
+// plane accumulation.  FP32: int32 fixed point; the caller pre-multiplies by the replica's
+// spread_scale so |x| < 2^21, and x + 1.5*2^23 rounds x to an integer whose bits sit in the
+// low mantissa -- a float-to-int conversion without a conversion instruction.  Integer
+// addition makes the plane independent of the order of the atomics.  FP64: FP64 atomics.
 template <typename T> struct Acc;
 template <> struct Acc<float> {
-    typedef unsigned long long type;
-    __device__ static void add(type *p, float v) { atomicAdd(p, (unsigned long long)__float2ll_rn(v * 1099511627776.0f)); }
-    __device__ static float get(type v) { return __ll2float_rn((long long)v) * (1.0f / 1099511627776.0f); }
+    typedef int type;
+    __device__ static void add(type *p, float x) { atomicAdd(p, __float_as_int(x + 12582912.0f) - 0x4B400000); }
+    __device__ static float get(type v, float inv) { return __int2float_rn(v) * inv; }
 };
 template <> struct Acc<double> {
     typedef double type;
     __device__ static void add(type *p, double v) { atomicAdd(p, v); }
-    __device__ static double get(type v) { return v; }
+    __device__ static double get(type v, double) { return v; }
 };
 
 // the 4x4 x-y stencil of every atom whose z stencil reaches plane z
 template <typename T>
 __device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *__restrict__ zstart,
                                              const int *__restrict__ zatoms, const typename vec4<T>::type *fr,
-                                             typename Acc<T>::type *acc)
+                                             typename Acc<T>::type *acc, T scale)
 {
     typedef typename vec4<T>::type T4;
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
@@ -197,7 +200,7 @@ __device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *
             bspline4<T>(f.z - (T)i3, th3, dt3);
             int j = i2 - 3 + t2;
             j = (j + 2 * n2) % n2;
-            T v = th2[t2] * th3[t3] * f.w;
+            T v = th2[t2] * th3[t3] * (f.w * scale);
             typename Acc<T>::type *row = acc + j * n1;
             int i0 = i1 - 3 + 2 * n1;
 #pragma unroll
@@ -352,17 +355,15 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
     const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
-    unsigned long long *acc = (unsigned long long *)smem;
-    float2 *A = (float2 *)smem;                 // the accumulator bytes, reused after conversion
+    float2 *A = (float2 *)smem;
     float2 *B = A + n1 * n2;
-    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0ull;
+    int *acc = (int *)B;                        // the accumulator lives in B until the first pass
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
     __syncthreads();
-    spread_plane<float>(R, w.z, zstart, zatoms, fr, acc);
+    spread_plane<float>(R, w.z, zstart, zatoms, fr, acc, R.spread_scale);
     __syncthreads();
-    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) {
-        float v = Acc<float>::get(acc[k]);
-        A[k] = make_float2(v, 0.f);
-    }
+    const float inv = R.spread_inv;
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) A[k] = make_float2(Acc<float>::get(acc[k], inv), 0.f);
     __syncthreads();
     // x: n2 rows of n1 (real input); last pass keeps kx < n1h, transposed to [kx][y]
     float2 *X = fft_lines<1, false>(p1, A, B, nullptr, n2, n1h, tab, tw);
@@ -396,11 +397,22 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     float2 *F = fft_lines<0, false>(p3, A, B, nullptr, tk, 0, tab, tw);
     float2 *Fo = F == A ? B : A;
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
+    // influence function with the replica constants converted once per thread:
+    // exp(-pi^2 m^2 / alpha^2) = 2^(-fac2 m^2), fac2 = pi^2 / alpha^2 * log2(e)
+    const float fac2 = (float)(R.pme_fac * 1.4426950408889634), pivol = (float)R.pivol;
+    const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
+    const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
+    const float mh1 = (float)w.kx * iL0, pb1 = pivol * bsp[w.kx];
     float en = 0.f;
     for (int c = warp; c < tk; c += 8) {
         const int ky = w.ky0 + c;
+        const float mh2 = (float)(ky < nf2 ? ky : ky - n2) * iL1;
+        const float pb12 = pb1 * bsp[n1 + ky], m12 = mh1 * mh1 + mh2 * mh2;
         for (int kz = lane; kz < n3; kz += 32) {
-            float et = eterm_of<float>(R, bsp, w.kx, ky, kz);
+            const float mh3 = (float)(kz < nf3 ? kz : kz - n3) * iL2;
+            const float msq = fmaf(mh3, mh3, m12);
+            float et = (w.kx == 0 && ky == 0 && kz == 0) ? 0.f
+                                                          : exp2f(-fac2 * msq) * __frcp_rn(pb12 * bsp[n1 + n2 + kz] * msq);
             float2 v = F[c * n3 + kz];
             en += wgt * et * (v.x * v.x + v.y * v.y);
             F[c * n3 + kz] = make_float2(v.x * et, -v.y * et);    // conj: the inverse runs forward
@@ -505,11 +517,11 @@ __global__ void __launch_bounds__(256) k_plane_fwd(const PlaneWork *__restrict__
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
     __syncthreads();
-    spread_plane<T>(R, w.z, zstart, zatoms, (const typename vec4<T>::type *)fr_v, acc);
+    spread_plane<T>(R, w.z, zstart, zatoms, (const typename vec4<T>::type *)fr_v, acc, (T)1);
     __syncthreads();
     C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
     for (int j = warp; j < n2; j += nwarp) {
-        for (int i = lane; i < n1; i += 32) { x[i].x = Acc<T>::get(acc[j * n1 + i]); x[i].y = 0; }
+        for (int i = lane; i < n1; i += 32) { x[i].x = Acc<T>::get(acc[j * n1 + i], (T)1); x[i].y = 0; }
         __syncwarp();
         C *res = warp_fft<C>(x, y, p1, tw + p1.tw0, lane);
         for (int k = lane; k < n1h; k += 32) P[j * pitch + k] = res[k];
@@ -926,6 +938,27 @@ __global__ void k_na_load(int natom, const double *__restrict__ coor, const doub
     srep[a] = 0;
 }
 
+// int32 plane scale from the largest charge (same rule as the handle path)
+__global__ void k_na_scale(int natom, const double *__restrict__ q, RepDev *__restrict__ reps)
+{
+    __shared__ double sh[256];
+    double m = 0;
+    for (int a = threadIdx.x; a < natom; a += blockDim.x) m = fmax(m, fabs(q[a]));
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double contrib = sh[0] * reps[0].fcd * (8.0 / 27.0);
+        int k = contrib > 0 ? (int)floor(log2(2097152.0 / contrib)) : 24;
+        k = min(24, max(8, k));
+        reps[0].spread_scale = (float)ldexp(1.0, k);
+        reps[0].spread_inv = (float)ldexp(1.0, -k);
+    }
+}
+
 // gradient from the four per-plane slots (grad_sum, pot/ewald_receip.f:815-970); overwrites dpot
 __global__ void k_na_grad(int natom, const RepDev *__restrict__ reps, const double *__restrict__ q,
                           const float *__restrict__ part, double *__restrict__ dpot)
@@ -1100,6 +1133,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
 #undef NA_CP
     k_na_load<<<(natom + 255) / 256, 256, 0, stream>>>(natom, d_coor, d_q, (float4 *)tmp.d_pos,
                                                        (float *)tmp.d_site_q, tmp.d_site_rep);
+    k_na_scale<<<1, 256, 0, stream>>>(natom, d_q, tmp.d_reps);
     pme_t<float>(&tmp);
     k_na_grad<<<(natom + 255) / 256, 256, 0, stream>>>(natom, tmp.d_reps, d_q, (const float *)tmp.d_part, d_dpot);
     k_na_energy<<<1, 256, 0, stream>>>((int)tmp.cols.size(), tmp.d_e_col, d_eout);
