@@ -25,6 +25,7 @@
 #define NB_MAX_FFT 128
 #define NB_TWO_OVER_SQRTPI 1.1283791670955126
 #define NB_EU 5                       // per-unit outputs: LJ prim, LJ img, Coul prim, Coul img, site pairs
+#define NB_WTILE 128                  // waters per block (and per shared tile) of the tiled water list
 
 // per-replica constants (read by every kernel)
 struct RepDev {
@@ -58,6 +59,7 @@ struct RepDev {
     double pme_fac;          // pi^2 / alpha^2
     double pivol;            // pi * volume
     int arith, hvdw0, lj_switch, has_water;
+    int wtiled;              // water-water lists built by tiled all-pairs (box of <= 64 cells)
     double e_self;
 };
 

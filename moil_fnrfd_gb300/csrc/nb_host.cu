@@ -81,7 +81,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_xl); free_ptr(c->d_count_tmp); free_ptr(c->d_ex_off); free_ptr(c->d_ex_j); free_ptr(c->d_p14_off);
     free_ptr(c->d_p14_j); free_ptr(c->d_p14_par); free_ptr(c->d_grad_site); free_ptr(c->d_e_unit);
     free_ptr(c->d_grad_ex); free_ptr(c->d_e_ex); free_ptr(c->d_plans); free_ptr(c->d_rep_plan); free_ptr(c->d_tw);
-    free_ptr(c->d_tab);
+    free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp);
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
@@ -330,6 +330,13 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         }
         R.nwat = nwat; R.noth = noth;
         wat0 += nwat; oth0 += noth;
+        // water-water list by tiled all-pairs when the 27-cell stencil already covers at
+        // least 40% of the box (small replicas: 2-4 cells per side)
+        {
+            double frac = 1.0;
+            for (int d = 0; d < 3; ++d) frac *= (double)std::min(R.nc[d], 3) / R.nc[d];
+            R.wtiled = (nwat > 0 && nwat <= 16384 && frac >= 0.4) ? 1 : 0;
+        }
         for (int i = 0; i < t->npt; ++i) {
             q.push_back(t->ptchg[i]);
             lj_e12.push_back(t->epsgm12[i]);
@@ -413,6 +420,13 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         NB_TRY(upload(c, c->d_p14_par, pp));
     }
     NB_TRY(upload(c, c->d_reps, c->rd));
+    c->wtiles.clear();
+    for (int r = 0; r < nrep; ++r) {
+        const RepDev &R = c->rd[r];
+        if (!R.wtiled) continue;
+        for (int i0 = 0; i0 < R.nwat; i0 += NB_WTILE) c->wtiles.push_back(make_int2(r, R.wat0 + i0));
+    }
+    if (!c->wtiles.empty()) NB_TRY(upload(c, c->d_wtiles, c->wtiles));
     const size_t ts = c->precision == MOIL_NB_FP64 ? 8 : 4;
     int64_t nu = c->nunit, ns = c->nsite;
     NB_CUDA_OK(c, cudaMalloc(&c->d_unit_key, sizeof(int) * nu));
@@ -460,6 +474,11 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_TRY(alloc_lists(c));
     c->h_e_rep.assign(16 * nrep, 0.0);
     NB_TRY(nb_pme_configure(c));
+    {
+        // tile sums for every scan: bins, per-water and per-atom counts, PME z-bins
+        int64_t nmax = std::max<int64_t>({2 * (int64_t)c->ncell, c->nW, c->nA, (int64_t)c->nzbin, 1});
+        NB_CUDA_OK(c, cudaMalloc(&c->d_scan_tmp, sizeof(long long) * (nmax / 4096 + 2)));
+    }
     NB_CUDA_OK(c, cudaDeviceSynchronize());
     c->need_rebuild = 1;
     c->evals_since_build = 0;
@@ -589,6 +608,8 @@ int moil_nb_create(moil_nb_ctx **out, int device)
         delete h;
         return MOIL_NB_ERR_CUDA;
     }
+    cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (h->nsm <= 0) h->nsm = 1;
     for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
     if (cudaMallocHost(&h->h_status, sizeof(int) * 8) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
         moil_nb_destroy(h);

@@ -34,6 +34,7 @@ struct RepHost {
 
 struct NbCtx {
     int device = 0;
+    int nsm = 152;                // multiprocessors: grids of the rebuild-gated kernels stay one wave
     cudaStream_t stream = nullptr;
     int precision = MOIL_NB_MIXED;
     int inited = 0;
@@ -79,6 +80,9 @@ struct NbCtx {
     int *d_xl_off = nullptr, *d_xl = nullptr;
     int64_t cap_wl1 = 0, cap_wl2 = 0, cap_xl = 0;
     int *d_count_tmp = nullptr;   // scratch counts
+    long long *d_scan_tmp = nullptr;   // tile sums of the three-phase scan
+    std::vector<int2> wtiles;     // (replica, first sorted water) of each tiled water-list block
+    int2 *d_wtiles = nullptr;
 
     // exclusion / 1-4 lists per caller atom (both directions)
     int *d_ex_off = nullptr, *d_ex_j = nullptr;

@@ -26,46 +26,67 @@ __global__ void k_unit_keys(int nunit, int nW, int ncell, const int *__restrict_
                             int *__restrict__ hist, int *st)
 {
     if (rebuild_off(st)) return;
-    int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= nunit) return;
-    const RepDev &R = reps[unit_rep[u]];
-    int a = unit_atom[u];
-    int ci[3];
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunit; u += gridDim.x * blockDim.x) {
+        const RepDev &R = reps[unit_rep[u]];
+        int a = unit_atom[u];
+        int ci[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double x = coor[3 * (size_t)a + d];
-        if (!(x == x) || fabs(x) > 1e7) { atomicOr(&st[1], NB_DEV_ERR_NAN); x = 0.0; }
-        double f = x * R.invLd[d] + 0.5;
-        f -= floor(f);
-        int q = (int)(f * R.nc[d]);
-        ci[d] = q >= R.nc[d] ? R.nc[d] - 1 : (q < 0 ? 0 : q);
+        for (int d = 0; d < 3; ++d) {
+            double x = coor[3 * (size_t)a + d];
+            if (!(x == x) || fabs(x) > 1e7) { atomicOr(&st[1], NB_DEV_ERR_NAN); x = 0.0; }
+            double f = x * R.invLd[d] + 0.5;
+            f -= floor(f);
+            int q = (int)(f * R.nc[d]);
+            ci[d] = q >= R.nc[d] ? R.nc[d] - 1 : (q < 0 ? 0 : q);
+        }
+        int cell = R.cell0 + ci[0] + R.nc[0] * (ci[1] + R.nc[1] * ci[2]);
+        int k = (u < nW ? 0 : ncell) + cell;
+        key[u] = k;
+        slot[u] = atomicAdd(&hist[k], 1);
     }
-    int cell = R.cell0 + ci[0] + R.nc[0] * (ci[1] + R.nc[1] * ci[2]);
-    int k = (u < nW ? 0 : ncell) + cell;
-    key[u] = k;
-    slot[u] = atomicAdd(&hist[k], 1);
 }
 
 __global__ void k_unit_scatter(int nunit, const int *__restrict__ key, const int *__restrict__ slot,
                                const int *__restrict__ start, int *__restrict__ sorted, const int *st)
 {
     if (rebuild_off(st)) return;
-    int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= nunit) return;
-    sorted[start[key[u]] + slot[u]] = u;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunit; u += gridDim.x * blockDim.x)
+        sorted[start[key[u]] + slot[u]] = u;
 }
 
-// deterministic order inside a bin: ascending unit id (insertion sort, bins are short)
-__global__ void k_bin_sort(int nbin, const int *__restrict__ start, int *__restrict__ sorted, const int *st)
+// deterministic order inside a bin: ascending unit id.  One warp per bin: the bin is staged
+// in shared memory and each unit goes to its rank (ids are distinct); bins longer than the
+// stage fall back to an insertion sort by one lane.
+#define NB_BIN_STAGE 1024
+__global__ void __launch_bounds__(128) k_bin_sort(int nbin, const int *__restrict__ start, int *__restrict__ sorted,
+                                                  const int *st)
 {
     if (rebuild_off(st)) return;
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbin) return;
-    int lo = start[b], hi = start[b + 1];
-    for (int i = lo + 1; i < hi; ++i) {
-        int v = sorted[i], j = i - 1;
-        while (j >= lo && sorted[j] > v) { sorted[j + 1] = sorted[j]; --j; }
-        sorted[j + 1] = v;
+    __shared__ int stage[4][NB_BIN_STAGE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *v = stage[warp];
+    for (int b = blockIdx.x * 4 + warp; b < nbin; b += gridDim.x * 4) {
+        const int lo = start[b], n = start[b + 1] - lo;
+        if (n <= 1) continue;
+        if (n > NB_BIN_STAGE) {
+            if (lane == 0)
+                for (int i = lo + 1; i < lo + n; ++i) {
+                    int x = sorted[i], j = i - 1;
+                    while (j >= lo && sorted[j] > x) { sorted[j + 1] = sorted[j]; --j; }
+                    sorted[j + 1] = x;
+                }
+            __syncwarp();
+            continue;
+        }
+        for (int k = lane; k < n; k += 32) v[k] = sorted[lo + k];
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) {
+            const int x = v[k];
+            int r = 0;
+            for (int m = 0; m < n; ++m) r += v[m] < x;
+            sorted[lo + r] = x;
+        }
+        __syncwarp();
     }
 }
 
@@ -79,29 +100,29 @@ __global__ void k_site_build(int nunit, int nW, const int *__restrict__ sorted, 
                              void *site_q_v, const int *st)
 {
     if (rebuild_off(st)) return;
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nunit) return;
-    int u = sorted[p];
-    int a0 = unit_atom[u];
-    int s0, ns;
-    if (p < nW) { s0 = 3 * p; ns = 3; } else { s0 = 3 * nW + (p - nW); ns = 1; }
     typedef typename cplx<T>::type T2;
     T2 *site_lj = (T2 *)site_lj_v;
     T *site_q = (T *)site_q_v;
-    for (int k = 0; k < ns; ++k) {
-        int a = a0 + k, s = s0 + k;
-        site_orig[s] = a;
-        site_of[a] = s;
-        site_rep[s] = atom_rep[a];
-        site_flags[s] = aflags[a];
-        if (sizeof(T) == 4) {
-            float2 v = lj_f[a];
-            ((float2 *)site_lj)[s] = v;
-        } else {
-            double2 v = lj_d[a];
-            ((double2 *)site_lj)[s] = v;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nunit; p += gridDim.x * blockDim.x) {
+        int u = sorted[p];
+        int a0 = unit_atom[u];
+        int s0, ns;
+        if (p < nW) { s0 = 3 * p; ns = 3; } else { s0 = 3 * nW + (p - nW); ns = 1; }
+        for (int k = 0; k < ns; ++k) {
+            int a = a0 + k, s = s0 + k;
+            site_orig[s] = a;
+            site_of[a] = s;
+            site_rep[s] = atom_rep[a];
+            site_flags[s] = aflags[a];
+            if (sizeof(T) == 4) {
+                float2 v = lj_f[a];
+                ((float2 *)site_lj)[s] = v;
+            } else {
+                double2 v = lj_d[a];
+                ((double2 *)site_lj)[s] = v;
+            }
+            site_q[s] = (T)q[a];
         }
-        site_q[s] = (T)q[a];
     }
 }
 
@@ -113,41 +134,41 @@ __global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_orig, 
                           void *woff_v, float4 *__restrict__ posb, float half_skin2, float rwat2, int snapshot,
                           int *st)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nsite) return;
     if (snapshot && rebuild_off(st)) return;
     typedef typename vec4<T>::type T4;
-    int a = site_orig[s];
-    double x = coor[3 * (size_t)a], y = coor[3 * (size_t)a + 1], z = coor[3 * (size_t)a + 2];
-    if (!(x == x && y == y && z == z) || fabs(x) > 1e7 || fabs(y) > 1e7 || fabs(z) > 1e7) {
-        atomicOr(&st[1], NB_DEV_ERR_NAN);
-        x = y = z = 0.0;
-    }
-    unsigned f = site_flags[s];
-    T qe = (f & SF_CHARGED) ? (T)q[a] : (T)0;
-    T4 p;
-    p.x = (T)x; p.y = (T)y; p.z = (T)z; p.w = qe;
-    ((T4 *)pos_v)[s] = p;
-    float4 pf = make_float4((float)x, (float)y, (float)z, 0.f);
-    if (snapshot) {
-        posb[s] = pf;
-    } else {
-        // lists stay valid while no site moved more than skin/2 since the build
-        float4 b = posb[s];
-        float dx = pf.x - b.x, dy = pf.y - b.y, dz = pf.z - b.z;
-        if (dx * dx + dy * dy + dz * dz > half_skin2) atomicOr(&st[0], 1);
-    }
-    if (s < 3 * nW && (s % 3) != 0) {
-        // water sites must stay within rwat of their oxygen (list radius assumption)
-        int o = site_orig[s - (s % 3)];
-        double ox = coor[3 * (size_t)o], oy = coor[3 * (size_t)o + 1], oz = coor[3 * (size_t)o + 2];
-        double d2 = (x - ox) * (x - ox) + (y - oy) * (y - oy) + (z - oz) * (z - oz);
-        if (d2 > rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
-        // H offset from its O, formed in FP64 so the water kernel's site displacements
-        // inherit no extra rounding from absolute FP32 positions
-        T4 off;
-        off.x = (T)(x - ox); off.y = (T)(y - oy); off.z = (T)(z - oz); off.w = (T)0;
-        ((T4 *)woff_v)[2 * (s / 3) + (s % 3) - 1] = off;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsite; s += gridDim.x * blockDim.x) {
+        int a = site_orig[s];
+        double x = coor[3 * (size_t)a], y = coor[3 * (size_t)a + 1], z = coor[3 * (size_t)a + 2];
+        if (!(x == x && y == y && z == z) || fabs(x) > 1e7 || fabs(y) > 1e7 || fabs(z) > 1e7) {
+            atomicOr(&st[1], NB_DEV_ERR_NAN);
+            x = y = z = 0.0;
+        }
+        unsigned f = site_flags[s];
+        T qe = (f & SF_CHARGED) ? (T)q[a] : (T)0;
+        T4 p;
+        p.x = (T)x; p.y = (T)y; p.z = (T)z; p.w = qe;
+        ((T4 *)pos_v)[s] = p;
+        float4 pf = make_float4((float)x, (float)y, (float)z, 0.f);
+        if (snapshot) {
+            posb[s] = pf;
+        } else {
+            // lists stay valid while no site moved more than skin/2 since the build
+            float4 b = posb[s];
+            float dx = pf.x - b.x, dy = pf.y - b.y, dz = pf.z - b.z;
+            if (dx * dx + dy * dy + dz * dz > half_skin2) atomicOr(&st[0], 1);
+        }
+        if (s < 3 * nW && (s % 3) != 0) {
+            // water sites must stay within rwat of their oxygen (list radius assumption)
+            int o = site_orig[s - (s % 3)];
+            double ox = coor[3 * (size_t)o], oy = coor[3 * (size_t)o + 1], oz = coor[3 * (size_t)o + 2];
+            double d2 = (x - ox) * (x - ox) + (y - oy) * (y - oy) + (z - oz) * (z - oz);
+            if (d2 > rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
+            // H offset from its O, formed in FP64 so the water kernel's site displacements
+            // inherit no extra rounding from absolute FP32 positions
+            T4 off;
+            off.x = (T)(x - ox); off.y = (T)(y - oy); off.z = (T)(z - oz); off.w = (T)0;
+            ((T4 *)woff_v)[2 * (s / 3) + (s % 3) - 1] = off;
+        }
     }
     (void)site_rep;
     (void)reps;
@@ -196,22 +217,25 @@ __device__ __forceinline__ bool nb_excluded(const int *__restrict__ ex_off, cons
     return false;
 }
 
-// 4. water lists W1 (water j) and W2 (non-water sites); FILL = 0 counts, 1 writes
+// 4. water lists W1 (water j) and W2 (non-water sites) of water i; FILL = 0 counts, 1 writes
 template <typename T, int FILL>
-__global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep, const void *pos_v,
-                        const int *__restrict__ bin_start, int ncell, const int *__restrict__ sorted,
-                        int *__restrict__ cnt1, int *__restrict__ cnt2, int *__restrict__ cntn,
-                        const int *__restrict__ off1, const int *__restrict__ off2, int *__restrict__ l1,
-                        int *__restrict__ l2, int64_t cap1, int64_t cap2, int *st)
+__device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restrict__ reps,
+                                          const int *__restrict__ site_rep, const void *pos_v,
+                                          const int *__restrict__ bin_start, int ncell, int *__restrict__ cnt1,
+                                          int *__restrict__ cnt2, int *__restrict__ cntn,
+                                          const int *__restrict__ off1, const int *__restrict__ off2,
+                                          int *__restrict__ l1, int *__restrict__ l2, int64_t cap1, int64_t cap2,
+                                          int *st)
 {
     // W1 entries are stored in two groups: molecules already inside the cutoff at build
     // time first, skin-only molecules after them, so lanes of a warp stay converged
-    if (rebuild_off(st)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nW) return;
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
     const RepDev &R = reps[site_rep[3 * i]];
+    if (R.wtiled && R.noth == 0) {   // W1 comes from k_wlist_tiled, W2 is empty
+        if (!FILL) cnt2[i] = 0;
+        return;
+    }
     T4 oi = pos[3 * i];
     int ci[3], cx[3], cy[3], cz[3];
     cell_of<T>(R, oi.x, oi.y, oi.z, ci);
@@ -225,8 +249,9 @@ __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__re
         for (int b = 0; b < ny; ++b)
             for (int d = 0; d < nx; ++d) {
                 int cell = R.cell0 + cx[d] + R.nc[0] * (cy[b] + R.nc[1] * cz[a]);
-                // waters in the cell: sorted positions [bin_start[cell], bin_start[cell+1])
-                for (int p = bin_start[cell]; p < bin_start[cell + 1]; ++p) {
+                // waters in the cell: sorted positions [bin_start[cell], bin_start[cell+1]);
+                // replicas with few cells get their water-water list from k_wlist_tiled
+                for (int p = R.wtiled ? 0 : bin_start[cell]; p < (R.wtiled ? 0 : bin_start[cell + 1]); ++p) {
                     if (p == i) continue;
                     T4 oj = pos[3 * p];
                     T r2 = mi_r2<T>(R, oi.x - oj.x, oi.y - oj.y, oi.z - oj.z);
@@ -250,20 +275,111 @@ __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__re
                     }
                 }
             }
-    if (!FILL) { cnt1[i] = n1; cnt2[i] = n2; cntn[i] = nn; }
+    if (!FILL) {
+        if (!R.wtiled) { cnt1[i] = n1; cntn[i] = nn; }
+        cnt2[i] = n2;
+    }
     else if ((int64_t)w1 + n1 > cap1 || (int64_t)w2 + n2 > cap2) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+}
+
+template <typename T, int FILL>
+__global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep, const void *pos_v,
+                        const int *__restrict__ bin_start, int ncell, int *__restrict__ cnt1,
+                        int *__restrict__ cnt2, int *__restrict__ cntn, const int *__restrict__ off1,
+                        const int *__restrict__ off2, int *__restrict__ l1, int *__restrict__ l2, int64_t cap1,
+                        int64_t cap2, int *st)
+{
+    if (rebuild_off(st)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nW; i += gridDim.x * blockDim.x)
+        wlist_one<T, FILL>(i, nW, reps, site_rep, pos_v, bin_start, ncell, cnt1, cnt2, cntn, off1, off2, l1, l2,
+                           cap1, cap2, st);
+}
+
+// oxygen position wrapped into [0, L) per axis, as FP32 (list geometry only)
+template <typename T>
+__device__ __forceinline__ float4 wrap_box(const RepDev &R, typename vec4<T>::type p)
+{
+    T x = p.x - rep_L<T>(R, 0) * floor(p.x * rep_invL<T>(R, 0));
+    T y = p.y - rep_L<T>(R, 1) * floor(p.y * rep_invL<T>(R, 1));
+    T z = p.z - rep_L<T>(R, 2) * floor(p.z * rep_invL<T>(R, 2));
+    return make_float4((float)x, (float)y, (float)z, 0.f);
+}
+
+// 4b. W1 for replicas whose cell stencil spans most of the box: all molecule pairs of the
+// replica, oxygens staged in shared-memory tiles of NB_WTILE and read by broadcast.  One
+// block = NB_WTILE consecutive sorted waters of one replica (blocks never straddle
+// replicas); j runs in sorted order, so the list order is fixed.  The near-first split
+// matches k_wlist.  FILL = 0 counts, 1 writes.
+template <typename T, int FILL>
+__device__ __forceinline__ void wlist_tile(int2 w, float4 *sj, const RepDev *__restrict__ reps, const void *pos_v,
+                                           int *__restrict__ cnt1, int *__restrict__ cntn,
+                                           const int *__restrict__ off1, int *__restrict__ l1, int64_t cap1, int *st)
+{
+    typedef typename vec4<T>::type T4;
+    const T4 *pos = (const T4 *)pos_v;
+    const RepDev &R = reps[w.x];
+    const int j0 = R.wat0, nw = R.nwat;
+    const int i = w.y + (int)threadIdx.x;
+    const bool act = i < j0 + nw;
+    const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
+    const float rl2 = R.rlist2, rc2 = R.rmax2;
+    float4 oi = act ? wrap_box<T>(R, pos[3 * (size_t)i]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    int n1 = 0, nn = 0, w1 = 0, wf = 0;
+    if (FILL && act) { w1 = off1[i]; wf = w1 + cntn[i]; }
+    for (int t0 = 0; t0 < nw; t0 += NB_WTILE) {
+        __syncthreads();
+        if (t0 + (int)threadIdx.x < nw) sj[threadIdx.x] = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
+        __syncthreads();
+        if (!act) continue;
+        const int tn = min(NB_WTILE, nw - t0);
+        const int self = i - j0 - t0;
+#pragma unroll 4
+        for (int k = 0; k < tn; ++k) {
+            float4 q = sj[k];
+            float dx = fabsf(oi.x - q.x), dy = fabsf(oi.y - q.y), dz = fabsf(oi.z - q.z);
+            dx = fminf(dx, L0 - dx);
+            dy = fminf(dy, L1 - dy);
+            dz = fminf(dz, L2 - dz);
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (r2 < rl2 && k != self) {
+                bool near = r2 <= rc2;
+                if (FILL) {
+                    int at = near ? w1 + nn : wf + (n1 - nn);
+                    if (at < cap1) l1[at] = j0 + t0 + k;
+                }
+                nn += near;
+                n1++;
+            }
+        }
+    }
+    if (!act) return;
+    if (!FILL) { cnt1[i] = n1; cntn[i] = nn; }
+    else if ((int64_t)w1 + n1 > cap1) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+}
+
+template <typename T, int FILL>
+__global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 *__restrict__ work,
+                                                          const RepDev *__restrict__ reps, const void *pos_v,
+                                                          int *__restrict__ cnt1, int *__restrict__ cntn,
+                                                          const int *__restrict__ off1, int *__restrict__ l1,
+                                                          int64_t cap1, int *st)
+{
+    if (rebuild_off(st)) return;
+    __shared__ float4 sj[NB_WTILE];
+    // every tile pass starts with a block barrier before it overwrites sj
+    for (int b = blockIdx.x; b < ntile; b += gridDim.x)
+        wlist_tile<T, FILL>(work[b], sj, reps, pos_v, cnt1, cntn, off1, l1, cap1, st);
 }
 
 // 5. non-water list X: every site j within reach, exclusions removed
 template <typename T, int FILL>
-__global__ void k_xlist(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
-                        const int *__restrict__ site_orig, const void *pos_v, const int *__restrict__ bin_start,
-                        int ncell, const int *__restrict__ ex_off, const int *__restrict__ ex_j,
-                        int *__restrict__ cnt, const int *__restrict__ off, int *__restrict__ l, int64_t cap, int *st)
+__device__ __forceinline__ void xlist_one(int k, int nW, const RepDev *__restrict__ reps,
+                                          const int *__restrict__ site_rep, const int *__restrict__ site_orig,
+                                          const void *pos_v, const int *__restrict__ bin_start, int ncell,
+                                          const int *__restrict__ ex_off, const int *__restrict__ ex_j,
+                                          int *__restrict__ cnt, const int *__restrict__ off, int *__restrict__ l,
+                                          int64_t cap, int *st)
 {
-    if (rebuild_off(st)) return;
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nA) return;
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
     int si = 3 * nW + k;
@@ -306,21 +422,24 @@ __global__ void k_xlist(int nA, int nW, const RepDev *__restrict__ reps, const i
     else if ((int64_t)w + n > cap) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
 }
 
-// single-CTA exclusive scan (n up to a few million); total -> *total; skips when rebuild is off
-__global__ void k_scan(const int *__restrict__ in, int *__restrict__ out, int n, int *total, const int *st,
-                       int gate)
+template <typename T, int FILL>
+__global__ void k_xlist(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                        const int *__restrict__ site_orig, const void *pos_v, const int *__restrict__ bin_start,
+                        int ncell, const int *__restrict__ ex_off, const int *__restrict__ ex_j,
+                        int *__restrict__ cnt, const int *__restrict__ off, int *__restrict__ l, int64_t cap, int *st)
 {
-    if (gate && rebuild_off(st)) return;
-    __shared__ long long warp_sums[32];
-    __shared__ long long carry_s;
-    int tid = threadIdx.x, nt = blockDim.x;
-    int chunk = (n + nt - 1) / nt;
-    int lo = tid * chunk, hi = min(n, lo + chunk);
-    long long s = 0;
-    for (int i = lo; i < hi; ++i) s += in[i];
-    // block exclusive scan of s
+    if (rebuild_off(st)) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nA; k += gridDim.x * blockDim.x)
+        xlist_one<T, FILL>(k, nW, reps, site_rep, site_orig, pos_v, bin_start, ncell, ex_off, ex_j, cnt, off, l, cap,
+                           st);
+}
+
+// exclusive scan of one int per thread over the block; returns the thread's prefix and the
+// block total in *tot (all threads)
+__device__ __forceinline__ long long block_excl_scan(long long s, long long *warp_sums, long long *tot)
+{
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5;
     long long v = s;
-    int lane = tid & 31, w = tid >> 5;
     for (int o = 1; o < 32; o <<= 1) {
         long long t = __shfl_up_sync(0xffffffffu, v, o);
         if (lane >= o) v += t;
@@ -334,69 +453,160 @@ __global__ void k_scan(const int *__restrict__ in, int *__restrict__ out, int n,
             if (lane >= o) x += t;
         }
         if (lane < (nt >> 5)) warp_sums[lane] = x;
-        if (lane == 31) carry_s = x;
     }
     __syncthreads();
-    long long base = v - s + (w > 0 ? warp_sums[w - 1] : 0);
-    for (int i = lo; i < hi; ++i) {
-        out[i] = (int)base;
-        base += in[i];
+    long long r = v - s + (w > 0 ? warp_sums[w - 1] : 0);
+    *tot = warp_sums[(nt >> 5) - 1];
+    __syncthreads();
+    return r;
+}
+
+// three-phase exclusive scan: tile sums, scan of the tile sums, tile scans.  A tile is
+// NB_SCAN_PER x 256 consecutive ints; each thread owns NB_SCAN_PER consecutive entries.
+#define NB_SCAN_PER 16
+#define NB_SCAN_TILE (NB_SCAN_PER * 256)
+__global__ void __launch_bounds__(256) k_scan_sums(const int *__restrict__ in, int n, long long *__restrict__ bsum,
+                                                   const int *st, int gate)
+{
+    if (gate && rebuild_off(st)) return;
+    __shared__ long long ws[8];
+    const int base = blockIdx.x * NB_SCAN_TILE;
+    long long s = 0;
+    for (int k = threadIdx.x; k < NB_SCAN_TILE; k += 256)
+        if (base + k < n) s += in[base + k];
+    long long tot;
+    block_excl_scan(s, ws, &tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(long long *__restrict__ bsum, int nb, int *__restrict__ out, int n,
+                                                   int *total, const int *st, int gate)
+{
+    if (gate && rebuild_off(st)) return;
+    __shared__ long long ws[32];
+    long long carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += 1024) {
+        const int b = b0 + threadIdx.x;
+        long long s = b < nb ? bsum[b] : 0, tot;
+        long long p = block_excl_scan(s, ws, &tot);
+        if (b < nb) bsum[b] = carry + p;
+        carry += tot;
     }
-    if (tid == nt - 1) {
-        out[n] = (int)(base);
-        if (total) *total = (int)min(base, (long long)0x7fffffff);
+    if (threadIdx.x == 0) {
+        out[n] = (int)carry;
+        if (total) *total = (int)min(carry, (long long)0x7fffffff);
     }
-    (void)carry_s;
+}
+
+__global__ void __launch_bounds__(256) k_scan_tiles(const int *__restrict__ in, int *__restrict__ out, int n,
+                                                    const long long *__restrict__ bsum, const int *st, int gate)
+{
+    if (gate && rebuild_off(st)) return;
+    __shared__ long long ws[8];
+    const int i0 = blockIdx.x * NB_SCAN_TILE + threadIdx.x * NB_SCAN_PER;
+    int v[NB_SCAN_PER];
+    long long s = 0;
+#pragma unroll
+    for (int k = 0; k < NB_SCAN_PER; ++k) {
+        v[k] = i0 + k < n ? in[i0 + k] : 0;
+        s += v[k];
+    }
+    long long tot;
+    long long p = bsum[blockIdx.x] + block_excl_scan(s, ws, &tot);
+#pragma unroll
+    for (int k = 0; k < NB_SCAN_PER; ++k) {
+        if (i0 + k < n) out[i0 + k] = (int)p;
+        p += v[k];
+    }
+}
+
+// single-CTA exclusive scan for short inputs (no scratch): chunks of 1024 with a carry
+__global__ void __launch_bounds__(1024) k_scan_small(const int *__restrict__ in, int *__restrict__ out, int n,
+                                                     int *total)
+{
+    __shared__ long long ws[32];
+    long long carry = 0;
+    for (int i0 = 0; i0 < n; i0 += 1024) {
+        const int i = i0 + threadIdx.x;
+        long long s = i < n ? in[i] : 0, tot;
+        long long p = block_excl_scan(s, ws, &tot);
+        if (i < n) out[i] = (int)(carry + p);
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        out[n] = (int)carry;
+        if (total) *total = (int)min(carry, (long long)0x7fffffff);
+    }
+}
+
+// out[0..n] = exclusive prefix sums of in[0..n), out[n] = total (also to *total when given);
+// gate: skip unless the rebuild flag is set
+void nb_scan(NbCtx *c, const int *in, int *out, int n, int *total, int gate)
+{
+    const int nb = std::max(1, (n + NB_SCAN_TILE - 1) / NB_SCAN_TILE);
+    cudaStream_t s = c->stream;
+    k_scan_sums<<<nb, 256, 0, s>>>(in, n, c->d_scan_tmp, c->d_status, gate);
+    k_scan_top<<<1, 1024, 0, s>>>(c->d_scan_tmp, nb, out, n, total, c->d_status, gate);
+    k_scan_tiles<<<nb, 256, 0, s>>>(in, out, n, c->d_scan_tmp, c->d_status, gate);
+    c->launches += 3;
 }
 
 template <typename T>
 void build_lists_t(NbCtx *c, const double *d_coor)
 {
+    // Every kernel below exits at once unless the device rebuild flag is set; grids are
+    // bounded to one wave (grid-stride loops) so the skipped launches stay short.
     const int B = 256;
     cudaStream_t s = c->stream;
+    auto grid = [&](int64_t n, int b) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>((n + b - 1) / b, (int64_t)c->nsm * (2048 / b)));
+    };
     int nbin = 2 * c->ncell;
     cudaMemsetAsync(c->d_bin_count, 0, sizeof(int) * (nbin + 1), s);
-    // histogram is gated by the rebuild flag inside the kernel; the memset is harmless
-    k_unit_keys<<<(int)((c->nunit + B - 1) / B), B, 0, s>>>((int)c->nunit, (int)c->nW, c->ncell, c->d_unit_atom,
-                                                           c->d_unit_rep, c->d_reps, d_coor, c->d_unit_key,
-                                                           c->d_unit_slot, c->d_bin_count, c->d_status);
-    k_scan<<<1, 1024, 0, s>>>(c->d_bin_count, c->d_bin_start, nbin, nullptr, c->d_status, 1);
-    k_unit_scatter<<<(int)((c->nunit + B - 1) / B), B, 0, s>>>((int)c->nunit, c->d_unit_key, c->d_unit_slot,
-                                                              c->d_bin_start, c->d_sorted_unit, c->d_status);
-    k_bin_sort<<<(nbin + B - 1) / B, B, 0, s>>>(nbin, c->d_bin_start, c->d_sorted_unit, c->d_status);
-    k_site_build<T><<<(int)((c->nunit + B - 1) / B), B, 0, s>>>(
+    k_unit_keys<<<grid(c->nunit, B), B, 0, s>>>((int)c->nunit, (int)c->nW, c->ncell, c->d_unit_atom, c->d_unit_rep,
+                                                c->d_reps, d_coor, c->d_unit_key, c->d_unit_slot, c->d_bin_count,
+                                                c->d_status);
+    nb_scan(c, c->d_bin_count, c->d_bin_start, nbin, nullptr, 1);
+    k_unit_scatter<<<grid(c->nunit, B), B, 0, s>>>((int)c->nunit, c->d_unit_key, c->d_unit_slot, c->d_bin_start,
+                                                   c->d_sorted_unit, c->d_status);
+    k_bin_sort<<<grid(nbin, 4), 128, 0, s>>>(nbin, c->d_bin_start, c->d_sorted_unit, c->d_status);
+    k_site_build<T><<<grid(c->nunit, B), B, 0, s>>>(
         (int)c->nunit, (int)c->nW, c->d_sorted_unit, c->d_unit_atom, c->d_atom_rep, c->d_aflags, c->d_lj_f,
         c->d_lj_d, c->d_q, c->d_site_orig, c->d_site_of, c->d_site_rep, c->d_site_flags, c->d_site_lj,
         c->d_site_q, c->d_status);
-    k_prepare<T><<<(int)((c->nsite + B - 1) / B), B, 0, s>>>(
+    k_prepare<T><<<grid(c->nsite, B), B, 0, s>>>(
         (int)c->nsite, (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_site_flags, c->d_q, c->d_reps, d_coor,
         c->d_pos, c->d_woff, c->d_posb, 0.f, c->rwat * c->rwat, 1, c->d_status);
-    c->launches += 6;
+    c->launches += 5;
     if (c->nW > 0) {
-        int nb = (int)((c->nW + 127) / 128);
-        k_wlist<T, 0><<<nb, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         c->d_sorted_unit, c->d_count_tmp, c->d_count_tmp + c->nW + 1,
-                                         c->d_count_tmp + 2 * (c->nW + 1), nullptr, nullptr, nullptr, nullptr, 0, 0,
-                                         c->d_status);
-        k_scan<<<1, 1024, 0, s>>>(c->d_count_tmp, c->d_wl1_off, (int)c->nW, c->d_status + 2, c->d_status, 1);
-        k_scan<<<1, 1024, 0, s>>>(c->d_count_tmp + c->nW + 1, c->d_wl2_off, (int)c->nW, c->d_status + 3,
-                                  c->d_status, 1);
-        k_wlist<T, 1><<<nb, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         c->d_sorted_unit, nullptr, nullptr, c->d_count_tmp + 2 * (c->nW + 1),
-                                         c->d_wl1_off, c->d_wl2_off, c->d_wl1, c->d_wl2, c->cap_wl1, c->cap_wl2,
-                                         c->d_status);
-        c->launches += 4;
+        const int gw = grid(c->nW, 128), nt = (int)c->wtiles.size();
+        const int gt = (int)std::min<int64_t>(nt, (int64_t)c->nsm * 16);
+        int *cnt1 = c->d_count_tmp, *cnt2 = c->d_count_tmp + c->nW + 1, *cntn = c->d_count_tmp + 2 * (c->nW + 1);
+        k_wlist<T, 0><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
+                                         cnt1, cnt2, cntn, nullptr, nullptr, nullptr, nullptr, 0, 0, c->d_status);
+        if (nt > 0)
+            k_wlist_tiled<T, 0><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, cnt1, cntn, nullptr,
+                                                        nullptr, 0, c->d_status);
+        nb_scan(c, cnt1, c->d_wl1_off, (int)c->nW, c->d_status + 2, 1);
+        nb_scan(c, cnt2, c->d_wl2_off, (int)c->nW, c->d_status + 3, 1);
+        k_wlist<T, 1><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
+                                         nullptr, nullptr, cntn, c->d_wl1_off, c->d_wl2_off, c->d_wl1, c->d_wl2,
+                                         c->cap_wl1, c->cap_wl2, c->d_status);
+        if (nt > 0)
+            k_wlist_tiled<T, 1><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, nullptr, cntn,
+                                                        c->d_wl1_off, c->d_wl1, c->cap_wl1, c->d_status);
+        c->launches += nt > 0 ? 4 : 2;
     }
     if (c->nA > 0) {
-        int nb = (int)((c->nA + 127) / 128);
-        k_xlist<T, 0><<<nb, 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos,
+        const int ga = grid(c->nA, 128);
+        k_xlist<T, 0><<<ga, 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos,
                                          c->d_bin_start, c->ncell, c->d_ex_off, c->d_ex_j, c->d_count_tmp, nullptr,
                                          nullptr, 0, c->d_status);
-        k_scan<<<1, 1024, 0, s>>>(c->d_count_tmp, c->d_xl_off, (int)c->nA, c->d_status + 4, c->d_status, 1);
-        k_xlist<T, 1><<<nb, 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos,
+        nb_scan(c, c->d_count_tmp, c->d_xl_off, (int)c->nA, c->d_status + 4, 1);
+        k_xlist<T, 1><<<ga, 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos,
                                          c->d_bin_start, c->ncell, c->d_ex_off, c->d_ex_j, nullptr, c->d_xl_off,
                                          c->d_xl, c->cap_xl, c->d_status);
-        c->launches += 3;
+        c->launches += 2;
     }
 }
 
@@ -405,7 +615,8 @@ void prepare_t(NbCtx *c, const double *d_coor, int check)
 {
     const int B = 256;
     float hs = 0.5f * c->skin;
-    k_prepare<T><<<(int)((c->nsite + B - 1) / B), B, 0, c->stream>>>(
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((c->nsite + B - 1) / B, (int64_t)c->nsm * 8));
+    k_prepare<T><<<g, B, 0, c->stream>>>(
         (int)c->nsite, (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_site_flags, c->d_q, c->d_reps, d_coor,
         c->d_pos, c->d_woff, c->d_posb, check ? hs * hs : 3.0e38f, c->rwat * c->rwat, 0, c->d_status);
     c->launches += 1;
@@ -427,6 +638,7 @@ void nb_launch_prepare(NbCtx *c, const double *d_coor, int check)
 
 void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_total)
 {
-    k_scan<<<1, 1024, 0, c->stream>>>(d_in, d_out, n, d_total, c->d_status, 0);
+    // PME z-bins: short, and also used by the allocation-free entry point (no scan scratch)
+    k_scan_small<<<1, 1024, 0, c->stream>>>(d_in, d_out, n, d_total);
     c->launches += 1;
 }
