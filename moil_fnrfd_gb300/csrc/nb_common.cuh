@@ -82,9 +82,30 @@ template <typename T> struct cplx;
 template <> struct cplx<float> { typedef float2 type; };
 template <> struct cplx<double> { typedef double2 type; };
 
+// single MUFU instructions, denormals flushed (arguments here are never denormal):
+// rsqrt/rcp/ex2 .approx.ftz.f32 (relative error of order 2^-22)
+__device__ __forceinline__ float nb_rsqrt_approx(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float nb_rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float nb_ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ float nb_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double nb_rint(double x) { return rint(x); }
-__device__ __forceinline__ float nb_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ float nb_rsqrt(float x) { return nb_rsqrt_approx(x); }
 __device__ __forceinline__ double nb_rsqrt(double x) { return rsqrt(x); }
 
 template <typename T> __device__ __forceinline__ T rep_L(const RepDev &r, int k);
@@ -111,12 +132,12 @@ __device__ __forceinline__ float nb_erfc_ex(float x, float x2log2e, float *ex)
 {
     const float C[ERFCX_NC] = ERFCX_COEFS;
     float xc = fminf(x, 4.5f);
-    float t = __frcp_rn(fmaf(ERFCX_P, xc, 1.0f));
+    float t = nb_rcp_approx(fmaf(ERFCX_P, xc, 1.0f));
     float u = fmaf(ERFCX_A, t, ERFCX_B);
     float p = C[ERFCX_NC - 1];
 #pragma unroll
     for (int k = ERFCX_NC - 2; k >= 0; --k) p = fmaf(p, u, C[k]);
-    float e = exp2f(-x2log2e);
+    float e = nb_ex2_approx(-x2log2e);
     *ex = e;
     return e * (t * p);
 }

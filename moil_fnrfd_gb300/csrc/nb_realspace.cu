@@ -123,7 +123,7 @@ __device__ __forceinline__ void flush(double g[], long long G[], int n)
 // them out of the register file.
 #define WBLOCK 128
 template <typename T>
-__global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 5 : 2) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+__global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                                                      const void *pos_v, const void *woff_v, const void *lj_v,
                                                      const unsigned *__restrict__ sflags,
                                                      const int *__restrict__ wl1_off, const int *__restrict__ wl1,
@@ -164,9 +164,16 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 5 : 2) k_water(int nW
     const T qOO = Consts<T>::qq(R, 0), qOH = Consts<T>::qq(R, 1), qHH = Consts<T>::qq(R, 2);
     const T w12 = Consts<T>::w12(R), w6 = Consts<T>::w6(R);
     int k0 = wl1_off[i], k1 = wl1_off[i + 1], cnt = 0;
+    // software pipeline: the next entry's index and oxygen are loaded one iteration ahead
+    int jn = k0 < k1 ? wl1[k0] : 0;
+    T4 ojn = pos[3 * jn];
     for (int k = k0; k < k1; ++k) {
-        int j = wl1[k];
-        T4 oj = pos[3 * j];
+        const int j = jn;
+        const T4 oj = ojn;
+        if (k + 1 < k1) {
+            jn = wl1[k + 1];
+            ojn = pos[3 * jn];
+        }
         T dx = oi0.x - oj.x, dy = oi0.y - oj.y, dz = oi0.z - oj.z;
         T nx = nb_rint(dx * iL0), ny = nb_rint(dy * iL1), nz = nb_rint(dz * iL2);
         dx = nb_shift(R, 0, dx, nx);
