@@ -58,6 +58,8 @@ struct RepDev {
     float spread_inv;        // a power of two chosen so one atom's contribution stays below 2^21
     double pme_fac;          // pi^2 / alpha^2
     double pivol;            // pi * volume
+    float pme_fac2f, pivolf; // FP32 path: pi^2 / alpha^2 * log2(e), pi * volume
+    float pme_gs[3];         // FP32 path: fc * n_d / L_d (PME gradient scale per unit charge)
     int arith, hvdw0, lj_switch, has_water;
     int wtiled;              // water-water lists built by tiled all-pairs (box of <= 64 cells)
     double e_self;

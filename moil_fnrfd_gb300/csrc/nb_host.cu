@@ -299,6 +299,9 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         }
         R.fcd = sqrt(epstmp);
         R.fc = (float)R.fcd;
+        R.pme_gs[0] = (float)(R.fcd * R.n1 * R.invLd[0]);
+        R.pme_gs[1] = (float)(R.fcd * R.n2 * R.invLd[1]);
+        R.pme_gs[2] = (float)(R.fcd * R.n3 * R.invLd[2]);
         {
             // int32 plane accumulation: one atom's largest stencil weight, q fc (2/3)^3, times
             // the scale stays below 2^21 (so the FP32 rounding trick is exact); power of two
@@ -312,6 +315,8 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         }
         R.pme_fac = M_PI * M_PI / (alpha * alpha);
         R.pivol = M_PI * p->a * p->b * p->c;
+        R.pme_fac2f = (float)(R.pme_fac * 1.4426950408889634);
+        R.pivolf = (float)R.pivol;
         // atoms and units
         R.wat0 = (int)wat0; R.oth0 = (int)oth0;
         int noth = 0;

@@ -96,27 +96,6 @@ template <typename C> __device__ __forceinline__ void bfly5(C *v)
     v[3] = csub(p2, mq2);
 }
 
-// MOIL fill_bspline for order 4 (ewald_receip.f:1022-1080)
-template <typename T>
-__device__ __forceinline__ void bspline4(T w, T th[4], T dth[4])
-{
-    th[3] = 0;
-    th[1] = w;
-    th[0] = (T)1 - w;
-    th[2] = (T)0.5 * w * th[1];
-    th[1] = (T)0.5 * ((w + (T)1) * th[0] + ((T)2 - w) * th[1]);
-    th[0] = (T)0.5 * ((T)1 - w) * th[0];
-    dth[0] = -th[0];
-    dth[1] = th[0] - th[1];
-    dth[2] = th[1] - th[2];
-    dth[3] = th[2] - th[3];
-    const T d3 = (T)(1.0 / 3.0);
-    th[3] = d3 * w * th[2];
-    th[2] = d3 * ((w + (T)1) * th[1] + ((T)3 - w) * th[2]);
-    th[1] = d3 * ((w + (T)2) * th[0] + ((T)2 - w) * th[1]);
-    th[0] = d3 * ((T)1 - w) * th[0];
-}
-
 __device__ __forceinline__ float nb_round(float x) { return roundf(x); }
 __device__ __forceinline__ double nb_round(double x) { return round(x); }
 
@@ -177,7 +156,32 @@ template <> struct Acc<double> {
     __device__ static double get(type v, double) { return v; }
 };
 
-// the 4x4 x-y stencil of every atom whose z stencil reaches plane z
+// Order-4 weights of fractional offset w in closed form (the cardinal cubic B-spline that
+// fill_bspline's recursion evaluates, ewald_receip.f:1022-1080):
+//   th = ((1-w)^3, 4 - 6w^2 + 3w^3, 1 + 3w + 3w^2 - 3w^3, w^3) / 6
+//   dth = (-(1-w)^2, 3w^2 - 4w, 1 + 2w - 3w^2, w^2) / 2
+template <typename T>
+__device__ __forceinline__ void bsp4_th(T w, T th[4])
+{
+    const T w2 = w * w, w3 = w2 * w, m = (T)1 - w, s = (T)(1.0 / 6.0);
+    th[0] = s * m * m * m;
+    th[1] = s * ((T)4 - (T)6 * w2 + (T)3 * w3);
+    th[2] = s * ((T)1 + (T)3 * (w + w2 - w3));
+    th[3] = s * w3;
+}
+template <typename T>
+__device__ __forceinline__ void bsp4_dth(T w, T d[4])
+{
+    const T w2 = w * w, m = (T)1 - w;
+    d[0] = (T)-0.5 * m * m;
+    d[1] = (T)0.5 * w * ((T)3 * w - (T)4);
+    d[2] = (T)0.5 * ((T)1 + (T)2 * w - (T)3 * w2);
+    d[3] = (T)0.5 * w2;
+}
+// grid index i in [-3, n] wrapped into [0, n)
+__device__ __forceinline__ int pme_wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// the 4x4 x-y stencil of every atom whose z stencil reaches plane z; one atom per thread
 template <typename T>
 __device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *__restrict__ zstart,
                                              const int *__restrict__ zatoms, const typename vec4<T>::type *fr,
@@ -188,23 +192,26 @@ __device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *
     for (int tp = 0; tp < 4; ++tp) {
         int zb = z + tp;
         zb = zb >= n3 ? zb - n3 : zb;
-        int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
-        int t3 = 3 - tp;
-        for (int idx = threadIdx.x; idx < (b1 - b0) * 4; idx += blockDim.x) {
-            int s = zatoms[b0 + (idx >> 2)], t2 = idx & 3;
-            T4 f = fr[s];
-            int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
-            T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
-            bspline4<T>(f.x - (T)i1, th1, dt1);
-            bspline4<T>(f.y - (T)i2, th2, dt2);
-            bspline4<T>(f.z - (T)i3, th3, dt3);
-            int j = i2 - 3 + t2;
-            j = (j + 2 * n2) % n2;
-            T v = th2[t2] * th3[t3] * (f.w * scale);
-            typename Acc<T>::type *row = acc + j * n1;
-            int i0 = i1 - 3 + 2 * n1;
+        const int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
+        const int t3 = 3 - tp;
+        for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
+            const T4 f = fr[zatoms[idx]];
+            const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            T th1[4], th2[4], th3[4];
+            bsp4_th<T>(f.x - (T)i1, th1);
+            bsp4_th<T>(f.y - (T)i2, th2);
+            bsp4_th<T>(f.z - (T)i3, th3);
+            const T qz = th3[t3] * (f.w * scale);
+            int xs[4];
 #pragma unroll
-            for (int t1 = 0; t1 < 4; ++t1) Acc<T>::add(row + (i0 + t1) % n1, v * th1[t1]);
+            for (int t1 = 0; t1 < 4; ++t1) xs[t1] = pme_wrap(i1 - 3 + t1, n1);
+#pragma unroll
+            for (int t2 = 0; t2 < 4; ++t2) {
+                typename Acc<T>::type *row = acc + pme_wrap(i2 - 3 + t2, n2) * n1;
+                const T v = th2[t2] * qz;
+#pragma unroll
+                for (int t1 = 0; t1 < 4; ++t1) Acc<T>::add(row + xs[t1], v * th1[t1]);
+            }
         }
     }
 }
@@ -220,26 +227,28 @@ __device__ __forceinline__ void gather_plane(const RepDev &R, int z, const int *
     for (int tp = 0; tp < 4; ++tp) {
         int zb = z + tp;
         zb = zb >= n3 ? zb - n3 : zb;
-        int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
-        int t3 = 3 - tp;
+        const int b0 = zstart[R.zb0 + zb], b1 = zstart[R.zb0 + zb + 1];
+        const int t3 = 3 - tp;
         for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
-            int s = zatoms[idx];
-            T4 f = fr[s];
-            int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            const int s = zatoms[idx];
+            const T4 f = fr[s];
+            const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
             T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
-            bspline4<T>(f.x - (T)i1, th1, dt1);
-            bspline4<T>(f.y - (T)i2, th2, dt2);
-            bspline4<T>(f.z - (T)i3, th3, dt3);
+            const T w1 = f.x - (T)i1, w2 = f.y - (T)i2, w3 = f.z - (T)i3;
+            bsp4_th<T>(w1, th1); bsp4_dth<T>(w1, dt1);
+            bsp4_th<T>(w2, th2); bsp4_dth<T>(w2, dt2);
+            bsp4_th<T>(w3, th3); bsp4_dth<T>(w3, dt3);
+            int xs[4];
+#pragma unroll
+            for (int t1 = 0; t1 < 4; ++t1) xs[t1] = pme_wrap(i1 - 3 + t1, n1);
             T gx = 0, gy = 0, gz = 0;
-            int i0 = i1 - 3 + 2 * n1;
 #pragma unroll
             for (int t2 = 0; t2 < 4; ++t2) {
-                int j = (i2 - 3 + t2 + 2 * n2) % n2;
-                const T *row = Rp + j * n1;
+                const T *row = Rp + pme_wrap(i2 - 3 + t2, n2) * n1;
                 T sx = 0, sy = 0;
 #pragma unroll
                 for (int t1 = 0; t1 < 4; ++t1) {
-                    T q = row[(i0 + t1) % n1];
+                    const T q = row[xs[t1]];
                     sx += q * dt1[t1];
                     sy += q * th1[t1];
                 }
@@ -380,7 +389,7 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
                                                  double *__restrict__ e_col)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double red[256];
+    __shared__ double red[8];
     const ColWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
@@ -397,9 +406,8 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     float2 *F = fft_lines<0, false>(p3, A, B, nullptr, tk, 0, tab, tw);
     float2 *Fo = F == A ? B : A;
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
-    // influence function with the replica constants converted once per thread:
-    // exp(-pi^2 m^2 / alpha^2) = 2^(-fac2 m^2), fac2 = pi^2 / alpha^2 * log2(e)
-    const float fac2 = (float)(R.pme_fac * 1.4426950408889634), pivol = (float)R.pivol;
+    // influence function: exp(-pi^2 m^2 / alpha^2) = 2^(-fac2 m^2), fac2 = pi^2 / alpha^2 * log2(e)
+    const float fac2 = R.pme_fac2f, pivol = R.pivolf;
     const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
     const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
     const float mh1 = (float)w.kx * iL0, pb1 = pivol * bsp[w.kx];
@@ -411,8 +419,9 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
         for (int kz = lane; kz < n3; kz += 32) {
             const float mh3 = (float)(kz < nf3 ? kz : kz - n3) * iL2;
             const float msq = fmaf(mh3, mh3, m12);
-            float et = (w.kx == 0 && ky == 0 && kz == 0) ? 0.f
-                                                          : exp2f(-fac2 * msq) * __frcp_rn(pb12 * bsp[n1 + n2 + kz] * msq);
+            float et = (w.kx == 0 && ky == 0 && kz == 0)
+                           ? 0.f
+                           : nb_ex2_approx(-fac2 * msq) * nb_rcp_approx(pb12 * bsp[n1 + n2 + kz] * msq);
             float2 v = F[c * n3 + kz];
             en += wgt * et * (v.x * v.x + v.y * v.y);
             F[c * n3 + kz] = make_float2(v.x * et, -v.y * et);    // conj: the inverse runs forward
@@ -422,13 +431,16 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     float2 *I = fft_lines<0, true>(p3, F, Fo, nullptr, tk, 0, tab, tw);
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) g[kz * zs + lane] = I[lane * n3 + kz];
-    red[threadIdx.x] = (double)en;
+    // fixed-order reduction: FP32 within each warp, FP64 over the 8 warp sums
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) en += __shfl_down_sync(0xffffffffu, en, o);
+    if (lane == 0) red[warp] = (double)en;
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int k = 0; k < 8; ++k) sum += red[k];
+        e_col[blockIdx.x] = sum;
     }
-    if (threadIdx.x == 0) e_col[blockIdx.x] = red[0];
 }
 
 __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
@@ -455,11 +467,11 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
     float2 *Yt = (p2.nst & 1) ? P1 : P0;
     // expand each ky row to the full Hermitian line of n1, conjugated again for the inverse
     float2 *Xs = Yt == P0 ? P1 : P0;
-    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) {
-        int ky = k / n1, i = k - ky * n1;
-        float2 v = i < n1h ? Yt[ky * n1h + i] : cconj(Yt[ky * n1h + (n1 - i)]);
-        Xs[k] = cconj(v);
-    }
+    for (int ky = threadIdx.x >> 5; ky < n2; ky += blockDim.x >> 5)
+        for (int i = threadIdx.x & 31; i < n1; i += 32) {
+            float2 v = i < n1h ? Yt[ky * n1h + i] : cconj(Yt[ky * n1h + (n1 - i)]);
+            Xs[ky * n1 + i] = cconj(v);
+        }
     __syncthreads();
     // x: n2 lines of n1; the last pass stores real parts into Rp[ky][x]
     fft_lines<2, false>(p1, Xs, Yt, Rp, n2, 0, tab, tw);
@@ -1062,6 +1074,8 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     R.alphad = alpha;
     R.pme_fac = M_PI * M_PI / (alpha * alpha);
     R.pivol = M_PI * box[0] * box[1] * box[2];
+    R.pme_fac2f = (float)(R.pme_fac * 1.4426950408889634);
+    R.pivolf = (float)R.pivol;
     R.natom = natom;
     FftPlanDev plans[3];
     int rep_plan[3];

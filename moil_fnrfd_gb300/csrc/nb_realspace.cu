@@ -116,6 +116,47 @@ __device__ __forceinline__ void flush(double g[], long long G[], int n)
     }
 }
 
+// water sites of molecule i against its W2 list of non-water atoms: atom semantics per site
+// pair; partial gradients and energies go to g / e4, flushed every CHUNK entries
+template <typename T, typename Flush>
+__device__ __forceinline__ void water_vs_atoms(const RepDev &R, int i, const typename vec4<T>::type *pos,
+                                               const void *lj_v, const unsigned *__restrict__ sflags,
+                                               const int *__restrict__ wl2_off, const int *__restrict__ wl2, T g[9],
+                                               T e4[4], int &npair, Flush &flush_all)
+{
+    typedef typename vec4<T>::type T4;
+    typedef typename cplx<T>::type T2;
+    const int q0 = wl2_off[i], q1 = wl2_off[i + 1];
+    if (q0 >= q1) return;
+    const T2 *lj = (const T2 *)lj_v;
+    const T4 si[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    const T2 lji[3] = {lj[3 * i], lj[3 * i + 1], lj[3 * i + 2]};
+    const unsigned fi[3] = {sflags[3 * i], sflags[3 * i + 1], sflags[3 * i + 2]};
+    int cnt = 0;
+    for (int k = q0; k < q1; ++k) {
+        int s = wl2[k];
+        T4 xj = pos[s];
+        T2 ljj = lj[s];
+        unsigned fj = sflags[s];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            T dx = si[a].x - xj.x, dy = si[a].y - xj.y, dz = si[a].z - xj.z;
+            bool img;
+            min_image<T>(R, dx, dy, dz, img);
+            T r2 = dx * dx + dy * dy + dz * dz;
+            T eel = 0, elj = 0;
+            T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj, npair);
+            g[3 * a] += df * dx;
+            g[3 * a + 1] += df * dy;
+            g[3 * a + 2] += df * dz;
+            e4[img ? 1 : 0] += elj;
+            e4[img ? 3 : 2] += eel;
+        }
+        if (++cnt == CHUNK) { flush_all(); cnt = 0; }
+    }
+    flush_all();
+}
+
 // ---------------------------------------------------------------------------------
 // water molecule per thread: W1 (water-water, 9 site pairs) then W2 (water-site x other).
 // Per-lane FP32 partial gradients and energies are flushed every CHUNK list entries into
@@ -224,38 +265,174 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
         if (++cnt == CHUNK) { flush_all(); cnt = 0; }
     }
     flush_all();
-    // water sites against non-water atoms: atom semantics per site pair
-    int q0 = wl2_off[i], q1 = wl2_off[i + 1];
-    if (q0 < q1) {
-        const T2 *lj = (const T2 *)lj_v;
-        const T4 si[3] = {oi0, pos[3 * i + 1], pos[3 * i + 2]};
-        const T2 lji[3] = {lj[3 * i], lj[3 * i + 1], lj[3 * i + 2]};
-        const unsigned fi[3] = {sflags[3 * i], sflags[3 * i + 1], sflags[3 * i + 2]};
-        cnt = 0;
-        for (int k = q0; k < q1; ++k) {
-            int s = wl2[k];
-            T4 xj = pos[s];
-            T2 ljj = lj[s];
-            unsigned fj = sflags[s];
+    water_vs_atoms<T>(R, i, pos, lj_v, sflags, wl2_off, wl2, g, e4, npair, flush_all);
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                T dx = si[a].x - xj.x, dy = si[a].y - xj.y, dz = si[a].z - xj.z;
-                bool img;
-                min_image<T>(R, dx, dy, dz, img);
-                T r2 = dx * dx + dy * dy + dz * dz;
-                T eel = 0, elj = 0;
-                T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj,
-                                    npair);
-                g[3 * a] += df * dx;
-                g[3 * a + 1] += df * dy;
-                g[3 * a + 2] += df * dz;
-                e4[img ? 1 : 0] += elj;
-                e4[img ? 3 : 2] += eel;
-            }
-            if (++cnt == CHUNK) { flush_all(); cnt = 0; }
+    for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
+    double *eu = e_unit + NB_EU * (size_t)i;
+    eu[0] = sE[0][t]; eu[1] = sE[1][t]; eu[2] = sE[2][t]; eu[3] = sE[3][t]; eu[4] = (double)npair;
+}
+
+// ---------------------------------------------------------------------------------
+// FP32 water kernel on the packed two-lane FP32 pipe: list entries are taken two at a
+// time and every quantity of the 9 site pairs is a float2 over (entry k, entry k+1).  A
+// molecule outside the O-O cutoff (or the missing partner of an odd tail) is moved 1e4 Å
+// away, where erfc and exp underflow to exactly zero, so it adds nothing without a branch.
+// Gradients are accumulated per lane as float2 and folded at each flush; W2 (water sites vs
+// non-water atoms) runs the scalar code of k_water.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__restrict__ reps,
+                                                       const int *__restrict__ site_rep, const float4 *__restrict__ pos,
+                                                       const float4 *__restrict__ woff, const void *lj_v,
+                                                       const unsigned *__restrict__ sflags,
+                                                       const int *__restrict__ wl1_off, const int *__restrict__ wl1,
+                                                       const int *__restrict__ wl2_off, const int *__restrict__ wl2,
+                                                       long long *__restrict__ grad, double *__restrict__ e_unit)
+{
+    __shared__ long long sG[9][WBLOCK];
+    __shared__ double sE[4][WBLOCK];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * WBLOCK + t;
+    if (i >= nW) return;
+    const RepDev &R = reps[site_rep[3 * i]];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) sG[k][t] = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sE[k][t] = 0.0;
+    const float4 oi0 = pos[3 * i];
+    const float4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
+    // H offsets of molecule i, duplicated into both lanes
+    const float2 hi[2][3] = {{f2(oi1.x), f2(oi1.y), f2(oi1.z)}, {f2(oi2.x), f2(oi2.y), f2(oi2.z)}};
+    float2 G[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) G[k] = f2(0.f);
+    float g[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) g[k] = 0.f;
+    float e4[4] = {0.f, 0.f, 0.f, 0.f};   // LJ prim, LJ img, Coulomb prim, Coulomb img
+    auto flush_all = [&]() {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            sG[k][t] += nb_fix(g[k] - (G[k].x + G[k].y));   // G holds minus the gradient
+            g[k] = 0.f;
+            G[k] = f2(0.f);
         }
-        flush_all();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { sE[k][t] += (double)e4[k]; e4[k] = 0.f; }
+    };
+    int npair = 0;
+    const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
+    const float rmax2 = R.rmax2, rv2 = R.rv2;
+    const float2 alpha = f2(R.alpha), ex2c = f2(R.ex2c);
+    const float2 w12 = f2(R.w12), nw6 = f2(-R.w6);
+    const float qqv[3] = {R.qq[0], R.qq[1], R.qq[2]};
+    const float c2a = R.c2a;
+    const int k0 = wl1_off[i], k1 = wl1_off[i + 1];
+    int cnt = 0;
+    // next pair of entries, loaded one iteration ahead
+    int ja = k0 < k1 ? wl1[k0] : 0;
+    int jb = k0 + 1 < k1 ? wl1[k0 + 1] : ja;
+    float4 oa = pos[3 * ja], ob = pos[3 * jb];
+    for (int k = k0; k < k1; k += 2) {
+        const bool hasb = k + 1 < k1;
+        const int j0 = ja, j1 = jb;
+        const float4 o0 = oa, o1 = ob;
+        if (k + 2 < k1) {
+            ja = wl1[k + 2];
+            jb = k + 3 < k1 ? wl1[k + 3] : ja;
+            oa = pos[3 * ja];
+            ob = pos[3 * jb];
+        }
+        // O-O minimum image per entry
+        float dx0 = oi0.x - o0.x, dy0 = oi0.y - o0.y, dz0 = oi0.z - o0.z;
+        float dx1 = oi0.x - o1.x, dy1 = oi0.y - o1.y, dz1 = oi0.z - o1.z;
+        const float nx0 = rintf(dx0 * iL0), ny0 = rintf(dy0 * iL1), nz0 = rintf(dz0 * iL2);
+        const float nx1 = rintf(dx1 * iL0), ny1 = rintf(dy1 * iL1), nz1 = rintf(dz1 * iL2);
+        dx0 = nb_shift(R, 0, dx0, nx0); dy0 = nb_shift(R, 1, dy0, ny0); dz0 = nb_shift(R, 2, dz0, nz0);
+        dx1 = nb_shift(R, 0, dx1, nx1); dy1 = nb_shift(R, 1, dy1, ny1); dz1 = nb_shift(R, 2, dz1, nz1);
+        const float r0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0, r1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
+        const bool in0 = r0 <= rmax2, in1 = hasb && r1 <= rmax2;
+        if (in0 || in1) {
+            const float4 a1 = woff[2 * j0], a2 = woff[2 * j0 + 1];
+            const float4 b1 = woff[2 * j1], b2 = woff[2 * j1 + 1];
+            if (!in0) { dx0 = 1.0e4f; dy0 = 0.f; dz0 = 0.f; }
+            if (!in1) { dx1 = 1.0e4f; dy1 = 0.f; dz1 = 0.f; }
+            // q[b] = (O_i - O_j - nL) - offset_j[b]; site displacement = offset_i[a] + q[b]
+            float2 eel = f2(0.f), elj = f2(0.f);
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                float2 q[3];
+                if (b == 0) {
+                    q[0] = f2(dx0, dx1); q[1] = f2(dy0, dy1); q[2] = f2(dz0, dz1);
+                } else if (b == 1) {
+                    q[0] = f2(dx0 - a1.x, dx1 - b1.x); q[1] = f2(dy0 - a1.y, dy1 - b1.y);
+                    q[2] = f2(dz0 - a1.z, dz1 - b1.z);
+                } else {
+                    q[0] = f2(dx0 - a2.x, dx1 - b2.x); q[1] = f2(dy0 - a2.y, dy1 - b2.y);
+                    q[2] = f2(dz0 - a2.z, dz1 - b2.z);
+                }
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float2 ddx = a ? __fadd2_rn(hi[a - 1][0], q[0]) : q[0];
+                    const float2 ddy = a ? __fadd2_rn(hi[a - 1][1], q[1]) : q[1];
+                    const float2 ddz = a ? __fadd2_rn(hi[a - 1][2], q[2]) : q[2];
+                    const float2 rr2 = __ffma2_rn(ddx, ddx, __ffma2_rn(ddy, ddy, __fmul2_rn(ddz, ddz)));
+                    const float2 rinv = f2(nb_rsqrt_approx(rr2.x), nb_rsqrt_approx(rr2.y));
+                    const float2 s2 = __fmul2_rn(rinv, rinv);
+                    const float2 x = __fmul2_rn(__fmul2_rn(alpha, rr2), rinv);
+                    const float2 arg = __fmul2_rn(rr2, ex2c);
+                    // erfc(x) = exp(-x^2) * t * P(A t + B), t = 1 / (1 + P x)
+                    const float2 den = __ffma2_rn(f2(ERFCX_P), f2(fminf(x.x, 4.5f), fminf(x.y, 4.5f)), f2(1.f));
+                    const float2 tt = f2(nb_rcp_approx(den.x), nb_rcp_approx(den.y));
+                    const float2 u = __ffma2_rn(f2(ERFCX_A), tt, f2(ERFCX_B));
+                    const float C[ERFCX_NC] = ERFCX_COEFS;
+                    float2 p = f2(C[ERFCX_NC - 1]);
+#pragma unroll
+                    for (int m = ERFCX_NC - 2; m >= 0; --m) p = __ffma2_rn(p, u, f2(C[m]));
+                    const float2 ex = f2(nb_ex2_approx(-arg.x), nb_ex2_approx(-arg.y));
+                    const float2 erfcv = __fmul2_rn(ex, __fmul2_rn(tt, p));
+                    const float qq = (a == 0 && b == 0) ? qqv[0] : ((a == 0 || b == 0) ? qqv[1] : qqv[2]);
+                    const float2 e = __fmul2_rn(__fmul2_rn(f2(qq), erfcv), rinv);
+                    // minus dE/dr / r
+                    float2 mdf = __fmul2_rn(__ffma2_rn(f2(qq * c2a), ex, e), s2);
+                    if (a == 0 && b == 0) {
+                        const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+                        const float2 A = __fmul2_rn(__fmul2_rn(w12, s6), s6);
+                        float2 e1 = __ffma2_rn(nw6, s6, A);   // A - B
+                        // -df1 = 6 s2 (A + e1)
+                        float2 m1 = __fmul2_rn(__fmul2_rn(f2(6.f), s2), __fadd2_rn(A, e1));
+                        if (R.lj_switch) {
+                            float d0 = -m1.x, d1 = -m1.y;
+                            lj_switch_apply<float>(R, rr2.x, e1.x, d0);
+                            lj_switch_apply<float>(R, rr2.y, e1.y, d1);
+                            m1 = f2(-d0, -d1);
+                        }
+                        const bool l0 = rr2.x <= rv2, l1 = rr2.y <= rv2;
+                        e1 = f2(l0 ? e1.x : 0.f, l1 ? e1.y : 0.f);
+                        m1 = f2(l0 ? m1.x : 0.f, l1 ? m1.y : 0.f);
+                        elj = __fadd2_rn(elj, e1);
+                        mdf = __fadd2_rn(mdf, m1);
+                    }
+                    eel = __fadd2_rn(eel, e);
+                    G[3 * a] = __ffma2_rn(mdf, ddx, G[3 * a]);
+                    G[3 * a + 1] = __ffma2_rn(mdf, ddy, G[3 * a + 1]);
+                    G[3 * a + 2] = __ffma2_rn(mdf, ddz, G[3 * a + 2]);
+                }
+            }
+            const bool img0 = (nx0 != 0.f) | (ny0 != 0.f) | (nz0 != 0.f);
+            const bool img1 = (nx1 != 0.f) | (ny1 != 0.f) | (nz1 != 0.f);
+            e4[img0 ? 1 : 0] += elj.x;
+            e4[img0 ? 3 : 2] += eel.x;
+            e4[img1 ? 1 : 0] += elj.y;
+            e4[img1 ? 3 : 2] += eel.y;
+            npair += 9 * ((int)in0 + (int)in1);
+        }
+        cnt += 2;
+        if (cnt >= CHUNK) { flush_all(); cnt = 0; }
     }
+    flush_all();
+    water_vs_atoms<float>(R, i, pos, lj_v, sflags, wl2_off, wl2, g, e4, npair, flush_all);
 #pragma unroll
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
@@ -379,6 +556,62 @@ __global__ void k_excl_water(int nW, const int *__restrict__ unit_atom, const in
     }
 }
 
+// FP32 path of the water exclusion corrections, one sorted water per thread: the three
+// intramolecular displacements come from the FP64-formed H offsets (O-H1, O-H2, H2-H1), so
+// no absolute FP32 coordinate enters; erf(x)/x from its Taylor series in u = x^2 (9 terms,
+// truncation below 6e-9 for u <= 0.5), erff beyond.  Results go to the caller-order arrays.
+__global__ void __launch_bounds__(128) k_excl_water_f(int nW, const int *__restrict__ site_orig,
+                                                      const int *__restrict__ site_rep,
+                                                      const RepDev *__restrict__ reps, const float4 *__restrict__ pos,
+                                                      const float4 *__restrict__ woff, double *__restrict__ grad,
+                                                      double *__restrict__ e_out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nW) return;
+    const RepDev &R = reps[site_rep[3 * p]];
+    const int a0 = site_orig[3 * p];
+    const float4 h1 = woff[2 * p], h2 = woff[2 * p + 1];
+    const float q[3] = {pos[3 * p].w, pos[3 * p + 1].w, pos[3 * p + 2].w};
+    // displacement x_a - x_b for the pairs (O,H1), (O,H2), (H1,H2)
+    const float d[3][3] = {{-h1.x, -h1.y, -h1.z}, {-h2.x, -h2.y, -h2.z}, {h1.x - h2.x, h1.y - h2.y, h1.z - h2.z}};
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    const float al = R.alpha, ke = (float)R.epstmp, c2 = (float)NB_TWO_OVER_SQRTPI;
+    float g[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}}, ecorr = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float rx = d[k][0], ry = d[k][1], rz = d[k][2];
+        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz)), u = al * al * r2;
+        const float qq = q[pa[k]] * q[pb[k]] * ke;
+        float e, df;
+        if (u <= 0.5f) {
+            float s = 1.f / 685440.f, ds = 8.f / 685440.f;
+            s = fmaf(s, u, -1.f / 75600.f); s = fmaf(s, u, 1.f / 9360.f); s = fmaf(s, u, -1.f / 1320.f);
+            s = fmaf(s, u, 1.f / 216.f); s = fmaf(s, u, -1.f / 42.f); s = fmaf(s, u, 0.1f);
+            s = fmaf(s, u, -1.f / 3.f); s = fmaf(s, u, 1.f);
+            ds = fmaf(ds, u, -7.f / 75600.f); ds = fmaf(ds, u, 6.f / 9360.f); ds = fmaf(ds, u, -5.f / 1320.f);
+            ds = fmaf(ds, u, 4.f / 216.f); ds = fmaf(ds, u, -3.f / 42.f); ds = fmaf(ds, u, 0.2f);
+            ds = fmaf(ds, u, -1.f / 3.f);
+            e = -qq * al * c2 * s;
+            df = -qq * 2.f * al * al * al * c2 * ds;
+        } else {
+            const float rij = sqrtf(r2), sinv = 1.f / rij, x = al * rij;
+            const float erfv = erff(x), derfc = c2 * expf(-x * x);
+            e = -qq * sinv * erfv;
+            df = qq * sinv * (sinv * sinv * erfv - sinv * al * derfc);
+        }
+        ecorr += e;
+        const int a = pa[k], b = pb[k];
+        g[a][0] += df * rx; g[a][1] += df * ry; g[a][2] += df * rz;
+        g[b][0] -= df * rx; g[b][1] -= df * ry; g[b][2] -= df * rz;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double *gp = grad + 3 * (size_t)(a0 + k), *ep = e_out + 3 * (size_t)(a0 + k);
+        gp[0] = g[k][0]; gp[1] = g[k][1]; gp[2] = g[k][2];
+        ep[0] = k == 0 ? (double)ecorr : 0.0; ep[1] = 0.0; ep[2] = 0.0;
+    }
+}
+
 // exclusion erf corrections (cdie_ewald.f:117-199) and 1-4 terms (ener14.f:38-95), FP64,
 // gathered per atom over both directions; raw (unimaged) displacements as MOIL uses.
 // With skip_water set, water atoms are left to k_excl_water.
@@ -442,22 +675,37 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
     if (a >= natom) return;
     const RepDev &R = reps[atom_rep[a]];
     int s = site_of[a];
-    double pg[3] = {0, 0, 0};
     const T *p = part + 12 * (size_t)s;
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        pg[0] += (double)p[3 * t];
-        pg[1] += (double)p[3 * t + 1];
-        pg[2] += (double)p[3 * t + 2];
-    }
-    double qf = q[a] * R.fcd;
-    double sc[3] = {qf * R.n1 * R.invLd[0], qf * R.n2 * R.invLd[1], qf * R.n3 * R.invLd[2]};
     bool bad = false;
+    if constexpr (sizeof(T) == 4) {
+        // FP32 path: the PME share is summed and scaled in FP32 (its own precision); FP64
+        // only where the fixed-point and FP64 terms meet, 4 operations per component
+        const float qs = (float)q[a];
+        const float pg[3] = {((p[0] + p[3]) + p[6]) + p[9], ((p[1] + p[4]) + p[7]) + p[10],
+                             ((p[2] + p[5]) + p[8]) + p[11]};
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double v = (double)grad_site[3 * (size_t)s + d] * NB_FIX_INV + grad_ex[3 * (size_t)a + d] + sc[d] * pg[d];
-        bad |= !(v == v);
-        dpot[3 * (size_t)a + d] = v;
+        for (int d = 0; d < 3; ++d) {
+            double v = fma((double)grad_site[3 * (size_t)s + d], NB_FIX_INV, grad_ex[3 * (size_t)a + d]) +
+                       (double)(qs * R.pme_gs[d] * pg[d]);
+            bad |= !(v == v);
+            dpot[3 * (size_t)a + d] = v;
+        }
+    } else {
+        double pg[3] = {0, 0, 0};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            pg[0] += (double)p[3 * t];
+            pg[1] += (double)p[3 * t + 1];
+            pg[2] += (double)p[3 * t + 2];
+        }
+        double qf = q[a] * R.fcd;
+        double sc[3] = {qf * R.n1 * R.invLd[0], qf * R.n2 * R.invLd[1], qf * R.n3 * R.invLd[2]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double v = (double)grad_site[3 * (size_t)s + d] * NB_FIX_INV + grad_ex[3 * (size_t)a + d] + sc[d] * pg[d];
+            bad |= !(v == v);
+            dpot[3 * (size_t)a + d] = v;
+        }
     }
     if (bad) atomicOr(&st[1], NB_DEV_ERR_NAN);
 }
@@ -513,9 +761,15 @@ void realspace_t(NbCtx *c)
     cudaStream_t s = c->stream;
     if (c->timing) cudaEventRecord(c->ev[2], s);
     if (c->nW > 0) {
-        k_water<T><<<(int)((c->nW + WBLOCK - 1) / WBLOCK), WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos,
-                                                              c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_off, c->d_wl1,
-                                                              c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
+        const int nb = (int)((c->nW + WBLOCK - 1) / WBLOCK);
+        if constexpr (sizeof(T) == 4)
+            k_water_f<<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos,
+                                            (const float4 *)c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_off,
+                                            c->d_wl1, c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
+        else
+            k_water<T><<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
+                                             c->d_site_lj, c->d_site_flags, c->d_wl1_off, c->d_wl1, c->d_wl2_off,
+                                             c->d_wl2, c->d_grad_site, c->d_e_unit);
         c->launches++;
     }
     if (c->timing) cudaEventRecord(c->ev[3], s);
@@ -540,8 +794,13 @@ void nb_launch_excl14(NbCtx *c, const double *d_coor)
 {
     const int fast = c->water_excl_fast && c->nW > 0;
     if (fast) {
-        k_excl_water<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
-            (int)c->nW, c->d_unit_atom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_grad_ex, c->d_e_ex);
+        if (c->precision == MOIL_NB_FP64)
+            k_excl_water<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
+                (int)c->nW, c->d_unit_atom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_grad_ex, c->d_e_ex);
+        else
+            k_excl_water_f<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
+                (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_reps, (const float4 *)c->d_pos,
+                (const float4 *)c->d_woff, c->d_grad_ex, c->d_e_ex);
         c->launches++;
     }
     if (!fast || c->nA > 0) {
