@@ -105,6 +105,9 @@ __device__ __forceinline__ float nb_ex2_approx(float x)
     return r;
 }
 
+// L1 prefetch hint; callers pass addresses inside their own allocation
+__device__ __forceinline__ void nb_prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ float nb_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double nb_rint(double x) { return rint(x); }
 __device__ __forceinline__ float nb_rsqrt(float x) { return nb_rsqrt_approx(x); }

@@ -338,6 +338,8 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
         const bool hasb = k + 1 < k1;
         const int j0 = ja, j1 = jb;
         const float4 o0 = oa, o1 = ob;
+        // each lane streams its own list (a DRAM stream): pull the line 32 entries ahead
+        nb_prefetch_l1(wl1 + min(k + 32, k1 - 1));
         if (k + 2 < k1) {
             ja = wl1[k + 2];
             jb = k + 3 < k1 ? wl1[k + 3] : ja;
