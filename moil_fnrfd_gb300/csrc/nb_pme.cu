@@ -99,7 +99,7 @@ template <typename C> __device__ __forceinline__ void bfly5(C *v)
 __device__ __forceinline__ float nb_round(float x) { return roundf(x); }
 __device__ __forceinline__ double nb_round(double x) { return round(x); }
 
-__device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+__host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 // ---------------------------------------------------------------------------------
 // binning (both precisions)
@@ -285,6 +285,7 @@ __device__ __forceinline__ T eterm_of(const RepDev &R, const T *bsp, int kx, int
 // One Stockham stage over L lines of length n.  Source line l at src + l*ss (contiguous).
 // Destination: MODE 0 natural (dst + l*ds), MODE 1 transposed (dst[k*L + l] for k < keep),
 // MODE 2 real part natural (rdst + l*ds).  CONJ_OUT conjugates the stored values.
+// tab / tw point into shared memory (fft_ctx_load).
 template <int RADIX, int MODE, bool CONJ_OUT>
 __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                            float *__restrict__ rdst, int L, int ss, int ds, int keep,
@@ -295,13 +296,13 @@ __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float
     for (int b = threadIdx.x; b < total; b += blockDim.x) {
         int line = nb == 1 ? b : (int)__umulhi((unsigned)b, magic);
         int j = b - line * nb;
-        int2 e = __ldg(tab + j);
+        int2 e = tab[j];
         const float2 *s = src + line * ss + j;
         float2 v[RADIX];
 #pragma unroll
         for (int r = 0; r < RADIX; ++r) v[r] = s[r * nb];
 #pragma unroll
-        for (int r = 1; r < RADIX; ++r) v[r] = cmul(v[r], __ldg(tw + r * e.x));
+        for (int r = 1; r < RADIX; ++r) v[r] = cmul(v[r], tw[r * e.x]);
         if (RADIX == 4) bfly4(v);
         else if (RADIX == 2) bfly2(v);
         else if (RADIX == 3) bfly3(v);
@@ -330,23 +331,53 @@ __device__ __forceinline__ void fft_pass(int R, const float2 *src, float2 *dst, 
     }
 }
 
-// Full forward FFT of L lines (length p.n, contiguous, line stride n) held in a; b is scratch.
+// A plan with its stage table and twiddles, staged in shared memory by fft_ctx_load so the
+// butterflies read them without global-memory latency.
+struct FftCtx {
+    const FftPlanDev *p;
+    const int2 *tab;      // plan-local: stage s at tab + p->off[s]
+    const float2 *tw;     // plan-local twiddles, n entries
+};
+
+// shared-memory bytes of one staged plan of length n
+size_t fft_ctx_bytes(int n);
+
+__device__ __forceinline__ unsigned char *fft_ctx_load(unsigned char *dst, const FftPlanDev *__restrict__ gp,
+                                                       const int2 *__restrict__ gtab, const float2 *__restrict__ gtw,
+                                                       FftCtx &ctx)
+{
+    const int n = gp->n, nst = gp->nst;
+    const int ntab = gp->off[nst - 1] + gp->nb[nst - 1];
+    FftPlanDev *sp = (FftPlanDev *)dst;
+    int2 *st = (int2 *)(dst + align16(sizeof(FftPlanDev)));
+    float2 *stw = (float2 *)((unsigned char *)st + align16(ntab * sizeof(int2)));
+    for (int k = threadIdx.x; k < (int)(sizeof(FftPlanDev) / 4); k += blockDim.x)
+        ((int *)sp)[k] = ((const int *)gp)[k];
+    for (int k = threadIdx.x; k < ntab; k += blockDim.x) st[k] = gtab[gp->tab0 + k];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) stw[k] = gtw[gp->tw0 + k];
+    ctx.p = sp;
+    ctx.tab = st;
+    ctx.tw = stw;
+    return (unsigned char *)stw + align16(n * sizeof(float2));
+}
+
+// Full forward FFT of L lines (length n, contiguous, line stride n) held in a; b is scratch.
 // The last pass is stored in the mode given; returns the buffer holding the result.
 // conj_last conjugates the final output (second half of an inverse transform).
 template <int LAST_MODE, bool CONJ_LAST>
-__device__ float2 *fft_lines(const FftPlanDev &p, float2 *a, float2 *b, float *rdst, int L, int keep,
-                             const int2 *tab, const float2 *tw)
+__device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst, int L, int keep)
 {
+    const FftPlanDev &p = *c.p;
     float2 *src = a, *dst = b;
-    const int n = p.n;
-    for (int s = 0; s < p.nst; ++s) {
-        const int2 *t = tab + p.tab0 + p.off[s];
-        if (s + 1 < p.nst) {
-            fft_pass<0, false>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s], t, tw + p.tw0);
+    const int n = p.n, nst = p.nst;
+    for (int s = 0; s < nst; ++s) {
+        const int2 *t = c.tab + p.off[s];
+        if (s + 1 < nst) {
+            fft_pass<0, false>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s], t, c.tw);
         } else {
             int ds = LAST_MODE == 1 ? 0 : n;
             fft_pass<LAST_MODE, CONJ_LAST>(p.rad[s], src, dst, rdst, L, n, ds, keep, p.ns[s], p.nb[s], p.magic[s], t,
-                                           tw + p.tw0);
+                                           c.tw);
         }
         float2 *x = src; src = dst; dst = x;
     }
@@ -363,10 +394,13 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
     const PlaneWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
-    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
     float2 *A = (float2 *)smem;
     float2 *B = A + n1 * n2;
     int *acc = (int *)B;                        // the accumulator lives in B until the first pass
+    FftCtx c1, c2;
+    unsigned char *ctx = (unsigned char *)(B + n1 * n2);
+    ctx = fft_ctx_load(ctx, plans + rep_plan[3 * w.rep], tab, tw, c1);
+    fft_ctx_load(ctx, plans + rep_plan[3 * w.rep + 1], tab, tw, c2);
     for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
     __syncthreads();
     spread_plane<float>(R, w.z, zstart, zatoms, fr, acc, R.spread_scale);
@@ -375,9 +409,9 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
     for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) A[k] = make_float2(Acc<float>::get(acc[k], inv), 0.f);
     __syncthreads();
     // x: n2 rows of n1 (real input); last pass keeps kx < n1h, transposed to [kx][y]
-    float2 *X = fft_lines<1, false>(p1, A, B, nullptr, n2, n1h, tab, tw);
+    float2 *X = fft_lines<1, false>(c1, A, B, nullptr, n2, n1h);
     // y: n1h lines of n2
-    float2 *Y = fft_lines<0, false>(p2, X, X == A ? B : A, nullptr, n1h, 0, tab, tw);
+    float2 *Y = fft_lines<0, false>(c2, X, X == A ? B : A, nullptr, n1h, 0);
     float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
     for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) g[k] = Y[k];
 }
@@ -394,16 +428,17 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
     const int tk = min(NB_TKF, n2 - w.ky0);
-    const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
     const float *bsp = bsp_all + R.bsp0;
     float2 *A = (float2 *)smem, *B = A + NB_TKF * n3;
+    FftCtx c3;
+    fft_ctx_load((unsigned char *)(B + NB_TKF * n3), plans + rep_plan[3 * w.rep + 2], tab, tw, c3);
     float2 *g = grid + R.g0 + (size_t)w.kx * n2 + w.ky0;
     const size_t zs = (size_t)n1h * n2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) A[lane * n3 + kz] = g[kz * zs + lane];
     __syncthreads();
-    float2 *F = fft_lines<0, false>(p3, A, B, nullptr, tk, 0, tab, tw);
+    float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0);
     float2 *Fo = F == A ? B : A;
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
     // influence function: exp(-pi^2 m^2 / alpha^2) = 2^(-fac2 m^2), fac2 = pi^2 / alpha^2 * log2(e)
@@ -428,7 +463,7 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
         }
     }
     __syncthreads();
-    float2 *I = fft_lines<0, true>(p3, F, Fo, nullptr, tk, 0, tab, tw);
+    float2 *I = fft_lines<0, true>(c3, F, Fo, nullptr, tk, 0);
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) g[kz * zs + lane] = I[lane * n3 + kz];
     // fixed-order reduction: FP32 within each warp, FP64 over the 8 warp sums
@@ -454,17 +489,20 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
     const PlaneWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
-    const FftPlanDev p1 = plans[rep_plan[3 * w.rep]], p2 = plans[rep_plan[3 * w.rep + 1]];
     float2 *P0 = (float2 *)smem, *P1 = P0 + n1 * n2, *Q = P1 + n1 * n2;
-    float *Rp = (float *)Q;       // the real plane reuses Q once Q has been read
+    float *Rp = (float *)Q;       // the real plane of n1 x n2 floats
+    FftCtx c1, c2;
+    unsigned char *ctx = (unsigned char *)(Q + n1h * n2);
+    ctx = fft_ctx_load(ctx, plans + rep_plan[3 * w.rep], tab, tw, c1);
+    fft_ctx_load(ctx, plans + rep_plan[3 * w.rep + 1], tab, tw, c2);
     const float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
     // [kx][ky] lines of n2, conjugated (inverse through the forward transform)
     for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) P0[k] = cconj(g[k]);
     __syncthreads();
-    // y: n1h lines; last pass conjugates back and stores transposed to Q[ky][kx]
-    fft_lines<1, true>(p2, P0, P1, nullptr, n1h, n2, tab, tw);
+    // y: n1h lines; last pass conjugates back and stores transposed to [ky][kx]
+    fft_lines<1, true>(c2, P0, P1, nullptr, n1h, n2);
     // which buffer got the transposed result depends on the pass count
-    float2 *Yt = (p2.nst & 1) ? P1 : P0;
+    float2 *Yt = (c2.p->nst & 1) ? P1 : P0;
     // expand each ky row to the full Hermitian line of n1, conjugated again for the inverse
     float2 *Xs = Yt == P0 ? P1 : P0;
     for (int ky = threadIdx.x >> 5; ky < n2; ky += blockDim.x >> 5)
@@ -474,7 +512,7 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
         }
     __syncthreads();
     // x: n2 lines of n1; the last pass stores real parts into Rp[ky][x]
-    fft_lines<2, false>(p1, Xs, Yt, Rp, n2, 0, tab, tw);
+    fft_lines<2, false>(c1, Xs, Yt, Rp, n2, 0);
     gather_plane<float>(R, w.z, zstart, zatoms, fr, Rp, part);
 }
 
@@ -742,10 +780,18 @@ int make_plan(int n, FftPlanDev *p, std::vector<int2> *tab)
     return 1;
 }
 
+size_t fft_ctx_bytes(int n)
+{
+    FftPlanDev p;
+    if (!make_plan(n, &p, nullptr)) return 0;
+    size_t ntab = (size_t)p.off[p.nst - 1] + p.nb[p.nst - 1];
+    return align16(sizeof(FftPlanDev)) + align16(ntab * sizeof(int2)) + align16(n * sizeof(float2));
+}
+
 template <typename T>
 size_t plane_fwd_smem(int n1, int n2)
 {
-    if (sizeof(T) == 4) return (size_t)2 * n1 * n2 * sizeof(float2);
+    if (sizeof(T) == 4) return (size_t)2 * n1 * n2 * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
     typedef typename cplx<T>::type C;
     size_t acc = (sizeof(typename Acc<T>::type) * n1 * n2 + 15) & ~(size_t)15;
     return acc + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -753,7 +799,8 @@ size_t plane_fwd_smem(int n1, int n2)
 template <typename T>
 size_t plane_inv_smem(int n1, int n2)
 {
-    if (sizeof(T) == 4) return (size_t)(2 * n1 + (n1 / 2 + 1)) * n2 * sizeof(float2);
+    if (sizeof(T) == 4)
+        return (size_t)(2 * n1 + (n1 / 2 + 1)) * n2 * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
     typedef typename cplx<T>::type C;
     size_t r = (sizeof(T) * n1 * n2 + 15) & ~(size_t)15;
     return r + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -761,7 +808,7 @@ size_t plane_inv_smem(int n1, int n2)
 template <typename T>
 size_t zconv_smem(int n3)
 {
-    if (sizeof(T) == 4) return (size_t)2 * NB_TKF * n3 * sizeof(float2);
+    if (sizeof(T) == 4) return (size_t)2 * NB_TKF * n3 * sizeof(float2) + fft_ctx_bytes(n3);
     typedef typename cplx<T>::type C;
     return sizeof(C) * NB_TK * (n3 | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
 }

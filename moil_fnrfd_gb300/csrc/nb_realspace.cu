@@ -134,6 +134,7 @@ __device__ __forceinline__ void water_vs_atoms(const RepDev &R, int i, const typ
     const unsigned fi[3] = {sflags[3 * i], sflags[3 * i + 1], sflags[3 * i + 2]};
     int cnt = 0;
     for (int k = q0; k < q1; ++k) {
+        nb_prefetch_l1(wl2 + min(k + 32, q1 - 1));
         int s = wl2[k];
         T4 xj = pos[s];
         T2 ljj = lj[s];
@@ -463,7 +464,9 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     long long G[3] = {0, 0, 0};
     double elp = 0, eli = 0, eep = 0, eei = 0;
     int cnt = 0, npair = 0;
-    for (int q = xl_off[k]; q < xl_off[k + 1]; ++q) {
+    const int q1 = xl_off[k + 1];
+    for (int q = xl_off[k]; q < q1; ++q) {
+        nb_prefetch_l1(xl + min(q + 32, q1 - 1));
         int s = xl[q];
         T4 xj = pos[s];
         T2 ljj = lj[s];
