@@ -81,7 +81,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_xl); free_ptr(c->d_count_tmp); free_ptr(c->d_ex_off); free_ptr(c->d_ex_j); free_ptr(c->d_p14_off);
     free_ptr(c->d_p14_j); free_ptr(c->d_p14_par); free_ptr(c->d_grad_site); free_ptr(c->d_e_unit);
     free_ptr(c->d_grad_ex); free_ptr(c->d_e_ex); free_ptr(c->d_plans); free_ptr(c->d_rep_plan); free_ptr(c->d_tw);
-    free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp);
+    free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp); free_ptr(c->d_wmask);
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
@@ -173,6 +173,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     std::vector<std::vector<int>> exn, p14n;
     std::vector<std::vector<double>> p14p;
     int64_t atom0 = 0, wat0 = 0, oth0 = 0, zb0 = 0, g0 = 0;
+    c->wmask_words = 0;
     int water_fast = 1;
     int cell0 = 0;
     for (int r = 0; r < nrep; ++r) {
@@ -341,6 +342,8 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
             double frac = 1.0;
             for (int d = 0; d < 3; ++d) frac *= (double)std::min(R.nc[d], 3) / R.nc[d];
             R.wtiled = (nwat > 0 && nwat <= 16384 && frac >= 0.4) ? 1 : 0;
+            R.wmask0 = c->wmask_words;
+            if (R.wtiled) c->wmask_words += (int64_t)nwat * ((nwat + 31) / 32);
         }
         for (int i = 0; i < t->npt; ++i) {
             q.push_back(t->ptchg[i]);
@@ -432,6 +435,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         for (int i0 = 0; i0 < R.nwat; i0 += NB_WTILE) c->wtiles.push_back(make_int2(r, R.wat0 + i0));
     }
     if (!c->wtiles.empty()) NB_TRY(upload(c, c->d_wtiles, c->wtiles));
+    if (c->wmask_words > 0) NB_CUDA_OK(c, cudaMalloc(&c->d_wmask, sizeof(unsigned) * c->wmask_words));
     const size_t ts = c->precision == MOIL_NB_FP64 ? 8 : 4;
     int64_t nu = c->nunit, ns = c->nsite;
     NB_CUDA_OK(c, cudaMalloc(&c->d_unit_key, sizeof(int) * nu));

@@ -82,6 +82,8 @@ struct NbCtx {
     int *d_count_tmp = nullptr;   // scratch counts
     long long *d_scan_tmp = nullptr;   // tile sums of the three-phase scan
     std::vector<int2> wtiles;     // (replica, first sorted water) of each tiled water-list block
+    unsigned *d_wmask = nullptr;  // molecule-pair bit matrices of the tiled replicas
+    int64_t wmask_words = 0;
     int2 *d_wtiles = nullptr;
 
     // exclusion / 1-4 lists per caller atom (both directions)

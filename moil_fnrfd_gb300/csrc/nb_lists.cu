@@ -232,7 +232,7 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
     const RepDev &R = reps[site_rep[3 * i]];
-    if (R.wtiled && R.noth == 0) {   // W1 comes from k_wlist_tiled, W2 is empty
+    if (R.wtiled && R.noth == 0) {   // W1 comes from the bit-matrix kernels, W2 is empty
         if (!FILL) cnt2[i] = 0;
         return;
     }
@@ -250,7 +250,7 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
             for (int d = 0; d < nx; ++d) {
                 int cell = R.cell0 + cx[d] + R.nc[0] * (cy[b] + R.nc[1] * cz[a]);
                 // waters in the cell: sorted positions [bin_start[cell], bin_start[cell+1]);
-                // replicas with few cells get their water-water list from k_wlist_tiled
+                // replicas with few cells get their water-water list from k_wmask_tiled/_fill
                 for (int p = R.wtiled ? 0 : bin_start[cell]; p < (R.wtiled ? 0 : bin_start[cell + 1]); ++p) {
                     if (p == i) continue;
                     T4 oj = pos[3 * p];
@@ -305,70 +305,114 @@ __device__ __forceinline__ float4 wrap_box(const RepDev &R, typename vec4<T>::ty
     return make_float4((float)x, (float)y, (float)z, 0.f);
 }
 
-// 4b. W1 for replicas whose cell stencil spans most of the box: all molecule pairs of the
-// replica, oxygens staged in shared-memory tiles of NB_WTILE and read by broadcast.  One
-// block = NB_WTILE consecutive sorted waters of one replica (blocks never straddle
-// replicas); j runs in sorted order, so the list order is fixed.  The near-first split
-// matches k_wlist.  FILL = 0 counts, 1 writes.
-template <typename T, int FILL>
-__device__ __forceinline__ void wlist_tile(int2 w, float4 *sj, const RepDev *__restrict__ reps, const void *pos_v,
-                                           int *__restrict__ cnt1, int *__restrict__ cntn,
-                                           const int *__restrict__ off1, int *__restrict__ l1, int64_t cap1, int *st)
+// 4b. W1 for replicas whose cell stencil spans most of the box, in two passes over a bit
+// matrix (one bit per molecule pair of the replica, word (w, i) at wmask0 + w*nwat + i):
+//   k_wmask_tiled  all pairs of the replica, oxygens staged in shared-memory tiles of
+//                  NB_WTILE and read by broadcast; sets the bits of pairs within the list
+//                  radius and counts them.  One block = NB_WTILE consecutive sorted waters
+//                  of one replica (blocks never straddle replicas).
+//   k_wmask_fill   expands each row in ascending j: molecules inside the cutoff are written
+//                  from the front of the row's list, skin-only molecules from the back, so
+//                  lanes of a warp stay converged over the in-cutoff part.
+template <typename T>
+__device__ __forceinline__ void wmask_tile(int2 w, float4 *sj, const RepDev *__restrict__ reps, const void *pos_v,
+                                           unsigned *__restrict__ mask, int *__restrict__ cnt1)
 {
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
     const RepDev &R = reps[w.x];
     const int j0 = R.wat0, nw = R.nwat;
-    const int i = w.y + (int)threadIdx.x;
-    const bool act = i < j0 + nw;
+    const int i = w.y + (int)threadIdx.x, il = i - j0;
+    const bool act = il < nw;
     const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
-    const float rl2 = R.rlist2, rc2 = R.rmax2;
+    const float rl2 = R.rlist2;
     float4 oi = act ? wrap_box<T>(R, pos[3 * (size_t)i]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    int n1 = 0, nn = 0, w1 = 0, wf = 0;
-    if (FILL && act) { w1 = off1[i]; wf = w1 + cntn[i]; }
+    unsigned *mrow = mask + R.wmask0 + il;
+    int n1 = 0;
     for (int t0 = 0; t0 < nw; t0 += NB_WTILE) {
         __syncthreads();
         if (t0 + (int)threadIdx.x < nw) sj[threadIdx.x] = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
         __syncthreads();
         if (!act) continue;
         const int tn = min(NB_WTILE, nw - t0);
-        const int self = i - j0 - t0;
-#pragma unroll 4
-        for (int k = 0; k < tn; ++k) {
-            float4 q = sj[k];
-            float dx = fabsf(oi.x - q.x), dy = fabsf(oi.y - q.y), dz = fabsf(oi.z - q.z);
-            dx = fminf(dx, L0 - dx);
-            dy = fminf(dy, L1 - dy);
-            dz = fminf(dz, L2 - dz);
-            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (r2 < rl2 && k != self) {
-                bool near = r2 <= rc2;
-                if (FILL) {
-                    int at = near ? w1 + nn : wf + (n1 - nn);
-                    if (at < cap1) l1[at] = j0 + t0 + k;
-                }
-                nn += near;
-                n1++;
+#pragma unroll
+        for (int q = 0; q < NB_WTILE / 32; ++q) {
+            const int nv = tn - 32 * q;
+            if (nv <= 0) break;
+            unsigned m = 0u;
+#pragma unroll 8
+            for (int b = 0; b < 32; ++b) {
+                const float4 p = sj[32 * q + b];
+                float dx = fabsf(oi.x - p.x), dy = fabsf(oi.y - p.y), dz = fabsf(oi.z - p.z);
+                dx = fminf(dx, L0 - dx);
+                dy = fminf(dy, L1 - dy);
+                dz = fminf(dz, L2 - dz);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                m |= (r2 < rl2 ? 1u : 0u) << b;
             }
+            if (nv < 32) m &= (1u << nv) - 1u;              // past the last molecule
+            const int self = il - t0 - 32 * q;
+            if ((unsigned)self < 32u) m &= ~(1u << self);
+            n1 += __popc(m);
+            mrow[(size_t)(t0 / 32 + q) * nw] = m;
         }
     }
-    if (!act) return;
-    if (!FILL) { cnt1[i] = n1; cntn[i] = nn; }
-    else if ((int64_t)w1 + n1 > cap1) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+    if (act) cnt1[i] = n1;
 }
 
-template <typename T, int FILL>
-__global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 *__restrict__ work,
+template <typename T>
+__global__ void __launch_bounds__(NB_WTILE) k_wmask_tiled(int ntile, const int2 *__restrict__ work,
                                                           const RepDev *__restrict__ reps, const void *pos_v,
-                                                          int *__restrict__ cnt1, int *__restrict__ cntn,
-                                                          const int *__restrict__ off1, int *__restrict__ l1,
-                                                          int64_t cap1, int *st)
+                                                          unsigned *__restrict__ mask, int *__restrict__ cnt1,
+                                                          const int *st)
 {
     if (rebuild_off(st)) return;
     __shared__ float4 sj[NB_WTILE];
     // every tile pass starts with a block barrier before it overwrites sj
-    for (int b = blockIdx.x; b < ntile; b += gridDim.x)
-        wlist_tile<T, FILL>(work[b], sj, reps, pos_v, cnt1, cntn, off1, l1, cap1, st);
+    for (int b = blockIdx.x; b < ntile; b += gridDim.x) wmask_tile<T>(work[b], sj, reps, pos_v, mask, cnt1);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NB_WTILE) k_wmask_fill(int ntile, const int2 *__restrict__ work,
+                                                         const RepDev *__restrict__ reps, const void *pos_v,
+                                                         const unsigned *__restrict__ mask,
+                                                         const int *__restrict__ off1, int *__restrict__ l1,
+                                                         int64_t cap1, int *st)
+{
+    if (rebuild_off(st)) return;
+    typedef typename vec4<T>::type T4;
+    const T4 *pos = (const T4 *)pos_v;
+    for (int b = blockIdx.x; b < ntile; b += gridDim.x) {
+        const int2 w = work[b];
+        const RepDev &R = reps[w.x];
+        const int j0 = R.wat0, nw = R.nwat;
+        const int i = w.y + (int)threadIdx.x, il = i - j0;
+        if (il >= nw) continue;
+        const int w1 = off1[i], n1 = off1[i + 1] - w1;
+        if ((int64_t)w1 + n1 > cap1) {
+            atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+            continue;
+        }
+        const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2], rc2 = R.rmax2;
+        const float4 oi = wrap_box<T>(R, pos[3 * (size_t)i]);
+        const unsigned *mrow = mask + R.wmask0 + il;
+        int front = w1, back = w1 + n1 - 1;
+        const int nwd = (nw + 31) >> 5;
+        for (int wd = 0; wd < nwd; ++wd) {
+            unsigned m = mrow[(size_t)wd * nw];
+            while (m) {
+                const int j = j0 + 32 * wd + __ffs(m) - 1;
+                m &= m - 1u;
+                const float4 p = wrap_box<T>(R, pos[3 * (size_t)j]);
+                float dx = fabsf(oi.x - p.x), dy = fabsf(oi.y - p.y), dz = fabsf(oi.z - p.z);
+                dx = fminf(dx, L0 - dx);
+                dy = fminf(dy, L1 - dy);
+                dz = fminf(dz, L2 - dz);
+                if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rc2) l1[front++] = j;
+                else l1[back--] = j;
+            }
+        }
+    }
 }
 
 // 5. non-water list X: every site j within reach, exclusions removed
@@ -585,16 +629,16 @@ void build_lists_t(NbCtx *c, const double *d_coor)
         k_wlist<T, 0><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
                                          cnt1, cnt2, cntn, nullptr, nullptr, nullptr, nullptr, 0, 0, c->d_status);
         if (nt > 0)
-            k_wlist_tiled<T, 0><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, cnt1, cntn, nullptr,
-                                                        nullptr, 0, c->d_status);
+            k_wmask_tiled<T><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wmask, cnt1,
+                                                     c->d_status);
         nb_scan(c, cnt1, c->d_wl1_off, (int)c->nW, c->d_status + 2, 1);
         nb_scan(c, cnt2, c->d_wl2_off, (int)c->nW, c->d_status + 3, 1);
         k_wlist<T, 1><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
                                          nullptr, nullptr, cntn, c->d_wl1_off, c->d_wl2_off, c->d_wl1, c->d_wl2,
                                          c->cap_wl1, c->cap_wl2, c->d_status);
         if (nt > 0)
-            k_wlist_tiled<T, 1><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, nullptr, cntn,
-                                                        c->d_wl1_off, c->d_wl1, c->cap_wl1, c->d_status);
+            k_wmask_fill<T><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wmask, c->d_wl1_off,
+                                                    c->d_wl1, c->cap_wl1, c->d_status);
         c->launches += nt > 0 ? 4 : 2;
     }
     if (c->nA > 0) {
