@@ -173,8 +173,10 @@ int moil_nb_get_timing(const moil_nb_ctx *h, moil_nb_timing *t);
 /* Pair-list entries of the last build and the unique site pairs inside the cutoff
  * predicate in the last evaluation (the pairs MOIL's kernels evaluate). */
 int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *site_pairs);
-/* Capture the device part of an evaluation into a CUDA graph (1) or launch
- * kernel by kernel (0, default).  Graph replays are used when on. */
+/* Replay the device part of an evaluation as a CUDA graph (1, default) or launch
+ * it kernel by kernel (0).  The graph is captured on first use and again whenever
+ * the coordinate / gradient pointers or the pair-list buffers change; evaluations
+ * with timing on always launch kernel by kernel.  No counterpart in the reference. */
 int moil_nb_set_graph(moil_nb_ctx *h, int on);
 
 /* ---- PME reciprocal sum without device allocation -------------------------

@@ -85,6 +85,10 @@ void release_device(NbCtx *c)
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
+    if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
+    c->h_e_rep = nullptr;
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
     c->inited = 0;
 }
 
@@ -150,6 +154,7 @@ int alloc_lists(NbCtx *c)
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl1, sizeof(int) * std::max<int64_t>(c->cap_wl1, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl2, sizeof(int) * std::max<int64_t>(c->cap_wl2, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl, sizeof(int) * std::max<int64_t>(c->cap_xl, 1)));
+    c->list_gen++;   // a captured evaluation graph refers to the old buffers
     return MOIL_NB_OK;
 }
 
@@ -444,6 +449,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_bin_start, sizeof(int) * (2 * c->ncell + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_sorted_unit, sizeof(int) * nu));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_orig, sizeof(int) * ns));
+    NB_CUDA_OK(c, cudaMemset(c->d_site_orig, 0, sizeof(int) * ns));   // valid indices before the first build
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_of, sizeof(int) * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_rep, sizeof(int) * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_flags, sizeof(unsigned) * ns));
@@ -481,7 +487,8 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         c->cap_xl += (int64_t)(R.noth * (vw * (3.0 * R.nwat + R.noth) / vol) * 1.5) + 32;
     }
     NB_TRY(alloc_lists(c));
-    c->h_e_rep.assign(16 * nrep, 0.0);
+    NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * 16 * nrep));
+    memset(c->h_e_rep, 0, sizeof(double) * 16 * nrep);
     NB_TRY(nb_pme_configure(c));
     {
         // tile sums for every scan: bins, per-water and per-atom counts, PME z-bins
@@ -496,16 +503,18 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     return MOIL_NB_OK;
 }
 
-int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
+// The device part of one evaluation, in stream order.  The sequence does not depend on host
+// state beyond the handle's fixed buffers and the two caller pointers: the rebuild decision
+// travels through the pinned word h_status[8], read by the first copy.  That makes it
+// capturable as a CUDA graph.
+void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
 {
     cudaStream_t s = c->stream;
     c->launches = 0;
-    bool forced = c->need_rebuild || (c->list_period > 0 && c->evals_since_build >= c->list_period);
     if (c->timing) cudaEventRecord(c->ev[0], s);
-    int init_status[2] = {forced ? 1 : 0, 0};
-    cudaMemcpyAsync(c->d_status, init_status, sizeof(init_status), cudaMemcpyHostToDevice, s);
-    if (!forced) nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
-    nb_launch_build_lists(c, d_coor);               // every kernel here is gated by the flag
+    cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 2, cudaMemcpyHostToDevice, s);
+    nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
+    nb_launch_build_lists(c, d_coor);  // every kernel here is gated by the flag
     if (c->timing) cudaEventRecord(c->ev[1], s);
     nb_launch_realspace(c);
     nb_launch_excl14(c, d_coor);
@@ -514,7 +523,54 @@ int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
     nb_launch_finalize(c, d_dpot);
     if (c->timing) cudaEventRecord(c->ev[10], s);
     cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(c->h_e_rep.data(), c->d_e_rep, sizeof(double) * 16 * c->nrep, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(c->h_e_rep, c->d_e_rep, sizeof(double) * 16 * c->nrep, cudaMemcpyDeviceToHost, s);
+}
+
+void drop_graph(NbCtx *c)
+{
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+}
+
+// replay the captured evaluation, capturing it first when the caller pointers or the list
+// buffers changed; returns false (graph mode switched off) if capture is not possible
+bool launch_graph(NbCtx *c, const double *d_coor, double *d_dpot)
+{
+    cudaStream_t s = c->stream;
+    if (!c->gexec || c->g_coor != d_coor || c->g_dpot != d_dpot || c->g_gen != c->list_gen) {
+        drop_graph(c);
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            c->use_graph = 0;
+            return false;
+        }
+        enqueue_eval(c, d_coor, d_dpot);
+        cudaError_t e1 = cudaStreamEndCapture(s, &g);
+        cudaError_t e2 = e1 == cudaSuccess ? cudaGraphInstantiate(&c->gexec, g, 0) : e1;
+        if (g) cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) {
+            cudaGetLastError();
+            c->gexec = nullptr;
+            c->use_graph = 0;
+            return false;
+        }
+        c->g_coor = d_coor;
+        c->g_dpot = d_dpot;
+        c->g_gen = c->list_gen;
+        c->graph_launches = c->launches;
+    }
+    c->launches = c->graph_launches;
+    return cudaGraphLaunch(c->gexec, s) == cudaSuccess;
+}
+
+int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
+{
+    cudaStream_t s = c->stream;
+    bool forced = c->need_rebuild || (c->list_period > 0 && c->evals_since_build >= c->list_period);
+    c->h_status[8] = forced ? 1 : 0;
+    c->h_status[9] = 0;
+    if (!(c->use_graph && !c->timing && launch_graph(c, d_coor, d_dpot))) enqueue_eval(c, d_coor, d_dpot);
     NB_CUDA_OK(c, cudaStreamSynchronize(s));
     NB_CUDA_OK(c, cudaGetLastError());
     int rebuilt = c->h_status[0] != 0;
@@ -571,7 +627,7 @@ int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
     if (rc != MOIL_NB_OK) return rc;
     if (e) {
         for (int r = 0; r < c->nrep; ++r) {
-            const double *o = c->h_e_rep.data() + 16 * r;
+            const double *o = c->h_e_rep + 16 * r;
             moil_energies &E = e[r];
             E.e_vdw = o[0]; E.e_el = o[1]; E.e_vsym = o[2]; E.e_lsym = o[3];
             E.e_el14 = o[4]; E.e_vdw14 = o[5]; E.e_corr = o[6]; E.e_self = o[7];
@@ -620,7 +676,7 @@ int moil_nb_create(moil_nb_ctx **out, int device)
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
     if (h->nsm <= 0) h->nsm = 1;
     for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
-    if (cudaMallocHost(&h->h_status, sizeof(int) * 8) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
+    if (cudaMallocHost(&h->h_status, sizeof(int) * 16) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
         moil_nb_destroy(h);
         return MOIL_NB_ERR_CUDA;
     }
@@ -750,7 +806,9 @@ int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *sit
 int moil_nb_set_graph(moil_nb_ctx *h, int on)
 {
     if (!h) return MOIL_NB_ERR_ARG;
+    cudaSetDevice(h->device);
     h->use_graph = on ? 1 : 0;
+    drop_graph(h);
     return MOIL_NB_OK;
 }
 

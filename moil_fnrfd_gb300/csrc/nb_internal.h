@@ -124,14 +124,14 @@ struct NbCtx {
 
     // energies
     double *d_e_rep = nullptr;         // nrep * 16
-    std::vector<double> h_e_rep;
+    double *h_e_rep = nullptr;         // pinned mirror
 
     // caller buffers used by host-pointer evaluations
     double *d_coor = nullptr, *d_dpot = nullptr;
 
     // device status: [0] rebuild flag, [1] error bits, [2..4] list totals, [5] rebuilt this eval
     int *d_status = nullptr;
-    int *h_status = nullptr;           // pinned mirror
+    int *h_status = nullptr;           // pinned: [0..7] mirror, [8..9] initial words of an evaluation
     int need_rebuild = 1;
     int evals_since_build = 0;
     int64_t last_list_entries = 0, last_water_pairs = 0, last_atom_pairs = 0, last_site_pairs = 0;
@@ -140,8 +140,14 @@ struct NbCtx {
     int timing = 0;
     cudaEvent_t ev[12];
     moil_nb_timing last_timing{};
-    int use_graph = 0;
     int launches = 0;
+
+    // CUDA graph of one evaluation, valid for the caller pointers and list buffers it captured
+    int use_graph = 1;
+    cudaGraphExec_t gexec = nullptr;
+    const double *g_coor = nullptr;
+    double *g_dpot = nullptr;
+    int g_gen = -1, list_gen = 0, graph_launches = 0;
 };
 
 // ---- launchers implemented in the kernel files -------------------------------------

@@ -134,7 +134,9 @@ __global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_orig, 
                           void *woff_v, float4 *__restrict__ posb, float half_skin2, float rwat2, int snapshot,
                           int *st)
 {
-    if (snapshot && rebuild_off(st)) return;
+    // snapshot mode runs only on a rebuild; check mode only without one (the site order it
+    // reads is the previous build's, which does not exist before the first build)
+    if (snapshot ? rebuild_off(st) : !rebuild_off(st)) return;
     typedef typename vec4<T>::type T4;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsite; s += gridDim.x * blockDim.x) {
         int a = site_orig[s];

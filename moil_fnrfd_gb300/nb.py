@@ -248,6 +248,10 @@ class Nonbonded:
     def set_timing(self, on=True):
         _check(self.L, self.h, self.L.moil_nb_set_timing(self.h, int(on)))
 
+    def set_graph(self, on=True):
+        """Replay evaluations as a captured CUDA graph (default) or launch kernel by kernel."""
+        _check(self.L, self.h, self.L.moil_nb_set_graph(self.h, int(on)))
+
     def timing(self) -> dict:
         t = Timing()
         _check(self.L, self.h, self.L.moil_nb_get_timing(self.h, ctypes.byref(t)))
