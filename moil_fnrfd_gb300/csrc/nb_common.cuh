@@ -154,7 +154,37 @@ __device__ __forceinline__ double nb_erfc_ex(double x, double /*unused*/, double
     return erfc(x);
 }
 
-// 64-bit fixed-point flush of an FP32 partial gradient
+// v * 2^32 rounded to nearest (ties away from zero) with integer operations only: a 64-bit
+// conversion instruction runs on the narrow FP64 pipe.  |v| >= 2^31, Inf and NaN saturate
+// to +-2^62.
+__device__ __forceinline__ long long nb_f2fix(float v)
+{
+    const unsigned b = __float_as_uint(v);
+    const int e = (int)((b >> 23) & 0xffu);
+    const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
+    const int sh = e - 118;    // v = m * 2^(e - 150), times 2^32
+    long long r;
+    if (sh > 38) r = 1LL << 62;
+    else if (sh >= 0) r = m << sh;
+    else if (sh > -26) r = (m + (1LL << (-sh - 1))) >> -sh;
+    else r = 0;
+    return (b >> 31) ? -r : r;
+}
+
+// x * 2^-32 as a double with integer operations only; exact for |x| < 2^53, truncated above
+__device__ __forceinline__ double nb_fix2d(long long x)
+{
+    if (x == 0) return 0.0;
+    const unsigned long long s = x < 0 ? 0x8000000000000000ull : 0ull;
+    const unsigned long long a = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    const int lz = __clzll((long long)a);
+    const unsigned long long m = lz >= 11 ? a << (lz - 11) : a >> (11 - lz);
+    const unsigned long long ex = (unsigned long long)(1023 + 31 - lz);
+    return __longlong_as_double((long long)(s | (ex << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
+
+// 64-bit fixed-point flush of an FP32 partial gradient (conversion instruction: cheaper
+// than nb_f2fix where the FP64 pipe is otherwise idle)
 __device__ __forceinline__ long long nb_fix(float v) { return __float2ll_rn(v * NB_FIX_SCALE_F); }
 __device__ __forceinline__ long long nb_fix(double v) { return __double2ll_rn(v * NB_FIX_SCALE); }
 

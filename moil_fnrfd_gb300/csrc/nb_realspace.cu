@@ -564,11 +564,12 @@ __global__ void k_excl_water(int nW, const int *__restrict__ unit_atom, const in
 // FP32 path of the water exclusion corrections, one sorted water per thread: the three
 // intramolecular displacements come from the FP64-formed H offsets (O-H1, O-H2, H2-H1), so
 // no absolute FP32 coordinate enters; erf(x)/x from its Taylor series in u = x^2 (9 terms,
-// truncation below 6e-9 for u <= 0.5), erff beyond.  Results go to the caller-order arrays.
+// truncation below 6e-9 for u <= 0.5), erff beyond.  Results go to the caller-order arrays,
+// gradients as 2^32 fixed point.
 __global__ void __launch_bounds__(128) k_excl_water_f(int nW, const int *__restrict__ site_orig,
                                                       const int *__restrict__ site_rep,
                                                       const RepDev *__restrict__ reps, const float4 *__restrict__ pos,
-                                                      const float4 *__restrict__ woff, double *__restrict__ grad,
+                                                      const float4 *__restrict__ woff, long long *__restrict__ grad,
                                                       double *__restrict__ e_out)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -611,8 +612,9 @@ __global__ void __launch_bounds__(128) k_excl_water_f(int nW, const int *__restr
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double *gp = grad + 3 * (size_t)(a0 + k), *ep = e_out + 3 * (size_t)(a0 + k);
-        gp[0] = g[k][0]; gp[1] = g[k][1]; gp[2] = g[k][2];
+        long long *gp = grad + 3 * (size_t)(a0 + k);
+        double *ep = e_out + 3 * (size_t)(a0 + k);
+        gp[0] = nb_fix(g[k][0]); gp[1] = nb_fix(g[k][1]); gp[2] = nb_fix(g[k][2]);
         ep[0] = k == 0 ? (double)ecorr : 0.0; ep[1] = 0.0; ep[2] = 0.0;
     }
 }
@@ -624,7 +626,7 @@ __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepD
                          const double *__restrict__ coor, const double *__restrict__ q, const int *__restrict__ ex_off,
                          const int *__restrict__ ex_j, const int *__restrict__ p_off, const int *__restrict__ p_j,
                          const double *__restrict__ p_par, const unsigned *__restrict__ aflags, int skip_water,
-                         double *__restrict__ grad, double *__restrict__ e_out)
+                         int fixed_out, double *__restrict__ grad, double *__restrict__ e_out)
 {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= natom) return;
@@ -664,7 +666,14 @@ __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepD
         evdw14 += 0.5 * e1;
         eel14 += 0.5 * e2;
     }
-    grad[3 * (size_t)a] = gx; grad[3 * (size_t)a + 1] = gy; grad[3 * (size_t)a + 2] = gz;
+    if (fixed_out) {   // mixed path: 2^32 fixed point, as k_excl_water_f
+        long long *gf = (long long *)grad + 3 * (size_t)a;
+        gf[0] = __double2ll_rn(gx * NB_FIX_SCALE);
+        gf[1] = __double2ll_rn(gy * NB_FIX_SCALE);
+        gf[2] = __double2ll_rn(gz * NB_FIX_SCALE);
+    } else {
+        grad[3 * (size_t)a] = gx; grad[3 * (size_t)a + 1] = gy; grad[3 * (size_t)a + 2] = gz;
+    }
     e_out[3 * (size_t)a] = ecorr; e_out[3 * (size_t)a + 1] = eel14; e_out[3 * (size_t)a + 2] = evdw14;
 }
 
@@ -683,17 +692,18 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
     const T *p = part + 12 * (size_t)s;
     bool bad = false;
     if constexpr (sizeof(T) == 4) {
-        // FP32 path: the PME share is summed and scaled in FP32 (its own precision); FP64
-        // only where the fixed-point and FP64 terms meet, 4 operations per component
+        // FP32 path: the PME share is summed and scaled in FP32 (its own precision) and
+        // joins the fixed-point real-space and correction terms as an integer; the double
+        // result is assembled with integer operations (no FP64 instruction)
+        const long long *gx = (const long long *)grad_ex + 3 * (size_t)a;
         const float qs = (float)q[a];
         const float pg[3] = {((p[0] + p[3]) + p[6]) + p[9], ((p[1] + p[4]) + p[7]) + p[10],
                              ((p[2] + p[5]) + p[8]) + p[11]};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            double v = fma((double)grad_site[3 * (size_t)s + d], NB_FIX_INV, grad_ex[3 * (size_t)a + d]) +
-                       (double)(qs * R.pme_gs[d] * pg[d]);
-            bad |= !(v == v);
-            dpot[3 * (size_t)a + d] = v;
+            const long long v = grad_site[3 * (size_t)s + d] + gx[d] + nb_f2fix(qs * R.pme_gs[d] * pg[d]);
+            bad |= (v > (1LL << 61)) | (v < -(1LL << 61));   // a saturated (non-finite) term
+            dpot[3 * (size_t)a + d] = nb_fix2d(v);
         }
     } else {
         double pg[3] = {0, 0, 0};
@@ -805,13 +815,13 @@ void nb_launch_excl14(NbCtx *c, const double *d_coor)
         else
             k_excl_water_f<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
                 (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_reps, (const float4 *)c->d_pos,
-                (const float4 *)c->d_woff, c->d_grad_ex, c->d_e_ex);
+                (const float4 *)c->d_woff, (long long *)c->d_grad_ex, c->d_e_ex);
         c->launches++;
     }
     if (!fast || c->nA > 0) {
         k_excl14<<<(int)((c->natom + 127) / 128), 128, 0, c->stream>>>(
             (int)c->natom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_ex_off, c->d_ex_j, c->d_p14_off,
-            c->d_p14_j, c->d_p14_par, c->d_aflags, fast, c->d_grad_ex, c->d_e_ex);
+            c->d_p14_j, c->d_p14_par, c->d_aflags, fast, c->precision != MOIL_NB_FP64, c->d_grad_ex, c->d_e_ex);
         c->launches++;
     }
 }
