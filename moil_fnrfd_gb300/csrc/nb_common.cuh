@@ -61,8 +61,7 @@ struct RepDev {
     float pme_fac2f, pivolf; // FP32 path: pi^2 / alpha^2 * log2(e), pi * volume
     float pme_gs[3];         // FP32 path: fc * n_d / L_d (PME gradient scale per unit charge)
     int arith, hvdw0, lj_switch, has_water;
-    int wtiled;              // water-water list from the all-pairs bit matrix (few cells per box)
-    long long wmask0;        // first word of this replica's bit matrix (nwat rows of ceil(nwat/32) words)
+    int wtiled;              // water-water list by tiled all-pairs (few cells per box)
     double e_self;
 };
 

@@ -77,11 +77,11 @@ void release_device(NbCtx *c)
     free_ptr(c->d_unit_slot); free_ptr(c->d_bin_count); free_ptr(c->d_bin_start); free_ptr(c->d_sorted_unit);
     free_ptr(c->d_site_orig); free_ptr(c->d_site_of); free_ptr(c->d_site_rep); free_ptr(c->d_site_flags);
     free_ptr(c->d_pos); free_ptr(c->d_posb); free_ptr(c->d_woff); free_ptr(c->d_site_lj); free_ptr(c->d_site_q);
-    free_ptr(c->d_wl1_off); free_ptr(c->d_wl1); free_ptr(c->d_wl2_off); free_ptr(c->d_wl2); free_ptr(c->d_xl_off);
+    free_ptr(c->d_wl1_cnt); free_ptr(c->d_wl1); free_ptr(c->d_wl2_off); free_ptr(c->d_wl2); free_ptr(c->d_xl_off);
     free_ptr(c->d_xl); free_ptr(c->d_count_tmp); free_ptr(c->d_ex_off); free_ptr(c->d_ex_j); free_ptr(c->d_p14_off);
     free_ptr(c->d_p14_j); free_ptr(c->d_p14_par); free_ptr(c->d_grad_site); free_ptr(c->d_e_unit);
     free_ptr(c->d_grad_ex); free_ptr(c->d_e_ex); free_ptr(c->d_plans); free_ptr(c->d_rep_plan); free_ptr(c->d_tw);
-    free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp); free_ptr(c->d_wmask);
+    free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp);
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
@@ -151,7 +151,7 @@ int alloc_lists(NbCtx *c)
     free_ptr(c->d_wl1);
     free_ptr(c->d_wl2);
     free_ptr(c->d_xl);
-    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1, sizeof(int) * std::max<int64_t>(c->cap_wl1, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1, sizeof(int) * std::max<int64_t>(c->nW * c->cap_row1, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl2, sizeof(int) * std::max<int64_t>(c->cap_wl2, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl, sizeof(int) * std::max<int64_t>(c->cap_xl, 1)));
     c->list_gen++;   // a captured evaluation graph refers to the old buffers
@@ -178,7 +178,6 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     std::vector<std::vector<int>> exn, p14n;
     std::vector<std::vector<double>> p14p;
     int64_t atom0 = 0, wat0 = 0, oth0 = 0, zb0 = 0, g0 = 0;
-    c->wmask_words = 0;
     int water_fast = 1;
     int cell0 = 0;
     for (int r = 0; r < nrep; ++r) {
@@ -347,8 +346,6 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
             double frac = 1.0;
             for (int d = 0; d < 3; ++d) frac *= (double)std::min(R.nc[d], 3) / R.nc[d];
             R.wtiled = (nwat > 0 && nwat <= 16384 && frac >= 0.4) ? 1 : 0;
-            R.wmask0 = c->wmask_words;
-            if (R.wtiled) c->wmask_words += (int64_t)nwat * ((nwat + 31) / 32);
         }
         for (int i = 0; i < t->npt; ++i) {
             q.push_back(t->ptchg[i]);
@@ -440,7 +437,6 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         for (int i0 = 0; i0 < R.nwat; i0 += NB_WTILE) c->wtiles.push_back(make_int2(r, R.wat0 + i0));
     }
     if (!c->wtiles.empty()) NB_TRY(upload(c, c->d_wtiles, c->wtiles));
-    if (c->wmask_words > 0) NB_CUDA_OK(c, cudaMalloc(&c->d_wmask, sizeof(unsigned) * c->wmask_words));
     const size_t ts = c->precision == MOIL_NB_FP64 ? 8 : 4;
     int64_t nu = c->nunit, ns = c->nsite;
     NB_CUDA_OK(c, cudaMalloc(&c->d_unit_key, sizeof(int) * nu));
@@ -458,7 +454,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_woff, 4 * ts * 2 * std::max<int64_t>(c->nW, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_lj, 2 * ts * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_q, ts * ns));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1_off, sizeof(int) * (c->nW + 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1_cnt, sizeof(int2) * std::max<int64_t>(c->nW, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl2_off, sizeof(int) * (c->nW + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl_off, sizeof(int) * (c->nA + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_count_tmp, sizeof(int) * (3 * std::max(c->nW, c->nA) + 3)));
@@ -476,16 +472,18 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMemset(c->d_grad_site, 0, sizeof(long long) * 3 * ns));
     NB_CUDA_OK(c, cudaMemset(c->d_e_unit, 0, sizeof(double) * NB_EU * std::max<int64_t>(nu, 1)));
     // list capacities from densities (grown on overflow)
-    c->cap_wl1 = c->cap_wl2 = c->cap_xl = 64;
+    c->cap_wl2 = c->cap_xl = 64;
+    double row1 = 32;
     for (int r = 0; r < nrep; ++r) {
         const RepDev &R = c->rd[r];
         double vol = R.Ld[0] * R.Ld[1] * R.Ld[2];
         double rl = sqrt((double)R.rlist2), rlw = sqrt((double)R.rlistw2);
         double sph = 4.0 / 3.0 * M_PI, vl = std::min(sph * rl * rl * rl, vol), vw = std::min(sph * rlw * rlw * rlw, vol);
-        c->cap_wl1 += (int64_t)(R.nwat * (vl * R.nwat / vol) * 1.3) + 32;
+        if (R.nwat > 0) row1 = std::max(row1, vl * R.nwat / vol * 1.4 + 32);
         c->cap_wl2 += (int64_t)(R.nwat * (vw * R.noth / vol) * 1.5) + 32;
         c->cap_xl += (int64_t)(R.noth * (vw * (3.0 * R.nwat + R.noth) / vol) * 1.5) + 32;
     }
+    c->cap_row1 = ((int)row1 + 31) & ~31;
     NB_TRY(alloc_lists(c));
     NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * 16 * nrep));
     memset(c->h_e_rep, 0, sizeof(double) * 16 * nrep);
@@ -512,7 +510,7 @@ void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
     cudaStream_t s = c->stream;
     c->launches = 0;
     if (c->timing) cudaEventRecord(c->ev[0], s);
-    cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 2, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 8, cudaMemcpyHostToDevice, s);
     nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
     nb_launch_build_lists(c, d_coor);  // every kernel here is gated by the flag
     if (c->timing) cudaEventRecord(c->ev[1], s);
@@ -569,7 +567,7 @@ int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
     cudaStream_t s = c->stream;
     bool forced = c->need_rebuild || (c->list_period > 0 && c->evals_since_build >= c->list_period);
     c->h_status[8] = forced ? 1 : 0;
-    c->h_status[9] = 0;
+    for (int k = 9; k < 16; ++k) c->h_status[k] = 0;
     if (!(c->use_graph && !c->timing && launch_graph(c, d_coor, d_dpot))) enqueue_eval(c, d_coor, d_dpot);
     NB_CUDA_OK(c, cudaStreamSynchronize(s));
     NB_CUDA_OK(c, cudaGetLastError());
@@ -616,8 +614,8 @@ int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
         rc = eval_once(c, d_coor, d_dpot);
         if (rc != MOIL_NB_ERR_OVERFLOW) break;
         // grow from the exact totals the count pass produced, then redo with a fresh build
-        int64_t need1 = c->h_status[2], need2 = c->h_status[3], need3 = c->h_status[4];
-        c->cap_wl1 = std::max<int64_t>(c->cap_wl1, need1 + need1 / 8 + 64);
+        int64_t need1 = c->h_status[6], need2 = c->h_status[3], need3 = c->h_status[4];
+        c->cap_row1 = std::max<int>(c->cap_row1, (int)((need1 + need1 / 8 + 32 + 31) & ~31));
         c->cap_wl2 = std::max<int64_t>(c->cap_wl2, need2 + need2 / 8 + 64);
         c->cap_xl = std::max<int64_t>(c->cap_xl, need3 + need3 / 8 + 64);
         int a = alloc_lists(c);

@@ -75,15 +75,15 @@ struct NbCtx {
     void *d_site_q = nullptr;     // float / double (PME charge)
 
     // pair lists (CSR)
-    int *d_wl1_off = nullptr, *d_wl1 = nullptr;
+    int2 *d_wl1_cnt = nullptr;    // W1 row counts (in-cutoff from the front, skin-only from the back)
+    int *d_wl1 = nullptr;         // W1 rows of cap_row1 entries (sorted water index of j)
+    int cap_row1 = 0;
     int *d_wl2_off = nullptr, *d_wl2 = nullptr;
     int *d_xl_off = nullptr, *d_xl = nullptr;
-    int64_t cap_wl1 = 0, cap_wl2 = 0, cap_xl = 0;
+    int64_t cap_wl2 = 0, cap_xl = 0;
     int *d_count_tmp = nullptr;   // scratch counts
     long long *d_scan_tmp = nullptr;   // tile sums of the three-phase scan
     std::vector<int2> wtiles;     // (replica, first sorted water) of each tiled water-list block
-    unsigned *d_wmask = nullptr;  // molecule-pair bit matrices of the tiled replicas
-    int64_t wmask_words = 0;
     int2 *d_wtiles = nullptr;
 
     // exclusion / 1-4 lists per caller atom (both directions)
@@ -129,7 +129,8 @@ struct NbCtx {
     // caller buffers used by host-pointer evaluations
     double *d_coor = nullptr, *d_dpot = nullptr;
 
-    // device status: [0] rebuild flag, [1] error bits, [2..4] list totals, [5] rebuilt this eval
+    // device status: [0] rebuild flag, [1] error bits, [2..4] W1 / W2 / X entry totals,
+    // [6] longest W1 row; all reset at the start of every evaluation
     int *d_status = nullptr;
     int *h_status = nullptr;           // pinned: [0..7] mirror, [8..9] initial words of an evaluation
     int need_rebuild = 1;

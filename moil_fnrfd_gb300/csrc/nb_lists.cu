@@ -6,10 +6,10 @@
 // distances (identical for cutoff <= L/2):
 //   units     : water molecules (anchor O, pot/nbondm.f:81-86) and non-water atoms
 //   sort      : counting sort of units by (class, replica, cell), ties by unit id
-//   lists     : W1  water i -> water j   (O-O < rmax + skin)             full list
-//               W2  water i -> non-water site j (O-x < rmax + skin + rwat)
-//               X   non-water i -> any site j (exclusions removed, as pot/nbond.f:95-103)
-// Every list is a full (both-direction) CSR list so each lane owns its gradient outright.
+//   lists     : W1  water i -> water j   (O-O < rmax + skin)      fixed-capacity rows
+//               W2  water i -> non-water site j (O-x < rmax + skin + rwat)     CSR
+//               X   non-water i -> any site j (exclusions removed, as pot/nbond.f:95-103)  CSR
+// Every list is full (both directions) so each lane owns its gradient outright.
 // All kernels that only run on a rebuild early-exit on the device rebuild flag, so the
 // whole evaluation can run without a host round trip.
 #include "nb_internal.h"
@@ -219,22 +219,45 @@ __device__ __forceinline__ bool nb_excluded(const int *__restrict__ ex_off, cons
     return false;
 }
 
-// 4. water lists W1 (water j) and W2 (non-water sites) of water i; FILL = 0 counts, 1 writes
+// W1 is a fixed-capacity row per water (ELL, cap entries): molecules inside the cutoff at
+// build time from the front of the row in ascending order of discovery, skin-only
+// molecules from the back, counts (near, far) in wcnt[i].  The pair kernel walks the front
+// part then the back part, so the lanes of a warp stay converged over the in-cutoff part.
+__device__ __forceinline__ void w1_put(int *__restrict__ row, int cap, bool near, int &nn, int &nf, int j)
+{
+    if (near) { if (nn < cap) row[nn] = j; ++nn; }
+    else { if (nf < cap) row[cap - 1 - nf] = j; ++nf; }
+}
+
+// a finished W1 row: counts, overflow flag, and the warp's entry total / longest row added
+// to st[2] / st[6] (for statistics and for regrowing the row capacity)
+__device__ __forceinline__ void w1_done(int i, int nn, int nf, int cap, int2 *__restrict__ wcnt, int *st)
+{
+    wcnt[i] = make_int2(nn, nf);
+    const int n = nn + nf;
+    if (n > cap) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+    const unsigned act = __activemask();
+    const int sum = __reduce_add_sync(act, n), mx = __reduce_max_sync(act, n);
+    if ((threadIdx.x & 31) == __ffs(act) - 1) {
+        atomicAdd(&st[2], sum);
+        atomicMax(&st[6], mx);
+    }
+}
+
+// 4. water lists of water i by cell search: W1 (water j, rows of wl1) in the FILL = 0 pass,
+// W2 (non-water sites, CSR) counted in the FILL = 0 pass and written in the FILL = 1 pass
 template <typename T, int FILL>
 __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restrict__ reps,
                                           const int *__restrict__ site_rep, const void *pos_v,
-                                          const int *__restrict__ bin_start, int ncell, int *__restrict__ cnt1,
-                                          int *__restrict__ cnt2, int *__restrict__ cntn,
-                                          const int *__restrict__ off1, const int *__restrict__ off2,
-                                          int *__restrict__ l1, int *__restrict__ l2, int64_t cap1, int64_t cap2,
-                                          int *st)
+                                          const int *__restrict__ bin_start, int ncell, int2 *__restrict__ wcnt,
+                                          int *__restrict__ cnt2, const int *__restrict__ off2, int *__restrict__ l1,
+                                          int cap_row, int *__restrict__ l2, int64_t cap2, int *st)
 {
-    // W1 entries are stored in two groups: molecules already inside the cutoff at build
-    // time first, skin-only molecules after them, so lanes of a warp stay converged
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
     const RepDev &R = reps[site_rep[3 * i]];
-    if (R.wtiled && R.noth == 0) {   // W1 comes from the bit-matrix kernels, W2 is empty
+    const bool do_w1 = !FILL && !R.wtiled;   // replicas with few cells: W1 from k_wlist_tiled
+    if (!do_w1 && R.noth == 0) {
         if (!FILL) cnt2[i] = 0;
         return;
     }
@@ -243,30 +266,23 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
     cell_of<T>(R, oi.x, oi.y, oi.z, ci);
     int nx = nb_axis_cells(ci[0], R.nc[0], cx), ny = nb_axis_cells(ci[1], R.nc[1], cy),
         nz = nb_axis_cells(ci[2], R.nc[2], cz);
-    int n1 = 0, n2 = 0, nn = 0;
-    int w1 = FILL ? off1[i] : 0, w2 = FILL ? off2[i] : 0, wf = FILL ? off1[i] + cntn[i] : 0;
+    int n2 = 0, nn = 0, nf = 0;
+    int w2 = FILL ? off2[i] : 0;
+    int *row = l1 + (size_t)i * cap_row;
     T rl2 = (T)R.rlist2, rw2 = (T)R.rlistw2, rc2 = (T)R.rmax2;
     int nW_i = nW;
     for (int a = 0; a < nz; ++a)
         for (int b = 0; b < ny; ++b)
             for (int d = 0; d < nx; ++d) {
                 int cell = R.cell0 + cx[d] + R.nc[0] * (cy[b] + R.nc[1] * cz[a]);
-                // waters in the cell: sorted positions [bin_start[cell], bin_start[cell+1]);
-                // replicas with few cells get their water-water list from k_wmask_tiled/_fill
-                for (int p = R.wtiled ? 0 : bin_start[cell]; p < (R.wtiled ? 0 : bin_start[cell + 1]); ++p) {
-                    if (p == i) continue;
-                    T4 oj = pos[3 * p];
-                    T r2 = mi_r2<T>(R, oi.x - oj.x, oi.y - oj.y, oi.z - oj.z);
-                    if (r2 < rl2) {
-                        bool near = r2 <= rc2;
-                        if (FILL) {
-                            int at = near ? w1 + nn : wf + (n1 - nn);
-                            if (at < cap1) l1[at] = p;
-                        }
-                        nn += near;
-                        n1++;
+                // waters in the cell: sorted positions [bin_start[cell], bin_start[cell+1])
+                if (do_w1)
+                    for (int p = bin_start[cell]; p < bin_start[cell + 1]; ++p) {
+                        if (p == i) continue;
+                        T4 oj = pos[3 * p];
+                        T r2 = mi_r2<T>(R, oi.x - oj.x, oi.y - oj.y, oi.z - oj.z);
+                        if (r2 < rl2) w1_put(row, cap_row, r2 <= rc2, nn, nf, p);
                     }
-                }
                 // non-water atoms in the cell
                 for (int p = bin_start[ncell + cell]; p < bin_start[ncell + cell + 1]; ++p) {
                     int s = 3 * nW_i + (p - nW_i);
@@ -278,23 +294,22 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
                 }
             }
     if (!FILL) {
-        if (!R.wtiled) { cnt1[i] = n1; cntn[i] = nn; }
         cnt2[i] = n2;
+        if (do_w1) w1_done(i, nn, nf, cap_row, wcnt, st);
     }
-    else if ((int64_t)w1 + n1 > cap1 || (int64_t)w2 + n2 > cap2) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+    else if ((int64_t)w2 + n2 > cap2) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
 }
 
 template <typename T, int FILL>
 __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep, const void *pos_v,
-                        const int *__restrict__ bin_start, int ncell, int *__restrict__ cnt1,
-                        int *__restrict__ cnt2, int *__restrict__ cntn, const int *__restrict__ off1,
-                        const int *__restrict__ off2, int *__restrict__ l1, int *__restrict__ l2, int64_t cap1,
-                        int64_t cap2, int *st)
+                        const int *__restrict__ bin_start, int ncell, int2 *__restrict__ wcnt,
+                        int *__restrict__ cnt2, const int *__restrict__ off2, int *__restrict__ l1, int cap_row,
+                        int *__restrict__ l2, int64_t cap2, int *st)
 {
     if (rebuild_off(st)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nW; i += gridDim.x * blockDim.x)
-        wlist_one<T, FILL>(i, nW, reps, site_rep, pos_v, bin_start, ncell, cnt1, cnt2, cntn, off1, off2, l1, l2,
-                           cap1, cap2, st);
+        wlist_one<T, FILL>(i, nW, reps, site_rep, pos_v, bin_start, ncell, wcnt, cnt2, off2, l1, cap_row, l2, cap2,
+                           st);
 }
 
 // oxygen position wrapped into [0, L) per axis, as FP32 (list geometry only)
@@ -307,18 +322,15 @@ __device__ __forceinline__ float4 wrap_box(const RepDev &R, typename vec4<T>::ty
     return make_float4((float)x, (float)y, (float)z, 0.f);
 }
 
-// 4b. W1 for replicas whose cell stencil spans most of the box, in two passes over a bit
-// matrix (one bit per molecule pair of the replica, word (w, i) at wmask0 + w*nwat + i):
-//   k_wmask_tiled  all pairs of the replica, oxygens staged in shared-memory tiles of
-//                  NB_WTILE and read by broadcast; sets the bits of pairs within the list
-//                  radius and counts them.  One block = NB_WTILE consecutive sorted waters
-//                  of one replica (blocks never straddle replicas).
-//   k_wmask_fill   expands each row in ascending j: molecules inside the cutoff are written
-//                  from the front of the row's list, skin-only molecules from the back, so
-//                  lanes of a warp stay converged over the in-cutoff part.
+// 4b. W1 for replicas whose cell stencil spans most of the box (k_wlist_tiled): all
+// molecule pairs of the replica in one pass, oxygens staged in shared-memory tiles of
+// NB_WTILE and read by broadcast.  One block = NB_WTILE consecutive sorted waters of one
+// replica (blocks never straddle replicas).  Each 32-molecule word of a tile gives a bit
+// set (within the list radius) and a near set (within the cutoff) whose members go to the
+// row in ascending j.
 template <typename T>
-__device__ __forceinline__ void wmask_tile(int2 w, float4 *sj, const RepDev *__restrict__ reps, const void *pos_v,
-                                           unsigned *__restrict__ mask, int *__restrict__ cnt1)
+__device__ __forceinline__ void wlist_tile(int2 w, float4 *sj, const RepDev *__restrict__ reps, const void *pos_v,
+                                           int2 *__restrict__ wcnt, int *__restrict__ l1, int cap_row, int *st)
 {
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
@@ -327,10 +339,10 @@ __device__ __forceinline__ void wmask_tile(int2 w, float4 *sj, const RepDev *__r
     const int i = w.y + (int)threadIdx.x, il = i - j0;
     const bool act = il < nw;
     const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
-    const float rl2 = R.rlist2;
+    const float rl2 = R.rlist2, rc2 = R.rmax2;
     float4 oi = act ? wrap_box<T>(R, pos[3 * (size_t)i]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    unsigned *mrow = mask + R.wmask0 + il;
-    int n1 = 0;
+    int *row = l1 + (size_t)i * cap_row;
+    int nn = 0, nf = 0;
     for (int t0 = 0; t0 < nw; t0 += NB_WTILE) {
         __syncthreads();
         if (t0 + (int)threadIdx.x < nw) sj[threadIdx.x] = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
@@ -341,7 +353,7 @@ __device__ __forceinline__ void wmask_tile(int2 w, float4 *sj, const RepDev *__r
         for (int q = 0; q < NB_WTILE / 32; ++q) {
             const int nv = tn - 32 * q;
             if (nv <= 0) break;
-            unsigned m = 0u;
+            unsigned m = 0u, mn = 0u;
 #pragma unroll 8
             for (int b = 0; b < 32; ++b) {
                 const float4 p = sj[32 * q + b];
@@ -351,70 +363,34 @@ __device__ __forceinline__ void wmask_tile(int2 w, float4 *sj, const RepDev *__r
                 dz = fminf(dz, L2 - dz);
                 const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                 m |= (r2 < rl2 ? 1u : 0u) << b;
+                mn |= (r2 <= rc2 ? 1u : 0u) << b;
             }
-            if (nv < 32) m &= (1u << nv) - 1u;              // past the last molecule
+            unsigned keep = nv < 32 ? (1u << nv) - 1u : 0xffffffffu;   // past the last molecule
             const int self = il - t0 - 32 * q;
-            if ((unsigned)self < 32u) m &= ~(1u << self);
-            n1 += __popc(m);
-            mrow[(size_t)(t0 / 32 + q) * nw] = m;
+            if ((unsigned)self < 32u) keep &= ~(1u << self);
+            m &= keep;
+            mn &= m;
+            const int jb = j0 + t0 + 32 * q;
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1u;
+                w1_put(row, cap_row, (mn >> b) & 1u, nn, nf, jb + b);
+            }
         }
     }
-    if (act) cnt1[i] = n1;
+    if (act) w1_done(i, nn, nf, cap_row, wcnt, st);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NB_WTILE) k_wmask_tiled(int ntile, const int2 *__restrict__ work,
+__global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 *__restrict__ work,
                                                           const RepDev *__restrict__ reps, const void *pos_v,
-                                                          unsigned *__restrict__ mask, int *__restrict__ cnt1,
-                                                          const int *st)
+                                                          int2 *__restrict__ wcnt, int *__restrict__ l1, int cap_row,
+                                                          int *st)
 {
     if (rebuild_off(st)) return;
     __shared__ float4 sj[NB_WTILE];
     // every tile pass starts with a block barrier before it overwrites sj
-    for (int b = blockIdx.x; b < ntile; b += gridDim.x) wmask_tile<T>(work[b], sj, reps, pos_v, mask, cnt1);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(NB_WTILE) k_wmask_fill(int ntile, const int2 *__restrict__ work,
-                                                         const RepDev *__restrict__ reps, const void *pos_v,
-                                                         const unsigned *__restrict__ mask,
-                                                         const int *__restrict__ off1, int *__restrict__ l1,
-                                                         int64_t cap1, int *st)
-{
-    if (rebuild_off(st)) return;
-    typedef typename vec4<T>::type T4;
-    const T4 *pos = (const T4 *)pos_v;
-    for (int b = blockIdx.x; b < ntile; b += gridDim.x) {
-        const int2 w = work[b];
-        const RepDev &R = reps[w.x];
-        const int j0 = R.wat0, nw = R.nwat;
-        const int i = w.y + (int)threadIdx.x, il = i - j0;
-        if (il >= nw) continue;
-        const int w1 = off1[i], n1 = off1[i + 1] - w1;
-        if ((int64_t)w1 + n1 > cap1) {
-            atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
-            continue;
-        }
-        const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2], rc2 = R.rmax2;
-        const float4 oi = wrap_box<T>(R, pos[3 * (size_t)i]);
-        const unsigned *mrow = mask + R.wmask0 + il;
-        int front = w1, back = w1 + n1 - 1;
-        const int nwd = (nw + 31) >> 5;
-        for (int wd = 0; wd < nwd; ++wd) {
-            unsigned m = mrow[(size_t)wd * nw];
-            while (m) {
-                const int j = j0 + 32 * wd + __ffs(m) - 1;
-                m &= m - 1u;
-                const float4 p = wrap_box<T>(R, pos[3 * (size_t)j]);
-                float dx = fabsf(oi.x - p.x), dy = fabsf(oi.y - p.y), dz = fabsf(oi.z - p.z);
-                dx = fminf(dx, L0 - dx);
-                dy = fminf(dy, L1 - dy);
-                dz = fminf(dz, L2 - dz);
-                if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rc2) l1[front++] = j;
-                else l1[back--] = j;
-            }
-        }
-    }
+    for (int b = blockIdx.x; b < ntile; b += gridDim.x) wlist_tile<T>(work[b], sj, reps, pos_v, wcnt, l1, cap_row, st);
 }
 
 // 5. non-water list X: every site j within reach, exclusions removed
@@ -627,21 +603,19 @@ void build_lists_t(NbCtx *c, const double *d_coor)
     if (c->nW > 0) {
         const int gw = grid(c->nW, 128), nt = (int)c->wtiles.size();
         const int gt = (int)std::min<int64_t>(nt, (int64_t)c->nsm * 16);
-        int *cnt1 = c->d_count_tmp, *cnt2 = c->d_count_tmp + c->nW + 1, *cntn = c->d_count_tmp + 2 * (c->nW + 1);
+        int *cnt2 = c->d_count_tmp;
+        // W1 rows (both kernels) and W2 counts in one pass; W2 scan and fill after
         k_wlist<T, 0><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         cnt1, cnt2, cntn, nullptr, nullptr, nullptr, nullptr, 0, 0, c->d_status);
+                                         c->d_wl1_cnt, cnt2, nullptr, c->d_wl1, c->cap_row1, nullptr, 0,
+                                         c->d_status);
         if (nt > 0)
-            k_wmask_tiled<T><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wmask, cnt1,
-                                                     c->d_status);
-        nb_scan(c, cnt1, c->d_wl1_off, (int)c->nW, c->d_status + 2, 1);
+            k_wlist_tiled<T><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wl1_cnt, c->d_wl1,
+                                                     c->cap_row1, c->d_status);
         nb_scan(c, cnt2, c->d_wl2_off, (int)c->nW, c->d_status + 3, 1);
         k_wlist<T, 1><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         nullptr, nullptr, cntn, c->d_wl1_off, c->d_wl2_off, c->d_wl1, c->d_wl2,
-                                         c->cap_wl1, c->cap_wl2, c->d_status);
-        if (nt > 0)
-            k_wmask_fill<T><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wmask, c->d_wl1_off,
-                                                    c->d_wl1, c->cap_wl1, c->d_status);
-        c->launches += nt > 0 ? 4 : 2;
+                                         nullptr, nullptr, c->d_wl2_off, nullptr, 0, c->d_wl2, c->cap_wl2,
+                                         c->d_status);
+        c->launches += nt > 0 ? 3 : 2;
     }
     if (c->nA > 0) {
         const int ga = grid(c->nA, 128);

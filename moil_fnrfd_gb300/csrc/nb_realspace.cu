@@ -164,13 +164,34 @@ __device__ __forceinline__ void water_vs_atoms(const RepDev &R, int i, const typ
 // int64 / FP64 accumulators kept in shared memory (one column per thread), which keeps
 // them out of the register file.
 #define WBLOCK 128
+
+// water i's W1 row: entry v is the v-th in-cutoff molecule from the front for v < nn, then
+// the skin-only molecules from the back of the row
+struct W1Row {
+    const int *row;
+    int nn, n, cap;
+    __device__ W1Row(const int2 *__restrict__ cnt, const int *__restrict__ wl1, int cap_row, int i)
+    {
+        const int2 c = cnt[i];
+        row = wl1 + (size_t)i * cap_row;
+        // an overflowed row (counts above the capacity) is read within the row; the
+        // evaluation reports the overflow and is redone with larger rows
+        nn = min(c.x, cap_row);
+        n = min(c.x + c.y, cap_row);
+        cap = cap_row;
+    }
+    __device__ const int *addr(int v) const { return row + (v < nn ? v : cap - 1 - (v - nn)); }
+    __device__ int at(int v) const { return *addr(v); }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                                                      const void *pos_v, const void *woff_v, const void *lj_v,
                                                      const unsigned *__restrict__ sflags,
-                                                     const int *__restrict__ wl1_off, const int *__restrict__ wl1,
-                                                     const int *__restrict__ wl2_off, const int *__restrict__ wl2,
-                                                     long long *__restrict__ grad, double *__restrict__ e_unit)
+                                                     const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
+                                                     int cap_row, const int *__restrict__ wl2_off,
+                                                     const int *__restrict__ wl2, long long *__restrict__ grad,
+                                                     double *__restrict__ e_unit)
 {
     __shared__ long long sG[9][WBLOCK];
     __shared__ double sE[4][WBLOCK];
@@ -205,15 +226,16 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
     const T rmax2 = (T)R.rmax2, rv2 = (T)R.rv2, alpha = Consts<T>::alpha(R), ex2c = (T)R.ex2c, c2a = (T)R.c2a;
     const T qOO = Consts<T>::qq(R, 0), qOH = Consts<T>::qq(R, 1), qHH = Consts<T>::qq(R, 2);
     const T w12 = Consts<T>::w12(R), w6 = Consts<T>::w6(R);
-    int k0 = wl1_off[i], k1 = wl1_off[i + 1], cnt = 0;
+    const W1Row L1(wl1_cnt, wl1, cap_row, i);
+    int cnt = 0;
     // software pipeline: the next entry's index and oxygen are loaded one iteration ahead
-    int jn = k0 < k1 ? wl1[k0] : 0;
+    int jn = L1.n > 0 ? L1.at(0) : 0;
     T4 ojn = pos[3 * jn];
-    for (int k = k0; k < k1; ++k) {
+    for (int k = 0; k < L1.n; ++k) {
         const int j = jn;
         const T4 oj = ojn;
-        if (k + 1 < k1) {
-            jn = wl1[k + 1];
+        if (k + 1 < L1.n) {
+            jn = L1.at(k + 1);
             ojn = pos[3 * jn];
         }
         T dx = oi0.x - oj.x, dy = oi0.y - oj.y, dz = oi0.z - oj.z;
@@ -287,9 +309,10 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                                                        const int *__restrict__ site_rep, const float4 *__restrict__ pos,
                                                        const float4 *__restrict__ woff, const void *lj_v,
                                                        const unsigned *__restrict__ sflags,
-                                                       const int *__restrict__ wl1_off, const int *__restrict__ wl1,
-                                                       const int *__restrict__ wl2_off, const int *__restrict__ wl2,
-                                                       long long *__restrict__ grad, double *__restrict__ e_unit)
+                                                       const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
+                                                       int cap_row, const int *__restrict__ wl2_off,
+                                                       const int *__restrict__ wl2, long long *__restrict__ grad,
+                                                       double *__restrict__ e_unit)
 {
     __shared__ long long sG[9][WBLOCK];
     __shared__ double sE[4][WBLOCK];
@@ -329,21 +352,22 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     const float2 w12 = f2(R.w12), nw6 = f2(-R.w6);
     const float qqv[3] = {R.qq[0], R.qq[1], R.qq[2]};
     const float c2a = R.c2a;
-    const int k0 = wl1_off[i], k1 = wl1_off[i + 1];
+    const W1Row L1(wl1_cnt, wl1, cap_row, i);
+    const int k1 = L1.n;
     int cnt = 0;
     // next pair of entries, loaded one iteration ahead
-    int ja = k0 < k1 ? wl1[k0] : 0;
-    int jb = k0 + 1 < k1 ? wl1[k0 + 1] : ja;
+    int ja = k1 > 0 ? L1.at(0) : 0;
+    int jb = k1 > 1 ? L1.at(1) : ja;
     float4 oa = pos[3 * ja], ob = pos[3 * jb];
-    for (int k = k0; k < k1; k += 2) {
+    for (int k = 0; k < k1; k += 2) {
         const bool hasb = k + 1 < k1;
         const int j0 = ja, j1 = jb;
         const float4 o0 = oa, o1 = ob;
-        // each lane streams its own list (a DRAM stream): pull the line 32 entries ahead
-        nb_prefetch_l1(wl1 + min(k + 32, k1 - 1));
+        // each lane streams its own row (a DRAM stream): pull the line 32 entries ahead
+        nb_prefetch_l1(L1.addr(min(k + 32, k1 - 1)));
         if (k + 2 < k1) {
-            ja = wl1[k + 2];
-            jb = k + 3 < k1 ? wl1[k + 3] : ja;
+            ja = L1.at(k + 2);
+            jb = k + 3 < k1 ? L1.at(k + 3) : ja;
             oa = pos[3 * ja];
             ob = pos[3 * jb];
         }
@@ -779,12 +803,13 @@ void realspace_t(NbCtx *c)
         const int nb = (int)((c->nW + WBLOCK - 1) / WBLOCK);
         if constexpr (sizeof(T) == 4)
             k_water_f<<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos,
-                                            (const float4 *)c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_off,
-                                            c->d_wl1, c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
+                                            (const float4 *)c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_cnt,
+                                            c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, c->d_grad_site,
+                                            c->d_e_unit);
         else
             k_water<T><<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
-                                             c->d_site_lj, c->d_site_flags, c->d_wl1_off, c->d_wl1, c->d_wl2_off,
-                                             c->d_wl2, c->d_grad_site, c->d_e_unit);
+                                             c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1,
+                                             c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
         c->launches++;
     }
     if (c->timing) cudaEventRecord(c->ev[3], s);
