@@ -271,3 +271,27 @@ def test_large_water_box_against_fp64_path():
     ref, eref = O.eforce(s, mode="mi")
     check(dp_, ep, ref, eref, MOIL_NB_FP64, "fp64 96k")
     check(dm, em, ref, eref, MOIL_NB_MIXED, "mixed 96k")
+
+
+def test_dense_cluster_regrows_lists():
+    """Waters packed into part of the box (2.4x the mean density there) overflow the pair-
+    list rows sized from the mean density; the evaluation regrows them and stays exact."""
+    s = S.water_box(3000, (3000 / S.WATER_DENSITY) ** (1 / 3), 91, name="cluster")
+    xyz = s.coor.reshape(-1, 3, 3)
+    o = xyz[:, 0, :]                  # the box is centred on the origin: pull molecules in
+    s.coor = (xyz - 0.25 * o[:, None, :]).reshape(-1, 3)
+    # precondition: the densest rows exceed the capacity sized from the mean density
+    # (rows of 4/3 pi (rc + skin)^3 * mean density * 1.4 + 32 entries, rounded up to 32)
+    o = s.coor.reshape(-1, 3, 3)[:, 0, :]
+    L = np.array(s.box)
+    rows = []
+    for k in range(0, 3000, 500):
+        d = o[k:k + 500, None, :] - o[None, :, :]
+        d -= L * np.round(d / L)
+        rows.append(((d * d).sum(-1) < 10.0 ** 2).sum(1) - 1)
+    assert np.concatenate(rows).max() > 256
+    nb = Nonbonded(s)
+    d, e = nb.eforce(s.coor)
+    ref, eref = O.eforce(s, mode="parity")
+    check(d, e, ref, eref, MOIL_NB_MIXED, "dense cluster")
+    nb.close()
