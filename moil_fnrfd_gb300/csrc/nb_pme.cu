@@ -478,12 +478,12 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     }
 }
 
+// inverse y and x transforms of plane z; the real potential plane (n1 x n2 floats) is stored
+// over the plane's own complex storage, which this block alone reads, for k_pme_gather_f
 __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
                                                      const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
                                                      const float2 *__restrict__ tw, const int2 *__restrict__ tab,
-                                                     const int *__restrict__ zstart, const int *__restrict__ zatoms,
-                                                     const float4 *__restrict__ fr, const float2 *__restrict__ grid,
-                                                     float *__restrict__ part)
+                                                     float2 *__restrict__ grid)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const PlaneWork w = work[blockIdx.x];
@@ -513,7 +513,59 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
     __syncthreads();
     // x: n2 lines of n1; the last pass stores real parts into Rp[ky][x]
     fft_lines<2, false>(c1, Xs, Yt, Rp, n2, 0);
-    gather_plane<float>(R, w.z, zstart, zatoms, fr, Rp, part);
+    float *gr = (float *)(grid + R.g0 + (size_t)w.z * n1h * n2);
+    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) gr[k] = Rp[k];
+}
+
+// PME gradient of each site from the real potential grid (grad_sum,
+// ewald_receip.f:815-970): order-4 weights and derivatives once per site, the 4x4x4 stencil
+// read from the grid planes k_plane_inv_f left in place; result (x, y, z) per site, to be
+// scaled by q * fc * n_d / L_d in the finalize
+__global__ void __launch_bounds__(256) k_pme_gather_f(int nsite, const int *__restrict__ site_rep,
+                                                      const RepDev *__restrict__ reps, const float4 *__restrict__ fr,
+                                                      const float2 *__restrict__ grid, float4 *__restrict__ part)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsite) return;
+    const float4 f = fr[s];
+    if (f.w == 0.f) { part[s] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
+    const RepDev &R = reps[site_rep[s]];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
+    const size_t zs = (size_t)R.n1h * n2 * 2;    // floats per plane
+    const float *Q = (const float *)(grid + R.g0);
+    const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+    float th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
+    const float w1 = f.x - (float)i1, w2 = f.y - (float)i2, w3 = f.z - (float)i3;
+    bsp4_th<float>(w1, th1); bsp4_dth<float>(w1, dt1);
+    bsp4_th<float>(w2, th2); bsp4_dth<float>(w2, dt2);
+    bsp4_th<float>(w3, th3); bsp4_dth<float>(w3, dt3);
+    int xs[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) xs[t] = pme_wrap(i1 - 3 + t, n1);
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+    for (int t3 = 0; t3 < 4; ++t3) {
+        const float *P = Q + pme_wrap(i3 - 3 + t3, n3) * zs;
+        float hx = 0.f, hy = 0.f, hz = 0.f;
+#pragma unroll
+        for (int t2 = 0; t2 < 4; ++t2) {
+            const float *row = P + pme_wrap(i2 - 3 + t2, n2) * n1;
+            float sx = 0.f, sy = 0.f;
+#pragma unroll
+            for (int t1 = 0; t1 < 4; ++t1) {
+                const float q = row[xs[t1]];
+                sx = fmaf(q, dt1[t1], sx);
+                sy = fmaf(q, th1[t1], sy);
+            }
+            hx = fmaf(sx, th2[t2], hx);
+            hy = fmaf(sy, dt2[t2], hy);
+            hz = fmaf(sy, th2[t2], hz);
+        }
+        gx = fmaf(hx, th3[t3], gx);
+        gy = fmaf(hy, th3[t3], gy);
+        gz = fmaf(hz, dt3[t3], gz);
+    }
+    part[s] = make_float4(gx, gy, gz, 0.f);
 }
 
 // =================================================================================
@@ -729,9 +781,11 @@ void pme_t(NbCtx *c)
                                                   (float2 *)c->d_grid, c->d_e_col);
         if (c->timing) cudaEventRecord(c->ev[8], s);
         k_plane_inv_f<<<np, 256, c->smem_plane_inv, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
-                                                           (const float2 *)c->d_tw, c->d_tab, c->d_zstart,
-                                                           c->d_zatoms, (const float4 *)c->d_fr,
-                                                           (const float2 *)c->d_grid, (float *)c->d_part);
+                                                           (const float2 *)c->d_tw, c->d_tab, (float2 *)c->d_grid);
+        k_pme_gather_f<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>(
+            (int)c->nsite, c->d_site_rep, c->d_reps, (const float4 *)c->d_fr, (const float2 *)c->d_grid,
+            (float4 *)c->d_part);
+        c->launches++;
     } else {
         k_plane_fwd<T><<<np, 256, c->smem_plane_fwd, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw,
                                                           c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid);
@@ -1025,11 +1079,8 @@ __global__ void k_na_grad(int natom, const RepDev *__restrict__ reps, const doub
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= natom) return;
     const RepDev &R = reps[0];
-    double pg[3] = {0, 0, 0};
-    const float *p = part + 12 * (size_t)a;
-#pragma unroll
-    for (int t = 0; t < 4; ++t)
-        for (int d = 0; d < 3; ++d) pg[d] += (double)p[3 * t + d];
+    const float4 p = ((const float4 *)part)[a];   // k_pme_gather_f: one (x, y, z) per atom
+    const double pg[3] = {(double)p.x, (double)p.y, (double)p.z};
     double qf = q[a] * R.fcd;
     dpot[3 * (size_t)a] = qf * R.n1 * R.invLd[0] * pg[0];
     dpot[3 * (size_t)a + 1] = qf * R.n2 * R.invLd[1] * pg[1];

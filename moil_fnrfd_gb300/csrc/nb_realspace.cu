@@ -713,16 +713,16 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
     if (a >= natom) return;
     const RepDev &R = reps[atom_rep[a]];
     int s = site_of[a];
-    const T *p = part + 12 * (size_t)s;
     bool bad = false;
     if constexpr (sizeof(T) == 4) {
-        // FP32 path: the PME share is summed and scaled in FP32 (its own precision) and
-        // joins the fixed-point real-space and correction terms as an integer; the double
-        // result is assembled with integer operations (no FP64 instruction)
+        // FP32 path: the PME share (one float4 per site from k_pme_gather_f) is scaled in
+        // FP32 (its own precision) and joins the fixed-point real-space and correction terms
+        // as an integer; the double result is assembled with integer operations (no FP64
+        // instruction)
         const long long *gx = (const long long *)grad_ex + 3 * (size_t)a;
         const float qs = (float)q[a];
-        const float pg[3] = {((p[0] + p[3]) + p[6]) + p[9], ((p[1] + p[4]) + p[7]) + p[10],
-                             ((p[2] + p[5]) + p[8]) + p[11]};
+        const float4 p4 = ((const float4 *)part)[s];
+        const float pg[3] = {p4.x, p4.y, p4.z};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const long long v = grad_site[3 * (size_t)s + d] + gx[d] + nb_f2fix(qs * R.pme_gs[d] * pg[d]);
@@ -730,6 +730,7 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
             dpot[3 * (size_t)a + d] = nb_fix2d(v);
         }
     } else {
+        const T *p = part + 12 * (size_t)s;   // 4 plane slots per site (k_plane_inv)
         double pg[3] = {0, 0, 0};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
