@@ -384,6 +384,15 @@ __device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst,
     return src;
 }
 
+// float2 elements of each of the two plane buffers of the FP32 plane kernels: the packed
+// rows (ceil(n2/2) lines of n1) or the half spectrum (n1/2+1 lines of n2), whichever is
+// larger; even, so the buffers after it stay 16-byte aligned
+__host__ __device__ __forceinline__ int plane_buf_elems(int n1, int n2)
+{
+    const int a = ((n2 + 1) / 2) * n1, b = (n1 / 2 + 1) * n2;
+    return ((a > b ? a : b) + 1) & ~1;
+}
+
 __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
                                                      const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
                                                      const float2 *__restrict__ tw, const int2 *__restrict__ tab,
@@ -393,25 +402,41 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
     extern __shared__ __align__(16) unsigned char smem[];
     const PlaneWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
-    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
-    float2 *A = (float2 *)smem;
-    float2 *B = A + n1 * n2;
-    int *acc = (int *)B;                        // the accumulator lives in B until the first pass
+    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h, n2p = (n2 + 1) >> 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float2 *B0 = (float2 *)smem, *B1 = B0 + plane_buf_elems(n1, n2);
+    int *acc = (int *)B0;                        // the int32 plane lives in B0 until it is packed
     FftCtx c1, c2;
-    unsigned char *ctx = (unsigned char *)(B + n1 * n2);
+    unsigned char *ctx = (unsigned char *)(B1 + plane_buf_elems(n1, n2));
     ctx = fft_ctx_load(ctx, plans + rep_plan[3 * w.rep], tab, tw, c1);
     fft_ctx_load(ctx, plans + rep_plan[3 * w.rep + 1], tab, tw, c2);
     for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
     __syncthreads();
     spread_plane<float>(R, w.z, zstart, zatoms, fr, acc, R.spread_scale);
     __syncthreads();
+    // x transform of real rows two at a time: line p carries row 2p as its real part and
+    // row 2p+1 as its imaginary part
     const float inv = R.spread_inv;
-    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) A[k] = make_float2(Acc<float>::get(acc[k], inv), 0.f);
+    for (int p = warp; p < n2p; p += nwarp)
+        for (int x = lane; x < n1; x += 32) {
+            const float re = Acc<float>::get(acc[2 * p * n1 + x], inv);
+            const float im = 2 * p + 1 < n2 ? Acc<float>::get(acc[(2 * p + 1) * n1 + x], inv) : 0.f;
+            B1[p * n1 + x] = make_float2(re, im);
+        }
     __syncthreads();
-    // x: n2 rows of n1 (real input); last pass keeps kx < n1h, transposed to [kx][y]
-    float2 *X = fft_lines<1, false>(c1, A, B, nullptr, n2, n1h);
+    float2 *Z = fft_lines<0, false>(c1, B1, B0, nullptr, n2p, 0);
+    float2 *T = Z == B1 ? B0 : B1;
+    // separate the two real transforms (X_2p = (Z_k + conj Z_-k)/2, X_2p+1 = -i (Z_k - conj Z_-k)/2)
+    // and keep kx < n1h, transposed to [kx][y] lines of n2
+    for (int p = warp; p < n2p; p += nwarp)
+        for (int k = lane; k < n1h; k += 32) {
+            const float2 a = Z[p * n1 + k], b = Z[p * n1 + (k == 0 ? 0 : n1 - k)];
+            T[k * n2 + 2 * p] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+            if (2 * p + 1 < n2) T[k * n2 + 2 * p + 1] = make_float2(0.5f * (a.y + b.y), 0.5f * (b.x - a.x));
+        }
+    __syncthreads();
     // y: n1h lines of n2
-    float2 *Y = fft_lines<0, false>(c2, X, X == A ? B : A, nullptr, n1h, 0);
+    float2 *Y = fft_lines<0, false>(c2, T, Z, nullptr, n1h, 0);
     float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
     for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) g[k] = Y[k];
 }
@@ -488,33 +513,43 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
     extern __shared__ __align__(16) unsigned char smem[];
     const PlaneWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
-    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h;
-    float2 *P0 = (float2 *)smem, *P1 = P0 + n1 * n2, *Q = P1 + n1 * n2;
-    float *Rp = (float *)Q;       // the real plane of n1 x n2 floats
+    const int n1 = R.n1, n2 = R.n2, n1h = R.n1h, n2p = (n2 + 1) >> 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float2 *B0 = (float2 *)smem, *B1 = B0 + plane_buf_elems(n1, n2);
     FftCtx c1, c2;
-    unsigned char *ctx = (unsigned char *)(Q + n1h * n2);
+    unsigned char *ctx = (unsigned char *)(B1 + plane_buf_elems(n1, n2));
     ctx = fft_ctx_load(ctx, plans + rep_plan[3 * w.rep], tab, tw, c1);
     fft_ctx_load(ctx, plans + rep_plan[3 * w.rep + 1], tab, tw, c2);
-    const float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
+    float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
     // [kx][ky] lines of n2, conjugated (inverse through the forward transform)
-    for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) P0[k] = cconj(g[k]);
+    for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) B0[k] = cconj(g[k]);
     __syncthreads();
-    // y: n1h lines; last pass conjugates back and stores transposed to [ky][kx]
-    fft_lines<1, true>(c2, P0, P1, nullptr, n1h, n2);
+    // y: n1h lines; last pass conjugates back and stores transposed to H[ky][kx]
+    fft_lines<1, true>(c2, B0, B1, nullptr, n1h, n2);
     // which buffer got the transposed result depends on the pass count
-    float2 *Yt = (c2.p->nst & 1) ? P1 : P0;
-    // expand each ky row to the full Hermitian line of n1, conjugated again for the inverse
-    float2 *Xs = Yt == P0 ? P1 : P0;
-    for (int ky = threadIdx.x >> 5; ky < n2; ky += blockDim.x >> 5)
-        for (int i = threadIdx.x & 31; i < n1; i += 32) {
-            float2 v = i < n1h ? Yt[ky * n1h + i] : cconj(Yt[ky * n1h + (n1 - i)]);
-            Xs[ky * n1 + i] = cconj(v);
+    float2 *H = (c2.p->nst & 1) ? B1 : B0;
+    float2 *Zc = H == B0 ? B1 : B0;
+    // x inverse of two real rows at a time: Z = H_2p + i H_2p+1 over the full Hermitian line of
+    // n1, conjugated so the forward transform inverts it; row 2p = Re, row 2p+1 = -Im of the result
+    for (int p = warp; p < n2p; p += nwarp)
+        for (int k = lane; k < n1; k += 32) {
+            const bool lo = k < n1h;
+            const int kk = lo ? k : n1 - k;
+            float2 a = H[2 * p * n1h + kk];
+            float2 b = 2 * p + 1 < n2 ? H[(2 * p + 1) * n1h + kk] : make_float2(0.f, 0.f);
+            if (!lo) { a = cconj(a); b = cconj(b); }
+            Zc[p * n1 + k] = make_float2(a.x - b.y, -(a.y + b.x));
         }
     __syncthreads();
-    // x: n2 lines of n1; the last pass stores real parts into Rp[ky][x]
-    fft_lines<2, false>(c1, Xs, Yt, Rp, n2, 0);
-    float *gr = (float *)(grid + R.g0 + (size_t)w.z * n1h * n2);
-    for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) gr[k] = Rp[k];
+    const float2 *W = fft_lines<0, false>(c1, Zc, H, nullptr, n2p, 0);
+    // the real potential plane over the plane's own complex storage (this block alone reads it)
+    float *gr = (float *)g;
+    for (int p = warp; p < n2p; p += nwarp)
+        for (int x = lane; x < n1; x += 32) {
+            const float2 v = W[p * n1 + x];
+            gr[2 * p * n1 + x] = v.x;
+            if (2 * p + 1 < n2) gr[(2 * p + 1) * n1 + x] = -v.y;
+        }
 }
 
 // PME gradient of each site from the real potential grid (grad_sum,
@@ -845,7 +880,7 @@ size_t fft_ctx_bytes(int n)
 template <typename T>
 size_t plane_fwd_smem(int n1, int n2)
 {
-    if (sizeof(T) == 4) return (size_t)2 * n1 * n2 * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
+    if (sizeof(T) == 4) return (size_t)2 * plane_buf_elems(n1, n2) * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
     typedef typename cplx<T>::type C;
     size_t acc = (sizeof(typename Acc<T>::type) * n1 * n2 + 15) & ~(size_t)15;
     return acc + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -853,8 +888,7 @@ size_t plane_fwd_smem(int n1, int n2)
 template <typename T>
 size_t plane_inv_smem(int n1, int n2)
 {
-    if (sizeof(T) == 4)
-        return (size_t)(2 * n1 + (n1 / 2 + 1)) * n2 * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
+    if (sizeof(T) == 4) return (size_t)2 * plane_buf_elems(n1, n2) * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
     typedef typename cplx<T>::type C;
     size_t r = (sizeof(T) * n1 * n2 + 15) & ~(size_t)15;
     return r + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
