@@ -126,20 +126,20 @@ __global__ void k_site_build(int nunit, int nW, const int *__restrict__ sorted, 
     }
 }
 
-// 3. per-evaluation coordinate conversion into site order; displacement check
+// 3. per-evaluation coordinate conversion into site order; displacement check.  One thread
+// per caller atom, so the caller's coordinates are read in order (they may live in host
+// memory the GPU addresses directly); the site-order outputs are scattered.
 template <typename T>
-__global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_orig, const int *__restrict__ site_rep,
-                          const unsigned *__restrict__ site_flags, const double *__restrict__ q,
-                          const RepDev *__restrict__ reps, const double *__restrict__ coor, void *pos_v,
-                          void *woff_v, float4 *__restrict__ posb, float half_skin2, float rwat2, int snapshot,
-                          int *st)
+__global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_of, const unsigned *__restrict__ site_flags,
+                          const double *__restrict__ q, const double *__restrict__ coor, void *pos_v, void *woff_v,
+                          float4 *__restrict__ posb, float half_skin2, float rwat2, int snapshot, int *st)
 {
     // snapshot mode runs only on a rebuild; check mode only without one (the site order it
     // reads is the previous build's, which does not exist before the first build)
     if (snapshot ? rebuild_off(st) : !rebuild_off(st)) return;
     typedef typename vec4<T>::type T4;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsite; s += gridDim.x * blockDim.x) {
-        int a = site_orig[s];
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nsite; a += gridDim.x * blockDim.x) {
+        const int s = site_of[a];
         double x = coor[3 * (size_t)a], y = coor[3 * (size_t)a + 1], z = coor[3 * (size_t)a + 2];
         if (!(x == x && y == y && z == z) || fabs(x) > 1e7 || fabs(y) > 1e7 || fabs(z) > 1e7) {
             atomicOr(&st[1], NB_DEV_ERR_NAN);
@@ -160,8 +160,9 @@ __global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_orig, 
             if (dx * dx + dy * dy + dz * dz > half_skin2) atomicOr(&st[0], 1);
         }
         if (s < 3 * nW && (s % 3) != 0) {
-            // water sites must stay within rwat of their oxygen (list radius assumption)
-            int o = site_orig[s - (s % 3)];
+            // water sites must stay within rwat of their oxygen (list radius assumption); a
+            // water's caller atoms are consecutive (O, H, H), as are its sites
+            const int o = a - (s % 3);
             double ox = coor[3 * (size_t)o], oy = coor[3 * (size_t)o + 1], oz = coor[3 * (size_t)o + 2];
             double d2 = (x - ox) * (x - ox) + (y - oy) * (y - oy) + (z - oz) * (z - oz);
             if (d2 > rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
@@ -172,8 +173,6 @@ __global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_orig, 
             ((T4 *)woff_v)[2 * (s / 3) + (s % 3) - 1] = off;
         }
     }
-    (void)site_rep;
-    (void)reps;
 }
 
 // unique neighbour cells along one axis
@@ -596,9 +595,9 @@ void build_lists_t(NbCtx *c, const double *d_coor)
         (int)c->nunit, (int)c->nW, c->d_sorted_unit, c->d_unit_atom, c->d_atom_rep, c->d_aflags, c->d_lj_f,
         c->d_lj_d, c->d_q, c->d_site_orig, c->d_site_of, c->d_site_rep, c->d_site_flags, c->d_site_lj,
         c->d_site_q, c->d_status);
-    k_prepare<T><<<grid(c->nsite, B), B, 0, s>>>(
-        (int)c->nsite, (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_site_flags, c->d_q, c->d_reps, d_coor,
-        c->d_pos, c->d_woff, c->d_posb, 0.f, c->rwat * c->rwat, 1, c->d_status);
+    k_prepare<T><<<grid(c->nsite, B), B, 0, s>>>((int)c->nsite, (int)c->nW, c->d_site_of, c->d_site_flags, c->d_q,
+                                                 d_coor, c->d_pos, c->d_woff, c->d_posb, 0.f, c->rwat * c->rwat, 1,
+                                                 c->d_status);
     c->launches += 5;
     if (c->nW > 0) {
         const int gw = grid(c->nW, 128), nt = (int)c->wtiles.size();
@@ -636,9 +635,9 @@ void prepare_t(NbCtx *c, const double *d_coor, int check)
     const int B = 256;
     float hs = 0.5f * c->skin;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((c->nsite + B - 1) / B, (int64_t)c->nsm * 8));
-    k_prepare<T><<<g, B, 0, c->stream>>>(
-        (int)c->nsite, (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_site_flags, c->d_q, c->d_reps, d_coor,
-        c->d_pos, c->d_woff, c->d_posb, check ? hs * hs : 3.0e38f, c->rwat * c->rwat, 0, c->d_status);
+    k_prepare<T><<<g, B, 0, c->stream>>>((int)c->nsite, (int)c->nW, c->d_site_of, c->d_site_flags, c->d_q, d_coor,
+                                         c->d_pos, c->d_woff, c->d_posb, check ? hs * hs : 3.0e38f,
+                                         c->rwat * c->rwat, 0, c->d_status);
     c->launches += 1;
 }
 

@@ -371,11 +371,11 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
             oa = pos[3 * ja];
             ob = pos[3 * jb];
         }
-        // O-O minimum image per entry
+        // O-O minimum image per entry; (x + 1.5*2^23) - 1.5*2^23 rounds x to nearest (|x| < 2^22)
         float dx0 = oi0.x - o0.x, dy0 = oi0.y - o0.y, dz0 = oi0.z - o0.z;
         float dx1 = oi0.x - o1.x, dy1 = oi0.y - o1.y, dz1 = oi0.z - o1.z;
-        const float nx0 = rintf(dx0 * iL0), ny0 = rintf(dy0 * iL1), nz0 = rintf(dz0 * iL2);
-        const float nx1 = rintf(dx1 * iL0), ny1 = rintf(dy1 * iL1), nz1 = rintf(dz1 * iL2);
+        const float nx0 = fmaf(dx0, iL0, 12582912.f) - 12582912.f, ny0 = fmaf(dy0, iL1, 12582912.f) - 12582912.f, nz0 = fmaf(dz0, iL2, 12582912.f) - 12582912.f;
+        const float nx1 = fmaf(dx1, iL0, 12582912.f) - 12582912.f, ny1 = fmaf(dy1, iL1, 12582912.f) - 12582912.f, nz1 = fmaf(dz1, iL2, 12582912.f) - 12582912.f;
         dx0 = nb_shift(R, 0, dx0, nx0); dy0 = nb_shift(R, 1, dy0, ny0); dz0 = nb_shift(R, 2, dz0, nz0);
         dx1 = nb_shift(R, 0, dx1, nx1); dy1 = nb_shift(R, 1, dy1, ny1); dz1 = nb_shift(R, 2, dz1, nz1);
         const float r0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0, r1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;

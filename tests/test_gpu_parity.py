@@ -100,6 +100,20 @@ def test_graph_replay_matches_kernel_launches(cfg0):
     k.close()
 
 
+def test_pinned_host_buffers_match_copies(cfg0):
+    """Pinned host buffers give the result of pageable ones bit for bit, call after call."""
+    torch = pytest.importorskip("torch")
+    nb = Nonbonded(cfg0)
+    d_page, e_page = nb.eforce(cfg0.coor)
+    hc = torch.from_numpy(np.ascontiguousarray(cfg0.coor)).pin_memory()
+    hd = torch.zeros_like(hc).pin_memory()
+    for _ in range(2):
+        e_pin = nb.eforce_into(hc.numpy(), hd.numpy())
+        assert np.array_equal(hd.numpy(), d_page)
+        assert e_pin[0] == e_page
+    nb.close()
+
+
 def test_batch_matches_single_systems_and_oracle(cfg0):
     sizes = [1503, 2406, 3300]
     reps = [S.water_box(n // 3, (n // 3 / S.WATER_DENSITY) ** (1 / 3), 500 + k, name=f"r{k}")
