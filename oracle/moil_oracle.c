@@ -892,7 +892,8 @@ static int wrapidx(int k0, int n)
     return k % n;   /* fr == nfft exactly lands on index 0 */
 }
 
-int ora_pme(const ora_input *in, double ewaldcof, double *dpot, double *eer, double *fpme_out)
+/* PME core; phi (nullable) receives dE_rec/dq per atom: fc * sum(theta * convolved grid) */
+static int pme_core(const ora_input *in, double ewaldcof, double *dpot, double *eer, double *fpme_out, double *phi)
 {
     int n1 = in->nfft1, n2 = in->nfft2, n3 = in->nfft3, order = in->order, N = in->npt;
     size_t ng = (size_t)n1 * n2 * n3;
@@ -993,6 +994,21 @@ int ora_pme(const ora_input *in, double ewaldcof, double *dpot, double *eer, dou
         }
         fx = rc1 * f1; fy = rc2 * f2; fz = rc3 * f3;
         dpot[3 * n] -= fx; dpot[3 * n + 1] -= fy; dpot[3 * n + 2] -= fz;
+        if (phi) {
+            double v = 0;
+            k0 = (int)fr[3 * n + 2] - order;
+            for (i3 = 0; i3 < order; i3++) {
+                int k = wrapidx(++k0, n3), j0 = j0b;
+                for (i2 = 0; i2 < order; i2++) {
+                    int j = wrapidx(++j0, n2), i0 = i0b;
+                    for (i1 = 0; i1 < order; i1++) {
+                        int i = wrapidx(++i0, n1);
+                        v += t[i1] * t[order + i2] * t[2 * order + i3] * qr[Q(i, j, k)];
+                    }
+                }
+            }
+            phi[n] += fc * v;
+        }
         fpme += fx * fx + fy * fy + fz * fz;
     }
 #undef Q
@@ -1000,6 +1016,11 @@ int ora_pme(const ora_input *in, double ewaldcof, double *dpot, double *eer, dou
     if (fpme_out) *fpme_out = sqrt(fpme / (3.0 * N));
     free(qr); free(qi); free(m1); free(m2); free(m3); free(th); free(fr);
     return 0;
+}
+
+int ora_pme(const ora_input *in, double ewaldcof, double *dpot, double *eer, double *fpme_out)
+{
+    return pme_core(in, ewaldcof, dpot, eer, fpme_out, 0);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1321,6 +1342,162 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
     }
     finish(out);
     free(mol); free(oxy);
+    ctx_free(c);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Parameter derivatives (no MOIL counterpart; pinned by finite differences of the energy):
+ * dE/dq_i (the electrostatic potential at i), dE/deps_i and dE/dsigma_i of atom i's LJ
+ * parameters, decoded from the epsgm encoding (connect/fillpt.f:136-184).  Same pair
+ * predicate as ora_eforce_mi; the LJ switch is not applied.  Water-water charge products
+ * use each site's own charge (MOIL uses the last water's, equal for identical waters). */
+static void lj_decode(const ora_input *in, int i, double *eps, double *sig)
+{
+    double e12 = in->epsgm12[i], e6 = in->epsgm6[i];
+    if (!in->arith) {
+        if (e12 > 0 && e6 > 0) {
+            double se = e6 * e6 / (2.0 * e12);   /* sqrt(eps): epsgm6 = 2 sqrt(eps) sigma^3 */
+            *sig = cbrt(e12 / e6);                /* epsgm12 / epsgm6 = sigma^3 */
+            *eps = se * se;
+        } else {
+            *eps = 0; *sig = 0;
+        }
+    } else {
+        *eps = 0.25 * e12 * e12;                  /* epsgm12 = 2 sqrt(eps) */
+        *sig = e6;                                /* epsgm6 = sigma */
+    }
+}
+
+/* pair LJ energy e = a - b (a ~ r^-12, b ~ r^-6 parts) into atoms i, j (0-based) */
+static void lj_adjoint(const ora_input *in, int i, int j, double a, double b, const double *eps,
+                       const double *sig, double *de, double *ds)
+{
+    double e = a - b, g = 6.0 * a - 3.0 * b;
+    if (de) {
+        if (eps[i] > 0) de[i] += e / (2.0 * eps[i]);
+        if (eps[j] > 0) de[j] += e / (2.0 * eps[j]);
+    }
+    if (ds) {
+        if (!in->arith) {
+            if (sig[i] > 0) ds[i] += g / sig[i];
+            if (sig[j] > 0) ds[j] += g / sig[j];
+        } else {
+            double sij = 0.5 * (sig[i] + sig[j]);
+            if (sij > 0) { ds[i] += g / sij; ds[j] += g / sij; }
+        }
+    }
+}
+
+int ora_adjoint_mi(const ora_input *in, double *dq, double *de, double *ds)
+{
+    ctx cc, *c = &cc;
+    int npt = in->npt, i, m, k;
+    int *mol, *oxy;
+    double box[3] = {in->a, in->b, in->c};
+    double rcut_el2, o12 = 0, o6 = 0, qq[3][3];
+    double *eps, *sig, *dpot;
+    int has_water = 0;
+    if (ctx_init(c, in)) return -1;
+    if (dq) memset(dq, 0, sizeof(double) * npt);
+    if (de) memset(de, 0, sizeof(double) * npt);
+    if (ds) memset(ds, 0, sizeof(double) * npt);
+    eps = (double *)malloc(sizeof(double) * npt);
+    sig = (double *)malloc(sizeof(double) * npt);
+    for (i = 0; i < npt; i++) lj_decode(in, i, eps + i, sig + i);
+    mol = (int *)malloc(sizeof(int) * (npt + 1));
+    oxy = (int *)calloc(npt + 1, sizeof(int));
+    for (m = 0; m < in->totmon; m++)
+        for (i = c->first[m]; i <= in->poipt[m]; i++) {
+            mol[i] = m;
+            if (c->iswat[m]) { oxy[i] = in->poipt[m] - 2; has_water = 1; }
+        }
+    if (has_water) water_consts(c, &o12, &o6, qq);
+    rcut_el2 = c->cutele2 > c->cutvdw2 ? c->cutele2 : c->cutvdw2;
+    /* self energy (ewald_init.f:131-150) and PME potential */
+    if (dq) {
+        for (i = 0; i < npt; i++) dq[i] += -2.0 * c->ewaldcof * sqrt(1.0 / PI_D) * c->epstmp * in->ptchg[i];
+        if (in->do_pme) {
+            double eer;
+            dpot = (double *)calloc(3 * (size_t)npt, sizeof(double));
+            pme_core(in, c->ewaldcof, dpot, &eer, 0, dq);
+            free(dpot);
+        }
+    }
+    /* exclusion corrections (cdie_ewald.f:117-199) */
+    for (i = 1; i <= npt - 1; i++)
+        for (k = in->exc1[i - 1] + 1; k <= in->exc1[i]; k++) {
+            int j = in->exc2[k - 1];
+            double rx = X(i) - X(j), ry = Y(i) - Y(j), rz = Z(i) - Z(j);
+            double rij = sqrt(rx * rx + ry * ry + rz * rz), f;
+            if (!dq) continue;
+            f = -c->epstmp * erf(c->ewaldcof * rij) / rij;
+            dq[i - 1] += f * in->ptchg[j - 1];
+            dq[j - 1] += f * in->ptchg[i - 1];
+        }
+    /* 1-4 (ener14.f:38-95): p14(3) = q_j q_k kofdie el14 / eps */
+    for (k = 0; k < in->totspe; k++) {
+        int j = in->spec1[k], l = in->spec2[k];
+        const double *p = in->p14 + 3 * k;
+        double rx = X(j) - X(l), ry = Y(j) - Y(l), rz = Z(j) - Z(l);
+        double r2 = rx * rx + ry * ry + rz * rz, s2 = 1.0 / r2, s6 = s2 * s2 * s2, s = sqrt(s2);
+        if (p[0] > 1e-12) lj_adjoint(in, j - 1, l - 1, p[0] * s6 * s6, p[1] * s6, eps, sig, de, ds);
+        if (dq && fabs(p[2]) > 1e-12) {
+            if (fabs(in->ptchg[j - 1]) > 1e-12) dq[j - 1] += p[2] / in->ptchg[j - 1] * s;
+            if (fabs(in->ptchg[l - 1]) > 1e-12) dq[l - 1] += p[2] / in->ptchg[l - 1] * s;
+        }
+    }
+    /* real space: all pairs, minimum image */
+    for (i = 1; i <= npt; i++) {
+        int j;
+        for (j = i + 1; j <= npt; j++) {
+            double rv[3], sh[3], r2 = 0, rr2, s2, s6;
+            int ww = 0;
+            if (oxy[i] && oxy[j] && mol[i] != mol[j]) {
+                ww = 1;
+                for (k = 0; k < 3; k++) {
+                    double a = c->coor[3 * (oxy[i] - 1) + k] - c->coor[3 * (oxy[j] - 1) + k];
+                    sh[k] = box[k] * round(a / box[k]);
+                    r2 += (a - sh[k]) * (a - sh[k]);
+                }
+                if (r2 > rcut_el2) continue;
+            } else {
+                if (excluded(in, i, j)) continue;
+                if (oxy[i] && oxy[j]) continue;   /* same water */
+                for (k = 0; k < 3; k++) {
+                    double a = c->coor[3 * (i - 1) + k] - c->coor[3 * (j - 1) + k];
+                    sh[k] = box[k] * round(a / box[k]);
+                    r2 += (a - sh[k]) * (a - sh[k]);
+                }
+                if (r2 >= rcut_el2 && !(r2 < c->cutvdw2)) continue;
+            }
+            for (k = 0; k < 3; k++) rv[k] = c->coor[3 * (i - 1) + k] - c->coor[3 * (j - 1) + k] - sh[k];
+            rr2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+            s2 = 1.0 / rr2;
+            s6 = s2 * s2 * s2;
+            if (ww) {
+                int a = i - oxy[i], b = j - oxy[j];
+                double rij = sqrt(rr2), f = c->epstmp * erfc(c->ewaldcof * rij) / rij;
+                if (a == 0 && b == 0 && rr2 <= c->cutvdw2) lj_adjoint(in, i - 1, j - 1, o12 * s6 * s6, o6 * s6, eps, sig, de, ds);
+                if (dq) { dq[i - 1] += f * in->ptchg[j - 1]; dq[j - 1] += f * in->ptchg[i - 1]; }
+            } else {
+                int hr = (!in->arith) && in->hvdw0 && rr2 < c->cutele2 &&
+                         (in->epsgm12[i - 1] < 1e-3 || in->epsgm12[j - 1] < 1e-3);
+                int both = c->flagchr[i - 1] && c->flagchr[j - 1];
+                if (rr2 < c->cutvdw2 && !hr) {
+                    double a, b;
+                    lj_ab(c, i, j, s2, &a, &b);
+                    lj_adjoint(in, i - 1, j - 1, a, b, eps, sig, de, ds);
+                }
+                if (both && rr2 < rcut_el2 && dq) {
+                    double rij = sqrt(rr2), f = c->epstmp * erfc(c->ewaldcof * rij) / rij;
+                    dq[i - 1] += f * in->ptchg[j - 1];
+                    dq[j - 1] += f * in->ptchg[i - 1];
+                }
+            }
+        }
+    }
+    free(eps); free(sig); free(mol); free(oxy);
     ctx_free(c);
     return 0;
 }

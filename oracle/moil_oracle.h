@@ -79,6 +79,10 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out);
 /* nevals evaluations with lists rebuilt every list_period (MOIL's '#lis'). */
 int ora_eforce_repeat(const ora_input *in, double *dpot, ora_output *out, int nevals, int list_period);
 
+/* Parameter derivatives at the given coordinates (arrays of npt, any may be NULL): dE/dq,
+ * dE/deps and dE/dsigma per atom, LJ parameters decoded from the epsgm encoding. */
+int ora_adjoint_mi(const ora_input *in, double *dEdq, double *dEdeps, double *dEdsig);
+
 /* Batch of independent systems, OpenMP over systems (CPU baseline); mi selects the
  * minimum-image evaluator, otherwise nevals/list_period as ora_eforce_repeat. */
 int ora_eforce_batch(int nsys, const ora_input *in, double **dpot, ora_output *out, int mi, int nthreads,

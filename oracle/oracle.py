@@ -91,6 +91,7 @@ def lib():
         L.ora_bsp_moduli.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
         L.ora_fft.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int]
         L.ora_pme.argtypes = [ctypes.POINTER(OraInput), ctypes.c_double, _dp, _dp, _dp]
+        L.ora_adjoint_mi.argtypes = [ctypes.POINTER(OraInput), _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -185,6 +186,17 @@ def eforce(s, mode: str = "parity", **kw):
     if rc != 0:
         raise RuntimeError(f"oracle failed ({rc})")
     return dpot, output_dict(out)
+
+
+def adjoint(s, mode: str = "parity", **kw):
+    """Parameter derivatives of the energy (moil_oracle.c ora_adjoint_mi): per atom dE/dq,
+    dE/deps and dE/dsigma, the LJ parameters decoded from the epsgm encoding."""
+    keep = _Keep()
+    inp = make_input(s, mode=mode, keep=keep, **kw)
+    dq, de, ds = (np.zeros(s.npt, dtype=np.float64) for _ in range(3))
+    if lib().ora_adjoint_mi(ctypes.byref(inp), _p(dq), _p(de), _p(ds)) != 0:
+        raise RuntimeError("oracle adjoint failed")
+    return dq, de, ds
 
 
 def eforce_batch(systems, mode: str = "parity", nthreads: int = 0, nevals: int = 1, list_period: int = 1, **kw):
