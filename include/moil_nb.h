@@ -154,6 +154,15 @@ int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies
  * (device pointers, same layout); energies still go to host memory. */
 int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *energies);
 
+/* Parameter derivatives of the nonbonded energy at coor (host, all replicas, caller order),
+ * one FP64 value per atom: dE/dq (the electrostatic potential, kcal/mol/e), dE/deps and
+ * dE/dsigma of the atom's LJ parameters decoded from the epsgm encoding
+ * (connect/fillpt.f:136-184).  Any output may be NULL; energies as moil_nb_eval.  No
+ * counterpart in the reference, which computes no parameter derivatives; mixed precision
+ * handles only (MOIL_NB_ERR_ARG otherwise).  The LJ switch extension is not differentiated. */
+int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dEdeps, double *dEdsig,
+                    moil_energies *energies);
+
 /* Force a list rebuild at the next evaluation (MOIL: nbondm() + syminit()). */
 int moil_nb_request_rebuild(moil_nb_ctx *h);
 

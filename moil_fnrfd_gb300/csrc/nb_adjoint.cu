@@ -1,0 +1,312 @@
+// nb_adjoint.cu -- parameter derivatives of the nonbonded energy: dE/dq, dE/deps and
+// dE/dsigma per atom (moil_nb_adjoint).  MOIL computes none of them; the oracle's
+// ora_adjoint_mi is the reference, itself checked against finite differences.
+//
+// One evaluation (moil_nb_eval semantics) leaves the lists, the site-ordered positions and,
+// on the mixed path, the convolved PME potential grid on the device; these kernels then
+// accumulate, in FP64:
+//   dE/dq_i     = sum over i's real-space partners of k q_j erfc(alpha r)/r
+//               - sum over i's excluded partners of k q_j erf(alpha r)/r
+//               + 1-4 Coulomb p14(3)/(q_i r) + fc * sum(theta * potential grid)
+//               - 2 alpha/sqrt(pi) k q_i                      (k = kofdie/eps, fc = sqrt(k))
+//   dE/deps_i   = sum over i's LJ pairs of (A - B) / (2 eps_i)     (A ~ r^-12, B ~ r^-6 parts)
+//   dE/dsigma_i = sum over i's LJ pairs of (6A - 3B) / sigma_i   (geometric: sigma_ij^6 =
+//                 sigma_i^3 sigma_j^3), or / sigma_ij with sigma_ij = (sigma_i + sigma_j)/2
+//                 (arithmetic)
+// with eps and sigma decoded from MOIL's epsgm encoding (connect/fillpt.f:136-184).  The
+// pair predicates are the energy kernels' (MOIL's, pot/watwat_ewald.f, pot/cdie_ewald.f);
+// water-water Coulomb uses each site's own charge (MOIL's water kernel the last water's,
+// the same for identical waters).  The LJ switch extension is not differentiated.
+#include "nb_internal.h"
+
+namespace {
+
+// geometric: epsgm12 = 2 sqrt(eps) sigma^6, epsgm6 = 2 sqrt(eps) sigma^3;
+// arithmetic: epsgm12 = 2 sqrt(eps), epsgm6 = sigma
+__device__ __forceinline__ void lj_decode(int arith, double e12, double e6, double &eps, double &sig)
+{
+    if (arith) {
+        eps = 0.25 * e12 * e12;
+        sig = e6;
+    } else if (e12 > 0.0 && e6 > 0.0) {
+        const double se = e6 * e6 / (2.0 * e12);
+        sig = cbrt(e12 / e6);
+        eps = se * se;
+    } else {
+        eps = 0.0;
+        sig = 0.0;
+    }
+}
+
+// the pair's LJ energy parts a (r^-12) and b (r^-6) into atom i's derivatives
+__device__ __forceinline__ void lj_adj(int arith, double a, double b, double eps_i, double sig_i, double sig_j,
+                                       double &de, double &ds)
+{
+    const double e = a - b, g = 6.0 * a - 3.0 * b;
+    if (eps_i > 0.0) de += e / (2.0 * eps_i);
+    if (!arith) {
+        if (sig_i > 0.0) ds += g / sig_i;
+    } else {
+        const double sij = 0.5 * (sig_i + sig_j);
+        if (sij > 0.0) ds += g / sij;
+    }
+}
+
+// LJ parts of a non-water pair (cdie_ewald.f:377-383 geometric, :432-472 arithmetic)
+__device__ __forceinline__ void lj_parts(int arith, double e12i, double e6i, double e12j, double e6j, double s2,
+                                         double &a, double &b)
+{
+    const double s6 = s2 * s2 * s2;
+    if (!arith) {
+        a = e12i * e12j * s6 * s6;
+        b = e6i * e6j * s6;
+    } else {
+        const double aa = e12i * e12j, sg = 0.5 * (e6i + e6j);
+        double b1 = sg * sg * sg;
+        b1 = b1 * b1;
+        b = aa * b1 * s6;
+        a = aa * b1 * b1 * s6 * s6;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ double2 lj_of(const void *lj_v, int s)
+{
+    typedef typename cplx<T>::type T2;
+    const T2 v = ((const T2 *)lj_v)[s];
+    return make_double2((double)v.x, (double)v.y);
+}
+
+// one non-water-semantics site pair (atom_pair of the energy kernels) into site i's sums
+template <typename T>
+__device__ __forceinline__ void atom_pair_adj(const RepDev &R, double r2, double qi, double qj, double2 lji,
+                                              double2 ljj, unsigned fi, unsigned fj, double &phi, double &de,
+                                              double &ds)
+{
+    const bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < (double)R.re2;
+    const bool lj = r2 < (double)R.rv2 && !hr;
+    const bool el = r2 < (double)R.rmax2 && qi * qj != 0.0;
+    if (el) {
+        const double r = sqrt(r2);
+        phi += R.epstmp * qj * erfc(R.alphad * r) / r;
+    }
+    if (lj) {
+        double a, b, ei, si, ej, sj;
+        lj_parts(R.arith, lji.x, lji.y, ljj.x, ljj.y, 1.0 / r2, a, b);
+        lj_decode(R.arith, lji.x, lji.y, ei, si);
+        lj_decode(R.arith, ljj.x, ljj.y, ej, sj);
+        lj_adj(R.arith, a, b, ei, si, sj, de, ds);
+    }
+}
+
+// water molecule per thread: W1 (nine site pairs per molecule pair) and W2
+template <typename T>
+__global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                            const int *__restrict__ site_orig, const void *pos_v, const void *woff_v,
+                            const void *lj_v, const unsigned *__restrict__ sflags, const int2 *__restrict__ wl1_cnt,
+                            const int *__restrict__ wl1, int cap_row, const int *__restrict__ wl2_off,
+                            const int *__restrict__ wl2, double *__restrict__ dq, double *__restrict__ de,
+                            double *__restrict__ ds)
+{
+    typedef typename vec4<T>::type T4;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nW) return;
+    const T4 *pos = (const T4 *)pos_v;
+    const T4 *woff = (const T4 *)woff_v;
+    const RepDev &R = reps[site_rep[3 * i]];
+    const T4 oi = pos[3 * i];
+    const T4 h1 = woff[2 * i], h2 = woff[2 * i + 1];
+    const T hi[3][3] = {{(T)0, (T)0, (T)0}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
+    double phi[3] = {0, 0, 0}, dE[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
+    double epsO, sigO;
+    const double2 ljO = lj_of<T>(lj_v, 3 * i);
+    lj_decode(R.arith, ljO.x, ljO.y, epsO, sigO);
+    const int2 c = wl1_cnt[i];
+    const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
+    const int *row = wl1 + (size_t)i * cap_row;
+    for (int v = 0; v < n; ++v) {
+        const int j = row[v < nn ? v : cap_row - 1 - (v - nn)];
+        const T4 oj = pos[3 * j];
+        T dx = oi.x - oj.x, dy = oi.y - oj.y, dz = oi.z - oj.z;
+        const T nx = nb_rint(dx * rep_invL<T>(R, 0)), ny = nb_rint(dy * rep_invL<T>(R, 1)),
+                nz = nb_rint(dz * rep_invL<T>(R, 2));
+        dx = nb_shift(R, 0, dx, nx);
+        dy = nb_shift(R, 1, dy, ny);
+        dz = nb_shift(R, 2, dz, nz);
+        const T r2oo = dx * dx + dy * dy + dz * dz;
+        if (r2oo > (T)R.rmax2) continue;
+        const T4 j1 = woff[2 * j], j2 = woff[2 * j + 1];
+        const T hj[3][3] = {{(T)0, (T)0, (T)0}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
+        const double qj[3] = {(double)oj.w, (double)pos[3 * j + 1].w, (double)pos[3 * j + 2].w};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const double ex = (double)(hi[a][0] + dx - hj[b][0]), ey = (double)(hi[a][1] + dy - hj[b][1]),
+                             ez = (double)(hi[a][2] + dz - hj[b][2]);
+                const double r = sqrt(ex * ex + ey * ey + ez * ez);
+                phi[a] += R.epstmp * qj[b] * erfc(R.alphad * r) / r;
+            }
+        if (r2oo <= (T)R.rv2) {
+            const double s2 = 1.0 / (double)r2oo, s6 = s2 * s2 * s2;
+            double ej, sj;
+            const double2 ljj = lj_of<T>(lj_v, 3 * j);
+            lj_decode(R.arith, ljj.x, ljj.y, ej, sj);
+            lj_adj(R.arith, R.w12d * s6 * s6, R.w6d * s6, epsO, sigO, sj, dE[0], dS[0]);
+        }
+    }
+    for (int k = wl2_off[i]; k < wl2_off[i + 1]; ++k) {
+        const int s = wl2[k];
+        const T4 xj = pos[s];
+        const double2 ljj = lj_of<T>(lj_v, s);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const T4 xi = pos[3 * i + a];
+            T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            dx = nb_shift(R, 0, dx, nb_rint(dx * rep_invL<T>(R, 0)));
+            dy = nb_shift(R, 1, dy, nb_rint(dy * rep_invL<T>(R, 1)));
+            dz = nb_shift(R, 2, dz, nb_rint(dz * rep_invL<T>(R, 2)));
+            atom_pair_adj<T>(R, (double)(dx * dx + dy * dy + dz * dz), (double)xi.w, (double)xj.w,
+                             lj_of<T>(lj_v, 3 * i + a), ljj, sflags[3 * i + a], sflags[s], phi[a], dE[a], dS[a]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int o = site_orig[3 * i + a];
+        dq[o] = phi[a];
+        de[o] = dE[a];
+        ds[o] = dS[a];
+    }
+}
+
+// non-water atom per thread over its X list
+template <typename T>
+__global__ void k_adj_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                           const int *__restrict__ site_orig, const void *pos_v, const void *lj_v,
+                           const unsigned *__restrict__ sflags, const int *__restrict__ xl_off,
+                           const int *__restrict__ xl, double *__restrict__ dq, double *__restrict__ de,
+                           double *__restrict__ ds)
+{
+    typedef typename vec4<T>::type T4;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nA) return;
+    const T4 *pos = (const T4 *)pos_v;
+    const int si = 3 * nW + k;
+    const RepDev &R = reps[site_rep[si]];
+    const T4 xi = pos[si];
+    const double2 lji = lj_of<T>(lj_v, si);
+    double phi = 0, dE = 0, dS = 0;
+    for (int q = xl_off[k]; q < xl_off[k + 1]; ++q) {
+        const int s = xl[q];
+        const T4 xj = pos[s];
+        T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        dx = nb_shift(R, 0, dx, nb_rint(dx * rep_invL<T>(R, 0)));
+        dy = nb_shift(R, 1, dy, nb_rint(dy * rep_invL<T>(R, 1)));
+        dz = nb_shift(R, 2, dz, nb_rint(dz * rep_invL<T>(R, 2)));
+        atom_pair_adj<T>(R, (double)(dx * dx + dy * dy + dz * dz), (double)xi.w, (double)xj.w, lji,
+                         lj_of<T>(lj_v, s), sflags[si], sflags[s], phi, dE, dS);
+    }
+    const int o = site_orig[si];
+    dq[o] = phi;
+    de[o] = dE;
+    ds[o] = dS;
+}
+
+// per caller atom: exclusion erf corrections, 1-4 terms, self energy (FP64 coordinates)
+__global__ void k_adj_excl14(int natom, const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
+                             const double *__restrict__ coor, const double *__restrict__ q,
+                             const double2 *__restrict__ lj, const int *__restrict__ ex_off,
+                             const int *__restrict__ ex_j, const int *__restrict__ p_off, const int *__restrict__ p_j,
+                             const double *__restrict__ p_par, double *__restrict__ dq, double *__restrict__ de,
+                             double *__restrict__ ds)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natom) return;
+    const RepDev &R = reps[atom_rep[a]];
+    const double xa = coor[3 * (size_t)a], ya = coor[3 * (size_t)a + 1], za = coor[3 * (size_t)a + 2];
+    double phi = -2.0 * R.alphad * (NB_TWO_OVER_SQRTPI * 0.5) * R.epstmp * q[a];   // self energy
+    double dE = 0, dS = 0, ea, sa;
+    lj_decode(R.arith, lj[a].x, lj[a].y, ea, sa);
+    for (int k = ex_off[a]; k < ex_off[a + 1]; ++k) {
+        const int b = ex_j[k];
+        const double rx = xa - coor[3 * (size_t)b], ry = ya - coor[3 * (size_t)b + 1], rz = za - coor[3 * (size_t)b + 2];
+        const double r = sqrt(rx * rx + ry * ry + rz * rz);
+        phi -= R.epstmp * q[b] * erf(R.alphad * r) / r;
+    }
+    for (int k = p_off[a]; k < p_off[a + 1]; ++k) {
+        const int b = p_j[k];
+        const double *p = p_par + 3 * (size_t)k;
+        const double rx = xa - coor[3 * (size_t)b], ry = ya - coor[3 * (size_t)b + 1], rz = za - coor[3 * (size_t)b + 2];
+        const double s2 = 1.0 / (rx * rx + ry * ry + rz * rz), s6 = s2 * s2 * s2;
+        if (p[0] > 1e-12) {
+            double eb, sb;
+            lj_decode(R.arith, lj[b].x, lj[b].y, eb, sb);
+            lj_adj(R.arith, p[0] * s6 * s6, p[1] * s6, ea, sa, sb, dE, dS);
+        }
+        if (fabs(p[2]) > 1e-12 && fabs(q[a]) > 1e-12) phi += p[2] / q[a] * sqrt(s2);
+    }
+    dq[a] += phi;
+    de[a] += dE;
+    ds[a] += dS;
+}
+
+// PME: fc * sum(theta * potential grid) at each site, from the real planes k_plane_inv_f
+// leaves in the grid storage (mixed path)
+__global__ void k_adj_pme_f(int nsite, const int *__restrict__ site_rep, const int *__restrict__ site_orig,
+                            const RepDev *__restrict__ reps, const float4 *__restrict__ fr,
+                            const float2 *__restrict__ grid, double *__restrict__ dq)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsite) return;
+    const RepDev &R = reps[site_rep[s]];
+    const float4 f = fr[s];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
+    const size_t zs = (size_t)R.n1h * n2 * 2;
+    const float *Q = (const float *)(grid + R.g0);
+    const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+    double th[3][4];
+    const double w[3] = {(double)f.x - i1, (double)f.y - i2, (double)f.z - i3};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double u = w[d], u2 = u * u, u3 = u2 * u, m = 1.0 - u;
+        th[d][0] = m * m * m / 6.0;
+        th[d][1] = (4.0 - 6.0 * u2 + 3.0 * u3) / 6.0;
+        th[d][2] = (1.0 + 3.0 * (u + u2 - u3)) / 6.0;
+        th[d][3] = u3 / 6.0;
+    }
+    auto wrap = [](int k, int n) { return k < 0 ? k + n : (k >= n ? k - n : k); };
+    double v = 0.0;
+    for (int t3 = 0; t3 < 4; ++t3) {
+        const float *P = Q + wrap(i3 - 3 + t3, n3) * zs;
+        for (int t2 = 0; t2 < 4; ++t2) {
+            const float *row = P + wrap(i2 - 3 + t2, n2) * n1;
+            double sx = 0.0;
+            for (int t1 = 0; t1 < 4; ++t1) sx += th[0][t1] * (double)row[wrap(i1 - 3 + t1, n1)];
+            v += sx * th[1][t2] * th[2][t3];
+        }
+    }
+    dq[site_orig[s]] += R.fcd * v;
+}
+
+}  // namespace
+
+int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds)
+{
+    cudaStream_t s = c->stream;
+    const int B = 128;
+    if (c->nW > 0)
+        k_adj_water<float><<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
+            (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_woff, c->d_site_lj,
+            c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, d_dq, d_de, d_ds);
+    if (c->nA > 0)
+        k_adj_atom<float><<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
+            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_site_lj,
+            c->d_site_flags, c->d_xl_off, c->d_xl, d_dq, d_de, d_ds);
+    k_adj_excl14<<<(int)((c->natom + B - 1) / B), B, 0, s>>>(
+        (int)c->natom, c->d_atom_rep, c->d_reps, c->d_coor, c->d_q, c->d_lj_d, c->d_ex_off, c->d_ex_j,
+        c->d_p14_off, c->d_p14_j, c->d_p14_par, d_dq, d_de, d_ds);
+    k_adj_pme_f<<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig, c->d_reps,
+                                                          (const float4 *)c->d_fr, (const float2 *)c->d_grid, d_dq);
+    NB_CUDA_OK(c, cudaGetLastError());
+    return MOIL_NB_OK;
+}

@@ -85,6 +85,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
+    free_ptr(c->d_adj);
     if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
     c->h_e_rep = nullptr;
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -733,6 +734,32 @@ int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies
     int rc = eval_impl(h, h->d_coor, h->d_dpot, e);
     if (rc != MOIL_NB_OK) return rc;
     NB_CUDA_OK(h, cudaMemcpyAsync(dpot, h->d_dpot, bytes, cudaMemcpyDeviceToHost, h->stream));
+    NB_CUDA_OK(h, cudaStreamSynchronize(h->stream));
+    return MOIL_NB_OK;
+}
+
+int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dEdeps, double *dEdsig,
+                    moil_energies *e)
+{
+    if (!h || !coor) return MOIL_NB_ERR_ARG;
+    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (h->precision == MOIL_NB_FP64) {
+        h->err = "parameter derivatives are computed on the mixed path only";
+        return MOIL_NB_ERR_ARG;
+    }
+    cudaSetDevice(h->device);
+    const size_t n = (size_t)h->natom;
+    NB_CUDA_OK(h, cudaMemcpyAsync(h->d_coor, coor, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+    int rc = eval_impl(h, h->d_coor, h->d_dpot, e);   // lists, positions and the potential grid
+    if (rc != MOIL_NB_OK) return rc;
+    if (!h->d_adj) NB_CUDA_OK(h, cudaMalloc(&h->d_adj, sizeof(double) * 3 * std::max<size_t>(n, 1)));
+    rc = nb_adjoint(h, h->d_adj, h->d_adj + n, h->d_adj + 2 * n);
+    if (rc != MOIL_NB_OK) return rc;
+    double *out[3] = {dEdq, dEdeps, dEdsig};
+    for (int k = 0; k < 3; ++k)
+        if (out[k])
+            NB_CUDA_OK(h, cudaMemcpyAsync(out[k], h->d_adj + k * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                          h->stream));
     NB_CUDA_OK(h, cudaStreamSynchronize(h->stream));
     return MOIL_NB_OK;
 }

@@ -128,6 +128,7 @@ struct NbCtx {
 
     // caller buffers used by host-pointer evaluations
     double *d_coor = nullptr, *d_dpot = nullptr;
+    double *d_adj = nullptr;           // parameter derivatives, 3 x natom (allocated on first use)
 
     // device status: [0] rebuild flag, [1] error bits, [2..4] W1 / W2 / X entry totals,
     // [6] longest W1 row; all reset at the start of every evaluation
@@ -164,6 +165,8 @@ void nb_launch_pme(NbCtx *c);
 int nb_pme_configure(NbCtx *c);
 // finalize (nb_realspace.cu)
 void nb_launch_finalize(NbCtx *c, double *d_dpot);
+// parameter derivatives after an evaluation of c->d_coor (nb_adjoint.cu), mixed path
+int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds);
 
 #define NB_CUDA_OK(c, call)                                                         \
     do {                                                                            \

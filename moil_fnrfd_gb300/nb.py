@@ -27,7 +27,7 @@ ENERGY_KEYS = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_el14", "e_vdw14", "e_corr
                "e_ew_receip", "e_total", "e_dir")
 
 EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_last_error", "moil_nb_init",
-            "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device",
+            "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device", "moil_nb_adjoint",
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
             "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_")
@@ -101,6 +101,7 @@ def load(build_if_missing: bool = True):
     L.moil_nb_get_alpha.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     L.moil_nb_eval.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(Energies)]
     L.moil_nb_eval_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Energies)]
+    L.moil_nb_adjoint.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.POINTER(Energies)]
     L.moil_nb_request_rebuild.argtypes = [ctypes.c_void_p]
     L.moil_nb_squeeze.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Topology), _dp]
     L.moil_nb_natoms.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
@@ -238,6 +239,21 @@ class Nonbonded:
         if not self.batch:
             return dpot, e[0]
         return [dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))], e
+
+    def adjoint(self, coor=None):
+        """Per-atom dE/dq, dE/deps, dE/dsigma (moil_nb_adjoint).  Single system: three
+        (natom,) arrays; batch: three lists of per-replica arrays."""
+        if coor is None:
+            coor = np.concatenate([s.coor for s in self.systems], axis=0)
+        elif self.batch and isinstance(coor, (list, tuple)):
+            coor = np.concatenate(coor, axis=0)
+        coor = np.ascontiguousarray(coor, dtype=np.float64).reshape(self.natom, 3)
+        out = [np.empty(self.natom, dtype=np.float64) for _ in range(3)]
+        _check(self.L, self.h, self.L.moil_nb_adjoint(self.h, coor.ctypes.data_as(_dp), *(o.ctypes.data_as(_dp)
+                                                                                              for o in out), self._e))
+        if not self.batch:
+            return tuple(out)
+        return tuple([o[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))] for o in out)
 
     def eforce_device(self, d_coor_ptr: int, d_dpot_ptr: int, want_energies: bool = True):
         """Evaluate on device-resident buffers (raw CUDA pointers)."""

@@ -415,22 +415,57 @@ def config1(seed: int = 2025, n_solute: int = 2489, n_ions: int = 7, n_waters: i
     return b.finish("solute_23556", box, rvmx=9.0, relx=9.0, alpha=0.35, nfft=(64, 64, 64), seed=seed)
 
 
-def perturbed_copies(base: MoilSystem, n_copies: int = 64, seed: int = 4000, rel: float = 0.01):
-    """Copies with seeded +-1% relative perturbations of eps, sigma and charge per LJ type.
+def lj_decode(s: MoilSystem):
+    """(eps, sigma) per atom from MOIL's epsgm encoding (connect/fillpt.f:136-184):
+    geometric epsgm12 = 2 sqrt(eps) sigma^6, epsgm6 = 2 sqrt(eps) sigma^3; arithmetic
+    epsgm12 = 2 sqrt(eps), epsgm6 = sigma.  Atoms without LJ decode to (0, 0)."""
+    e12, e6 = s.epsgm12, s.epsgm6
+    if s.arith:
+        return 0.25 * e12 * e12, e6.copy()
+    eps, sig = np.zeros(s.npt), np.zeros(s.npt)
+    ok = (e12 > 0) & (e6 > 0)
+    sig[ok] = np.cbrt(e12[ok] / e6[ok])
+    eps[ok] = (e6[ok] ** 2 / (2.0 * e12[ok])) ** 2
+    return eps, sig
 
-    Charges stay neutral: the charge perturbation is re-centred over the solute.
-    """
+
+def with_lj(s: MoilSystem, eps: np.ndarray, sig: np.ndarray) -> MoilSystem:
+    """A copy of s with every atom's LJ parameters set from (eps, sigma) and the 1-4
+    parameters re-derived (generic/wconn.f:286-325)."""
+    t = s.copy()
+    t.epsgm6, t.epsgm12 = lj_encode(eps, sig, s.arith)
+    if len(t.spec1):
+        spec = list(zip(t.spec1 - 1, t.spec2 - 1))
+        t.p14 = np_p14(spec, t.ptchg, t.epsgm6, t.epsgm12, t.arith, eps=t.eps, hvdw0=t.hvdw0)
+    return t
+
+
+def perturbed_copies(base: MoilSystem, n_copies: int = 64, seed: int = 4000, rel: float = 0.01):
+    """Copies with seeded relative perturbations in [-rel, rel]: eps and sigma per LJ type
+    (atoms sharing one (eps, sigma) pair, the water oxygen among them), charges per solute
+    atom.  The charge perturbation is re-centred over the solute so every copy stays
+    neutral; waters keep their charges (the water kernel assumes identical waters)."""
     rng = np.random.Generator(np.random.PCG64(seed))
+    eps, sig = lj_decode(base)
+    types, tid = np.unique(np.round(np.stack([eps, sig], axis=1), 12), axis=0, return_inverse=True)
+    tid = tid.reshape(-1)
+    solute = np.zeros(base.npt, dtype=bool)
+    first = 0
+    for m in range(base.totmon):
+        last = int(base.poipt[m])
+        if base.montype[m] == MON_OTHER:
+            solute[first:last] = True
+        first = last
     out = []
     for k in range(n_copies):
+        fe = 1.0 + rng.uniform(-rel, rel, size=len(types))
+        fs = 1.0 + rng.uniform(-rel, rel, size=len(types))
         s = base.copy()
-        f = 1.0 + rng.uniform(-rel, rel, size=3)
-        s.epsgm12 = s.epsgm12 * math.sqrt(f[0])
-        if s.arith:
-            s.epsgm6 = s.epsgm6 * f[1]
-        dq = s.ptchg * (f[2] - 1.0)
-        dq -= dq.mean()
-        s.ptchg = s.ptchg + dq
+        s.ptchg = base.ptchg.copy()
+        if solute.any():
+            dq = base.ptchg[solute] * rng.uniform(-rel, rel, size=int(solute.sum()))
+            s.ptchg[solute] += dq - dq.mean()
+        s = with_lj(s, eps * fe[tid], sig * fs[tid])
         s.name = f"{base.name}_pert{k}"
         out.append(s)
     return out

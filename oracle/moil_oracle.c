@@ -308,7 +308,7 @@ static void build_lists(const ctx *c, lists *L)
     double *cent = (double *)malloc(sizeof(double) * 3 * M);
     int *pointm = (int *)malloc(sizeof(int) * (M + 2));
     ivec nblistm = {0};
-    int i, j, k, l, m, nlist = 0, iwat = 0, nflag = 0;
+    int i, j, l, m, nlist = 0, iwat = 0, nflag = 0;
     int nwl1 = 0, nwl2 = 0;
     memset(L, 0, sizeof(*L));
 

@@ -28,27 +28,8 @@ def energy(s, terms):
     return sum(e[k] for k in terms)
 
 
-def decode(s):
-    e12, e6 = s.epsgm12, s.epsgm6
-    if s.arith:
-        return 0.25 * e12 * e12, e6.copy()
-    eps, sig = np.zeros(s.npt), np.zeros(s.npt)
-    ok = (e12 > 0) & (e6 > 0)
-    sig[ok] = np.cbrt(e12[ok] / e6[ok])
-    eps[ok] = (e6[ok] ** 2 / (2.0 * e12[ok])) ** 2
-    return eps, sig
-
-
-def encode(s, eps, sig):
-    """A copy of s with the LJ parameters of every atom set from (eps, sigma)."""
-    t = s.copy()
-    if s.arith:
-        t.epsgm12 = 2.0 * np.sqrt(eps)
-        t.epsgm6 = sig.copy()
-    else:
-        t.epsgm12 = 2.0 * np.sqrt(eps) * sig ** 6
-        t.epsgm6 = 2.0 * np.sqrt(eps) * sig ** 3
-    return rewrite_p14(t)
+decode = S.lj_decode
+encode = S.with_lj
 
 
 def rewrite_p14(t):
@@ -154,3 +135,83 @@ def test_lj_scaling_identities(solute):
     dn = encode(s, eps, sig / l)
     want = (energy(up, LJ) - energy(dn, LJ)) / (np.log(l) * 2.0)
     assert np.dot(sig, ds) == pytest.approx(want, rel=1e-4)
+
+
+# ---- GPU adjoint (moil_nb_adjoint) against the oracle's ---------------------------------
+# The mixed path evaluates pair terms in FP32 with fixed-point accumulation, so the per-atom
+# derivatives carry FP32 pair rounding; 1e-5 relative RMS is the force tolerance of the path.
+ADJ_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def neutral():
+    """The small solute with all seven counterions (the GPU library refuses charged systems,
+    as MOIL's Ewald setup does)."""
+    return S.config1(seed=7, n_solute=60, n_ions=7, n_waters=300, box=24.0)
+
+
+def _gpu_adjoint_close(got, want, tol=ADJ_TOL):
+    from conftest import rel_rms
+    for g, w, name in zip(got, want, ("dE/dq", "dE/deps", "dE/dsigma")):
+        assert np.all(np.isfinite(g)), name
+        assert rel_rms(g, w) < tol, (name, rel_rms(g, w))
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_water216(cfg0):
+    from moil_fnrfd_gb300.nb import Nonbonded
+    nb = Nonbonded(cfg0)
+    _gpu_adjoint_close(nb.adjoint(cfg0.coor), O.adjoint(cfg0))
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_solute(neutral):
+    from moil_fnrfd_gb300.nb import Nonbonded
+    nb = Nonbonded(neutral)
+    got = nb.adjoint(neutral.coor)
+    _gpu_adjoint_close(got, O.adjoint(neutral))
+    again = nb.adjoint(neutral.coor)
+    for g, a in zip(got, again):
+        assert np.array_equal(g, a)            # deterministic run to run
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_batch_matches_single(cfg0, neutral):
+    from moil_fnrfd_gb300.nb import Nonbonded
+    nb = Nonbonded([cfg0, neutral])
+    got = nb.adjoint()
+    for k, s in enumerate((cfg0, neutral)):
+        _gpu_adjoint_close([g[k] for g in got], O.adjoint(s))
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_refused_on_fp64_handle(cfg0):
+    from moil_fnrfd_gb300.nb import MOIL_NB_FP64, MoilNbError, Nonbonded
+    nb = Nonbonded(cfg0, precision=MOIL_NB_FP64)
+    with pytest.raises(MoilNbError):
+        nb.adjoint(cfg0.coor)
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_perturbed_copies_batch(cfg1):
+    """The parameter-sensitivity workload: 64 seeded +-1% perturbed copies of the 23,556-atom
+    solute system (eps and sigma per LJ type, solute charges per atom) in one batch.  Two
+    copies against the oracle's adjoint; every copy against the homogeneity identities of
+    the same call's energies: E_elec is quadratic in the charges (sum q dE/dq = 2 E_elec)
+    and E_LJ is of degree one in the eps (sum eps dE/deps = E_LJ)."""
+    from conftest import energy_scale
+    from moil_fnrfd_gb300.nb import Nonbonded
+    copies = S.perturbed_copies(cfg1, 64)
+    nb = Nonbonded(copies)
+    dq, de, ds = nb.adjoint()
+    es = nb.energies()
+    for k in (0, 63):
+        _gpu_adjoint_close([dq[k], de[k], ds[k]], O.adjoint(copies[k]))
+    for k, s in enumerate(copies):
+        e = es[k]
+        scale = energy_scale(e)
+        eps, _ = S.lj_decode(s)
+        assert abs(np.dot(s.ptchg, dq[k]) - 2.0 * sum(e[t] for t in ELEC)) < 1e-5 * scale, k
+        assert abs(np.dot(eps, de[k]) - sum(e[t] for t in LJ)) < 1e-5 * scale, k
+        # per-type sums, the quantities a parameter fit consumes, are finite
+        assert np.all(np.isfinite(ds[k])), k
