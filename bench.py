@@ -15,6 +15,8 @@ roofline   : the dominant kernel against the FP32 pipe (pair math is FP32-bound)
 cpu_baseline: the oracle (a C restatement of MOIL's FP64 routines, MOIL's own list path
              and erfc table) on a bounded sample of replicas, one host thread
 plain_fp64 : the plain FP64 GPU path, one replica per launch, on a sample of replicas
+single_system_md: one 96,000-atom water box through a 1,000-step rigid-water trajectory
+             (lists every 10 steps, 1.5 Å skin), evaluations timed, with the FP64 path beside it
 """
 from __future__ import annotations
 
@@ -132,6 +134,56 @@ def cpu_baseline(reps, budget_s=12.0):
                       f"{dt:.1f} s"}
 
 
+def md_leg(local, steps=1000, warmup=20):
+    """One 96,000-atom water box (32,000 TIP3P, 98.6 Å, rc 10, alpha 0.32, grid 100^3) through
+    a rigid-water leapfrog trajectory: 2 fs steps from 300 K, pair lists rebuilt every 10
+    steps with a 1.5 Å skin.  Evaluations are timed with CUDA events on the library's stream
+    (the harness's own SETTLE/leapfrog operations between them are not)."""
+    import torch
+    from moil_fnrfd_gb300 import dyna, systems
+    from moil_fnrfd_gb300.nb import MOIL_NB_FP64, Nonbonded
+    s = systems.config2()
+    nb = Nonbonded(s, device=local, skin=1.5, list_period=10)
+    md = dyna.RigidWaterDynamics(nb, s, dt=0.002, temperature=300.0, seed=11)
+    md.step(warmup)
+    e0 = md.energies[0]["e_total"] + md.kinetic()
+    st = md.stream
+    ev = []
+    for _ in range(steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        md.evaluate()
+        b.record(st)
+        ev.append((a, b))
+        with torch.cuda.stream(st):
+            md.advance()
+    torch.cuda.synchronize()
+    eval_ms = [a.elapsed_time(b) for a, b in ev]
+    e1 = md.energies[0]["e_total"] + md.kinetic()
+    out = {"workload": "32,000 TIP3P waters (96,000 atoms), 98.6 Å box, rc 10 Å, alpha 0.32, PME 100^3, "
+                       "rigid-water leapfrog at 2 fs from 300 K, lists every 10 steps, 1.5 Å skin",
+           "steps": steps, "value": s.npt * steps / (sum(eval_ms) / 1e3), "unit": "atom-evals/s",
+           "ms_per_eval": statistics.mean(eval_ms), "ms_per_eval_max": max(eval_ms),
+           "energy_total_start_end": [e0, e1], "constraint_err_A": md.constraint_error()}
+    nb.close()
+    p = Nonbonded(s, precision=MOIL_NB_FP64, device=local)
+    dc = torch.from_numpy(s.coor).to(f"cuda:{local}")
+    dd = torch.empty_like(dc)
+    p.eforce_device(dc.data_ptr(), dd.data_ptr())
+    stp = torch.cuda.ExternalStream(p.stream())
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stp)
+    for _ in range(3):
+        p.eforce_device(dc.data_ptr(), dd.data_ptr())
+    b.record(stp)
+    torch.cuda.synchronize()
+    out["plain_fp64_ms_per_eval"] = a.elapsed_time(b) / 3
+    p.close()
+    return out
+
+
 def run_reference(args):
     """Reference arm: MOIL's algorithm (the oracle restatement; MOIL's Fortran cannot be
     built here) on all host cores, same workload, metric and units."""
@@ -173,6 +225,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 leg")
     ap.add_argument("--replicas", type=int, default=512, help="first R replicas only (profiling captures)")
+    ap.add_argument("--no-md", action="store_true", help="skip the single-system trajectory leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -338,6 +391,9 @@ def main():
         out["speedup_vs_plain_fp64"] = value / fp64_value
         out["force_err_vs_fp64"] = {"max_rel_rms": max(errs), "replicas": len(errs)}
     nb.close()
+
+    if not args.no_md and rank == 0:
+        out["single_system_md"] = md_leg(local)
 
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline(reps)
