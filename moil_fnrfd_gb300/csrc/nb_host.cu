@@ -473,6 +473,10 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_dpot, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMemset(c->d_grad_site, 0, sizeof(long long) * 3 * ns));
     NB_CUDA_OK(c, cudaMemset(c->d_e_unit, 0, sizeof(double) * NB_EU * std::max<int64_t>(nu, 1)));
+    // the mixed path never writes the water atoms' entries (their corrections are in the
+    // water kernel): they stay zero
+    NB_CUDA_OK(c, cudaMemset(c->d_grad_ex, 0, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMemset(c->d_e_ex, 0, sizeof(double) * 3 * c->natom));
     // list capacities from densities (grown on overflow)
     c->cap_wl2 = c->cap_xl = 64;
     double row1 = 32;

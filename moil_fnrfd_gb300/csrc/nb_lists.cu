@@ -127,52 +127,81 @@ __global__ void k_site_build(int nunit, int nW, const int *__restrict__ sorted, 
 }
 
 // 3. per-evaluation coordinate conversion into site order; displacement check.  One thread
-// per caller atom, so the caller's coordinates are read in order (they may live in host
-// memory the GPU addresses directly); the site-order outputs are scattered.
+// per sorted water (its three consecutive caller atoms, 72 contiguous bytes) or non-water
+// site, so every site-order array is read and written coalesced.
 template <typename T>
-__global__ void k_prepare(int nsite, int nW, const int *__restrict__ site_of, const unsigned *__restrict__ site_flags,
-                          const double *__restrict__ q, const double *__restrict__ coor, void *pos_v, void *woff_v,
+__device__ __forceinline__ void prepare_site(int s, const double *x, const unsigned *__restrict__ site_flags,
+                                             const T *__restrict__ site_q, void *pos_v, float4 *__restrict__ posb,
+                                             float half_skin2, int snapshot, bool &moved)
+{
+    typedef typename vec4<T>::type T4;
+    const unsigned f = site_flags[s];
+    T4 p;
+    p.x = (T)x[0]; p.y = (T)x[1]; p.z = (T)x[2];
+    p.w = (f & SF_CHARGED) ? site_q[s] : (T)0;
+    ((T4 *)pos_v)[s] = p;
+    const float4 pf = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
+    if (snapshot) {
+        posb[s] = pf;
+    } else {
+        // lists stay valid while no site moved more than skin/2 since the build
+        const float4 b = posb[s];
+        const float dx = pf.x - b.x, dy = pf.y - b.y, dz = pf.z - b.z;
+        moved |= dx * dx + dy * dy + dz * dz > half_skin2;
+    }
+}
+
+// coordinates of one caller atom; a non-finite or absurd one is reported and replaced by 0
+__device__ __forceinline__ void load_atom(const double *__restrict__ coor, int a, double *x, int *st)
+{
+    x[0] = coor[3 * (size_t)a]; x[1] = coor[3 * (size_t)a + 1]; x[2] = coor[3 * (size_t)a + 2];
+    if (!(x[0] == x[0] && x[1] == x[1] && x[2] == x[2]) || fabs(x[0]) > 1e7 || fabs(x[1]) > 1e7 ||
+        fabs(x[2]) > 1e7) {
+        atomicOr(&st[1], NB_DEV_ERR_NAN);
+        x[0] = x[1] = x[2] = 0.0;
+    }
+}
+
+template <typename T>
+__global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, const unsigned *__restrict__ site_flags,
+                          const void *site_q_v, const double *__restrict__ coor, void *pos_v, void *woff_v,
                           float4 *__restrict__ posb, float half_skin2, float rwat2, int snapshot, int *st)
 {
     // snapshot mode runs only on a rebuild; check mode only without one (the site order it
     // reads is the previous build's, which does not exist before the first build)
     if (snapshot ? rebuild_off(st) : !rebuild_off(st)) return;
     typedef typename vec4<T>::type T4;
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nsite; a += gridDim.x * blockDim.x) {
-        const int s = site_of[a];
-        double x = coor[3 * (size_t)a], y = coor[3 * (size_t)a + 1], z = coor[3 * (size_t)a + 2];
-        if (!(x == x && y == y && z == z) || fabs(x) > 1e7 || fabs(y) > 1e7 || fabs(z) > 1e7) {
-            atomicOr(&st[1], NB_DEV_ERR_NAN);
-            x = y = z = 0.0;
-        }
-        unsigned f = site_flags[s];
-        T qe = (f & SF_CHARGED) ? (T)q[a] : (T)0;
-        T4 p;
-        p.x = (T)x; p.y = (T)y; p.z = (T)z; p.w = qe;
-        ((T4 *)pos_v)[s] = p;
-        float4 pf = make_float4((float)x, (float)y, (float)z, 0.f);
-        if (snapshot) {
-            posb[s] = pf;
+    const T *site_q = (const T *)site_q_v;
+    bool moved = false;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nW + nA; u += gridDim.x * blockDim.x) {
+        if (u < nW) {
+            // a water's caller atoms are consecutive (O, H, H), as are its sites
+            const int a = site_orig[3 * u];
+            double x[3][3];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) load_atom(coor, a + m, x[m], st);
+#pragma unroll
+            for (int m = 0; m < 3; ++m)
+                prepare_site<T>(3 * u + m, x[m], site_flags, site_q, pos_v, posb, half_skin2, snapshot, moved);
+#pragma unroll
+            for (int m = 1; m < 3; ++m) {
+                // H offset from its O, formed in FP64 so the water kernel's site displacements
+                // inherit no extra rounding from absolute FP32 positions; water sites must stay
+                // within rwat of their oxygen (list radius assumption)
+                const double ox = x[m][0] - x[0][0], oy = x[m][1] - x[0][1], oz = x[m][2] - x[0][2];
+                if (ox * ox + oy * oy + oz * oz > rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
+                T4 off;
+                off.x = (T)ox; off.y = (T)oy; off.z = (T)oz; off.w = (T)0;
+                ((T4 *)woff_v)[2 * u + m - 1] = off;
+            }
         } else {
-            // lists stay valid while no site moved more than skin/2 since the build
-            float4 b = posb[s];
-            float dx = pf.x - b.x, dy = pf.y - b.y, dz = pf.z - b.z;
-            if (dx * dx + dy * dy + dz * dz > half_skin2) atomicOr(&st[0], 1);
-        }
-        if (s < 3 * nW && (s % 3) != 0) {
-            // water sites must stay within rwat of their oxygen (list radius assumption); a
-            // water's caller atoms are consecutive (O, H, H), as are its sites
-            const int o = a - (s % 3);
-            double ox = coor[3 * (size_t)o], oy = coor[3 * (size_t)o + 1], oz = coor[3 * (size_t)o + 2];
-            double d2 = (x - ox) * (x - ox) + (y - oy) * (y - oy) + (z - oz) * (z - oz);
-            if (d2 > rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
-            // H offset from its O, formed in FP64 so the water kernel's site displacements
-            // inherit no extra rounding from absolute FP32 positions
-            T4 off;
-            off.x = (T)(x - ox); off.y = (T)(y - oy); off.z = (T)(z - oz); off.w = (T)0;
-            ((T4 *)woff_v)[2 * (s / 3) + (s % 3) - 1] = off;
+            const int s = 3 * nW + (u - nW);
+            double x[3];
+            load_atom(coor, site_orig[s], x, st);
+            prepare_site<T>(s, x, site_flags, site_q, pos_v, posb, half_skin2, snapshot, moved);
         }
     }
+    if (moved) atomicOr(&st[0], 1);
 }
 
 // unique neighbour cells along one axis
@@ -595,9 +624,9 @@ void build_lists_t(NbCtx *c, const double *d_coor)
         (int)c->nunit, (int)c->nW, c->d_sorted_unit, c->d_unit_atom, c->d_atom_rep, c->d_aflags, c->d_lj_f,
         c->d_lj_d, c->d_q, c->d_site_orig, c->d_site_of, c->d_site_rep, c->d_site_flags, c->d_site_lj,
         c->d_site_q, c->d_status);
-    k_prepare<T><<<grid(c->nsite, B), B, 0, s>>>((int)c->nsite, (int)c->nW, c->d_site_of, c->d_site_flags, c->d_q,
-                                                 d_coor, c->d_pos, c->d_woff, c->d_posb, 0.f, c->rwat * c->rwat, 1,
-                                                 c->d_status);
+    k_prepare<T><<<grid(c->nW + c->nA, B), B, 0, s>>>((int)c->nW, (int)c->nA, c->d_site_orig, c->d_site_flags,
+                                                      c->d_site_q, d_coor, c->d_pos, c->d_woff, c->d_posb, 0.f,
+                                                      c->rwat * c->rwat, 1, c->d_status);
     c->launches += 5;
     if (c->nW > 0) {
         const int gw = grid(c->nW, 128), nt = (int)c->wtiles.size();
@@ -634,9 +663,10 @@ void prepare_t(NbCtx *c, const double *d_coor, int check)
 {
     const int B = 256;
     float hs = 0.5f * c->skin;
-    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((c->nsite + B - 1) / B, (int64_t)c->nsm * 8));
-    k_prepare<T><<<g, B, 0, c->stream>>>((int)c->nsite, (int)c->nW, c->d_site_of, c->d_site_flags, c->d_q, d_coor,
-                                         c->d_pos, c->d_woff, c->d_posb, check ? hs * hs : 3.0e38f,
+    const int64_t items = c->nW + c->nA;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((items + B - 1) / B, (int64_t)c->nsm * 8));
+    k_prepare<T><<<g, B, 0, c->stream>>>((int)c->nW, (int)c->nA, c->d_site_orig, c->d_site_flags, c->d_site_q,
+                                         d_coor, c->d_pos, c->d_woff, c->d_posb, check ? hs * hs : 3.0e38f,
                                          c->rwat * c->rwat, 0, c->d_status);
     c->launches += 1;
 }

@@ -293,6 +293,49 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
     eu[0] = sE[0][t]; eu[1] = sE[1][t]; eu[2] = sE[2][t]; eu[3] = sE[3][t]; eu[4] = (double)npair;
+    eu[5] = 0.0;
+}
+
+// FP32 water exclusion corrections (cdie_ewald.f:117-199 for the pairs O-H1, O-H2, H1-H2 of
+// one rigid water): the three intramolecular displacements come from the FP64-formed H
+// offsets h1, h2, so no absolute FP32 coordinate enters; erf(x)/x from its Taylor series in
+// u = x^2 (9 terms, truncation below 6e-9 for u <= 0.5), erff beyond.  Adds the gradient of
+// the three sites to g[3 * site + axis] and returns the energy.
+__device__ __forceinline__ float water_intra_f(const RepDev &R, float4 h1, float4 h2, const float q[3], float g[9])
+{
+    // displacement x_a - x_b for the pairs (O,H1), (O,H2), (H1,H2)
+    const float d[3][3] = {{-h1.x, -h1.y, -h1.z}, {-h2.x, -h2.y, -h2.z}, {h1.x - h2.x, h1.y - h2.y, h1.z - h2.z}};
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    const float al = R.alpha, ke = (float)R.epstmp, c2 = (float)NB_TWO_OVER_SQRTPI;
+    float ecorr = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float rx = d[k][0], ry = d[k][1], rz = d[k][2];
+        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz)), u = al * al * r2;
+        const float qq = q[pa[k]] * q[pb[k]] * ke;
+        float e, df;
+        if (u <= 0.5f) {
+            float s = 1.f / 685440.f, ds = 8.f / 685440.f;
+            s = fmaf(s, u, -1.f / 75600.f); s = fmaf(s, u, 1.f / 9360.f); s = fmaf(s, u, -1.f / 1320.f);
+            s = fmaf(s, u, 1.f / 216.f); s = fmaf(s, u, -1.f / 42.f); s = fmaf(s, u, 0.1f);
+            s = fmaf(s, u, -1.f / 3.f); s = fmaf(s, u, 1.f);
+            ds = fmaf(ds, u, -7.f / 75600.f); ds = fmaf(ds, u, 6.f / 9360.f); ds = fmaf(ds, u, -5.f / 1320.f);
+            ds = fmaf(ds, u, 4.f / 216.f); ds = fmaf(ds, u, -3.f / 42.f); ds = fmaf(ds, u, 0.2f);
+            ds = fmaf(ds, u, -1.f / 3.f);
+            e = -qq * al * c2 * s;
+            df = -qq * 2.f * al * al * al * c2 * ds;
+        } else {
+            const float rij = sqrtf(r2), sinv = 1.f / rij, x = al * rij;
+            const float erfv = erff(x), derfc = c2 * expf(-x * x);
+            e = -qq * sinv * erfv;
+            df = qq * sinv * (sinv * sinv * erfv - sinv * al * derfc);
+        }
+        ecorr += e;
+        const int a = pa[k], b = pb[k];
+        g[3 * a] += df * rx; g[3 * a + 1] += df * ry; g[3 * a + 2] += df * rz;
+        g[3 * b] -= df * rx; g[3 * b + 1] -= df * ry; g[3 * b + 2] -= df * rz;
+    }
+    return ecorr;
 }
 
 // ---------------------------------------------------------------------------------
@@ -312,7 +355,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                                                        const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
                                                        int cap_row, const int *__restrict__ wl2_off,
                                                        const int *__restrict__ wl2, long long *__restrict__ grad,
-                                                       double *__restrict__ e_unit)
+                                                       double *__restrict__ e_unit, int intra)
 {
     __shared__ long long sG[9][WBLOCK];
     __shared__ double sE[4][WBLOCK];
@@ -335,6 +378,12 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
 #pragma unroll
     for (int k = 0; k < 9; ++k) g[k] = 0.f;
     float e4[4] = {0.f, 0.f, 0.f, 0.f};   // LJ prim, LJ img, Coulomb prim, Coulomb img
+    // the molecule's own exclusion corrections (every water excludes exactly its three pairs)
+    float ecorr = 0.f;
+    if (intra) {
+        const float qs[3] = {oi0.w, pos[3 * i + 1].w, pos[3 * i + 2].w};
+        ecorr = water_intra_f(R, oi1, oi2, qs, g);
+    }
     auto flush_all = [&]() {
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
@@ -464,6 +513,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
     eu[0] = sE[0][t]; eu[1] = sE[1][t]; eu[2] = sE[2][t]; eu[3] = sE[3][t]; eu[4] = (double)npair;
+    eu[5] = (double)ecorr;
 }
 
 // non-water atom per thread over its full site list
@@ -510,7 +560,7 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     grad[(size_t)3 * si + 1] = G[1];
     grad[(size_t)3 * si + 2] = G[2];
     double *eu = e_unit + NB_EU * (size_t)(nW + k);
-    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei; eu[4] = (double)npair;
+    eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei; eu[4] = (double)npair; eu[5] = 0.0;
 }
 
 // ---------------------------------------------------------------------------------
@@ -585,64 +635,6 @@ __global__ void k_excl_water(int nW, const int *__restrict__ unit_atom, const in
     }
 }
 
-// FP32 path of the water exclusion corrections, one sorted water per thread: the three
-// intramolecular displacements come from the FP64-formed H offsets (O-H1, O-H2, H2-H1), so
-// no absolute FP32 coordinate enters; erf(x)/x from its Taylor series in u = x^2 (9 terms,
-// truncation below 6e-9 for u <= 0.5), erff beyond.  Results go to the caller-order arrays,
-// gradients as 2^32 fixed point.
-__global__ void __launch_bounds__(128) k_excl_water_f(int nW, const int *__restrict__ site_orig,
-                                                      const int *__restrict__ site_rep,
-                                                      const RepDev *__restrict__ reps, const float4 *__restrict__ pos,
-                                                      const float4 *__restrict__ woff, long long *__restrict__ grad,
-                                                      double *__restrict__ e_out)
-{
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nW) return;
-    const RepDev &R = reps[site_rep[3 * p]];
-    const int a0 = site_orig[3 * p];
-    const float4 h1 = woff[2 * p], h2 = woff[2 * p + 1];
-    const float q[3] = {pos[3 * p].w, pos[3 * p + 1].w, pos[3 * p + 2].w};
-    // displacement x_a - x_b for the pairs (O,H1), (O,H2), (H1,H2)
-    const float d[3][3] = {{-h1.x, -h1.y, -h1.z}, {-h2.x, -h2.y, -h2.z}, {h1.x - h2.x, h1.y - h2.y, h1.z - h2.z}};
-    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
-    const float al = R.alpha, ke = (float)R.epstmp, c2 = (float)NB_TWO_OVER_SQRTPI;
-    float g[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}}, ecorr = 0.f;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float rx = d[k][0], ry = d[k][1], rz = d[k][2];
-        const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz)), u = al * al * r2;
-        const float qq = q[pa[k]] * q[pb[k]] * ke;
-        float e, df;
-        if (u <= 0.5f) {
-            float s = 1.f / 685440.f, ds = 8.f / 685440.f;
-            s = fmaf(s, u, -1.f / 75600.f); s = fmaf(s, u, 1.f / 9360.f); s = fmaf(s, u, -1.f / 1320.f);
-            s = fmaf(s, u, 1.f / 216.f); s = fmaf(s, u, -1.f / 42.f); s = fmaf(s, u, 0.1f);
-            s = fmaf(s, u, -1.f / 3.f); s = fmaf(s, u, 1.f);
-            ds = fmaf(ds, u, -7.f / 75600.f); ds = fmaf(ds, u, 6.f / 9360.f); ds = fmaf(ds, u, -5.f / 1320.f);
-            ds = fmaf(ds, u, 4.f / 216.f); ds = fmaf(ds, u, -3.f / 42.f); ds = fmaf(ds, u, 0.2f);
-            ds = fmaf(ds, u, -1.f / 3.f);
-            e = -qq * al * c2 * s;
-            df = -qq * 2.f * al * al * al * c2 * ds;
-        } else {
-            const float rij = sqrtf(r2), sinv = 1.f / rij, x = al * rij;
-            const float erfv = erff(x), derfc = c2 * expf(-x * x);
-            e = -qq * sinv * erfv;
-            df = qq * sinv * (sinv * sinv * erfv - sinv * al * derfc);
-        }
-        ecorr += e;
-        const int a = pa[k], b = pb[k];
-        g[a][0] += df * rx; g[a][1] += df * ry; g[a][2] += df * rz;
-        g[b][0] -= df * rx; g[b][1] -= df * ry; g[b][2] -= df * rz;
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        long long *gp = grad + 3 * (size_t)(a0 + k);
-        double *ep = e_out + 3 * (size_t)(a0 + k);
-        gp[0] = nb_fix(g[k][0]); gp[1] = nb_fix(g[k][1]); gp[2] = nb_fix(g[k][2]);
-        ep[0] = k == 0 ? (double)ecorr : 0.0; ep[1] = 0.0; ep[2] = 0.0;
-    }
-}
-
 // exclusion erf corrections (cdie_ewald.f:117-199) and 1-4 terms (ener14.f:38-95), FP64,
 // gathered per atom over both directions; raw (unimaged) displacements as MOIL uses.
 // With skip_water set, water atoms are left to k_excl_water.
@@ -690,7 +682,7 @@ __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepD
         evdw14 += 0.5 * e1;
         eel14 += 0.5 * e2;
     }
-    if (fixed_out) {   // mixed path: 2^32 fixed point, as k_excl_water_f
+    if (fixed_out) {   // mixed path: 2^32 fixed point, as the site gradients
         long long *gf = (long long *)grad + 3 * (size_t)a;
         gf[0] = __double2ll_rn(gx * NB_FIX_SCALE);
         gf[1] = __double2ll_rn(gy * NB_FIX_SCALE);
@@ -707,7 +699,7 @@ template <typename T>
 __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const int *__restrict__ atom_rep,
                              const RepDev *__restrict__ reps, const long long *__restrict__ grad_site,
                              const double *__restrict__ grad_ex, const T *__restrict__ part,
-                             const double *__restrict__ q, double *__restrict__ dpot, int *st)
+                             const double *__restrict__ q, int nsw, double *__restrict__ dpot, int *st)
 {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= natom) return;
@@ -718,14 +710,16 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
         // FP32 path: the PME share (one float4 per site from k_pme_gather_f) is scaled in
         // FP32 (its own precision) and joins the fixed-point real-space and correction terms
         // as an integer; the double result is assembled with integer operations (no FP64
-        // instruction)
+        // instruction).  Sites below nsw (waters whose corrections the water kernel added)
+        // have no correction term.
         const long long *gx = (const long long *)grad_ex + 3 * (size_t)a;
+        const bool ex = s >= nsw;
         const float qs = (float)q[a];
         const float4 p4 = ((const float4 *)part)[s];
         const float pg[3] = {p4.x, p4.y, p4.z};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const long long v = grad_site[3 * (size_t)s + d] + gx[d] + nb_f2fix(qs * R.pme_gs[d] * pg[d]);
+            const long long v = grad_site[3 * (size_t)s + d] + (ex ? gx[d] : 0LL) + nb_f2fix(qs * R.pme_gs[d] * pg[d]);
             bad |= (v > (1LL << 61)) | (v < -(1LL << 61));   // a saturated (non-finite) term
             dpot[3 * (size_t)a + d] = nb_fix2d(v);
         }
@@ -750,42 +744,69 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
     if (bad) atomicOr(&st[1], NB_DEV_ERR_NAN);
 }
 
-// per-replica energies: fixed-order block reductions (deterministic)
-__device__ double block_sum(double v, double *sh)
+// Per-replica energies, one block of NB_FE_THREADS (a multiple of 32, of NB_EU and of 3) per
+// replica: every thread streams the replica's flat per-unit and per-atom arrays with a stride
+// that keeps its slot fixed, so the reads are coalesced and each thread adds one slot; the
+// slots are then summed in a fixed order (deterministic).
+#define NB_FE_THREADS 384
+__global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const RepDev *__restrict__ reps,
+                                                                const double *__restrict__ e_unit,
+                                                                const double *__restrict__ e_ex,
+                                                                const double *__restrict__ e_col,
+                                                                const int *__restrict__ col_begin,
+                                                                double *__restrict__ e_rep)
 {
-    int t = threadIdx.x;
-    sh[t] = v;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (t < o) sh[t] += sh[t + o];
-        __syncthreads();
-    }
-    double r = sh[0];
-    __syncthreads();
-    return r;
-}
-
-__global__ void k_final_energy(int nW, const RepDev *__restrict__ reps, const double *__restrict__ e_unit,
-                               const double *__restrict__ e_ex, const double *__restrict__ e_col,
-                               const int *__restrict__ col_begin, double *__restrict__ e_rep)
-{
-    __shared__ double sh[256];
-    int r = blockIdx.x;
+    static_assert(NB_FE_THREADS % NB_EU == 0 && NB_FE_THREADS % 3 == 0, "slot-preserving stride");
+    __shared__ double sh[NB_FE_THREADS];
+    __shared__ double part[NB_EU + 3 + 1];
+    const int r = blockIdx.x, t = threadIdx.x;
     const RepDev &R = reps[r];
-    double acc[NB_EU] = {0, 0, 0, 0, 0}, ex[3] = {0, 0, 0}, ec = 0;
-    for (int u = R.wat0 + threadIdx.x; u < R.wat0 + R.nwat; u += blockDim.x)
-        for (int k = 0; k < NB_EU; ++k) acc[k] += e_unit[NB_EU * (size_t)u + k];
-    for (int u = nW + R.oth0 + threadIdx.x; u < nW + R.oth0 + R.noth; u += blockDim.x)
-        for (int k = 0; k < NB_EU; ++k) acc[k] += e_unit[NB_EU * (size_t)u + k];
-    for (int a = R.atom0 + threadIdx.x; a < R.atom0 + R.natom; a += blockDim.x)
-        for (int k = 0; k < 3; ++k) ex[k] += e_ex[3 * (size_t)a + k];
-    for (int w = col_begin[r] + threadIdx.x; w < col_begin[r + 1]; w += blockDim.x) ec += e_col[w];
-    double elp = 0.5 * block_sum(acc[0], sh), eli = 0.5 * block_sum(acc[1], sh);
-    double eep = 0.5 * block_sum(acc[2], sh), eei = 0.5 * block_sum(acc[3], sh);
-    double ecorr = block_sum(ex[0], sh), eel14 = block_sum(ex[1], sh), evdw14 = block_sum(ex[2], sh);
-    double erec = 0.5 * block_sum(ec, sh);
-    double npairs = 0.5 * block_sum(acc[4], sh);
-    if (threadIdx.x == 0) {
+    // units: the replica's waters, then its other units, NB_EU doubles each
+    double u = 0.0, x = 0.0, cl = 0.0;
+    {
+        const double *b = e_unit + NB_EU * (size_t)R.wat0;
+        const int n = NB_EU * R.nwat;
+        for (int k = t; k < n; k += NB_FE_THREADS) u += b[k];
+        b = e_unit + NB_EU * ((size_t)nW + R.oth0);
+        const int m = NB_EU * R.noth;
+        for (int k = t; k < m; k += NB_FE_THREADS) u += b[k];
+    }
+    {
+        const double *b = e_ex + 3 * (size_t)R.atom0;
+        const int n = 3 * R.natom;
+        for (int k = t; k < n; k += NB_FE_THREADS) x += b[k];
+    }
+    for (int w = col_begin[r] + t; w < col_begin[r + 1]; w += NB_FE_THREADS) cl += e_col[w];
+    // slot sums: unit slot t % NB_EU, correction slot t % 3, columns summed over all threads
+    sh[t] = u;
+    __syncthreads();
+    if (t < NB_EU) {
+        double v = 0.0;
+        for (int k = t; k < NB_FE_THREADS; k += NB_EU) v += sh[k];
+        part[t] = v;
+    }
+    __syncthreads();
+    sh[t] = x;
+    __syncthreads();
+    if (t < 3) {
+        double v = 0.0;
+        for (int k = t; k < NB_FE_THREADS; k += 3) v += sh[k];
+        part[NB_EU + t] = v;
+    }
+    __syncthreads();
+    sh[t] = cl;
+    __syncthreads();
+    if (t == 0) {
+        double v = 0.0;
+        for (int k = 0; k < NB_FE_THREADS; ++k) v += sh[k];
+        part[NB_EU + 3] = v;
+    }
+    __syncthreads();
+    if (t == 0) {
+        const double elp = 0.5 * part[0], eli = 0.5 * part[1], eep = 0.5 * part[2], eei = 0.5 * part[3];
+        const double npairs = 0.5 * part[4];
+        const double ecorr = part[NB_EU] + part[5], eel14 = part[NB_EU + 1], evdw14 = part[NB_EU + 2];
+        const double erec = 0.5 * part[NB_EU + 3];
         double *o = e_rep + 16 * (size_t)r;
         o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym
         o[4] = eel14; o[5] = evdw14; o[6] = ecorr; o[7] = R.e_self; o[8] = erec;
@@ -806,7 +827,7 @@ void realspace_t(NbCtx *c)
             k_water_f<<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos,
                                             (const float4 *)c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_cnt,
                                             c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, c->d_grad_site,
-                                            c->d_e_unit);
+                                            c->d_e_unit, c->water_excl_fast);
         else
             k_water<T><<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
                                              c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1,
@@ -834,14 +855,10 @@ void nb_launch_realspace(NbCtx *c)
 void nb_launch_excl14(NbCtx *c, const double *d_coor)
 {
     const int fast = c->water_excl_fast && c->nW > 0;
-    if (fast) {
-        if (c->precision == MOIL_NB_FP64)
-            k_excl_water<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
-                (int)c->nW, c->d_unit_atom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_grad_ex, c->d_e_ex);
-        else
-            k_excl_water_f<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
-                (int)c->nW, c->d_site_orig, c->d_site_rep, c->d_reps, (const float4 *)c->d_pos,
-                (const float4 *)c->d_woff, (long long *)c->d_grad_ex, c->d_e_ex);
+    // mixed path: the water kernel adds each water's own corrections (k_water_f)
+    if (fast && c->precision == MOIL_NB_FP64) {
+        k_excl_water<<<(int)((c->nW + 127) / 128), 128, 0, c->stream>>>(
+            (int)c->nW, c->d_unit_atom, c->d_atom_rep, c->d_reps, d_coor, c->d_q, c->d_grad_ex, c->d_e_ex);
         c->launches++;
     }
     if (!fast || c->nA > 0) {
@@ -858,12 +875,12 @@ void nb_launch_finalize(NbCtx *c, double *d_dpot)
     if (c->precision == MOIL_NB_FP64)
         k_final_grad<double><<<(int)((c->natom + 255) / 256), 256, 0, s>>>(
             (int)c->natom, c->d_site_of, c->d_atom_rep, c->d_reps, c->d_grad_site, c->d_grad_ex,
-            (const double *)c->d_part, c->d_q, d_dpot, c->d_status);
+            (const double *)c->d_part, c->d_q, 0, d_dpot, c->d_status);
     else
         k_final_grad<float><<<(int)((c->natom + 255) / 256), 256, 0, s>>>(
             (int)c->natom, c->d_site_of, c->d_atom_rep, c->d_reps, c->d_grad_site, c->d_grad_ex,
-            (const float *)c->d_part, c->d_q, d_dpot, c->d_status);
-    k_final_energy<<<c->nrep, 256, 0, s>>>((int)c->nW, c->d_reps, c->d_e_unit, c->d_e_ex, c->d_e_col, c->d_col_begin,
+            (const float *)c->d_part, c->d_q, c->water_excl_fast ? (int)(3 * c->nW) : 0, d_dpot, c->d_status);
+    k_final_energy<<<c->nrep, NB_FE_THREADS, 0, s>>>((int)c->nW, c->d_reps, c->d_e_unit, c->d_e_ex, c->d_e_col, c->d_col_begin,
                                            c->d_e_rep);
     c->launches += 2;
 }
