@@ -2,23 +2,24 @@
 real-space kernels (written to ``erfcx_coef.h``).
 
 Method: the substitution t = 1 / (1 + p x) of Hastings (1955), used in
-Abramowitz & Stegun 7.1.26, with p = 0.47047; erfcx(x) is written as
+Abramowitz & Stegun 7.1.26 (there with p = 0.47047; p = 0.55 here, the value
+that minimises the degree-7 error); erfcx(x) is written as
 t * P(u), u = a t + b the affine map of t in [1/(1 + p X), 1] onto [-1, 1],
-and P of degree 8 is a least-squares fit of the *relative* error in a
+and P of degree 7 is a least-squares fit of the *relative* error in a
 Chebyshev basis of u at 8000 Chebyshev nodes in x on [0, X], X = 4.5
 (alpha * r_cut is 3.15 for alpha 0.35 / 9 Å and 3.2 for 0.32 / 10 Å).  The
 Chebyshev series is converted to monomials in u for Horner evaluation.
 
 Reference values come from scipy.special.erfcx (double precision).  Measured
-FP32 error of the Horner evaluation over [0, 4.5]: max 3.7e-7, rms 9e-8
-relative.  Run:  python fit_erfcx.py > erfcx_coef.h
+FP32 error of the Horner evaluation over [0, 4.5]: max 3.5e-7, rms 8.6e-8
+relative (degree 8 with p = 0.47047: 3.7e-7, 9.0e-8; degree 6: 6.5e-7 at best).  Run:  python fit_erfcx.py > erfcx_coef.h
 """
 import numpy as np
 from scipy.special import erfcx
 
 X_MAX = 4.5
-P_SUB = 0.47047
-DEG = 8
+P_SUB = 0.55
+DEG = 7
 
 
 def fit():

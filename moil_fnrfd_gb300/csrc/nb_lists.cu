@@ -151,12 +151,17 @@ __device__ __forceinline__ void prepare_site(int s, const double *x, const unsig
     }
 }
 
-// coordinates of one caller atom; a non-finite or absurd one is reported and replaced by 0
+// coordinates of one caller atom; a non-finite or absurd one (|x| > 1e7, NaN, inf) is
+// reported and replaced by 0.  The test runs on the bit pattern: |x| > 1e7 exactly when the
+// magnitude bits exceed those of 1e7 (0x416312D000000000), NaN and inf included, and costs
+// no FP64 instruction (the FP64 pipe is a small fraction of the FP32 one)
 __device__ __forceinline__ void load_atom(const double *__restrict__ coor, int a, double *x, int *st)
 {
     x[0] = coor[3 * (size_t)a]; x[1] = coor[3 * (size_t)a + 1]; x[2] = coor[3 * (size_t)a + 2];
-    if (!(x[0] == x[0] && x[1] == x[1] && x[2] == x[2]) || fabs(x[0]) > 1e7 || fabs(x[1]) > 1e7 ||
-        fabs(x[2]) > 1e7) {
+    const unsigned long long m = 0x7fffffffffffffffULL, lim = 0x416312D000000000ULL;
+    if (((unsigned long long)__double_as_longlong(x[0]) & m) > lim ||
+        ((unsigned long long)__double_as_longlong(x[1]) & m) > lim ||
+        ((unsigned long long)__double_as_longlong(x[2]) & m) > lim) {
         atomicOr(&st[1], NB_DEV_ERR_NAN);
         x[0] = x[1] = x[2] = 0.0;
     }
@@ -188,10 +193,10 @@ __global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, con
                 // H offset from its O, formed in FP64 so the water kernel's site displacements
                 // inherit no extra rounding from absolute FP32 positions; water sites must stay
                 // within rwat of their oxygen (list radius assumption)
-                const double ox = x[m][0] - x[0][0], oy = x[m][1] - x[0][1], oz = x[m][2] - x[0][2];
-                if (ox * ox + oy * oy + oz * oz > rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
                 T4 off;
-                off.x = (T)ox; off.y = (T)oy; off.z = (T)oz; off.w = (T)0;
+                off.x = (T)(x[m][0] - x[0][0]); off.y = (T)(x[m][1] - x[0][1]); off.z = (T)(x[m][2] - x[0][2]);
+                off.w = (T)0;
+                if (off.x * off.x + off.y * off.y + off.z * off.z > (T)rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
                 ((T4 *)woff_v)[2 * u + m - 1] = off;
             }
         } else {

@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                                                        double *__restrict__ e_unit, int intra)
 {
     __shared__ long long sG[9][WBLOCK];
-    __shared__ double sE[4][WBLOCK];
+    __shared__ float2 sE[4][WBLOCK];     // energies as unevaluated sums hi + lo (no FP64 pipe)
     const int t = threadIdx.x;
     const int i = blockIdx.x * WBLOCK + t;
     if (i >= nW) return;
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
 #pragma unroll
     for (int k = 0; k < 9; ++k) sG[k][t] = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) sE[k][t] = 0.0;
+    for (int k = 0; k < 4; ++k) sE[k][t] = make_float2(0.f, 0.f);
     const float4 oi0 = pos[3 * i];
     const float4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
     // H offsets of molecule i, duplicated into both lanes
@@ -392,7 +392,13 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
             G[k] = f2(0.f);
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) { sE[k][t] += (double)e4[k]; e4[k] = 0.f; }
+        for (int k = 0; k < 4; ++k) {
+            // TwoSum (Knuth): hi + e4 = s + err exactly; the errors collect in lo
+            const float2 a = sE[k][t];
+            const float sm = a.x + e4[k], bb = sm - a.x, err = (a.x - (sm - bb)) + (e4[k] - bb);
+            sE[k][t] = make_float2(sm, a.y + err);
+            e4[k] = 0.f;
+        }
     };
     int npair = 0;
     const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
@@ -512,7 +518,9 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
 #pragma unroll
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
-    eu[0] = sE[0][t]; eu[1] = sE[1][t]; eu[2] = sE[2][t]; eu[3] = sE[3][t]; eu[4] = (double)npair;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) eu[k] = (double)sE[k][t].x + (double)sE[k][t].y;
+    eu[4] = (double)npair;
     eu[5] = (double)ecorr;
 }
 
@@ -754,28 +762,31 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
                                                                 const double *__restrict__ e_ex,
                                                                 const double *__restrict__ e_col,
                                                                 const int *__restrict__ col_begin,
-                                                                double *__restrict__ e_rep)
+                                                                int water_ex_zero, double *__restrict__ e_rep)
 {
     static_assert(NB_FE_THREADS % NB_EU == 0 && NB_FE_THREADS % 3 == 0, "slot-preserving stride");
     __shared__ double sh[NB_FE_THREADS];
     __shared__ double part[NB_EU + 3 + 1];
     const int r = blockIdx.x, t = threadIdx.x;
     const RepDev &R = reps[r];
-    // units: the replica's waters, then its other units, NB_EU doubles each
-    double u = 0.0, x = 0.0, cl = 0.0;
-    {
-        const double *b = e_unit + NB_EU * (size_t)R.wat0;
-        const int n = NB_EU * R.nwat;
-        for (int k = t; k < n; k += NB_FE_THREADS) u += b[k];
-        b = e_unit + NB_EU * ((size_t)nW + R.oth0);
-        const int m = NB_EU * R.noth;
-        for (int k = t; k < m; k += NB_FE_THREADS) u += b[k];
-    }
-    {
-        const double *b = e_ex + 3 * (size_t)R.atom0;
-        const int n = 3 * R.natom;
-        for (int k = t; k < n; k += NB_FE_THREADS) x += b[k];
-    }
+    // units: the replica's waters, then its other units, NB_EU doubles each; four loads in
+    // flight per thread (four partial sums, added in a fixed order)
+    auto stream_sum = [t](const double *__restrict__ b, int n) {
+        double p[4] = {0.0, 0.0, 0.0, 0.0};
+        int k = t;
+        for (; k + 3 * NB_FE_THREADS < n; k += 4 * NB_FE_THREADS) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) p[j] += b[k + j * NB_FE_THREADS];
+        }
+        if (k < n) p[0] += b[k];
+        if (k + NB_FE_THREADS < n) p[1] += b[k + NB_FE_THREADS];
+        if (k + 2 * NB_FE_THREADS < n) p[2] += b[k + 2 * NB_FE_THREADS];
+        return (p[0] + p[1]) + (p[2] + p[3]);
+    };
+    double u = stream_sum(e_unit + NB_EU * (size_t)R.wat0, NB_EU * R.nwat) +
+               stream_sum(e_unit + NB_EU * ((size_t)nW + R.oth0), NB_EU * R.noth);
+    // per-atom corrections: none in a replica of waters whose corrections the water kernel added
+    double x = (water_ex_zero && R.noth == 0) ? 0.0 : stream_sum(e_ex + 3 * (size_t)R.atom0, 3 * R.natom), cl = 0.0;
     for (int w = col_begin[r] + t; w < col_begin[r + 1]; w += NB_FE_THREADS) cl += e_col[w];
     // slot sums: unit slot t % NB_EU, correction slot t % 3, columns summed over all threads
     sh[t] = u;
@@ -880,7 +891,8 @@ void nb_launch_finalize(NbCtx *c, double *d_dpot)
         k_final_grad<float><<<(int)((c->natom + 255) / 256), 256, 0, s>>>(
             (int)c->natom, c->d_site_of, c->d_atom_rep, c->d_reps, c->d_grad_site, c->d_grad_ex,
             (const float *)c->d_part, c->d_q, c->water_excl_fast ? (int)(3 * c->nW) : 0, d_dpot, c->d_status);
-    k_final_energy<<<c->nrep, NB_FE_THREADS, 0, s>>>((int)c->nW, c->d_reps, c->d_e_unit, c->d_e_ex, c->d_e_col, c->d_col_begin,
-                                           c->d_e_rep);
+    k_final_energy<<<c->nrep, NB_FE_THREADS, 0, s>>>(
+        (int)c->nW, c->d_reps, c->d_e_unit, c->d_e_ex, c->d_e_col, c->d_col_begin,
+        c->precision != MOIL_NB_FP64 && c->water_excl_fast, c->d_e_rep);
     c->launches += 2;
 }
