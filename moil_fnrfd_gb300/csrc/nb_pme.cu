@@ -124,7 +124,14 @@ __global__ void k_pme_bin(int nsite, const int *__restrict__ site_rep, const Rep
     ((T4 *)fr_v)[s] = o;
     int zb = (int)f3;
     zb = zb >= R.n3 ? zb - R.n3 : (zb < 0 ? 0 : zb);
-    zslot[s] = atomicAdd(&zcount[R.zb0 + zb], 1);
+    // one atomic per distinct bin of the warp (a warp's sites are neighbours in space)
+    const int key = R.zb0 + zb, lane = threadIdx.x & 31;
+    const unsigned same = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(same) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&zcount[key], __popc(same));
+    base = __shfl_sync(same, base, leader);
+    zslot[s] = base + __popc(same & ((1u << lane) - 1));
 }
 
 __global__ void k_pme_scatter(int nsite, const int *__restrict__ site_rep, const RepDev *__restrict__ reps,

@@ -788,31 +788,29 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
     // per-atom corrections: none in a replica of waters whose corrections the water kernel added
     double x = (water_ex_zero && R.noth == 0) ? 0.0 : stream_sum(e_ex + 3 * (size_t)R.atom0, 3 * R.natom), cl = 0.0;
     for (int w = col_begin[r] + t; w < col_begin[r + 1]; w += NB_FE_THREADS) cl += e_col[w];
-    // slot sums: unit slot t % NB_EU, correction slot t % 3, columns summed over all threads
-    sh[t] = u;
-    __syncthreads();
-    if (t < NB_EU) {
-        double v = 0.0;
-        for (int k = t; k < NB_FE_THREADS; k += NB_EU) v += sh[k];
-        part[t] = v;
-    }
-    __syncthreads();
-    sh[t] = x;
-    __syncthreads();
-    if (t < 3) {
-        double v = 0.0;
-        for (int k = t; k < NB_FE_THREADS; k += 3) v += sh[k];
-        part[NB_EU + t] = v;
-    }
-    __syncthreads();
-    sh[t] = cl;
-    __syncthreads();
-    if (t == 0) {
-        double v = 0.0;
-        for (int k = 0; k < NB_FE_THREADS; ++k) v += sh[k];
-        part[NB_EU + 3] = v;
-    }
-    __syncthreads();
+    // slot sums by halving trees (fixed order): while the live range halves into a multiple
+    // of the slot count, thread k adds k + half, which holds the same slot; the few left
+    // are added serially
+    auto tree = [&](double v, int width, double *out) {
+        sh[t] = v;
+        __syncthreads();
+        int live = NB_FE_THREADS;
+        while (live % 2 == 0 && (live / 2) % width == 0) {
+            const int h = live / 2;
+            if (t < h) sh[t] += sh[t + h];
+            __syncthreads();
+            live = h;
+        }
+        if (t < width) {
+            double w = 0.0;
+            for (int k = t; k < live; k += width) w += sh[k];
+            out[t] = w;
+        }
+        __syncthreads();
+    };
+    tree(u, NB_EU, part);
+    tree(x, 3, part + NB_EU);
+    tree(cl, 1, part + NB_EU + 3);
     if (t == 0) {
         const double elp = 0.5 * part[0], eli = 0.5 * part[1], eep = 0.5 * part[2], eei = 0.5 * part[3];
         const double npairs = 0.5 * part[4];
