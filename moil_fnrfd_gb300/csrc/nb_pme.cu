@@ -289,11 +289,21 @@ __device__ __forceinline__ T eterm_of(const RepDev &R, const T *bsp, int kx, int
 
 #define NB_TKF 32     // z lines per zconv CTA (FP32 path)
 
-// One Stockham stage over L lines of length n.  Source line l at src + l*ss (contiguous).
-// Destination: MODE 0 natural (dst + l*ds), MODE 1 transposed (dst[k*L + l] for k < keep),
-// MODE 2 real part natural (rdst + l*ds).  CONJ_OUT conjugates the stored values.
-// tab / tw point into shared memory (fft_ctx_load).
-template <int RADIX, int MODE, bool CONJ_OUT>
+// Shared-memory layout of the intermediate results between Stockham stages: element e of a
+// buffer is stored at e + e/16 (one spare slot per 16 float2, i.e. per 128 bytes), so the
+// strided stores of the early stages (stride R for radix R) and the strided reads of the
+// later ones spread over all banks.  Inputs and outputs of a transform keep the caller's
+// layout.
+__host__ __device__ __forceinline__ int swz(int e) { return e + (e >> 4); }
+// float2 slots that hold m elements in the spread layout
+__host__ __device__ __forceinline__ int swz_elems(int m) { return m + (m >> 4) + 1; }
+
+// One Stockham stage over L lines of length n.  Source line l at src + l*ss (contiguous),
+// or in the spread layout (SW_IN).  Destination: MODE 0 natural (dst + l*ds, spread if
+// SW_OUT), MODE 1 transposed (dst[k*ds + l] for k < keep), MODE 2 real part natural
+// (rdst + l*ds).  CONJ_OUT conjugates the stored values.  tab / tw point into shared memory
+// (fft_ctx_load).
+template <int RADIX, int MODE, bool CONJ_OUT, bool SW_IN, bool SW_OUT>
 __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                            float *__restrict__ rdst, int L, int ss, int ds, int keep,
                                            int Ns, int nb, unsigned magic, const int2 *__restrict__ tab,
@@ -304,10 +314,10 @@ __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float
         int line = nb == 1 ? b : (int)__umulhi((unsigned)b, magic);
         int j = b - line * nb;
         int2 e = tab[j];
-        const float2 *s = src + line * ss + j;
+        const int s0 = line * ss + j;
         float2 v[RADIX];
 #pragma unroll
-        for (int r = 0; r < RADIX; ++r) v[r] = s[r * nb];
+        for (int r = 0; r < RADIX; ++r) v[r] = src[SW_IN ? swz(s0 + r * nb) : s0 + r * nb];
 #pragma unroll
         for (int r = 1; r < RADIX; ++r) v[r] = cmul(v[r], tw[r * e.x]);
         if (RADIX == 4) bfly4(v);
@@ -318,23 +328,23 @@ __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float
         for (int r = 0; r < RADIX; ++r) {
             float2 o = CONJ_OUT ? cconj(v[r]) : v[r];
             int k = e.y + r * Ns;
-            if (MODE == 0) dst[line * ds + k] = o;
-            else if (MODE == 1) { if (k < keep) dst[k * L + line] = o; }
+            if (MODE == 0) { const int d = line * ds + k; dst[SW_OUT ? swz(d) : d] = o; }
+            else if (MODE == 1) { if (k < keep) dst[k * ds + line] = o; }
             else rdst[line * ds + k] = o.x;
         }
     }
     __syncthreads();
 }
 
-template <int MODE, bool CONJ_OUT>
+template <int MODE, bool CONJ_OUT, bool SW_IN, bool SW_OUT>
 __device__ __forceinline__ void fft_pass(int R, const float2 *src, float2 *dst, float *rdst, int L, int ss, int ds,
                                          int keep, int Ns, int nb, unsigned magic, const int2 *tab, const float2 *tw)
 {
     switch (R) {
-    case 4: fft_pass_r<4, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
-    case 2: fft_pass_r<2, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
-    case 3: fft_pass_r<3, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
-    default: fft_pass_r<5, MODE, CONJ_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    case 4: fft_pass_r<4, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    case 2: fft_pass_r<2, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    case 3: fft_pass_r<3, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    default: fft_pass_r<5, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
     }
 }
 
@@ -368,11 +378,13 @@ __device__ __forceinline__ unsigned char *fft_ctx_load(unsigned char *dst, const
     return (unsigned char *)stw + align16(n * sizeof(float2));
 }
 
-// Full forward FFT of L lines (length n, contiguous, line stride n) held in a; b is scratch.
-// The last pass is stored in the mode given; returns the buffer holding the result.
-// conj_last conjugates the final output (second half of an inverse transform).
+// Full forward FFT of L lines of length n held in a (line stride in_ss); b is scratch.  The
+// last pass is stored in the mode given with stride out_ds (MODE 1: the transposed row
+// stride); the stages between keep the spread layout.  Returns the buffer holding the
+// result; CONJ_LAST conjugates the final output (second half of an inverse transform).
 template <int LAST_MODE, bool CONJ_LAST>
-__device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst, int L, int keep)
+__device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst, int L, int keep, int in_ss,
+                             int out_ds)
 {
     const FftPlanDev &p = *c.p;
     float2 *src = a, *dst = b;
@@ -380,23 +392,42 @@ __device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst,
     for (int s = 0; s < nst; ++s) {
         const int2 *t = c.tab + p.off[s];
         if (s + 1 < nst) {
-            fft_pass<0, false>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s], t, c.tw);
+            if (s == 0)
+                fft_pass<0, false, false, true>(p.rad[s], src, dst, nullptr, L, in_ss, n, 0, p.ns[s], p.nb[s],
+                                                p.magic[s], t, c.tw);
+            else
+                fft_pass<0, false, true, true>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s],
+                                               t, c.tw);
+        } else if (s == 0) {
+            fft_pass<LAST_MODE, CONJ_LAST, false, false>(p.rad[s], src, dst, rdst, L, in_ss, out_ds, keep, p.ns[s],
+                                                         p.nb[s], p.magic[s], t, c.tw);
         } else {
-            int ds = LAST_MODE == 1 ? 0 : n;
-            fft_pass<LAST_MODE, CONJ_LAST>(p.rad[s], src, dst, rdst, L, n, ds, keep, p.ns[s], p.nb[s], p.magic[s], t,
-                                           c.tw);
+            fft_pass<LAST_MODE, CONJ_LAST, true, false>(p.rad[s], src, dst, rdst, L, n, out_ds, keep, p.ns[s],
+                                                        p.nb[s], p.magic[s], t, c.tw);
         }
         float2 *x = src; src = dst; dst = x;
     }
     return src;
 }
 
-// float2 elements of each of the two plane buffers of the FP32 plane kernels: the packed
-// rows (ceil(n2/2) lines of n1) or the half spectrum (n1/2+1 lines of n2), whichever is
-// larger; even, so the buffers after it stay 16-byte aligned
+// float2 slots of each of the two plane buffers of the FP32 plane kernels: the packed rows
+// (ceil(n2/2) lines of n1), the half spectrum (n1/2+1 lines of n2, stored with the odd row
+// stride n2|1 after the forward x pass), the transposed inverse y output (n2 rows of stride
+// (n1/2+1)|1), and either kind in the spread layout of the stages between; even, so the
+// buffers after it stay 16-byte aligned
 __host__ __device__ __forceinline__ int plane_buf_elems(int n1, int n2)
 {
-    const int a = ((n2 + 1) / 2) * n1, b = (n1 / 2 + 1) * n2;
+    const int n1h = n1 / 2 + 1, a = ((n2 + 1) / 2) * n1, b = n1h * n2;
+    int m = swz_elems(a > b ? a : b);
+    m = m > n1h * (n2 | 1) ? m : n1h * (n2 | 1);
+    m = m > n2 * (n1h | 1) ? m : n2 * (n1h | 1);
+    return (m + 1) & ~1;
+}
+
+// float2 slots of each zconv buffer: NB_TKF lines of n3 at the odd stride n3|1 or spread
+__host__ __device__ __forceinline__ int zconv_buf_elems(int n3)
+{
+    const int a = swz_elems(NB_TKF * n3), b = NB_TKF * (n3 | 1);
     return ((a > b ? a : b) + 1) & ~1;
 }
 
@@ -431,19 +462,21 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
             B1[p * n1 + x] = make_float2(re, im);
         }
     __syncthreads();
-    float2 *Z = fft_lines<0, false>(c1, B1, B0, nullptr, n2p, 0);
+    float2 *Z = fft_lines<0, false>(c1, B1, B0, nullptr, n2p, 0, n1, n1);
     float2 *T = Z == B1 ? B0 : B1;
     // separate the two real transforms (X_2p = (Z_k + conj Z_-k)/2, X_2p+1 = -i (Z_k - conj Z_-k)/2)
-    // and keep kx < n1h, transposed to [kx][y] lines of n2
+    // and keep kx < n1h, transposed to [kx][y] lines of n2 at the odd row stride sT (the lanes'
+    // stores then fall in distinct banks)
+    const int sT = n2 | 1;
     for (int p = warp; p < n2p; p += nwarp)
         for (int k = lane; k < n1h; k += 32) {
             const float2 a = Z[p * n1 + k], b = Z[p * n1 + (k == 0 ? 0 : n1 - k)];
-            T[k * n2 + 2 * p] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
-            if (2 * p + 1 < n2) T[k * n2 + 2 * p + 1] = make_float2(0.5f * (a.y + b.y), 0.5f * (b.x - a.x));
+            T[k * sT + 2 * p] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+            if (2 * p + 1 < n2) T[k * sT + 2 * p + 1] = make_float2(0.5f * (a.y + b.y), 0.5f * (b.x - a.x));
         }
     __syncthreads();
     // y: n1h lines of n2
-    float2 *Y = fft_lines<0, false>(c2, T, Z, nullptr, n1h, 0);
+    float2 *Y = fft_lines<0, false>(c2, T, Z, nullptr, n1h, 0, sT, n2);
     float2 *g = grid + R.g0 + (size_t)w.z * n1h * n2;
     for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) g[k] = Y[k];
 }
@@ -461,16 +494,17 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
     const int tk = min(NB_TKF, n2 - w.ky0);
     const float *bsp = bsp_all + R.bsp0;
-    float2 *A = (float2 *)smem, *B = A + NB_TKF * n3;
+    float2 *A = (float2 *)smem, *B = A + zconv_buf_elems(n3);
     FftCtx c3;
-    fft_ctx_load((unsigned char *)(B + NB_TKF * n3), plans + rep_plan[3 * w.rep + 2], tab, tw, c3);
+    fft_ctx_load((unsigned char *)(B + zconv_buf_elems(n3)), plans + rep_plan[3 * w.rep + 2], tab, tw, c3);
+    const int sA = n3 | 1;    // odd line stride of the columns as loaded and stored
     float2 *g = grid + R.g0 + (size_t)w.kx * n2 + w.ky0;
     const size_t zs = (size_t)n1h * n2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int kz = warp; kz < n3; kz += 8)
-        if (lane < tk) A[lane * n3 + kz] = g[kz * zs + lane];
+        if (lane < tk) A[lane * sA + kz] = g[kz * zs + lane];
     __syncthreads();
-    float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0);
+    float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0, sA, n3);
     float2 *Fo = F == A ? B : A;
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
     // influence function: exp(-pi^2 m^2 / alpha^2) = 2^(-fac2 m^2), fac2 = pi^2 / alpha^2 * log2(e)
@@ -495,9 +529,9 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
         }
     }
     __syncthreads();
-    float2 *I = fft_lines<0, true>(c3, F, Fo, nullptr, tk, 0);
+    float2 *I = fft_lines<0, true>(c3, F, Fo, nullptr, tk, 0, n3, sA);
     for (int kz = warp; kz < n3; kz += 8)
-        if (lane < tk) g[kz * zs + lane] = I[lane * n3 + kz];
+        if (lane < tk) g[kz * zs + lane] = I[lane * sA + kz];
     // fixed-order reduction: FP32 within each warp, FP64 over the 8 warp sums
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) en += __shfl_down_sync(0xffffffffu, en, o);
@@ -531,8 +565,10 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
     // [kx][ky] lines of n2, conjugated (inverse through the forward transform)
     for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) B0[k] = cconj(g[k]);
     __syncthreads();
-    // y: n1h lines; last pass conjugates back and stores transposed to H[ky][kx]
-    fft_lines<1, true>(c2, B0, B1, nullptr, n1h, n2);
+    // y: n1h lines; last pass conjugates back and stores transposed to H[ky][kx] at the odd
+    // row stride hs
+    const int hs = n1h | 1;
+    fft_lines<1, true>(c2, B0, B1, nullptr, n1h, n2, n2, hs);
     // which buffer got the transposed result depends on the pass count
     float2 *H = (c2.p->nst & 1) ? B1 : B0;
     float2 *Zc = H == B0 ? B1 : B0;
@@ -542,13 +578,13 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
         for (int k = lane; k < n1; k += 32) {
             const bool lo = k < n1h;
             const int kk = lo ? k : n1 - k;
-            float2 a = H[2 * p * n1h + kk];
-            float2 b = 2 * p + 1 < n2 ? H[(2 * p + 1) * n1h + kk] : make_float2(0.f, 0.f);
+            float2 a = H[2 * p * hs + kk];
+            float2 b = 2 * p + 1 < n2 ? H[(2 * p + 1) * hs + kk] : make_float2(0.f, 0.f);
             if (!lo) { a = cconj(a); b = cconj(b); }
             Zc[p * n1 + k] = make_float2(a.x - b.y, -(a.y + b.x));
         }
     __syncthreads();
-    const float2 *W = fft_lines<0, false>(c1, Zc, H, nullptr, n2p, 0);
+    const float2 *W = fft_lines<0, false>(c1, Zc, H, nullptr, n2p, 0, n1, n1);
     // the real potential plane over the plane's own complex storage (this block alone reads it)
     float *gr = (float *)g;
     for (int p = warp; p < n2p; p += nwarp)
@@ -903,7 +939,7 @@ size_t plane_inv_smem(int n1, int n2)
 template <typename T>
 size_t zconv_smem(int n3)
 {
-    if (sizeof(T) == 4) return (size_t)2 * NB_TKF * n3 * sizeof(float2) + fft_ctx_bytes(n3);
+    if (sizeof(T) == 4) return (size_t)2 * zconv_buf_elems(n3) * sizeof(float2) + fft_ctx_bytes(n3);
     typedef typename cplx<T>::type C;
     return sizeof(C) * NB_TK * (n3 | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
 }
