@@ -692,7 +692,12 @@ void nb_launch_prepare(NbCtx *c, const double *d_coor, int check)
 
 void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_total)
 {
-    // PME z-bins: short, and also used by the allocation-free entry point (no scan scratch)
+    // PME z-bins: the three-phase scan when the handle has its tile-sum scratch; one CTA
+    // for the allocation-free entry point, which has none
+    if (c->d_scan_tmp) {
+        nb_scan(c, d_in, d_out, n, d_total, 0);
+        return;
+    }
     k_scan_small<<<1, 1024, 0, c->stream>>>(d_in, d_out, n, d_total);
     c->launches += 1;
 }
