@@ -154,6 +154,18 @@ int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies
  * (device pointers, same layout); energies still go to host memory. */
 int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *energies);
 
+/* LJ virial terms of the last evaluation for one replica, as MOIL's PRESS build accumulates
+ * them into COMMON/ENERGY.BLOCK:94-96 (virvdw1..virvdw5): virvdw = -sum df1 r^2 over the
+ * LJ pairs, df1 = (dE_LJ/dr)/r, for water-water pairs in the primary box
+ * (pot/watwat_ewald_press.f:146-152) and across images (symm/symwat_ewald_press.f:161-168),
+ * other pairs in the primary box (pot/cdie_ewald_press.f:413-419, :499-505) and across
+ * images (symm/symcdie_ewald_press.f:164-167, :279-281), and 1-4 pairs
+ * (pot/ener14_press.f:51-59).  dynamics/write_press.f:43-48 forms the pressure from these,
+ * the constraint virial and the energies (virele = -(e_dir + e_ew_receip + e_self + e_corr)).
+ * With the LJ switch extension on, df1 is the switched derivative.  On the mixed path
+ * virvdw1 and virvdw2 are zero unless moil_nb_set_virial(h, 1) was called. */
+int moil_nb_get_virial(moil_nb_ctx *h, int replica, double *virvdw);
+
 /* Parameter derivatives of the nonbonded energy at coor (host, all replicas, caller order),
  * one FP64 value per atom: dE/dq (the electrostatic potential, kcal/mol/e), dE/deps and
  * dE/dsigma of the atom's LJ parameters decoded from the epsgm encoding
@@ -187,6 +199,12 @@ int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *sit
  * the coordinate / gradient pointers or the pair-list buffers change; evaluations
  * with timing on always launch kernel by kernel.  No counterpart in the reference. */
 int moil_nb_set_graph(moil_nb_ctx *h, int on);
+
+/* Accumulate the water-water LJ virial terms (virvdw1, virvdw2 of moil_nb_get_virial) on
+ * the mixed path (1), or leave them zero (0, default: the extra accumulators cost the
+ * FP32 water kernel registers).  The other virial terms and the plain FP64 path always
+ * accumulate them.  No counterpart in the reference (its PRESS build always does). */
+int moil_nb_set_virial(moil_nb_ctx *h, int on);
 
 /* ---- PME reciprocal sum without device allocation -------------------------
  * No counterpart in the reference (MOIL's ewald_receip() works on static COMMON
@@ -228,6 +246,10 @@ void ewald_init_gpu_(const int *npt, const double *ptchg, const double *epsgm6, 
                      const double *params11, const int *iparams8, int *status);
 void nblist_gpu_(int *status);
 void eforce_nb_gpu_(const int *npt, const double *coor, double *dpot, double *enb, int *status);
+/* The PRESS build's eforce (pot/eforce_press.f): as eforce_nb_gpu, plus virvdw(5) =
+ * virvdw1..virvdw5 of the evaluation (moil_nb_get_virial). */
+void eforce_nb_press_gpu_(const int *npt, const double *coor, double *dpot, double *enb, double *virvdw,
+                          int *status);
 
 #ifdef __cplusplus
 }

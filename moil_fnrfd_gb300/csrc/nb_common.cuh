@@ -24,8 +24,10 @@
 #define NB_PLANE_SCALE 1099511627776.0  // 2^40: PME plane accumulation
 #define NB_MAX_FFT 128
 #define NB_TWO_OVER_SQRTPI 1.1283791670955126
-#define NB_EU 6                       // per-unit outputs: LJ prim, LJ img, Coul prim, Coul img, site pairs,
-                                      // intramolecular water correction (mixed path)
+#define NB_EU 8                       // per-unit outputs: LJ prim, LJ img, Coul prim, Coul img, site pairs,
+                                      // intramolecular water correction (mixed path), LJ virial prim, img
+#define NB_EX 4                       // per-atom outputs: exclusion correction, 1-4 Coulomb, 1-4 LJ, 1-4 LJ virial
+#define NB_EREP 24                    // per-replica results (energies, pair count, LJ virial terms)
 #define NB_WTILE 128                  // waters per block (and per shared tile) of the tiled water list
 
 // per-replica constants (read by every kernel)

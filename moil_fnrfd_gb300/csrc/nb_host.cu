@@ -463,12 +463,12 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_grad_site, sizeof(long long) * 3 * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_e_unit, sizeof(double) * NB_EU * std::max<int64_t>(nu, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_grad_ex, sizeof(double) * 3 * c->natom));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_e_ex, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_ex, sizeof(double) * NB_EX * c->natom));
     NB_CUDA_OK(c, cudaMalloc(&c->d_zcount, sizeof(int) * (c->nzbin + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_zstart, sizeof(int) * (c->nzbin + 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_zslot, sizeof(int) * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_zatoms, sizeof(int) * ns));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_e_rep, sizeof(double) * 16 * nrep));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_e_rep, sizeof(double) * NB_EREP * nrep));
     NB_CUDA_OK(c, cudaMalloc(&c->d_coor, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMalloc(&c->d_dpot, sizeof(double) * 3 * c->natom));
     NB_CUDA_OK(c, cudaMemset(c->d_grad_site, 0, sizeof(long long) * 3 * ns));
@@ -476,7 +476,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     // the mixed path never writes the water atoms' entries (their corrections are in the
     // water kernel): they stay zero
     NB_CUDA_OK(c, cudaMemset(c->d_grad_ex, 0, sizeof(double) * 3 * c->natom));
-    NB_CUDA_OK(c, cudaMemset(c->d_e_ex, 0, sizeof(double) * 3 * c->natom));
+    NB_CUDA_OK(c, cudaMemset(c->d_e_ex, 0, sizeof(double) * NB_EX * c->natom));
     // list capacities from densities (grown on overflow)
     c->cap_wl2 = c->cap_xl = 64;
     double row1 = 32;
@@ -491,8 +491,8 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     }
     c->cap_row1 = ((int)row1 + 31) & ~31;
     NB_TRY(alloc_lists(c));
-    NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * 16 * nrep));
-    memset(c->h_e_rep, 0, sizeof(double) * 16 * nrep);
+    NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * NB_EREP * nrep));
+    memset(c->h_e_rep, 0, sizeof(double) * NB_EREP * nrep);
     NB_TRY(nb_pme_configure(c));
     {
         // tile sums for every scan: bins, per-water and per-atom counts, PME z-bins
@@ -527,7 +527,7 @@ void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
     nb_launch_finalize(c, d_dpot);
     if (c->timing) cudaEventRecord(c->ev[10], s);
     cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(c->h_e_rep, c->d_e_rep, sizeof(double) * 16 * c->nrep, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(c->h_e_rep, c->d_e_rep, sizeof(double) * NB_EREP * c->nrep, cudaMemcpyDeviceToHost, s);
 }
 
 void drop_graph(NbCtx *c)
@@ -631,7 +631,7 @@ int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
     if (rc != MOIL_NB_OK) return rc;
     if (e) {
         for (int r = 0; r < c->nrep; ++r) {
-            const double *o = c->h_e_rep + 16 * r;
+            const double *o = c->h_e_rep + NB_EREP * r;
             moil_energies &E = e[r];
             E.e_vdw = o[0]; E.e_el = o[1]; E.e_vsym = o[2]; E.e_lsym = o[3];
             E.e_el14 = o[4]; E.e_vdw14 = o[5]; E.e_corr = o[6]; E.e_self = o[7];
@@ -640,7 +640,7 @@ int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
     }
     {
         double np = 0;
-        for (int r = 0; r < c->nrep; ++r) np += c->h_e_rep[16 * r + 11];
+        for (int r = 0; r < c->nrep; ++r) np += c->h_e_rep[NB_EREP * r + 11];
         c->last_site_pairs = (int64_t)(np + 0.5);
     }
     return MOIL_NB_OK;
@@ -768,6 +768,19 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
     return MOIL_NB_OK;
 }
 
+int moil_nb_get_virial(moil_nb_ctx *h, int replica, double *virvdw)
+{
+    if (!h || !virvdw) return MOIL_NB_ERR_ARG;
+    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (replica < 0 || replica >= h->nrep) {
+        h->err = "replica index out of range";
+        return MOIL_NB_ERR_ARG;
+    }
+    const double *o = h->h_e_rep + NB_EREP * (size_t)replica;
+    for (int k = 0; k < 5; ++k) virvdw[k] = o[12 + k];
+    return MOIL_NB_OK;
+}
+
 int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *e)
 {
     if (!h || !d_coor || !d_dpot) return MOIL_NB_ERR_ARG;
@@ -845,6 +858,15 @@ int moil_nb_set_graph(moil_nb_ctx *h, int on)
     return MOIL_NB_OK;
 }
 
+int moil_nb_set_virial(moil_nb_ctx *h, int on)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    cudaSetDevice(h->device);
+    h->virial = on ? 1 : 0;
+    drop_graph(h);
+    return MOIL_NB_OK;
+}
+
 // ---- Fortran entry points --------------------------------------------------------
 void ewald_init_gpu_(const int *npt, const double *ptchg, const double *epsgm6, const double *epsgm12,
                      const int *exc1, const int *exc2, const int *totspe, const int *spec1, const int *spec2,
@@ -900,6 +922,19 @@ void eforce_nb_gpu_(const int *npt, const double *coor, double *dpot, double *en
         }
     }
     *status = rc;
+}
+
+void eforce_nb_press_gpu_(const int *npt, const double *coor, double *dpot, double *enb, double *virvdw,
+                          int *status)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_fortran_mu);
+        if (g_fortran_ctx && !g_fortran_ctx->virial) moil_nb_set_virial(g_fortran_ctx, 1);
+    }
+    eforce_nb_gpu_(npt, coor, dpot, enb, status);
+    if (!status || *status != MOIL_NB_OK || !virvdw) return;
+    std::lock_guard<std::mutex> lk(g_fortran_mu);
+    *status = moil_nb_get_virial(g_fortran_ctx, 0, virvdw);
 }
 
 }  // extern "C"

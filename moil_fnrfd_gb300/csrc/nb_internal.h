@@ -146,6 +146,7 @@ struct NbCtx {
 
     // CUDA graph of one evaluation, valid for the caller pointers and list buffers it captured
     int use_graph = 1;
+    int virial = 0;                    // water-water LJ virial in the FP32 water kernel
     cudaGraphExec_t gexec = nullptr;
     const double *g_coor = nullptr;
     double *g_dpot = nullptr;

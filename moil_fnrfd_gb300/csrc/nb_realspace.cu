@@ -48,9 +48,10 @@ template <> struct Consts<double> {
 };
 
 // one non-water-type pair (cdie_ewald list1/2/3 semantics); d already minimum-imaged
+// vir receives MOIL's LJ virial term of the pair, -df1 r^2 (cdie_ewald_press.f:413-419)
 template <typename T>
 __device__ __forceinline__ T atom_pair(const RepDev &R, T r2, T qi, T qj, T e12i, T e6i, T e12j, T e6j,
-                                       unsigned fi, unsigned fj, T &eel, T &elj, int &npair)
+                                       unsigned fi, unsigned fj, T &eel, T &elj, T &vir, int &npair)
 {
     bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < (T)R.re2;
     bool lj = r2 < (T)R.rv2 && !hr;
@@ -86,6 +87,7 @@ __device__ __forceinline__ T atom_pair(const RepDev &R, T r2, T qi, T qj, T e12i
         T df1 = (T)-6 * s2 * (A + e1);
         lj_switch_apply<T>(R, r2, e1, df1);
         elj += e1;
+        vir -= df1 * r2;
         df += df1;
     }
     return df;
@@ -145,8 +147,9 @@ __device__ __forceinline__ void water_vs_atoms(const RepDev &R, int i, const typ
             bool img;
             min_image<T>(R, dx, dy, dz, img);
             T r2 = dx * dx + dy * dy + dz * dz;
-            T eel = 0, elj = 0;
-            T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj, npair);
+            T eel = 0, elj = 0, vir = 0;   // the virial of these pairs is counted by k_atom
+            T df = atom_pair<T>(R, r2, si[a].w, xj.w, lji[a].x, lji[a].y, ljj.x, ljj.y, fi[a], fj, eel, elj, vir,
+                                npair);
             g[3 * a] += df * dx;
             g[3 * a + 1] += df * dy;
             g[3 * a + 2] += df * dz;
@@ -194,7 +197,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
                                                      double *__restrict__ e_unit)
 {
     __shared__ long long sG[9][WBLOCK];
-    __shared__ double sE[4][WBLOCK];
+    __shared__ double sE[6][WBLOCK];
     const int t = threadIdx.x;
     int i = blockIdx.x * WBLOCK + t;
     if (i >= nW) return;
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
 #pragma unroll
     for (int k = 0; k < 9; ++k) sG[k][t] = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) sE[k][t] = 0.0;
+    for (int k = 0; k < 6; ++k) sE[k][t] = 0.0;
     const T4 oi0 = pos[3 * i];
     // i-site offsets from O (a = 0 is O itself)
     const T4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
@@ -214,12 +217,12 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
     T g[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) g[k] = 0;
-    T e4[4] = {0, 0, 0, 0};    // LJ prim, LJ img, Coulomb prim, Coulomb img
+    T e4[6] = {0, 0, 0, 0, 0, 0};   // LJ prim, LJ img, Coulomb prim, Coulomb img, LJ virial prim, img
     auto flush_all = [&]() {
 #pragma unroll
         for (int k = 0; k < 9; ++k) { sG[k][t] += nb_fix(g[k]); g[k] = 0; }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) { sE[k][t] += (double)e4[k]; e4[k] = 0; }
+        for (int k = 0; k < 6; ++k) { sE[k][t] += (double)e4[k]; e4[k] = 0; }
     };
     int npair = 0;
     const T iL0 = rep_invL<T>(R, 0), iL1 = rep_invL<T>(R, 1), iL2 = rep_invL<T>(R, 2);
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
             T4 oj1 = woff[2 * j], oj2 = woff[2 * j + 1];
             // q[b] = (O_i - O_j - nL) - offset_j[b]; site displacement = offset_i[a] + q[b]
             const T q[3][3] = {{dx, dy, dz}, {dx - oj1.x, dy - oj1.y, dz - oj1.z}, {dx - oj2.x, dy - oj2.y, dz - oj2.z}};
-            T e_el = 0, e_lj = 0;
+            T e_el = 0, e_lj = 0, v_lj = 0;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
 #pragma unroll
@@ -271,6 +274,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
                             T e1 = A - B, df1 = (T)-6 * s2 * (A + e1);
                             lj_switch_apply<T>(R, rr2, e1, df1);
                             e_lj += e1;
+                            v_lj -= df1 * rr2;   // watwat_ewald_press.f:146-152
                             df += df1;
                         }
                     }
@@ -283,6 +287,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
             const bool img = (nx != (T)0) | (ny != (T)0) | (nz != (T)0);
             e4[img ? 1 : 0] += e_lj;
             e4[img ? 3 : 2] += e_el;
+            e4[img ? 5 : 4] += v_lj;
             npair += 9;
         }
         if (++cnt == CHUNK) { flush_all(); cnt = 0; }
@@ -293,7 +298,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
     eu[0] = sE[0][t]; eu[1] = sE[1][t]; eu[2] = sE[2][t]; eu[3] = sE[3][t]; eu[4] = (double)npair;
-    eu[5] = 0.0;
+    eu[5] = 0.0; eu[6] = sE[4][t]; eu[7] = sE[5][t];
 }
 
 // FP32 water exclusion corrections (cdie_ewald.f:117-199 for the pairs O-H1, O-H2, H1-H2 of
@@ -348,6 +353,9 @@ __device__ __forceinline__ float water_intra_f(const RepDev &R, float4 h1, float
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
+// VIR: also the water-water LJ virial terms (two more accumulators, which the 128-register
+// budget of the plain evaluation does not hold without spilling; off unless requested)
+template <bool VIR>
 __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__restrict__ reps,
                                                        const int *__restrict__ site_rep, const float4 *__restrict__ pos,
                                                        const float4 *__restrict__ woff, const void *lj_v,
@@ -358,7 +366,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                                                        double *__restrict__ e_unit, int intra)
 {
     __shared__ long long sG[9][WBLOCK];
-    __shared__ float2 sE[4][WBLOCK];     // energies as unevaluated sums hi + lo (no FP64 pipe)
+    __shared__ float2 sE[6][WBLOCK];     // energies as unevaluated sums hi + lo (no FP64 pipe)
     const int t = threadIdx.x;
     const int i = blockIdx.x * WBLOCK + t;
     if (i >= nW) return;
@@ -366,7 +374,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
 #pragma unroll
     for (int k = 0; k < 9; ++k) sG[k][t] = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) sE[k][t] = make_float2(0.f, 0.f);
+    for (int k = 0; k < 6; ++k) sE[k][t] = make_float2(0.f, 0.f);
     const float4 oi0 = pos[3 * i];
     const float4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
     // H offsets of molecule i, duplicated into both lanes
@@ -377,7 +385,11 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     float g[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) g[k] = 0.f;
-    float e4[4] = {0.f, 0.f, 0.f, 0.f};   // LJ prim, LJ img, Coulomb prim, Coulomb img
+    // LJ prim, LJ img, Coulomb prim, Coulomb img (, LJ virial prim, LJ virial img)
+    constexpr int NE = VIR ? 6 : 4;
+    float e4[NE];
+#pragma unroll
+    for (int k = 0; k < NE; ++k) e4[k] = 0.f;
     // the molecule's own exclusion corrections (every water excludes exactly its three pairs)
     float ecorr = 0.f;
     if (intra) {
@@ -392,7 +404,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
             G[k] = f2(0.f);
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < NE; ++k) {
             // TwoSum (Knuth): hi + e4 = s + err exactly; the errors collect in lo
             const float2 a = sE[k][t];
             const float sm = a.x + e4[k], bb = sm - a.x, err = (a.x - (sm - bb)) + (e4[k] - bb);
@@ -441,7 +453,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
             if (!in0) { dx0 = 1.0e4f; dy0 = 0.f; dz0 = 0.f; }
             if (!in1) { dx1 = 1.0e4f; dy1 = 0.f; dz1 = 0.f; }
             // q[b] = (O_i - O_j - nL) - offset_j[b]; site displacement = offset_i[a] + q[b]
-            float2 eel = f2(0.f), elj = f2(0.f);
+            float2 eel = f2(0.f), elj = f2(0.f), vlj = f2(0.f);
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
                 float2 q[3];
@@ -494,6 +506,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                         e1 = f2(l0 ? e1.x : 0.f, l1 ? e1.y : 0.f);
                         m1 = f2(l0 ? m1.x : 0.f, l1 ? m1.y : 0.f);
                         elj = __fadd2_rn(elj, e1);
+                        if (VIR) vlj = __fmul2_rn(m1, rr2);   // -df1 r^2 (watwat_ewald_press.f:146-152)
                         mdf = __fadd2_rn(mdf, m1);
                     }
                     eel = __fadd2_rn(eel, e);
@@ -506,8 +519,10 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
             const bool img1 = (nx1 != 0.f) | (ny1 != 0.f) | (nz1 != 0.f);
             e4[img0 ? 1 : 0] += elj.x;
             e4[img0 ? 3 : 2] += eel.x;
+            if (VIR) e4[img0 ? NE - 1 : NE - 2] += vlj.x;
             e4[img1 ? 1 : 0] += elj.y;
             e4[img1 ? 3 : 2] += eel.y;
+            if (VIR) e4[img1 ? NE - 1 : NE - 2] += vlj.y;
             npair += 9 * ((int)in0 + (int)in1);
         }
         cnt += 2;
@@ -522,6 +537,8 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     for (int k = 0; k < 4; ++k) eu[k] = (double)sE[k][t].x + (double)sE[k][t].y;
     eu[4] = (double)npair;
     eu[5] = (double)ecorr;
+    eu[6] = VIR ? (double)sE[4][t].x + (double)sE[4][t].y : 0.0;
+    eu[7] = VIR ? (double)sE[5][t].x + (double)sE[5][t].y : 0.0;
 }
 
 // non-water atom per thread over its full site list
@@ -544,7 +561,7 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     unsigned fi = sflags[si];
     T g[3] = {0, 0, 0};
     long long G[3] = {0, 0, 0};
-    double elp = 0, eli = 0, eep = 0, eei = 0;
+    double elp = 0, eli = 0, eep = 0, eei = 0, vp = 0, vi = 0;
     int cnt = 0, npair = 0;
     const int q1 = xl_off[k + 1];
     for (int q = xl_off[k]; q < q1; ++q) {
@@ -556,11 +573,14 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
         bool img;
         min_image<T>(R, dx, dy, dz, img);
         T r2 = dx * dx + dy * dy + dz * dz;
-        T eel = 0, elj = 0;
-        T df = atom_pair<T>(R, r2, xi.w, xj.w, lji.x, lji.y, ljj.x, ljj.y, fi, sflags[s], eel, elj, npair);
+        T eel = 0, elj = 0, vir = 0;
+        T df = atom_pair<T>(R, r2, xi.w, xj.w, lji.x, lji.y, ljj.x, ljj.y, fi, sflags[s], eel, elj, vir, npair);
         g[0] += df * dx; g[1] += df * dy; g[2] += df * dz;
-        if (img) { eei += (double)eel; eli += (double)elj; }
-        else { eep += (double)eel; elp += (double)elj; }
+        // LJ virial: a water partner's side of the pair (its W2 list) adds none, so it counts
+        // twice here; pairs of two non-water atoms are seen from both sides
+        const double wv = (double)vir * (s < 3 * nW ? 2.0 : 1.0);
+        if (img) { eei += (double)eel; eli += (double)elj; vi += wv; }
+        else { eep += (double)eel; elp += (double)elj; vp += wv; }
         if (++cnt == CHUNK) { flush(g, G, 3); cnt = 0; }
     }
     flush(g, G, 3);
@@ -569,6 +589,7 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     grad[(size_t)3 * si + 2] = G[2];
     double *eu = e_unit + NB_EU * (size_t)(nW + k);
     eu[0] = elp; eu[1] = eli; eu[2] = eep; eu[3] = eei; eu[4] = (double)npair; eu[5] = 0.0;
+    eu[6] = vp; eu[7] = vi;
 }
 
 // ---------------------------------------------------------------------------------
@@ -637,9 +658,9 @@ __global__ void k_excl_water(int nW, const int *__restrict__ unit_atom, const in
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double *gp = grad + 3 * (size_t)(a0 + k), *ep = e_out + 3 * (size_t)(a0 + k);
+        double *gp = grad + 3 * (size_t)(a0 + k), *ep = e_out + NB_EX * (size_t)(a0 + k);
         gp[0] = g[k][0]; gp[1] = g[k][1]; gp[2] = g[k][2];
-        ep[0] = k == 0 ? ecorr : 0.0; ep[1] = 0.0; ep[2] = 0.0;
+        ep[0] = k == 0 ? ecorr : 0.0; ep[1] = 0.0; ep[2] = 0.0; ep[3] = 0.0;
     }
 }
 
@@ -657,7 +678,7 @@ __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepD
     if (skip_water && (aflags[a] & SF_WATER)) return;
     const RepDev &R = reps[atom_rep[a]];
     double xa = coor[3 * (size_t)a], ya = coor[3 * (size_t)a + 1], za = coor[3 * (size_t)a + 2];
-    double gx = 0, gy = 0, gz = 0, ecorr = 0, eel14 = 0, evdw14 = 0;
+    double gx = 0, gy = 0, gz = 0, ecorr = 0, eel14 = 0, evdw14 = 0, vir14 = 0;
     double qa = q[a] * R.epstmp, al = R.alphad;
     for (int k = ex_off[a]; k < ex_off[a + 1]; ++k) {
         int b = ex_j[k];
@@ -679,6 +700,7 @@ __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepD
             double s6 = s2 * s2 * s2, A = p[0] * s6 * s6, B = p[1] * s6;
             e1 = A - B;
             df1 = -6.0 * s2 * (A + e1);
+            vir14 -= 0.5 * df1 * r2;   // ener14_press.f:51-59
         }
         if (fabs(p[2]) > 1e-12) {
             double s = sqrt(s2);
@@ -698,7 +720,8 @@ __global__ void k_excl14(int natom, const int *__restrict__ atom_rep, const RepD
     } else {
         grad[3 * (size_t)a] = gx; grad[3 * (size_t)a + 1] = gy; grad[3 * (size_t)a + 2] = gz;
     }
-    e_out[3 * (size_t)a] = ecorr; e_out[3 * (size_t)a + 1] = eel14; e_out[3 * (size_t)a + 2] = evdw14;
+    double *eo = e_out + NB_EX * (size_t)a;
+    eo[0] = ecorr; eo[1] = eel14; eo[2] = evdw14; eo[3] = vir14;
 }
 
 // ---------------------------------------------------------------------------------
@@ -764,9 +787,9 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
                                                                 const int *__restrict__ col_begin,
                                                                 int water_ex_zero, double *__restrict__ e_rep)
 {
-    static_assert(NB_FE_THREADS % NB_EU == 0 && NB_FE_THREADS % 3 == 0, "slot-preserving stride");
+    static_assert(NB_FE_THREADS % NB_EU == 0 && NB_FE_THREADS % NB_EX == 0, "slot-preserving stride");
     __shared__ double sh[NB_FE_THREADS];
-    __shared__ double part[NB_EU + 3 + 1];
+    __shared__ double part[2 * NB_EU + NB_EX + 1];   // water units, other units, atoms, columns
     const int r = blockIdx.x, t = threadIdx.x;
     const RepDev &R = reps[r];
     // units: the replica's waters, then its other units, NB_EU doubles each; four loads in
@@ -783,10 +806,11 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
         if (k + 2 * NB_FE_THREADS < n) p[2] += b[k + 2 * NB_FE_THREADS];
         return (p[0] + p[1]) + (p[2] + p[3]);
     };
-    double u = stream_sum(e_unit + NB_EU * (size_t)R.wat0, NB_EU * R.nwat) +
-               stream_sum(e_unit + NB_EU * ((size_t)nW + R.oth0), NB_EU * R.noth);
+    const double uw = stream_sum(e_unit + NB_EU * (size_t)R.wat0, NB_EU * R.nwat);
+    const double uo = stream_sum(e_unit + NB_EU * ((size_t)nW + R.oth0), NB_EU * R.noth);
     // per-atom corrections: none in a replica of waters whose corrections the water kernel added
-    double x = (water_ex_zero && R.noth == 0) ? 0.0 : stream_sum(e_ex + 3 * (size_t)R.atom0, 3 * R.natom), cl = 0.0;
+    double x = (water_ex_zero && R.noth == 0) ? 0.0 : stream_sum(e_ex + NB_EX * (size_t)R.atom0, NB_EX * R.natom);
+    double cl = 0.0;
     for (int w = col_begin[r] + t; w < col_begin[r + 1]; w += NB_FE_THREADS) cl += e_col[w];
     // slot sums by halving trees (fixed order): while the live range halves into a multiple
     // of the slot count, thread k adds k + half, which holds the same slot; the few left
@@ -808,20 +832,26 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
         }
         __syncthreads();
     };
-    tree(u, NB_EU, part);
-    tree(x, 3, part + NB_EU);
-    tree(cl, 1, part + NB_EU + 3);
+    tree(uw, NB_EU, part);
+    tree(uo, NB_EU, part + NB_EU);
+    tree(x, NB_EX, part + 2 * NB_EU);
+    tree(cl, 1, part + 2 * NB_EU + NB_EX);
     if (t == 0) {
-        const double elp = 0.5 * part[0], eli = 0.5 * part[1], eep = 0.5 * part[2], eei = 0.5 * part[3];
-        const double npairs = 0.5 * part[4];
-        const double ecorr = part[NB_EU] + part[5], eel14 = part[NB_EU + 1], evdw14 = part[NB_EU + 2];
-        const double erec = 0.5 * part[NB_EU + 3];
-        double *o = e_rep + 16 * (size_t)r;
+        const double *pw = part, *po = part + NB_EU, *px = part + 2 * NB_EU;
+        const double elp = 0.5 * (pw[0] + po[0]), eli = 0.5 * (pw[1] + po[1]);
+        const double eep = 0.5 * (pw[2] + po[2]), eei = 0.5 * (pw[3] + po[3]);
+        const double npairs = 0.5 * (pw[4] + po[4]);
+        const double ecorr = px[0] + pw[5] + po[5], eel14 = px[1], evdw14 = px[2];
+        const double erec = 0.5 * part[2 * NB_EU + NB_EX];
+        double *o = e_rep + NB_EREP * (size_t)r;
         o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym
         o[4] = eel14; o[5] = evdw14; o[6] = ecorr; o[7] = R.e_self; o[8] = erec;
         o[9] = elp + eep + eli + eei + eel14 + evdw14 + ecorr + R.e_self + erec;
         o[10] = eep + eei;
         o[11] = npairs;                                           // in-cutoff site pairs
+        // LJ virial terms virvdw1..5 (MOIL's PRESS build): water-water primary and images,
+        // other pairs primary and images, 1-4
+        o[12] = 0.5 * pw[6]; o[13] = 0.5 * pw[7]; o[14] = 0.5 * po[6]; o[15] = 0.5 * po[7]; o[16] = px[3];
     }
 }
 
@@ -833,10 +863,10 @@ void realspace_t(NbCtx *c)
     if (c->nW > 0) {
         const int nb = (int)((c->nW + WBLOCK - 1) / WBLOCK);
         if constexpr (sizeof(T) == 4)
-            k_water_f<<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos,
-                                            (const float4 *)c->d_woff, c->d_site_lj, c->d_site_flags, c->d_wl1_cnt,
-                                            c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, c->d_grad_site,
-                                            c->d_e_unit, c->water_excl_fast);
+            (c->virial ? k_water_f<true> : k_water_f<false>)<<<nb, WBLOCK, 0, s>>>(
+                (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float4 *)c->d_woff,
+                c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2,
+                c->d_grad_site, c->d_e_unit, c->water_excl_fast);
         else
             k_water<T><<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
                                              c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1,

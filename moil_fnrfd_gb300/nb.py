@@ -30,7 +30,7 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device", "moil_nb_adjoint",
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
-            "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_")
+            "moil_nb_get_virial", "moil_nb_set_virial", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -111,6 +111,8 @@ def load(build_if_missing: bool = True):
     L.moil_nb_get_timing.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timing)]
     L.moil_nb_pair_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.moil_nb_set_graph.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.moil_nb_get_virial.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+    L.moil_nb_set_virial.argtypes = [ctypes.c_void_p, ctypes.c_int]
     _lib = L
     return L
 
@@ -217,6 +219,20 @@ class Nonbonded:
     def energies(self):
         """Per-replica energies of the last evaluation."""
         return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+
+    def set_virial(self, on=True):
+        """Accumulate the water-water LJ virial terms on the mixed path (off by default)."""
+        _check(self.L, self.h, self.L.moil_nb_set_virial(self.h, int(on)))
+
+    def virial(self):
+        """MOIL's LJ virial terms virvdw1..virvdw5 of the last evaluation, per replica (a
+        (5,) array for a single system)."""
+        out = []
+        for r in range(len(self.systems)):
+            v = np.zeros(5)
+            _check(self.L, self.h, self.L.moil_nb_get_virial(self.h, r, v.ctypes.data_as(_dp)))
+            out.append(v)
+        return out if self.batch else out[0]
 
     def eforce_into(self, coor: np.ndarray, dpot: np.ndarray, want_energies: bool = True):
         """Evaluate into caller-owned (natom,3) float64 arrays; returns per-replica energies."""

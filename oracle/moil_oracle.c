@@ -563,7 +563,7 @@ static void lj_ab(const ctx *c, int i, int j, double s2, double *a, double *b)
  * kind 1: LJ if r2 <= cutvdw2, Coulomb always; 2: LJ only (r2 <= cutvdw2);
  * 3: Coulomb if r2 <= cutele2.  xi are the (possibly translated) i coordinates. */
 static void atom_pair(const ctx *c, int kind, int i, double xi, double yi, double zi, int j,
-                      double *dpot, int addi, double *evdw, double *eel, ora_output *out)
+                      double *dpot, int addi, double *evdw, double *eel, double *vir, ora_output *out)
 {
     const ora_input *in = c->in;
     double rx = xi - X(j), ry = yi - Y(j), rz = zi - Z(j);
@@ -581,6 +581,7 @@ static void atom_pair(const ctx *c, int kind, int i, double xi, double yi, doubl
         df1 = -6.0 * s2 * (a + e1);
         lj_switch(c, r2, &e1, &df1);
         *evdw += e1;
+        *vir -= df1 * r2;            /* cdie_ewald_press.f:413-419 */
         out->lj_pairs++;
     }
     if (el) {
@@ -602,7 +603,7 @@ static void atom_pair(const ctx *c, int kind, int i, double xi, double yi, doubl
  * o_i is the i oxygen, sh the translation added to the i molecule. */
 static void water_pair(const ctx *c, int list, int oi, int oj, const double sh[3],
                        double oosgm12, double oosgm6, const double qq[3][3],
-                       double *dpot, double *evdw, double *eel, ora_output *out)
+                       double *dpot, double *evdw, double *eel, double *vir, ora_output *out)
 {
     double xi[3][3], dfi[3][3] = {{0}};
     int a, b, k;
@@ -624,6 +625,7 @@ static void water_pair(const ctx *c, int list, int oi, int oj, const double sh[3
                 df = -6.0 * s2 * (aa + e1);
                 lj_switch(c, rr2, &e1, &df);
                 *evdw += e1;
+                *vir -= df * rr2;    /* watwat_ewald_press.f:146-152 (LJ part only) */
                 out->lj_pairs++;
             }
             erfc_pair(c, c->ewaldcof * rij, &erfcc, &derfc);
@@ -706,6 +708,7 @@ static void ener14(const ctx *c, double *dpot, double *ev14, double *eel14, ora_
             double s6 = s2 * s2 * s2, a = p[0] * s6 * s6, b = p[1] * s6;
             e1 = a - b;
             df1 = -6.0 * s2 * (a + e1);
+            out->virvdw[4] -= df1 * r2;   /* ener14_press.f:51-59 */
         }
         if (fabs(p[2]) > 1e-12) {
             double s = sqrt(s2);
@@ -1077,11 +1080,11 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
     for (i = 1; i <= in->npt - 1; i++) {
         double xi = X(i), yi = Y(i), zi = Z(i);
         for (k = L.point1[i - 1] + 1; k <= L.point1[i]; k++)
-            atom_pair(c, 1, i, xi, yi, zi, L.list1.v[k - 1], dpot, 1, &out->e_vdw, &out->e_el, out);
+            atom_pair(c, 1, i, xi, yi, zi, L.list1.v[k - 1], dpot, 1, &out->e_vdw, &out->e_el, &out->virvdw[2], out);
         for (k = L.point2[i - 1] + 1; k <= L.point2[i]; k++)
-            atom_pair(c, 2, i, xi, yi, zi, L.list2.v[k - 1], dpot, 1, &out->e_vdw, &out->e_el, out);
+            atom_pair(c, 2, i, xi, yi, zi, L.list2.v[k - 1], dpot, 1, &out->e_vdw, &out->e_el, &out->virvdw[2], out);
         for (k = L.point3[i - 1] + 1; k <= L.point3[i]; k++)
-            atom_pair(c, 3, i, xi, yi, zi, L.list3.v[k - 1], dpot, 1, &out->e_vdw, &out->e_el, out);
+            atom_pair(c, 3, i, xi, yi, zi, L.list3.v[k - 1], dpot, 1, &out->e_vdw, &out->e_el, &out->virvdw[2], out);
     }
     /* PME is periodic through anint (ewald_receip.f:250-260): squeezing does not change it */
     if (in->do_pme) ora_pme(in, c->ewaldcof, dpot, &out->e_ew_receip, &out->fpme);
@@ -1095,10 +1098,10 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
             int oi = in->poipt[L.indxwat[iw]] - 2, kk;
             for (kk = L.poinwat1[iw] + 1; kk <= L.poinwat1[iw + 1]; kk++)
                 water_pair(c, 1, oi, in->poipt[L.listwt1.v[kk - 1]] - 2, zero, o12, o6, qq, dpot,
-                           &out->e_vdw, &out->e_el, out);
+                           &out->e_vdw, &out->e_el, &out->virvdw[0], out);
             for (kk = L.poinwat2[iw] + 1; kk <= L.poinwat2[iw + 1]; kk++)
                 water_pair(c, 2, oi, in->poipt[L.listwt2.v[kk - 1]] - 2, zero, o12, o6, qq, dpot,
-                           &out->e_vdw, &out->e_el, out);
+                           &out->e_vdw, &out->e_el, &out->virvdw[0], out);
         }
     }
     /* ener14 */
@@ -1116,7 +1119,7 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
                 int ir = L.symreal1.v[ii - 1], je = L.psym1.v[ii - 1];
                 for (k = (int)jb1; k <= je; k++)
                     atom_pair(c, 1, ir, X(ir) + sh[0], Y(ir) + sh[1], Z(ir) + sh[2], L.list1.v[k - 1], dpot, 1,
-                              &out->e_vsym, &out->e_lsym, out);
+                              &out->e_vsym, &out->e_lsym, &out->virvdw[3], out);
                 jb1 = je + 1;
             }
             is1 = L.iblock1[isym] + 1;
@@ -1124,7 +1127,7 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
                 int ir = L.symreal2.v[ii - 1], je = L.psym2.v[ii - 1];
                 for (k = (int)jb2; k <= je; k++)
                     atom_pair(c, 2, ir, X(ir) + sh[0], Y(ir) + sh[1], Z(ir) + sh[2], L.list2.v[k - 1], dpot, 1,
-                              &out->e_vsym, &out->e_lsym, out);
+                              &out->e_vsym, &out->e_lsym, &out->virvdw[3], out);
                 jb2 = je + 1;
             }
             is2 = L.iblock2[isym] + 1;
@@ -1132,7 +1135,7 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
                 int ir = L.symreal3.v[ii - 1], je = L.psym3.v[ii - 1];
                 for (k = (int)jb3; k <= je; k++)
                     atom_pair(c, 3, ir, X(ir) + sh[0], Y(ir) + sh[1], Z(ir) + sh[2], L.list3.v[k - 1], dpot, 1,
-                              &out->e_vsym, &out->e_lsym, out);
+                              &out->e_vsym, &out->e_lsym, &out->virvdw[3], out);
                 jb3 = je + 1;
             }
             is3 = L.iblock3[isym] + 1;
@@ -1152,7 +1155,7 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
                 int oi = in->poipt[L.symmwat1.v[ii - 1]] - 2, je = L.psymwt1.v[ii - 1];
                 for (k = (int)jb1; k <= je; k++)
                     water_pair(c, 1, oi, in->poipt[L.listwt1.v[k - 1]] - 2, sh, o12, o6, qq, dpot,
-                               &out->e_vsym, &out->e_lsym, out);
+                               &out->e_vsym, &out->e_lsym, &out->virvdw[1], out);
                 jb1 = je + 1;
             }
             is1 = L.iblckwt1[isym] + 1;
@@ -1160,7 +1163,7 @@ static void eforce_lists(ctx *c, lists *LL, double *dpot, ora_output *out)
                 int oi = in->poipt[L.symmwat2.v[ii - 1]] - 2, je = L.psymwt2.v[ii - 1];
                 for (k = (int)jb2; k <= je; k++)
                     water_pair(c, 2, oi, in->poipt[L.listwt2.v[k - 1]] - 2, sh, o12, o6, qq, dpot,
-                               &out->e_vsym, &out->e_lsym, out);
+                               &out->e_vsym, &out->e_lsym, &out->virvdw[1], out);
                 jb2 = je + 1;
             }
             is2 = L.iblckwt2[isym] + 1;
@@ -1289,6 +1292,7 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
                                 int lj, el;
                                 double *ev = img > 0 ? &out->e_vsym : &out->e_vdw;
                                 double *ee = img > 0 ? &out->e_lsym : &out->e_el;
+                                double *vv = &out->virvdw[(ww ? 0 : 2) + (img > 0)];
                                 if (ww) {
                                     int a = i - oxy[i], b = j - oxy[j];
                                     lj = (a == 0 && b == 0) && rr2 <= c->cutvdw2;
@@ -1325,7 +1329,7 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
                                         df2 = -q * s * (s2 * erfcc + s * c->ewaldcof * derfc);
                                     }
                                 }
-                                if (lj) { lj_switch(c, rr2, &e1, &df1); out->lj_pairs++; }
+                                if (lj) { lj_switch(c, rr2, &e1, &df1); out->lj_pairs++; *vv -= df1 * rr2; }
                                 out->site_pairs++;
                                 *ev += e1;
                                 *ee += e2;

@@ -67,6 +67,12 @@ typedef struct ora_output {
     long long excl_pairs;    /* exclusion-correction pairs */
     long long n14;           /* 1-4 pairs */
     long long list_sizes[8]; /* list1,list2,list3,listwt1,listwt2 (primary + images) */
+    /* LJ virial terms of MOIL's PRESS build (pot/watwat_ewald_press.f:146-152,
+     * symm/symwat_ewald_press.f:161-168, pot/cdie_ewald_press.f:413-419,
+     * symm/symcdie_ewald_press.f:164-167, pot/ener14_press.f:51-59): virvdw = -sum df1 r^2
+     * over the LJ pairs (df1 = (dE/dr)/r of the LJ part) of water-water primary, water-water
+     * images, other primary, other images, and 1-4 pairs */
+    double virvdw[5];
 } ora_output;
 
 /* MOIL path: squeeze (optional) -> nbondm/nbond -> syminit -> eforce nonbonded block. */

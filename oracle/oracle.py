@@ -57,7 +57,7 @@ class OraOutput(ctypes.Structure):
         "e_ew_receip", "e_total", "e_dir", "ewaldcof", "fpme")] + [
         ("site_pairs", ctypes.c_longlong), ("lj_pairs", ctypes.c_longlong),
         ("excl_pairs", ctypes.c_longlong), ("n14", ctypes.c_longlong),
-        ("list_sizes", ctypes.c_longlong * 8)]
+        ("list_sizes", ctypes.c_longlong * 8), ("virvdw", ctypes.c_double * 5)]
 
 
 ENERGY_KEYS = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_el14", "e_vdw14", "e_corr", "e_self",
@@ -172,6 +172,7 @@ def output_dict(out: OraOutput) -> dict:
     d["excl_pairs"] = int(out.excl_pairs)
     d["n14"] = int(out.n14)
     d["list_sizes"] = [int(x) for x in out.list_sizes]
+    d["virvdw"] = [float(x) for x in out.virvdw]
     return d
 
 
