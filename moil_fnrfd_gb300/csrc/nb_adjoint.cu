@@ -105,7 +105,7 @@ __global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *
                             const int *__restrict__ site_orig, const void *pos_v, const void *woff_v,
                             const void *lj_v, const unsigned *__restrict__ sflags, const int2 *__restrict__ wl1_cnt,
                             const int *__restrict__ wl1, int cap_row, const int *__restrict__ wl2_off,
-                            const int *__restrict__ wl2, double *__restrict__ dq, double *__restrict__ de,
+                            const int *__restrict__ wl2, int cap2, double *__restrict__ dq, double *__restrict__ de,
                             double *__restrict__ ds)
 {
     typedef typename vec4<T>::type T4;
@@ -155,7 +155,7 @@ __global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *
             lj_adj(R.arith, R.w12d * s6 * s6, R.w6d * s6, epsO, sigO, sj, dE[0], dS[0]);
         }
     }
-    for (int k = wl2_off[i]; k < wl2_off[i + 1]; ++k) {
+    for (int k = min(wl2_off[i], cap2); k < min(wl2_off[i + 1], cap2); ++k) {
         const int s = wl2[k];
         const T4 xj = pos[s];
         const double2 ljj = lj_of<T>(lj_v, s);
@@ -184,7 +184,7 @@ template <typename T>
 __global__ void k_adj_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                            const int *__restrict__ site_orig, const void *pos_v, const void *lj_v,
                            const unsigned *__restrict__ sflags, const int *__restrict__ xl_off,
-                           const int *__restrict__ xl, double *__restrict__ dq, double *__restrict__ de,
+                           const int *__restrict__ xl, int capx, double *__restrict__ dq, double *__restrict__ de,
                            double *__restrict__ ds)
 {
     typedef typename vec4<T>::type T4;
@@ -196,7 +196,7 @@ __global__ void k_adj_atom(int nA, int nW, const RepDev *__restrict__ reps, cons
     const T4 xi = pos[si];
     const double2 lji = lj_of<T>(lj_v, si);
     double phi = 0, dE = 0, dS = 0;
-    for (int q = xl_off[k]; q < xl_off[k + 1]; ++q) {
+    for (int q = min(xl_off[k], capx); q < min(xl_off[k + 1], capx); ++q) {
         const int s = xl[q];
         const T4 xj = pos[s];
         T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
@@ -297,11 +297,12 @@ int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds)
     if (c->nW > 0)
         k_adj_water<float><<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
             (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_woff, c->d_site_lj,
-            c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, d_dq, d_de, d_ds);
+            c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), d_dq,
+            d_de, d_ds);
     if (c->nA > 0)
         k_adj_atom<float><<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
             (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_site_lj,
-            c->d_site_flags, c->d_xl_off, c->d_xl, d_dq, d_de, d_ds);
+            c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), d_dq, d_de, d_ds);
     k_adj_excl14<<<(int)((c->natom + B - 1) / B), B, 0, s>>>(
         (int)c->natom, c->d_atom_rep, c->d_reps, c->d_coor, c->d_q, c->d_lj_d, c->d_ex_off, c->d_ex_j,
         c->d_p14_off, c->d_p14_j, c->d_p14_par, d_dq, d_de, d_ds);

@@ -153,6 +153,9 @@ struct NbCtx {
     int g_gen = -1, list_gen = 0, graph_launches = 0;
 };
 
+// list capacity as the int the kernels compare CSR offsets against
+inline int cap_int(int64_t cap) { return cap > 0x7fffffff ? 0x7fffffff : (int)cap; }
+
 // ---- launchers implemented in the kernel files -------------------------------------
 // lists (nb_lists.cu)
 void nb_launch_build_lists(NbCtx *c, const double *d_coor);

@@ -123,12 +123,14 @@ __device__ __forceinline__ void flush(double g[], long long G[], int n)
 template <typename T, typename Flush>
 __device__ __forceinline__ void water_vs_atoms(const RepDev &R, int i, const typename vec4<T>::type *pos,
                                                const void *lj_v, const unsigned *__restrict__ sflags,
-                                               const int *__restrict__ wl2_off, const int *__restrict__ wl2, T g[9],
-                                               T e4[4], int &npair, Flush &flush_all)
+                                               const int *__restrict__ wl2_off, const int *__restrict__ wl2, int cap2,
+                                               T g[9], T e4[4], int &npair, Flush &flush_all)
 {
     typedef typename vec4<T>::type T4;
     typedef typename cplx<T>::type T2;
-    const int q0 = wl2_off[i], q1 = wl2_off[i + 1];
+    // an overflowed list (offsets past the capacity) is read within the buffer; the
+    // evaluation reports the overflow and is redone with a larger one
+    const int q0 = min(wl2_off[i], cap2), q1 = min(wl2_off[i + 1], cap2);
     if (q0 >= q1) return;
     const T2 *lj = (const T2 *)lj_v;
     const T4 si[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
                                                      const unsigned *__restrict__ sflags,
                                                      const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
                                                      int cap_row, const int *__restrict__ wl2_off,
-                                                     const int *__restrict__ wl2, long long *__restrict__ grad,
+                                                     const int *__restrict__ wl2, int cap2, long long *__restrict__ grad,
                                                      double *__restrict__ e_unit)
 {
     __shared__ long long sG[9][WBLOCK];
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
         if (++cnt == CHUNK) { flush_all(); cnt = 0; }
     }
     flush_all();
-    water_vs_atoms<T>(R, i, pos, lj_v, sflags, wl2_off, wl2, g, e4, npair, flush_all);
+    water_vs_atoms<T>(R, i, pos, lj_v, sflags, wl2_off, wl2, cap2, g, e4, npair, flush_all);
 #pragma unroll
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                                                        const unsigned *__restrict__ sflags,
                                                        const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
                                                        int cap_row, const int *__restrict__ wl2_off,
-                                                       const int *__restrict__ wl2, long long *__restrict__ grad,
+                                                       const int *__restrict__ wl2, int cap2, long long *__restrict__ grad,
                                                        double *__restrict__ e_unit, int intra)
 {
     __shared__ long long sG[9][WBLOCK];
@@ -529,7 +531,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
         if (cnt >= CHUNK) { flush_all(); cnt = 0; }
     }
     flush_all();
-    water_vs_atoms<float>(R, i, pos, lj_v, sflags, wl2_off, wl2, g, e4, npair, flush_all);
+    water_vs_atoms<float>(R, i, pos, lj_v, sflags, wl2_off, wl2, cap2, g, e4, npair, flush_all);
 #pragma unroll
     for (int k = 0; k < 9; ++k) grad[(size_t)9 * i + k] = sG[k][t];
     double *eu = e_unit + NB_EU * (size_t)i;
@@ -545,7 +547,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
 template <typename T>
 __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                                               const void *pos_v, const void *lj_v, const unsigned *__restrict__ sflags,
-                                              const int *__restrict__ xl_off, const int *__restrict__ xl,
+                                              const int *__restrict__ xl_off, const int *__restrict__ xl, int capx,
                                               long long *__restrict__ grad, double *__restrict__ e_unit)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -563,8 +565,9 @@ __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__re
     long long G[3] = {0, 0, 0};
     double elp = 0, eli = 0, eep = 0, eei = 0, vp = 0, vi = 0;
     int cnt = 0, npair = 0;
-    const int q1 = xl_off[k + 1];
-    for (int q = xl_off[k]; q < q1; ++q) {
+    // an overflowed list is read within the buffer (the evaluation is redone)
+    const int q1 = min(xl_off[k + 1], capx);
+    for (int q = min(xl_off[k], capx); q < q1; ++q) {
         nb_prefetch_l1(xl + min(q + 32, q1 - 1));
         int s = xl[q];
         T4 xj = pos[s];
@@ -866,18 +869,19 @@ void realspace_t(NbCtx *c)
             (c->virial ? k_water_f<true> : k_water_f<false>)<<<nb, WBLOCK, 0, s>>>(
                 (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float4 *)c->d_woff,
                 c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2,
-                c->d_grad_site, c->d_e_unit, c->water_excl_fast);
+                cap_int(c->cap_wl2), c->d_grad_site, c->d_e_unit, c->water_excl_fast);
         else
             k_water<T><<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
                                              c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1,
-                                             c->d_wl2_off, c->d_wl2, c->d_grad_site, c->d_e_unit);
+                                             c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), c->d_grad_site,
+                                             c->d_e_unit);
         c->launches++;
     }
     if (c->timing) cudaEventRecord(c->ev[3], s);
     if (c->nA > 0) {
         k_atom<T><<<(int)((c->nA + 127) / 128), 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep,
                                                              c->d_pos, c->d_site_lj, c->d_site_flags, c->d_xl_off,
-                                                             c->d_xl, c->d_grad_site, c->d_e_unit);
+                                                             c->d_xl, cap_int(c->cap_xl), c->d_grad_site, c->d_e_unit);
         c->launches++;
     }
     if (c->timing) cudaEventRecord(c->ev[4], s);

@@ -348,15 +348,16 @@ def _self_avoiding_chain(rng, n, bond, radius, dmin, max_tries=200):
 
 
 def config1(seed: int = 2025, n_solute: int = 2489, n_ions: int = 7, n_waters: int = 7020,
-            box: float = 62.2) -> MoilSystem:
+            box: float = 62.2, arith: bool = True, tiny_h: bool = False) -> MoilSystem:
     """Protein-like solute + 7 Na+ + TIP3P in a 62.2 Å cube (N = 23,556 with 7,020 waters).
 
     The stated 23,558 cannot be formed from 2,489 solute atoms, 7 ions and
     whole three-site waters (21,062 is not a multiple of 3); 7,020 waters
-    give 23,556 atoms.
+    give 23,556 atoms.  arith=False switches to MOIL's geometric encoding; tiny_h makes
+    every third solute atom a hydrogen with eps 0.01, Rmin/2 0.2245 (epsgm12 < 1e-3 under
+    the geometric rule, so MOIL's hvdw0 rule applies to its pairs, pot/nbond.f:115-126).
     """
     rng = np.random.Generator(np.random.PCG64(seed))
-    arith = True
     # solute: compact self-avoiding chain at protein-like density (~0.083 atoms/Å^3)
     radius = (3.0 * (n_solute / 0.083) / (4.0 * math.pi)) ** (1.0 / 3.0)
     chain = _self_avoiding_chain(rng, n_solute, 1.5, radius, 2.0)
@@ -368,6 +369,9 @@ def config1(seed: int = 2025, n_solute: int = 2489, n_ions: int = 7, n_waters: i
     typ = np.arange(n_solute) % 4
     sig = np.array([rmin2_to_sigma(r) for r in rm2_t])[typ]
     eps = eps_t[typ]
+    if tiny_h:
+        h = np.arange(n_solute) % 3 == 2
+        sig[h], eps[h] = rmin2_to_sigma(0.2245), 0.01
     b = _Builder(arith=arith)
     # monomers of three beads; bonded exclusions and 1-4 pairs span monomers
     n_mono = (n_solute + 2) // 3
@@ -392,8 +396,9 @@ def config1(seed: int = 2025, n_solute: int = 2489, n_ions: int = 7, n_waters: i
         ions.append(p)
     for p in ions:
         b.add_monomer(p[None, :], [1.0], [0.0469], [rmin2_to_sigma(1.3638)], MON_ION)
-    # water: lattice of candidate sites, drop those within 2.4 Å of solute or ions, seeded pick
-    m = 21
+    # water: lattice of candidate sites at ~2.96 Å spacing (21 per side of the 62.2 Å box),
+    # drop those within 2.4 Å of solute or ions, seeded pick
+    m = max(2, int(round(box / 2.962)))
     cand = _lattice_sites(m, box) + rng.uniform(-0.3, 0.3, size=(m ** 3, 3))
     frame_sites = _place_waters(rng, cand).reshape(-1, 3, 3)
     heavy = np.concatenate([chain, np.asarray(ions)], axis=0)

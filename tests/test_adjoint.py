@@ -86,8 +86,8 @@ def test_lj_derivatives_match_fd(solute, which):
     eps, sig = decode(s)
     for i in (3, 40, 60):
         base = eps[i] if which == "eps" else sig[i]
-        # the solute packs atoms inside each other's LJ cores (E_LJ ~ 1e8 kcal/mol), so the
-        # steps are larger than for the charges, where the energy is exactly quadratic:
+        # the compact solute's LJ energy (~2e3 kcal/mol) is large next to one atom's share, so
+        # the steps are larger than for the charges, where the energy is exactly quadratic:
         # eps enters as sqrt (central-difference error h^2/8), sigma as sigma^12 and sigma^6
         h = (1e-2 if which == "eps" else 1e-3) * base
 
