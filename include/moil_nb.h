@@ -206,6 +206,15 @@ int moil_nb_set_graph(moil_nb_ctx *h, int on);
  * accumulate them.  No counterpart in the reference (its PRESS build always does). */
 int moil_nb_set_virial(moil_nb_ctx *h, int on);
 
+/* Replica groups for the next moil_nb_init_batch: 0 automatic (two groups for batches of
+ * at least a million atoms in 8 or more replicas), 1 none, P >= 2 that many.  A grouped
+ * handle evaluates contiguous replica ranges concurrently, each with its own stream, lists
+ * and graph, so one group's host copies and latency-bound kernels overlap another's work;
+ * every replica's result is bit-identical to the ungrouped evaluation.  moil_nb_groups
+ * returns the number in use.  No counterpart in the reference. */
+int moil_nb_set_groups(moil_nb_ctx *h, int groups);
+int moil_nb_groups(const moil_nb_ctx *h);
+
 /* ---- PME reciprocal sum without device allocation -------------------------
  * No counterpart in the reference (MOIL's ewald_receip() works on static COMMON
  * arrays and never allocates).  This entry point is for callers that cannot call

@@ -568,14 +568,19 @@ bool launch_graph(NbCtx *c, const double *d_coor, double *d_dpot)
     return cudaGraphLaunch(c->gexec, s) == cudaSuccess;
 }
 
-int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
+// queue one evaluation on the context's stream (no synchronisation)
+void eval_launch(NbCtx *c, const double *d_coor, double *d_dpot)
 {
-    cudaStream_t s = c->stream;
     bool forced = c->need_rebuild || (c->list_period > 0 && c->evals_since_build >= c->list_period);
     c->h_status[8] = forced ? 1 : 0;
     for (int k = 9; k < 16; ++k) c->h_status[k] = 0;
     if (!(c->use_graph && !c->timing && launch_graph(c, d_coor, d_dpot))) enqueue_eval(c, d_coor, d_dpot);
-    NB_CUDA_OK(c, cudaStreamSynchronize(s));
+}
+
+// wait for the queued evaluation and read its status words
+int eval_complete(NbCtx *c)
+{
+    NB_CUDA_OK(c, cudaStreamSynchronize(c->stream));
     NB_CUDA_OK(c, cudaGetLastError());
     int rebuilt = c->h_status[0] != 0;
     if (rebuilt) {
@@ -613,22 +618,15 @@ int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
     return MOIL_NB_OK;
 }
 
-int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
+int eval_once(NbCtx *c, const double *d_coor, double *d_dpot)
 {
-    int rc = MOIL_NB_OK;
-    for (int attempt = 0; attempt < 4; ++attempt) {
-        rc = eval_once(c, d_coor, d_dpot);
-        if (rc != MOIL_NB_ERR_OVERFLOW) break;
-        // grow from the exact totals the count pass produced, then redo with a fresh build
-        int64_t need1 = c->h_status[6], need2 = c->h_status[3], need3 = c->h_status[4];
-        c->cap_row1 = std::max<int>(c->cap_row1, (int)((need1 + need1 / 8 + 32 + 31) & ~31));
-        c->cap_wl2 = std::max<int64_t>(c->cap_wl2, need2 + need2 / 8 + 64);
-        c->cap_xl = std::max<int64_t>(c->cap_xl, need3 + need3 / 8 + 64);
-        int a = alloc_lists(c);
-        if (a != MOIL_NB_OK) return a;
-        c->need_rebuild = 1;
-    }
-    if (rc != MOIL_NB_OK) return rc;
+    eval_launch(c, d_coor, d_dpot);
+    return eval_complete(c);
+}
+
+// per-replica energies and the pair count of the last completed evaluation
+void read_energies(NbCtx *c, moil_energies *e)
+{
     if (e) {
         for (int r = 0; r < c->nrep; ++r) {
             const double *o = c->h_e_rep + NB_EREP * r;
@@ -638,12 +636,119 @@ int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
             E.e_ew_receip = o[8]; E.e_total = o[9]; E.e_dir = o[10];
         }
     }
-    {
-        double np = 0;
-        for (int r = 0; r < c->nrep; ++r) np += c->h_e_rep[NB_EREP * r + 11];
-        c->last_site_pairs = (int64_t)(np + 0.5);
+    double np = 0;
+    for (int r = 0; r < c->nrep; ++r) np += c->h_e_rep[NB_EREP * r + 11];
+    c->last_site_pairs = (int64_t)(np + 0.5);
+}
+
+// an evaluation whose first attempt (if any) has completed with status rc: on a list
+// overflow, grow the lists from the counts and redo
+int eval_retry(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e, int rc, bool done)
+{
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        if (!done || attempt > 0) rc = eval_once(c, d_coor, d_dpot);
+        if (rc != MOIL_NB_ERR_OVERFLOW) break;
+        // grow from the exact totals the count pass produced, then redo with a fresh build
+        int64_t need1 = c->h_status[6], need2 = c->h_status[3], need3 = c->h_status[4];
+        c->cap_row1 = std::max<int>(c->cap_row1, (int)((need1 + need1 / 8 + 32 + 31) & ~31));
+        c->cap_wl2 = std::max<int64_t>(c->cap_wl2, need2 + need2 / 8 + 64);
+        c->cap_xl = std::max<int64_t>(c->cap_xl, need3 + need3 / 8 + 64);
+        int a = alloc_lists(c);
+        if (a != MOIL_NB_OK) return a;
+        c->need_rebuild = 1;
+        done = false;
     }
+    if (rc != MOIL_NB_OK) return rc;
+    read_energies(c, e);
     return MOIL_NB_OK;
+}
+
+int eval_impl(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e)
+{
+    return eval_retry(c, d_coor, d_dpot, e, MOIL_NB_OK, false);
+}
+
+// ---- replica groups ------------------------------------------------------------------
+// A large batch is split into contiguous replica ranges, each a complete context with its own
+// stream, lists, PME work and graph.  The groups' evaluations are queued together and run
+// concurrently: one group's host copies overlap another's kernels, and one group's
+// latency-bound PME kernels share the multiprocessors with another's pair kernel.  Every
+// replica's result is computed by the same kernels in the same order as without groups.
+int group_of(const NbCtx *h, int r)
+{
+    int g = 0;
+    while (g + 1 < (int)h->grp.size() && h->grp_rep0[g + 1] <= r) ++g;
+    return g;
+}
+
+int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bool host)
+{
+    const int P = (int)h->grp.size();
+    // device-resident callers may have queued their coordinates on the handle's stream
+    NB_CUDA_OK(h, cudaEventRecord(h->ev[11], h->stream));
+    auto slice_bytes = [&](int g) { return sizeof(double) * 3 * (size_t)(h->grp_atom0[g + 1] - h->grp_atom0[g]); };
+    auto launch = [&](int g) -> int {
+        NbCtx *c = h->grp[g];
+        NB_CUDA_OK(c, cudaStreamWaitEvent(c->stream, h->ev[11], 0));
+        const double *src = coor + 3 * h->grp_atom0[g];
+        double *dst = dpot + 3 * h->grp_atom0[g];
+        if (host) {
+            NB_CUDA_OK(c, cudaMemcpyAsync(c->d_coor, src, slice_bytes(g), cudaMemcpyHostToDevice, c->stream));
+            eval_launch(c, c->d_coor, c->d_dpot);
+            NB_CUDA_OK(c, cudaMemcpyAsync(dst, c->d_dpot, slice_bytes(g), cudaMemcpyDeviceToHost, c->stream));
+        } else {
+            eval_launch(c, src, dst);
+        }
+        return MOIL_NB_OK;
+    };
+    auto finish = [&](int g) -> int {
+        NbCtx *c = h->grp[g];
+        const double *dc = host ? c->d_coor : coor + 3 * h->grp_atom0[g];
+        double *dd = host ? c->d_dpot : dpot + 3 * h->grp_atom0[g];
+        const int first = eval_complete(c);
+        int rc = eval_retry(c, dc, dd, e ? e + h->grp_rep0[g] : nullptr, first, true);
+        if (rc == MOIL_NB_OK && host && first == MOIL_NB_ERR_OVERFLOW) {
+            // redone after an overflow: the gradient copied with the first attempt is stale
+            NB_CUDA_OK(c, cudaMemcpyAsync(dpot + 3 * h->grp_atom0[g], c->d_dpot, slice_bytes(g),
+                                          cudaMemcpyDeviceToHost, c->stream));
+            NB_CUDA_OK(c, cudaStreamSynchronize(c->stream));
+        }
+        return rc;
+    };
+    int rc = MOIL_NB_OK;
+    if (h->timing) {
+        // diagnostic mode: one group after the other, stage times summed
+        moil_nb_timing sum{};
+        for (int g = 0; g < P && rc == MOIL_NB_OK; ++g) {
+            rc = launch(g);
+            if (rc == MOIL_NB_OK) rc = finish(g);
+            const moil_nb_timing &t = h->grp[g]->last_timing;
+            sum.prepare_ms += t.prepare_ms; sum.list_ms += t.list_ms; sum.water_ms += t.water_ms;
+            sum.atom_ms += t.atom_ms; sum.excl_ms += t.excl_ms; sum.pme_spread_fft_ms += t.pme_spread_fft_ms;
+            sum.pme_conv_ms += t.pme_conv_ms; sum.pme_gather_ms += t.pme_gather_ms;
+            sum.finalize_ms += t.finalize_ms; sum.total_ms += t.total_ms;
+            sum.list_rebuilt |= t.list_rebuilt; sum.launches += t.launches;
+        }
+        h->last_timing = sum;
+    } else {
+        for (int g = 0; g < P && rc == MOIL_NB_OK; ++g) rc = launch(g);
+        for (int g = 0; g < P; ++g) {
+            int r = finish(g);
+            if (r != MOIL_NB_OK && rc == MOIL_NB_OK) rc = r;
+        }
+    }
+    int64_t pairs = 0, entries = 0;
+    int launches = 0;
+    for (NbCtx *c : h->grp) {
+        pairs += c->last_site_pairs;
+        entries += c->last_list_entries;
+        launches += c->launches;
+        if (!c->err.empty() && h->err.empty()) h->err = c->err;
+    }
+    h->last_site_pairs = pairs;
+    h->last_list_entries = entries;
+    h->launches = launches;
+    return rc;
 }
 
 std::mutex g_fortran_mu;
@@ -653,6 +758,63 @@ std::vector<double> g_fortran_buf;
 }  // namespace
 
 struct moil_nb_ctx : NbCtx {};
+
+namespace {
+
+void destroy_groups(NbCtx *h)
+{
+    for (NbCtx *c : h->grp) moil_nb_destroy(static_cast<moil_nb_ctx *>(c));
+    h->grp.clear();
+    h->grp_rep0.clear();
+    h->grp_atom0.clear();
+}
+
+// groups for a batch: automatic for batches of at least a million atoms in 8 or more
+// replicas (two groups), where copy/kernel overlap pays; none for smaller ones
+int choose_groups(const NbCtx *h, int nrep, int64_t natom)
+{
+    if (h->want_groups == 1 || nrep < 2) return 1;
+    if (h->want_groups >= 2) return std::min(h->want_groups, nrep);
+    return (nrep >= 8 && natom >= 1000000) ? 2 : 1;
+}
+
+int init_groups(moil_nb_ctx *h, int nrep, const moil_replica *reps, int P)
+{
+    int64_t total = 0;
+    for (int r = 0; r < nrep; ++r) total += reps[r].topo ? reps[r].topo->npt : 0;
+    // contiguous replica ranges of about total / P atoms
+    h->grp_rep0.assign(1, 0);
+    h->grp_atom0.assign(1, 0);
+    int64_t acc = 0;
+    for (int r = 0; r < nrep; ++r) {
+        acc += reps[r].topo->npt;
+        const int g = (int)h->grp_rep0.size();
+        if (g < P && r + 1 < nrep && acc >= (total * g + P - 1) / P) {
+            h->grp_rep0.push_back(r + 1);
+            h->grp_atom0.push_back(acc);
+        }
+    }
+    h->grp_rep0.push_back(nrep);
+    h->grp_atom0.push_back(total);
+    for (size_t g = 0; g + 1 < h->grp_rep0.size(); ++g) {
+        moil_nb_ctx *c = nullptr;
+        int rc = moil_nb_create(&c, h->device);
+        if (rc != MOIL_NB_OK) { h->err = "creating a replica group"; destroy_groups(h); return rc; }
+        c->use_graph = h->use_graph;
+        c->virial = h->virial;
+        c->timing = h->timing;
+        h->grp.push_back(c);
+        rc = init_impl(c, h->grp_rep0[g + 1] - h->grp_rep0[g], reps + h->grp_rep0[g]);
+        if (rc != MOIL_NB_OK) { h->err = c->err; destroy_groups(h); return rc; }
+    }
+    h->nrep = nrep;
+    h->natom = total;
+    h->precision = h->grp[0]->precision;
+    h->inited = 1;
+    return MOIL_NB_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -694,6 +856,7 @@ void moil_nb_destroy(moil_nb_ctx *h)
     if (!h) return;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    destroy_groups(h);
     release_device(h);
     for (int k = 0; k < 12; ++k)
         if (h->ev[k]) cudaEventDestroy(h->ev[k]);
@@ -708,6 +871,7 @@ int moil_nb_init(moil_nb_ctx *h, const moil_nb_params *p, const moil_topology *t
     if (!h || !p || !t) return MOIL_NB_ERR_ARG;
     moil_replica r = {p, t};
     cudaSetDevice(h->device);
+    destroy_groups(h);
     return init_impl(h, 1, &r);
 }
 
@@ -715,12 +879,26 @@ int moil_nb_init_batch(moil_nb_ctx *h, int nrep, const moil_replica *reps)
 {
     if (!h) return MOIL_NB_ERR_ARG;
     cudaSetDevice(h->device);
-    return init_impl(h, nrep, reps);
+    destroy_groups(h);
+    int64_t natom = 0;
+    for (int r = 0; r < nrep && reps; ++r) {
+        if (!reps[r].params || !reps[r].topo) { h->err = "replica without parameters or topology"; return MOIL_NB_ERR_ARG; }
+        natom += reps[r].topo->npt;
+    }
+    const int P = reps ? choose_groups(h, nrep, natom) : 1;
+    if (P <= 1) return init_impl(h, nrep, reps);
+    if (h->inited) release_device(h);
+    h->inited = 0;
+    return init_groups(h, nrep, reps, P);
 }
 
 int moil_nb_get_alpha(const moil_nb_ctx *h, int r, double *alpha)
 {
     if (!h || !alpha || !h->inited || r < 0 || r >= h->nrep) return MOIL_NB_ERR_ARG;
+    if (!h->grp.empty()) {
+        const int g = group_of(h, r);
+        return moil_nb_get_alpha(static_cast<const moil_nb_ctx *>(h->grp[g]), r - h->grp_rep0[g], alpha);
+    }
     *alpha = h->rh[r].alpha;
     return MOIL_NB_OK;
 }
@@ -730,6 +908,7 @@ int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies
     if (!h || !coor || !dpot) return MOIL_NB_ERR_ARG;
     if (!h->inited) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
+    if (!h->grp.empty()) return eval_groups(h, coor, dpot, e, true);
     // staged through device copies even for pinned buffers: on GB300 the finalize kernel
     // storing 63 MB of gradient straight into pinned host memory took 1.15 ms, while copying
     // the coordinates in and the gradient out took 0.7 ms together
@@ -752,6 +931,16 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
         return MOIL_NB_ERR_ARG;
     }
     cudaSetDevice(h->device);
+    if (!h->grp.empty()) {
+        for (size_t g = 0; g < h->grp.size(); ++g) {
+            const int64_t a0 = h->grp_atom0[g];
+            auto at = [&](double *p) { return p ? p + a0 : nullptr; };
+            int rc = moil_nb_adjoint(static_cast<moil_nb_ctx *>(h->grp[g]), coor + 3 * a0, at(dEdq), at(dEdeps),
+                                     at(dEdsig), e ? e + h->grp_rep0[g] : nullptr);
+            if (rc != MOIL_NB_OK) { h->err = h->grp[g]->err; return rc; }
+        }
+        return MOIL_NB_OK;
+    }
     const size_t n = (size_t)h->natom;
     NB_CUDA_OK(h, cudaMemcpyAsync(h->d_coor, coor, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
     int rc = eval_impl(h, h->d_coor, h->d_dpot, e);   // lists, positions and the potential grid
@@ -776,6 +965,10 @@ int moil_nb_get_virial(moil_nb_ctx *h, int replica, double *virvdw)
         h->err = "replica index out of range";
         return MOIL_NB_ERR_ARG;
     }
+    if (!h->grp.empty()) {
+        const int g = group_of(h, replica);
+        return moil_nb_get_virial(static_cast<moil_nb_ctx *>(h->grp[g]), replica - h->grp_rep0[g], virvdw);
+    }
     const double *o = h->h_e_rep + NB_EREP * (size_t)replica;
     for (int k = 0; k < 5; ++k) virvdw[k] = o[12 + k];
     return MOIL_NB_OK;
@@ -786,6 +979,7 @@ int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, mo
     if (!h || !d_coor || !d_dpot) return MOIL_NB_ERR_ARG;
     if (!h->inited) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
+    if (!h->grp.empty()) return eval_groups(h, d_coor, d_dpot, e, false);
     return eval_impl(h, d_coor, d_dpot, e);
 }
 
@@ -793,6 +987,7 @@ int moil_nb_request_rebuild(moil_nb_ctx *h)
 {
     if (!h) return MOIL_NB_ERR_ARG;
     h->need_rebuild = 1;
+    for (NbCtx *c : h->grp) c->need_rebuild = 1;
     return MOIL_NB_OK;
 }
 
@@ -831,6 +1026,7 @@ int moil_nb_set_timing(moil_nb_ctx *h, int on)
 {
     if (!h) return MOIL_NB_ERR_ARG;
     h->timing = on ? 1 : 0;
+    for (NbCtx *c : h->grp) c->timing = h->timing;
     return MOIL_NB_OK;
 }
 
@@ -855,6 +1051,7 @@ int moil_nb_set_graph(moil_nb_ctx *h, int on)
     cudaSetDevice(h->device);
     h->use_graph = on ? 1 : 0;
     drop_graph(h);
+    for (NbCtx *c : h->grp) { c->use_graph = h->use_graph; drop_graph(c); }
     return MOIL_NB_OK;
 }
 
@@ -864,7 +1061,20 @@ int moil_nb_set_virial(moil_nb_ctx *h, int on)
     cudaSetDevice(h->device);
     h->virial = on ? 1 : 0;
     drop_graph(h);
+    for (NbCtx *c : h->grp) { c->virial = h->virial; drop_graph(c); }
     return MOIL_NB_OK;
+}
+
+int moil_nb_set_groups(moil_nb_ctx *h, int groups)
+{
+    if (!h || groups < 0) return MOIL_NB_ERR_ARG;
+    h->want_groups = groups;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_groups(const moil_nb_ctx *h)
+{
+    return h ? std::max<int>(1, (int)h->grp.size()) : 0;
 }
 
 // ---- Fortran entry points --------------------------------------------------------

@@ -147,6 +147,13 @@ struct NbCtx {
     // CUDA graph of one evaluation, valid for the caller pointers and list buffers it captured
     int use_graph = 1;
     int virial = 0;                    // water-water LJ virial in the FP32 water kernel
+
+    // replica groups (nb_host.cu): a batch evaluated as concurrent contiguous replica ranges,
+    // each a complete context; this context then holds no device buffers of its own
+    std::vector<NbCtx *> grp;
+    std::vector<int> grp_rep0;         // first replica of each group, then nrep
+    std::vector<int64_t> grp_atom0;    // first caller atom of each group, then natom
+    int want_groups = 0;               // 0: automatic, 1: none, P: P groups (next init)
     cudaGraphExec_t gexec = nullptr;
     const double *g_coor = nullptr;
     double *g_dpot = nullptr;

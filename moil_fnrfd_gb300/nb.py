@@ -30,7 +30,7 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device", "moil_nb_adjoint",
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
-            "moil_nb_get_virial", "moil_nb_set_virial", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
+            "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -113,6 +113,8 @@ def load(build_if_missing: bool = True):
     L.moil_nb_set_graph.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.moil_nb_get_virial.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     L.moil_nb_set_virial.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.moil_nb_set_groups.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.moil_nb_groups.argtypes = [ctypes.c_void_p]
     _lib = L
     return L
 
@@ -174,11 +176,12 @@ class Nonbonded:
     """One device handle over one system or a batch of independent replicas."""
 
     def __init__(self, systems, precision=MOIL_NB_MIXED, device=0, skin=1.0, list_period=0,
-                 lj_switch=False, timing=False):
+                 lj_switch=False, timing=False, groups=0):
         self.L = load()
         h = ctypes.c_void_p()
         _check(self.L, None, self.L.moil_nb_create(ctypes.byref(h), int(device)))
         self.h = h
+        _check(self.L, self.h, self.L.moil_nb_set_groups(self.h, int(groups)))
         self.batch = isinstance(systems, (list, tuple))
         self.systems = list(systems) if self.batch else [systems]
         keep = _Keep()
@@ -219,6 +222,10 @@ class Nonbonded:
     def energies(self):
         """Per-replica energies of the last evaluation."""
         return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
+
+    def groups(self) -> int:
+        """Number of concurrently evaluated replica groups (1: none)."""
+        return int(self.L.moil_nb_groups(self.h))
 
     def set_virial(self, on=True):
         """Accumulate the water-water LJ virial terms on the mixed path (off by default)."""
