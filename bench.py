@@ -15,8 +15,8 @@ roofline   : the dominant kernel against the FP32 pipe (pair math is FP32-bound)
 cpu_baseline: the oracle (a C restatement of MOIL's FP64 routines, MOIL's own list path
              and erfc table) on a bounded sample of replicas, one host thread
 plain_fp64 : the plain FP64 GPU path, one replica per launch, on a sample of replicas
-single_system_md: one 96,000-atom water box through a 1,000-step rigid-water trajectory
-             (lists every 10 steps, 1.5 Å skin), evaluations timed, with the FP64 path beside it
+single_system_md: one 96,000-atom water box through a 1,000-step rigid-water trajectory on the
+             device (lists every 10 steps, 1.5 Å skin), whole steps timed, the FP64 path beside it
 """
 from __future__ import annotations
 
@@ -136,50 +136,49 @@ def cpu_baseline(reps, budget_s=12.0):
 
 def md_leg(local, steps=1000, warmup=20):
     """One 96,000-atom water box (32,000 TIP3P, 98.6 Å, rc 10, alpha 0.32, grid 100^3) through
-    a rigid-water leapfrog trajectory: 2 fs steps from 300 K, pair lists rebuilt every 10
-    steps with a 1.5 Å skin.  Evaluations are timed with CUDA events on the library's stream
-    (the harness's own SETTLE/leapfrog operations between them are not)."""
+    a rigid-water leapfrog trajectory on the device (moil_nb_md_step: evaluation, leapfrog and
+    SETTLE each step, nothing copied to the host): 2 fs steps from 300 K, pair lists rebuilt
+    every 10 steps with a 1.5 Å skin.  Timed by wall clock around the whole trajectory."""
     import torch
     from moil_fnrfd_gb300 import dyna, systems
     from moil_fnrfd_gb300.nb import MOIL_NB_FP64, Nonbonded
     s = systems.config2()
     nb = Nonbonded(s, device=local, skin=1.5, list_period=10)
-    md = dyna.RigidWaterDynamics(nb, s, dt=0.002, temperature=300.0, seed=11)
-    md.step(warmup)
-    e0 = md.energies[0]["e_total"] + md.kinetic()
-    st = md.stream
-    ev = []
-    for _ in range(steps):
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(st)
-        md.evaluate()
-        b.record(st)
-        ev.append((a, b))
-        with torch.cuda.stream(st):
-            md.advance()
+    start = dyna.RigidWaterDynamics(nb, s, dt=0.002, temperature=300.0, seed=11)   # initial velocities
+    x, v = start.x.clone(), start.v.clone()
+    m = torch.tensor(dyna._masses(s)[0], dtype=torch.float64, device=x.device)
     torch.cuda.synchronize()
-    eval_ms = [a.elapsed_time(b) for a, b in ev]
-    e1 = md.energies[0]["e_total"] + md.kinetic()
+    nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.002, warmup)
+    e, ek = nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.002, 1)
+    e0 = e[0]["e_total"] + ek
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e, ek = nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.002, steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    e1 = e[0]["e_total"] + ek
+    a, b, c = (x[k::3] for k in range(3))
+    cerr = float((torch.linalg.vector_norm(b - a, dim=1) - systems.TIP3_ROH).abs().max())
     out = {"workload": "32,000 TIP3P waters (96,000 atoms), 98.6 Å box, rc 10 Å, alpha 0.32, PME 100^3, "
-                       "rigid-water leapfrog at 2 fs from 300 K, lists every 10 steps, 1.5 Å skin",
-           "steps": steps, "value": s.npt * steps / (sum(eval_ms) / 1e3), "unit": "atom-evals/s",
-           "ms_per_eval": statistics.mean(eval_ms), "ms_per_eval_max": max(eval_ms),
-           "energy_total_start_end": [e0, e1], "constraint_err_A": md.constraint_error()}
+                       "rigid-water leapfrog (SETTLE) at 2 fs from 300 K on the device, lists every 10 steps, "
+                       "1.5 Å skin",
+           "steps": steps, "value": s.npt * steps / wall, "unit": "atom-evals/s (whole MD steps)",
+           "ms_per_step": 1e3 * wall / steps, "ns_per_day": steps * 0.002e-3 / wall * 86400.0,
+           "energy_total_start_end": [e0, e1], "constraint_err_A": cerr}
     nb.close()
     p = Nonbonded(s, precision=MOIL_NB_FP64, device=local)
     dc = torch.from_numpy(s.coor).to(f"cuda:{local}")
     dd = torch.empty_like(dc)
     p.eforce_device(dc.data_ptr(), dd.data_ptr())
     stp = torch.cuda.ExternalStream(p.stream())
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    a.record(stp)
+    ta = torch.cuda.Event(enable_timing=True)
+    tb = torch.cuda.Event(enable_timing=True)
+    ta.record(stp)
     for _ in range(3):
         p.eforce_device(dc.data_ptr(), dd.data_ptr())
-    b.record(stp)
+    tb.record(stp)
     torch.cuda.synchronize()
-    out["plain_fp64_ms_per_eval"] = a.elapsed_time(b) / 3
+    out["plain_fp64_ms_per_eval"] = ta.elapsed_time(tb) / 3
     p.close()
     return out
 

@@ -241,6 +241,28 @@ int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int natom, cons
                         const int *grid, double alpha, double eps, double *d_dpot, double *e_recip,
                         void *stream);
 
+/* ---- Molecular dynamics around the evaluation (device-resident) ------------
+ * nsteps leapfrog steps of the handle's system(s): each step evaluates the nonbonded
+ * gradient at d_coor, then v -= dt * 418.4 * dpot / m and x += dt * v (Å, ps, amu,
+ * kcal/mol), water molecules held rigid by SETTLE (Miyamoto & Kollman 1992) at the
+ * distances water_geom = (O-H, H-H) (NULL: TIP3P, O-H 0.9572 and H-O-H 104.52 degrees),
+ * other atoms free (the
+ * library holds no bonded terms).  Stands in for dynamics/dyna.f:183-330 with SHAKE on
+ * water (dynamics/shakept.f, mshakpt.f) when the nonbonded terms are the whole force field.
+ *   d_coor, d_vel (3*natom, caller order, updated in place; d_vel holds v(t - dt/2) on entry
+ *   and v(t + dt/2) on return), d_mass (natom), dt in ps
+ *   energies: those of the last step's evaluation; *ekin: kinetic energy of the returned
+ *   half-step velocities (kcal/mol), either may be NULL.  No counterpart in the reference's
+ *   C/Fortran interface (its integrator stays in Fortran). */
+int moil_nb_md_step(moil_nb_ctx *h, double *d_coor, double *d_vel, const double *d_mass, double dt, int nsteps,
+                    const double *water_geom, moil_energies *energies, double *ekin);
+
+/* Trajectory frames in the binary format of dynamics/wdyncrd.f (Fortran unformatted
+ * sequential records): with first != 0 the file is created with the header ('CORD' + 20
+ * integers, nframes in the first; a title record; the atom count) before the frame; else
+ * the frame is appended.  A frame is three records of natom floats (x, y, z). */
+int moil_nb_dcd_write(const char *path, int first, int nframes, int natom, const double *coor);
+
 /* ---- Fortran entry points (gfortran naming, all arguments by reference) --
  * A maintainer replaces the nonbonded block of pot/eforce.f:122-204 with
  *     call eforce_nb_gpu(npt, coor, dpot, enb, status)

@@ -85,7 +85,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
-    free_ptr(c->d_adj);
+    free_ptr(c->d_adj); free_ptr(c->d_md_dpot);
     if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
     c->h_e_rep = nullptr;
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -756,8 +756,6 @@ moil_nb_ctx *g_fortran_ctx = nullptr;
 std::vector<double> g_fortran_buf;
 
 }  // namespace
-
-struct moil_nb_ctx : NbCtx {};
 
 namespace {
 

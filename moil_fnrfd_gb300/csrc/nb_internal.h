@@ -129,6 +129,7 @@ struct NbCtx {
     // caller buffers used by host-pointer evaluations
     double *d_coor = nullptr, *d_dpot = nullptr;
     double *d_adj = nullptr;           // parameter derivatives, 3 x natom (allocated on first use)
+    double *d_md_dpot = nullptr;       // gradient of the MD steps (moil_nb_md_step, first use)
 
     // device status: [0] rebuild flag, [1] error bits, [2..4] W1 / W2 / X entry totals,
     // [6] longest W1 row; all reset at the start of every evaluation
@@ -159,6 +160,9 @@ struct NbCtx {
     double *g_dpot = nullptr;
     int g_gen = -1, list_gen = 0, graph_launches = 0;
 };
+
+// the public handle is the context itself
+struct moil_nb_ctx : NbCtx {};
 
 // list capacity as the int the kernels compare CSR offsets against
 inline int cap_int(int64_t cap) { return cap > 0x7fffffff ? 0x7fffffff : (int)cap; }

@@ -30,7 +30,8 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device", "moil_nb_adjoint",
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
-            "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
+            "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "moil_nb_md_step",
+            "moil_nb_dcd_write", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -114,6 +115,9 @@ def load(build_if_missing: bool = True):
     L.moil_nb_get_virial.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     L.moil_nb_set_virial.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.moil_nb_set_groups.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.moil_nb_md_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_double, ctypes.c_int, _dp, ctypes.POINTER(Energies), _dp]
+    L.moil_nb_dcd_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
     L.moil_nb_groups.argtypes = [ctypes.c_void_p]
     _lib = L
     return L
@@ -223,6 +227,20 @@ class Nonbonded:
         """Per-replica energies of the last evaluation."""
         return [{k: getattr(self._e[r], k) for k in ENERGY_KEYS} for r in range(len(self.systems))]
 
+    def md_step(self, d_coor_ptr: int, d_vel_ptr: int, d_mass_ptr: int, dt: float, nsteps: int = 1,
+                water_geom=None):
+        """nsteps device-resident leapfrog steps with rigid waters (moil_nb_md_step) on raw
+        CUDA pointers; returns (per-replica energies of the last step, kinetic energy)."""
+        ek = ctypes.c_double()
+        wg = None
+        if water_geom is not None:
+            wg = np.ascontiguousarray(water_geom, dtype=np.float64)
+        _check(self.L, self.h, self.L.moil_nb_md_step(
+            self.h, ctypes.c_void_p(d_coor_ptr), ctypes.c_void_p(d_vel_ptr), ctypes.c_void_p(d_mass_ptr),
+            float(dt), int(nsteps), wg.ctypes.data_as(_dp) if wg is not None else None, self._e,
+            ctypes.byref(ek)))
+        return self.energies(), ek.value
+
     def groups(self) -> int:
         """Number of concurrently evaluated replica groups (1: none)."""
         return int(self.L.moil_nb_groups(self.h))
@@ -303,6 +321,13 @@ class Nonbonded:
 
     def stream(self) -> int:
         return self.L.moil_nb_stream(self.h) or 0
+
+
+def dcd_write(path: str, coor: np.ndarray, first: bool, nframes: int = 1):
+    """Append a frame (or start a file) in the binary format of dynamics/wdyncrd.f."""
+    L = load()
+    c = np.ascontiguousarray(coor, dtype=np.float64).reshape(-1, 3)
+    _check(L, None, L.moil_nb_dcd_write(path.encode(), int(first), int(nframes), c.shape[0], c.ctypes.data_as(_dp)))
 
 
 def squeeze(s, coor: np.ndarray) -> np.ndarray:

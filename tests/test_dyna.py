@@ -85,3 +85,103 @@ def test_trajectory_conserves_energy_and_matches_oracle(cfg0):
     ref, eref = O.eforce(t, mode="parity")
     assert rel_rms(dpot, ref) < 1e-5
     assert abs(e["e_total"] - eref["e_total"]) < 1e-6 * energy_scale(eref)
+
+
+# ---- native integrator (moil_nb_md_step) and trajectory writer --------------------
+def read_dcd(path):
+    """Parse Fortran unformatted records: header, title, atom count, then x/y/z per frame."""
+    import struct
+    recs = []
+    with open(path, "rb") as f:
+        data = f.read()
+    k = 0
+    while k < len(data):
+        n = struct.unpack_from("<i", data, k)[0]
+        recs.append(data[k + 4:k + 4 + n])
+        assert struct.unpack_from("<i", data, k + 4 + n)[0] == n
+        k += 8 + n
+    assert recs[0][:4] == b"CORD"
+    vari = struct.unpack_from("<20i", recs[0], 4)
+    natom = struct.unpack("<i", recs[2])[0]
+    frames = []
+    for f0 in range(3, len(recs), 3):
+        frames.append(np.stack([np.frombuffer(recs[f0 + d], dtype="<f4") for d in range(3)], axis=1))
+    return vari, natom, frames
+
+
+def test_dcd_writer_format(tmp_path, cfg0):
+    from moil_fnrfd_gb300.nb import dcd_write
+    p = str(tmp_path / "t.dcd")
+    dcd_write(p, cfg0.coor, first=True, nframes=2)
+    dcd_write(p, cfg0.coor + 1.0, first=False)
+    vari, natom, frames = read_dcd(p)
+    assert vari[0] == 2 and natom == cfg0.npt and len(frames) == 2
+    assert np.array_equal(frames[0], cfg0.coor.astype(np.float32))
+    assert np.array_equal(frames[1], (cfg0.coor + 1.0).astype(np.float32))
+
+
+def _masses_of(s):
+    return D._masses(s)[0]
+
+
+@pytest.mark.gpu
+def test_native_steps_follow_the_harness(cfg0):
+    """The library's leapfrog + SETTLE steps against the torch harness from the same state."""
+    from moil_fnrfd_gb300.nb import Nonbonded
+    s = cfg0
+    nb = Nonbonded(s, skin=1.5, list_period=10)
+    md = D.RigidWaterDynamics(nb, s, dt=0.001, temperature=300.0, seed=3)
+    x = md.x.clone()
+    v = md.v.clone()
+    m = torch.tensor(_masses_of(s), dtype=torch.float64, device="cuda")
+    nb2 = Nonbonded(s, skin=1.5, list_period=10)
+    # one step from the same state: the same forces, two FP64 SETTLE implementations
+    md.step(1)
+    torch.cuda.synchronize()
+    e, ek = nb2.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.001, 1)
+    assert float((x - md.x).abs().max()) < 1e-12
+    assert float((v - md.v).abs().max()) < 1e-9
+    assert ek == pytest.approx(md.kinetic(), rel=1e-12)
+    # twenty more: a last-bit difference in a position can flip the FP32 rounding of a site,
+    # which the dynamics then carries along, so the trajectories separate slowly
+    md.step(20)
+    e, ek = nb2.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.001, 20)
+    dx, dv = float((x - md.x).abs().max()), float((v - md.v).abs().max())
+    assert dx < 1e-4 and dv < 1e-2, (dx, dv)
+    assert ek == pytest.approx(md.kinetic(), rel=1e-5)
+
+
+@pytest.mark.gpu
+def test_native_trajectory_conserves_energy(cfg0):
+    from conftest import energy_scale
+    from moil_fnrfd_gb300.nb import Nonbonded
+    s = cfg0
+    nb = Nonbonded(s, skin=1.5, list_period=10)
+    md = D.RigidWaterDynamics(nb, s, dt=0.001, temperature=300.0, seed=3)   # initial velocities
+    x, v = md.x.clone(), md.v.clone()
+    m = torch.tensor(_masses_of(s), dtype=torch.float64, device="cuda")
+    total = []
+    for _ in range(20):
+        e, ek = nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.001, 10)
+        total.append(e[0]["e_total"] + ek)
+    total = np.array(total)
+    assert total.max() - total.min() < 3e-3 * energy_scale(e[0])
+    a, b, c = (x[k::3] for k in range(3))
+    assert float((torch.linalg.vector_norm(b - a, dim=1) - S.TIP3_ROH).abs().max()) < 1e-9
+
+
+@pytest.mark.gpu
+def test_native_steps_grouped_batch_is_bit_identical():
+    from moil_fnrfd_gb300.nb import Nonbonded
+    reps = S.config3(6, seed=77)
+    coor = torch.tensor(np.concatenate([r.coor for r in reps]), dtype=torch.float64, device="cuda")
+    m = torch.tensor(np.concatenate([_masses_of(r) for r in reps]), dtype=torch.float64, device="cuda")
+    out = []
+    for groups in (1, 3):
+        nb = Nonbonded(reps, skin=1.5, list_period=10, groups=groups)
+        x, v = coor.clone(), torch.zeros_like(coor)
+        torch.cuda.synchronize()
+        e, ek = nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.002, 15)
+        out.append((x, v, e, ek))
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
