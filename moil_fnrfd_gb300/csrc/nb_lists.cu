@@ -357,13 +357,16 @@ __device__ __forceinline__ float4 wrap_box(const RepDev &R, typename vec4<T>::ty
 
 // 4b. W1 for replicas whose cell stencil spans most of the box (k_wlist_tiled): all
 // molecule pairs of the replica in one pass, oxygens staged in shared-memory tiles of
-// NB_WTILE and read by broadcast.  One block = NB_WTILE consecutive sorted waters of one
-// replica (blocks never straddle replicas).  Each 32-molecule word of a tile gives a bit
-// set (within the list radius) and a near set (within the cutoff) whose members go to the
-// row in ascending j.
+// NB_WTILE (x, y and z arrays) and read by broadcast, two molecules per packed FP32x2
+// operation.  One block = NB_WTILE consecutive sorted waters of one replica (blocks never
+// straddle replicas).  Each 32-molecule word of a tile gives a bit set (within the list
+// radius) and a near set (within the cutoff) whose members go to the row in ascending j.
+__device__ __forceinline__ float2 pf2(float a) { return make_float2(a, a); }
+
 template <typename T>
-__device__ __forceinline__ void wlist_tile(int2 w, float4 *sj, const RepDev *__restrict__ reps, const void *pos_v,
-                                           int2 *__restrict__ wcnt, int *__restrict__ l1, int cap_row, int *st)
+__device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const RepDev *__restrict__ reps,
+                                           const void *pos_v, int2 *__restrict__ wcnt, int *__restrict__ l1,
+                                           int cap_row, int *st)
 {
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
@@ -371,14 +374,24 @@ __device__ __forceinline__ void wlist_tile(int2 w, float4 *sj, const RepDev *__r
     const int j0 = R.wat0, nw = R.nwat;
     const int i = w.y + (int)threadIdx.x, il = i - j0;
     const bool act = il < nw;
-    const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
     const float rl2 = R.rlist2, rc2 = R.rmax2;
-    float4 oi = act ? wrap_box<T>(R, pos[3 * (size_t)i]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 oi = act ? wrap_box<T>(R, pos[3 * (size_t)i]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    // minimum image of positions wrapped into [0, L): d - L rint(d / L), the rounding by the
+    // 1.5 * 2^23 shift (|d / L| < 1)
+    const float2 o[3] = {pf2(oi.x), pf2(oi.y), pf2(oi.z)};
+    const float2 iL[3] = {pf2(R.invL[0]), pf2(R.invL[1]), pf2(R.invL[2])};
+    const float2 nL[3] = {pf2(-R.L[0]), pf2(-R.L[1]), pf2(-R.L[2])};
+    const float2 mg = pf2(12582912.f), nmg = pf2(-12582912.f), m1 = pf2(-1.f);
     int *row = l1 + (size_t)i * cap_row;
     int nn = 0, nf = 0;
     for (int t0 = 0; t0 < nw; t0 += NB_WTILE) {
         __syncthreads();
-        if (t0 + (int)threadIdx.x < nw) sj[threadIdx.x] = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
+        if (t0 + (int)threadIdx.x < nw) {
+            const float4 p = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
+            sj[0][threadIdx.x] = p.x;
+            sj[1][threadIdx.x] = p.y;
+            sj[2][threadIdx.x] = p.z;
+        }
         __syncthreads();
         if (!act) continue;
         const int tn = min(NB_WTILE, nw - t0);
@@ -387,16 +400,19 @@ __device__ __forceinline__ void wlist_tile(int2 w, float4 *sj, const RepDev *__r
             const int nv = tn - 32 * q;
             if (nv <= 0) break;
             unsigned m = 0u, mn = 0u;
-#pragma unroll 8
-            for (int b = 0; b < 32; ++b) {
-                const float4 p = sj[32 * q + b];
-                float dx = fabsf(oi.x - p.x), dy = fabsf(oi.y - p.y), dz = fabsf(oi.z - p.z);
-                dx = fminf(dx, L0 - dx);
-                dy = fminf(dy, L1 - dy);
-                dz = fminf(dz, L2 - dz);
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                m |= (r2 < rl2 ? 1u : 0u) << b;
-                mn |= (r2 <= rc2 ? 1u : 0u) << b;
+#pragma unroll 4
+            for (int b = 0; b < 32; b += 2) {
+                float2 r2 = pf2(0.f);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float2 p = *reinterpret_cast<const float2 *>(&sj[d][32 * q + b]);
+                    float2 x = __ffma2_rn(p, m1, o[d]);                               // o - p
+                    const float2 n = __fadd2_rn(__ffma2_rn(x, iL[d], mg), nmg);
+                    x = __ffma2_rn(n, nL[d], x);
+                    r2 = __ffma2_rn(x, x, r2);
+                }
+                m |= ((unsigned)(r2.x < rl2) << b) | ((unsigned)(r2.y < rl2) << (b + 1));
+                mn |= ((unsigned)(r2.x <= rc2) << b) | ((unsigned)(r2.y <= rc2) << (b + 1));
             }
             unsigned keep = nv < 32 ? (1u << nv) - 1u : 0xffffffffu;   // past the last molecule
             const int self = il - t0 - 32 * q;
@@ -421,7 +437,7 @@ __global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 
                                                           int *st)
 {
     if (rebuild_off(st)) return;
-    __shared__ float4 sj[NB_WTILE];
+    __shared__ __align__(16) float sj[3][NB_WTILE];
     // every tile pass starts with a block barrier before it overwrites sj
     for (int b = blockIdx.x; b < ntile; b += gridDim.x) wlist_tile<T>(work[b], sj, reps, pos_v, wcnt, l1, cap_row, st);
 }
