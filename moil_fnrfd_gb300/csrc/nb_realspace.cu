@@ -17,7 +17,7 @@
 
 namespace {
 
-#define CHUNK 32
+#define CHUNK 64
 
 template <typename T>
 __device__ __forceinline__ void lj_switch_apply(const RepDev &R, T r2, T &e1, T &df1)
