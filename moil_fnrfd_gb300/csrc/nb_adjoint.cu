@@ -100,11 +100,11 @@ __device__ __forceinline__ void atom_pair_adj(const RepDev &R, double r2, double
 }
 
 // water molecule per thread: W1 (nine site pairs per molecule pair) and W2
-template <typename T>
+template <typename T, typename E>
 __global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                             const int *__restrict__ site_orig, const void *pos_v, const void *woff_v,
                             const void *lj_v, const unsigned *__restrict__ sflags, const int2 *__restrict__ wl1_cnt,
-                            const int *__restrict__ wl1, int cap_row, const int *__restrict__ wl2_off,
+                            const void *__restrict__ wl1, int cap_row, const int *__restrict__ wl2_off,
                             const int *__restrict__ wl2, int cap2, double *__restrict__ dq, double *__restrict__ de,
                             double *__restrict__ ds)
 {
@@ -123,9 +123,10 @@ __global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *
     lj_decode(R.arith, ljO.x, ljO.y, epsO, sigO);
     const int2 c = wl1_cnt[i];
     const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
-    const int *row = wl1 + (size_t)i * cap_row;
+    const E *row = (const E *)wl1 + (size_t)i * cap_row;
+    const int base = sizeof(E) == 2 ? R.wat0 : 0;   // uint16 entries: offsets from the replica's first water
     for (int v = 0; v < n; ++v) {
-        const int j = row[v < nn ? v : cap_row - 1 - (v - nn)];
+        const int j = base + (int)row[v < nn ? v : cap_row - 1 - (v - nn)];
         const T4 oj = pos[3 * j];
         T dx = oi.x - oj.x, dy = oi.y - oj.y, dz = oi.z - oj.z;
         const T nx = nb_rint(dx * rep_invL<T>(R, 0)), ny = nb_rint(dy * rep_invL<T>(R, 1)),
@@ -295,7 +296,7 @@ int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds)
     cudaStream_t s = c->stream;
     const int B = 128;
     if (c->nW > 0)
-        k_adj_water<float><<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
+        (c->row16 ? k_adj_water<float, unsigned short> : k_adj_water<float, int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
             (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_woff, c->d_site_lj,
             c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), d_dq,
             d_de, d_ds);

@@ -152,7 +152,8 @@ int alloc_lists(NbCtx *c)
     free_ptr(c->d_wl1);
     free_ptr(c->d_wl2);
     free_ptr(c->d_xl);
-    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1, sizeof(int) * std::max<int64_t>(c->nW * c->cap_row1, 1)));
+    const size_t entry = c->row16 ? sizeof(unsigned short) : sizeof(int);
+    NB_CUDA_OK(c, cudaMalloc(&c->d_wl1, entry * std::max<int64_t>(c->nW * c->cap_row1, 2)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl2, sizeof(int) * std::max<int64_t>(c->cap_wl2, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl, sizeof(int) * std::max<int64_t>(c->cap_xl, 1)));
     c->list_gen++;   // a captured evaluation graph refers to the old buffers
@@ -385,6 +386,8 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     c->natom = atom0;
     c->nW = wat0;
     c->nA = oth0;
+    c->row16 = 1;
+    for (int r = 0; r < nrep; ++r) c->row16 &= c->rd[r].nwat < 65536;
     c->nsite = 3 * c->nW + c->nA;
     c->nunit = c->nW + c->nA;
     c->ncell = cell0;

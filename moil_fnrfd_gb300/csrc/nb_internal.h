@@ -76,7 +76,9 @@ struct NbCtx {
 
     // pair lists (CSR)
     int2 *d_wl1_cnt = nullptr;    // W1 row counts (in-cutoff from the front, skin-only from the back)
-    int *d_wl1 = nullptr;         // W1 rows of cap_row1 entries (sorted water index of j)
+    int *d_wl1 = nullptr;         // W1 rows of cap_row1 entries: sorted water index of j (int32), or
+                                  // with row16 its offset from the replica's first water (uint16)
+    int row16 = 0;                // every replica has fewer than 65,536 waters
     int cap_row1 = 0;
     int *d_wl2_off = nullptr, *d_wl2 = nullptr;
     int *d_xl_off = nullptr, *d_xl = nullptr;

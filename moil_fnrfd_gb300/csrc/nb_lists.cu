@@ -256,11 +256,16 @@ __device__ __forceinline__ bool nb_excluded(const int *__restrict__ ex_off, cons
 // build time from the front of the row in ascending order of discovery, skin-only
 // molecules from the back, counts (near, far) in wcnt[i].  The pair kernel walks the front
 // part then the back part, so the lanes of a warp stay converged over the in-cutoff part.
-__device__ __forceinline__ void w1_put(int *__restrict__ row, int cap, bool near, int &nn, int &nf, int j)
+// E: the row entry type, int32 sorted water indices or (every replica below 65,536 waters)
+// uint16 indices relative to the replica's first water, which halves the row stream the
+// water kernel reads every evaluation
+template <typename E>
+__device__ __forceinline__ void w1_put(E *__restrict__ row, int cap, bool near, int &nn, int &nf, int j)
 {
-    if (near) { if (nn < cap) row[nn] = j; ++nn; }
-    else { if (nf < cap) row[cap - 1 - nf] = j; ++nf; }
+    if (near) { if (nn < cap) row[nn] = (E)j; ++nn; }
+    else { if (nf < cap) row[cap - 1 - nf] = (E)j; ++nf; }
 }
+template <typename E> __device__ __forceinline__ int row_base(const RepDev &R) { return sizeof(E) == 2 ? R.wat0 : 0; }
 
 // a finished W1 row: counts, overflow flag, and the warp's entry total / longest row added
 // to st[2] / st[6] (for statistics and for regrowing the row capacity)
@@ -279,11 +284,11 @@ __device__ __forceinline__ void w1_done(int i, int nn, int nf, int cap, int2 *__
 
 // 4. water lists of water i by cell search: W1 (water j, rows of wl1) in the FILL = 0 pass,
 // W2 (non-water sites, CSR) counted in the FILL = 0 pass and written in the FILL = 1 pass
-template <typename T, int FILL>
+template <typename T, int FILL, typename E>
 __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restrict__ reps,
                                           const int *__restrict__ site_rep, const void *pos_v,
                                           const int *__restrict__ bin_start, int ncell, int2 *__restrict__ wcnt,
-                                          int *__restrict__ cnt2, const int *__restrict__ off2, int *__restrict__ l1,
+                                          int *__restrict__ cnt2, const int *__restrict__ off2, void *__restrict__ l1,
                                           int cap_row, int *__restrict__ l2, int64_t cap2, int *st)
 {
     typedef typename vec4<T>::type T4;
@@ -301,7 +306,7 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
         nz = nb_axis_cells(ci[2], R.nc[2], cz);
     int n2 = 0, nn = 0, nf = 0;
     int w2 = FILL ? off2[i] : 0;
-    int *row = l1 + (size_t)i * cap_row;
+    E *row = (E *)l1 + (size_t)i * cap_row;
     T rl2 = (T)R.rlist2, rw2 = (T)R.rlistw2, rc2 = (T)R.rmax2;
     int nW_i = nW;
     for (int a = 0; a < nz; ++a)
@@ -314,7 +319,7 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
                         if (p == i) continue;
                         T4 oj = pos[3 * p];
                         T r2 = mi_r2<T>(R, oi.x - oj.x, oi.y - oj.y, oi.z - oj.z);
-                        if (r2 < rl2) w1_put(row, cap_row, r2 <= rc2, nn, nf, p);
+                        if (r2 < rl2) w1_put(row, cap_row, r2 <= rc2, nn, nf, p - row_base<E>(R));
                     }
                 // non-water atoms in the cell
                 for (int p = bin_start[ncell + cell]; p < bin_start[ncell + cell + 1]; ++p) {
@@ -333,15 +338,15 @@ __device__ __forceinline__ void wlist_one(int i, int nW, const RepDev *__restric
     else if ((int64_t)w2 + n2 > cap2) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
 }
 
-template <typename T, int FILL>
+template <typename T, int FILL, typename E>
 __global__ void k_wlist(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep, const void *pos_v,
                         const int *__restrict__ bin_start, int ncell, int2 *__restrict__ wcnt,
-                        int *__restrict__ cnt2, const int *__restrict__ off2, int *__restrict__ l1, int cap_row,
+                        int *__restrict__ cnt2, const int *__restrict__ off2, void *__restrict__ l1, int cap_row,
                         int *__restrict__ l2, int64_t cap2, int *st)
 {
     if (rebuild_off(st)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nW; i += gridDim.x * blockDim.x)
-        wlist_one<T, FILL>(i, nW, reps, site_rep, pos_v, bin_start, ncell, wcnt, cnt2, off2, l1, cap_row, l2, cap2,
+        wlist_one<T, FILL, E>(i, nW, reps, site_rep, pos_v, bin_start, ncell, wcnt, cnt2, off2, l1, cap_row, l2, cap2,
                            st);
 }
 
@@ -363,9 +368,9 @@ __device__ __forceinline__ float4 wrap_box(const RepDev &R, typename vec4<T>::ty
 // radius) and a near set (within the cutoff) whose members go to the row in ascending j.
 __device__ __forceinline__ float2 pf2(float a) { return make_float2(a, a); }
 
-template <typename T>
+template <typename T, typename E>
 __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const RepDev *__restrict__ reps,
-                                           const void *pos_v, int2 *__restrict__ wcnt, int *__restrict__ l1,
+                                           const void *pos_v, int2 *__restrict__ wcnt, void *__restrict__ l1,
                                            int cap_row, int *st)
 {
     typedef typename vec4<T>::type T4;
@@ -382,7 +387,7 @@ __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const 
     const float2 iL[3] = {pf2(R.invL[0]), pf2(R.invL[1]), pf2(R.invL[2])};
     const float2 nL[3] = {pf2(-R.L[0]), pf2(-R.L[1]), pf2(-R.L[2])};
     const float2 mg = pf2(12582912.f), nmg = pf2(-12582912.f), m1 = pf2(-1.f);
-    int *row = l1 + (size_t)i * cap_row;
+    E *row = (E *)l1 + (size_t)i * cap_row;
     int nn = 0, nf = 0;
     for (int t0 = 0; t0 < nw; t0 += NB_WTILE) {
         __syncthreads();
@@ -423,23 +428,23 @@ __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const 
             while (m) {
                 const int b = __ffs(m) - 1;
                 m &= m - 1u;
-                w1_put(row, cap_row, (mn >> b) & 1u, nn, nf, jb + b);
+                w1_put(row, cap_row, (mn >> b) & 1u, nn, nf, jb + b - row_base<E>(R));
             }
         }
     }
     if (act) w1_done(i, nn, nf, cap_row, wcnt, st);
 }
 
-template <typename T>
+template <typename T, typename E>
 __global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 *__restrict__ work,
                                                           const RepDev *__restrict__ reps, const void *pos_v,
-                                                          int2 *__restrict__ wcnt, int *__restrict__ l1, int cap_row,
+                                                          int2 *__restrict__ wcnt, void *__restrict__ l1, int cap_row,
                                                           int *st)
 {
     if (rebuild_off(st)) return;
     __shared__ __align__(16) float sj[3][NB_WTILE];
     // every tile pass starts with a block barrier before it overwrites sj
-    for (int b = blockIdx.x; b < ntile; b += gridDim.x) wlist_tile<T>(work[b], sj, reps, pos_v, wcnt, l1, cap_row, st);
+    for (int b = blockIdx.x; b < ntile; b += gridDim.x) wlist_tile<T, E>(work[b], sj, reps, pos_v, wcnt, l1, cap_row, st);
 }
 
 // 5. non-water list X: every site j within reach, exclusions removed
@@ -649,23 +654,29 @@ void build_lists_t(NbCtx *c, const double *d_coor)
                                                       c->d_site_q, d_coor, c->d_pos, c->d_woff, c->d_posb, 0.f,
                                                       c->rwat * c->rwat, 1, c->d_status);
     c->launches += 5;
-    if (c->nW > 0) {
+    // water lists with the row entry type of the handle (uint16 when every replica has fewer
+    // than 65,536 waters)
+    auto water_lists = [&](auto e_tag) {
+        typedef decltype(e_tag) E;
+        if (c->nW <= 0) return;
         const int gw = grid(c->nW, 128), nt = (int)c->wtiles.size();
         const int gt = (int)std::min<int64_t>(nt, (int64_t)c->nsm * 16);
         int *cnt2 = c->d_count_tmp;
         // W1 rows (both kernels) and W2 counts in one pass; W2 scan and fill after
-        k_wlist<T, 0><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         c->d_wl1_cnt, cnt2, nullptr, c->d_wl1, c->cap_row1, nullptr, 0,
-                                         c->d_status);
+        k_wlist<T, 0, E><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start,
+                                            c->ncell, c->d_wl1_cnt, cnt2, nullptr, c->d_wl1, c->cap_row1, nullptr, 0,
+                                            c->d_status);
         if (nt > 0)
-            k_wlist_tiled<T><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wl1_cnt, c->d_wl1,
-                                                     c->cap_row1, c->d_status);
+            k_wlist_tiled<T, E><<<gt, NB_WTILE, 0, s>>>(nt, c->d_wtiles, c->d_reps, c->d_pos, c->d_wl1_cnt,
+                                                        c->d_wl1, c->cap_row1, c->d_status);
         nb_scan(c, cnt2, c->d_wl2_off, (int)c->nW, c->d_status + 3, 1);
-        k_wlist<T, 1><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start, c->ncell,
-                                         nullptr, nullptr, c->d_wl2_off, nullptr, 0, c->d_wl2, c->cap_wl2,
-                                         c->d_status);
+        k_wlist<T, 1, E><<<gw, 128, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_bin_start,
+                                            c->ncell, nullptr, nullptr, c->d_wl2_off, nullptr, 0, c->d_wl2, c->cap_wl2,
+                                            c->d_status);
         c->launches += nt > 0 ? 3 : 2;
-    }
+    };
+    if (c->row16) water_lists((unsigned short)0);
+    else water_lists(0);
     if (c->nA > 0) {
         const int ga = grid(c->nA, 128);
         k_xlist<T, 0><<<ga, 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos,

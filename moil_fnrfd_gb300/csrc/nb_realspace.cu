@@ -172,28 +172,30 @@ __device__ __forceinline__ void water_vs_atoms(const RepDev &R, int i, const typ
 
 // water i's W1 row: entry v is the v-th in-cutoff molecule from the front for v < nn, then
 // the skin-only molecules from the back of the row
+template <typename E>
 struct W1Row {
-    const int *row;
-    int nn, n, cap;
-    __device__ W1Row(const int2 *__restrict__ cnt, const int *__restrict__ wl1, int cap_row, int i)
+    const E *row;
+    int nn, n, cap, base;
+    __device__ W1Row(const int2 *__restrict__ cnt, const void *wl1, int cap_row, int i, int base_)
     {
         const int2 c = cnt[i];
-        row = wl1 + (size_t)i * cap_row;
+        row = (const E *)wl1 + (size_t)i * cap_row;
         // an overflowed row (counts above the capacity) is read within the row; the
         // evaluation reports the overflow and is redone with larger rows
         nn = min(c.x, cap_row);
         n = min(c.x + c.y, cap_row);
         cap = cap_row;
+        base = sizeof(E) == 2 ? base_ : 0;     // uint16 entries are offsets from the replica's first water
     }
-    __device__ const int *addr(int v) const { return row + (v < nn ? v : cap - 1 - (v - nn)); }
-    __device__ int at(int v) const { return *addr(v); }
+    __device__ const E *addr(int v) const { return row + (v < nn ? v : cap - 1 - (v - nn)); }
+    __device__ int at(int v) const { return base + (int)*addr(v); }
 };
 
-template <typename T>
+template <typename T, typename E>
 __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                                                      const void *pos_v, const void *woff_v, const void *lj_v,
                                                      const unsigned *__restrict__ sflags,
-                                                     const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
+                                                     const int2 *__restrict__ wl1_cnt, const void *__restrict__ wl1,
                                                      int cap_row, const int *__restrict__ wl2_off,
                                                      const int *__restrict__ wl2, int cap2, long long *__restrict__ grad,
                                                      double *__restrict__ e_unit)
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
     const T rmax2 = (T)R.rmax2, rv2 = (T)R.rv2, alpha = Consts<T>::alpha(R), ex2c = (T)R.ex2c, c2a = (T)R.c2a;
     const T qOO = Consts<T>::qq(R, 0), qOH = Consts<T>::qq(R, 1), qHH = Consts<T>::qq(R, 2);
     const T w12 = Consts<T>::w12(R), w6 = Consts<T>::w6(R);
-    const W1Row L1(wl1_cnt, wl1, cap_row, i);
+    const W1Row<E> L1(wl1_cnt, wl1, cap_row, i, R.wat0);
     int cnt = 0;
     // software pipeline: the next entry's index and oxygen are loaded one iteration ahead
     int jn = L1.n > 0 ? L1.at(0) : 0;
@@ -357,12 +359,12 @@ __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b
 
 // VIR: also the water-water LJ virial terms (two more accumulators, which the 128-register
 // budget of the plain evaluation does not hold without spilling; off unless requested)
-template <bool VIR>
+template <bool VIR, typename E>
 __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__restrict__ reps,
                                                        const int *__restrict__ site_rep, const float4 *__restrict__ pos,
                                                        const float4 *__restrict__ woff, const void *lj_v,
                                                        const unsigned *__restrict__ sflags,
-                                                       const int2 *__restrict__ wl1_cnt, const int *__restrict__ wl1,
+                                                       const int2 *__restrict__ wl1_cnt, const void *__restrict__ wl1,
                                                        int cap_row, const int *__restrict__ wl2_off,
                                                        const int *__restrict__ wl2, int cap2, long long *__restrict__ grad,
                                                        double *__restrict__ e_unit, int intra)
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     const float2 w12 = f2(R.w12), nw6 = f2(-R.w6);
     const float qqv[3] = {R.qq[0], R.qq[1], R.qq[2]};
     const float c2a = R.c2a;
-    const W1Row L1(wl1_cnt, wl1, cap_row, i);
+    const W1Row<E> L1(wl1_cnt, wl1, cap_row, i, R.wat0);
     const int k1 = L1.n;
     int cnt = 0;
     // next pair of entries, loaded one iteration ahead
@@ -866,12 +868,13 @@ void realspace_t(NbCtx *c)
     if (c->nW > 0) {
         const int nb = (int)((c->nW + WBLOCK - 1) / WBLOCK);
         if constexpr (sizeof(T) == 4)
-            (c->virial ? k_water_f<true> : k_water_f<false>)<<<nb, WBLOCK, 0, s>>>(
+            (c->virial ? (c->row16 ? k_water_f<true, unsigned short> : k_water_f<true, int>)
+                       : (c->row16 ? k_water_f<false, unsigned short> : k_water_f<false, int>))<<<nb, WBLOCK, 0, s>>>(
                 (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float4 *)c->d_woff,
                 c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2,
                 cap_int(c->cap_wl2), c->d_grad_site, c->d_e_unit, c->water_excl_fast);
         else
-            k_water<T><<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
+            (c->row16 ? k_water<T, unsigned short> : k_water<T, int>)<<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
                                              c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1,
                                              c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), c->d_grad_site,
                                              c->d_e_unit);

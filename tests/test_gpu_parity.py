@@ -309,3 +309,16 @@ def test_dense_cluster_regrows_lists():
     ref, eref = O.eforce(s, mode="parity")
     check(d, e, ref, eref, MOIL_NB_MIXED, "dense cluster")
     nb.close()
+
+
+def test_int32_rows_for_a_box_of_more_than_65535_waters():
+    """66,000 waters in one replica: the pair-list rows hold int32 water indices (below 65,536
+    waters per replica they hold uint16 offsets); against the oracle (its 128^3 grid is beyond
+    the FP64 plane kernels' shared memory)."""
+    n = 66000
+    s = S.water_box(n, (n / S.WATER_DENSITY) ** (1 / 3), 17, name="w66k", rc=9.0, alpha=0.35)
+    mixed = Nonbonded(s)
+    dm, em = mixed.eforce(s.coor)
+    mixed.close()
+    ref, eref = O.eforce(s, mode="mi")
+    check(dm, em, ref, eref, MOIL_NB_MIXED, "66k waters")
