@@ -115,7 +115,7 @@ __global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *
     const T4 *woff = (const T4 *)woff_v;
     const RepDev &R = reps[site_rep[3 * i]];
     const T4 oi = pos[3 * i];
-    const T4 h1 = woff[2 * i], h2 = woff[2 * i + 1];
+    const T4 h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
     const T hi[3][3] = {{(T)0, (T)0, (T)0}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
     double phi[3] = {0, 0, 0}, dE[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
     double epsO, sigO;
@@ -136,7 +136,7 @@ __global__ void k_adj_water(int nW, const RepDev *__restrict__ reps, const int *
         dz = nb_shift(R, 2, dz, nz);
         const T r2oo = dx * dx + dy * dy + dz * dz;
         if (r2oo > (T)R.rmax2) continue;
-        const T4 j1 = woff[2 * j], j2 = woff[2 * j + 1];
+        const T4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
         const T hj[3][3] = {{(T)0, (T)0, (T)0}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
         const double qj[3] = {(double)oj.w, (double)pos[3 * j + 1].w, (double)pos[3 * j + 2].w};
 #pragma unroll

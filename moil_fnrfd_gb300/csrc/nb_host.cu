@@ -456,7 +456,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_flags, sizeof(unsigned) * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_pos, 4 * ts * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_posb, sizeof(float4) * ns));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_woff, 4 * ts * 2 * std::max<int64_t>(c->nW, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_woff, 4 * ts * 3 * std::max<int64_t>(c->nW, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_lj, 2 * ts * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_site_q, ts * ns));
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl1_cnt, sizeof(int2) * std::max<int64_t>(c->nW, 1)));

@@ -70,7 +70,8 @@ struct NbCtx {
     unsigned *d_site_flags = nullptr;
     void *d_pos = nullptr;        // float4 / double4 (x, y, z, q_eff)
     float4 *d_posb = nullptr;     // positions at the last list build
-    void *d_woff = nullptr;       // float4 / double4: water H offsets from O, 2 per molecule (FP64-computed)
+    void *d_woff = nullptr;       // float4 / double4 per water, 3 in a row: O position (and charge),
+                                  // then the two H offsets from O (FP64-computed)
     void *d_site_lj = nullptr;    // float2 / double2
     void *d_site_q = nullptr;     // float / double (PME charge)
 

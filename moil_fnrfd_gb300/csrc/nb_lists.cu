@@ -188,6 +188,8 @@ __global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, con
 #pragma unroll
             for (int m = 0; m < 3; ++m)
                 prepare_site<T>(3 * u + m, x[m], site_flags, site_q, pos_v, posb, half_skin2, snapshot, moved);
+            // the molecule record of the water kernel: O position (and charge), then the offsets
+            ((T4 *)woff_v)[3 * u] = ((const T4 *)pos_v)[3 * u];
 #pragma unroll
             for (int m = 1; m < 3; ++m) {
                 // H offset from its O, formed in FP64 so the water kernel's site displacements
@@ -197,7 +199,7 @@ __global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, con
                 off.x = (T)(x[m][0] - x[0][0]); off.y = (T)(x[m][1] - x[0][1]); off.z = (T)(x[m][2] - x[0][2]);
                 off.w = (T)0;
                 if (off.x * off.x + off.y * off.y + off.z * off.z > (T)rwat2) atomicOr(&st[1], NB_DEV_ERR_RWAT);
-                ((T4 *)woff_v)[2 * u + m - 1] = off;
+                ((T4 *)woff_v)[3 * u + m] = off;
             }
         } else {
             const int s = 3 * nW + (u - nW);

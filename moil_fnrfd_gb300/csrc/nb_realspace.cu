@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
     for (int k = 0; k < 6; ++k) sE[k][t] = 0.0;
     const T4 oi0 = pos[3 * i];
     // i-site offsets from O (a = 0 is O itself)
-    const T4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
+    const T4 oi1 = woff[3 * i + 1], oi2 = woff[3 * i + 2];
     const T oi[3][3] = {{(T)0, (T)0, (T)0}, {oi1.x, oi1.y, oi1.z}, {oi2.x, oi2.y, oi2.z}};
     T g[9];
 #pragma unroll
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
         dz = nb_shift(R, 2, dz, nz);
         T r2oo = dx * dx + dy * dy + dz * dz;
         if (r2oo <= rmax2) {
-            T4 oj1 = woff[2 * j], oj2 = woff[2 * j + 1];
+            T4 oj1 = woff[3 * j + 1], oj2 = woff[3 * j + 2];
             // q[b] = (O_i - O_j - nL) - offset_j[b]; site displacement = offset_i[a] + q[b]
             const T q[3][3] = {{dx, dy, dz}, {dx - oj1.x, dy - oj1.y, dz - oj1.z}, {dx - oj2.x, dy - oj2.y, dz - oj2.z}};
             T e_el = 0, e_lj = 0, v_lj = 0;
@@ -379,8 +379,8 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     for (int k = 0; k < 9; ++k) sG[k][t] = 0;
 #pragma unroll
     for (int k = 0; k < 6; ++k) sE[k][t] = make_float2(0.f, 0.f);
-    const float4 oi0 = pos[3 * i];
-    const float4 oi1 = woff[2 * i], oi2 = woff[2 * i + 1];
+    const float4 oi0 = woff[3 * i];
+    const float4 oi1 = woff[3 * i + 1], oi2 = woff[3 * i + 2];
     // H offsets of molecule i, duplicated into both lanes
     const float2 hi[2][3] = {{f2(oi1.x), f2(oi1.y), f2(oi1.z)}, {f2(oi2.x), f2(oi2.y), f2(oi2.z)}};
     float2 G[9];
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     // next pair of entries, loaded one iteration ahead
     int ja = k1 > 0 ? L1.at(0) : 0;
     int jb = k1 > 1 ? L1.at(1) : ja;
-    float4 oa = pos[3 * ja], ob = pos[3 * jb];
+    float4 oa = woff[3 * ja], ob = woff[3 * jb];
     for (int k = 0; k < k1; k += 2) {
         const bool hasb = k + 1 < k1;
         const int j0 = ja, j1 = jb;
@@ -439,8 +439,8 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
         if (k + 2 < k1) {
             ja = L1.at(k + 2);
             jb = k + 3 < k1 ? L1.at(k + 3) : ja;
-            oa = pos[3 * ja];
-            ob = pos[3 * jb];
+            oa = woff[3 * ja];
+            ob = woff[3 * jb];
         }
         // O-O minimum image per entry; (x + 1.5*2^23) - 1.5*2^23 rounds x to nearest (|x| < 2^22)
         float dx0 = oi0.x - o0.x, dy0 = oi0.y - o0.y, dz0 = oi0.z - o0.z;
@@ -452,8 +452,8 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
         const float r0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0, r1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
         const bool in0 = r0 <= rmax2, in1 = hasb && r1 <= rmax2;
         if (in0 || in1) {
-            const float4 a1 = woff[2 * j0], a2 = woff[2 * j0 + 1];
-            const float4 b1 = woff[2 * j1], b2 = woff[2 * j1 + 1];
+            const float4 a1 = woff[3 * j0 + 1], a2 = woff[3 * j0 + 2];
+            const float4 b1 = woff[3 * j1 + 1], b2 = woff[3 * j1 + 2];
             if (!in0) { dx0 = 1.0e4f; dy0 = 0.f; dz0 = 0.f; }
             if (!in1) { dx1 = 1.0e4f; dy1 = 0.f; dz1 = 0.f; }
             // q[b] = (O_i - O_j - nL) - offset_j[b]; site displacement = offset_i[a] + q[b]
