@@ -370,10 +370,26 @@ __device__ __forceinline__ float4 wrap_box(const RepDev &R, typename vec4<T>::ty
 // radius) and a near set (within the cutoff) whose members go to the row in ascending j.
 __device__ __forceinline__ float2 pf2(float a) { return make_float2(a, a); }
 
+// bounding boxes: each warp's i molecules and each 32-molecule word of a tile (positions
+// wrapped into [0, L)); a word whose box is farther than the list radius from the warp's box
+// in every image is skipped by the whole warp
+__device__ __forceinline__ void warp_box(bool valid, float x, float y, float z, float lo[3], float hi[3])
+{
+    lo[0] = valid ? x : 3.0e38f; lo[1] = valid ? y : 3.0e38f; lo[2] = valid ? z : 3.0e38f;
+    hi[0] = valid ? x : -3.0e38f; hi[1] = valid ? y : -3.0e38f; hi[2] = valid ? z : -3.0e38f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+}
+
 template <typename T, typename E>
-__device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const RepDev *__restrict__ reps,
-                                           const void *pos_v, int2 *__restrict__ wcnt, void *__restrict__ l1,
-                                           int cap_row, int *st)
+__device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], float (*sbb)[6],
+                                           const RepDev *__restrict__ reps, const void *pos_v,
+                                           int2 *__restrict__ wcnt, void *__restrict__ l1, int cap_row, int *st)
 {
     typedef typename vec4<T>::type T4;
     const T4 *pos = (const T4 *)pos_v;
@@ -391,13 +407,25 @@ __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const 
     const float2 mg = pf2(12582912.f), nmg = pf2(-12582912.f), m1 = pf2(-1.f);
     E *row = (E *)l1 + (size_t)i * cap_row;
     int nn = 0, nf = 0;
+    float ilo[3], ihi[3];
+    warp_box(act, oi.x, oi.y, oi.z, ilo, ihi);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int t0 = 0; t0 < nw; t0 += NB_WTILE) {
         __syncthreads();
-        if (t0 + (int)threadIdx.x < nw) {
-            const float4 p = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
+        const bool has = t0 + (int)threadIdx.x < nw;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (has) {
+            p = wrap_box<T>(R, pos[3 * (size_t)(j0 + t0 + threadIdx.x)]);
             sj[0][threadIdx.x] = p.x;
             sj[1][threadIdx.x] = p.y;
             sj[2][threadIdx.x] = p.z;
+        }
+        {
+            // the box of the word this warp loaded
+            float lo[3], hi[3];
+            warp_box(has, p.x, p.y, p.z, lo, hi);
+            if (lane == 0)
+                for (int d = 0; d < 3; ++d) { sbb[warp][d] = lo[d]; sbb[warp][3 + d] = hi[d]; }
         }
         __syncthreads();
         if (!act) continue;
@@ -406,6 +434,19 @@ __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], const 
         for (int q = 0; q < NB_WTILE / 32; ++q) {
             const int nv = tn - 32 * q;
             if (nv <= 0) break;
+            {
+                // separation of the boxes over the images (-L, 0, +L) per axis
+                float s2 = 0.f;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float jlo = sbb[q][d], jhi = sbb[q][3 + d], L = R.L[d];
+                    const float s0 = fmaxf(0.f, fmaxf(jlo - ihi[d], ilo[d] - jhi));
+                    const float sp = fmaxf(0.f, jlo + L - ihi[d]), sm = fmaxf(0.f, ilo[d] - jhi + L);
+                    const float sd = fminf(s0, fminf(sp, sm));
+                    s2 = fmaf(sd, sd, s2);
+                }
+                if (s2 >= rl2) continue;
+            }
             unsigned m = 0u, mn = 0u;
 #pragma unroll 4
             for (int b = 0; b < 32; b += 2) {
@@ -445,8 +486,10 @@ __global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 
 {
     if (rebuild_off(st)) return;
     __shared__ __align__(16) float sj[3][NB_WTILE];
-    // every tile pass starts with a block barrier before it overwrites sj
-    for (int b = blockIdx.x; b < ntile; b += gridDim.x) wlist_tile<T, E>(work[b], sj, reps, pos_v, wcnt, l1, cap_row, st);
+    __shared__ float sbb[NB_WTILE / 32][6];
+    // every tile pass starts with a block barrier before it overwrites sj and sbb
+    for (int b = blockIdx.x; b < ntile; b += gridDim.x)
+        wlist_tile<T, E>(work[b], sj, sbb, reps, pos_v, wcnt, l1, cap_row, st);
 }
 
 // 5. non-water list X: every site j within reach, exclusions removed
