@@ -522,11 +522,28 @@ void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
     cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 8, cudaMemcpyHostToDevice, s);
     nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
     nb_launch_build_lists(c, d_coor);  // every kernel here is gated by the flag
-    if (c->timing) cudaEventRecord(c->ev[1], s);
-    nb_launch_realspace(c);
-    nb_launch_excl14(c, d_coor);
-    if (c->timing) cudaEventRecord(c->ev[5], s);
-    nb_launch_pme(c);
+    if (c->timing) {
+        // stage timing: one stream, stage after stage
+        cudaEventRecord(c->ev[1], s);
+        nb_launch_realspace(c);
+        nb_launch_excl14(c, d_coor);
+        cudaEventRecord(c->ev[5], s);
+        nb_launch_pme(c);
+    } else {
+        // the PME branch (binning, planes, columns, gather) runs on a second stream beside the
+        // pair and correction kernels: they read the same site positions and write disjoint
+        // outputs, and the latency-bound plane kernels fill the multiprocessors the pair
+        // kernel leaves idle
+        cudaEventRecord(c->ev_fork, s);
+        cudaStreamWaitEvent(c->stream2, c->ev_fork, 0);
+        std::swap(c->stream, c->stream2);
+        nb_launch_pme(c);
+        std::swap(c->stream, c->stream2);
+        cudaEventRecord(c->ev_join, c->stream2);
+        nb_launch_realspace(c);
+        nb_launch_excl14(c, d_coor);
+        cudaStreamWaitEvent(s, c->ev_join, 0);
+    }
     nb_launch_finalize(c, d_dpot);
     if (c->timing) cudaEventRecord(c->ev[10], s);
     cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * 8, cudaMemcpyDeviceToHost, s);
@@ -836,7 +853,13 @@ int moil_nb_create(moil_nb_ctx **out, int device)
     if (device < 0 || device >= ndev) return MOIL_NB_ERR_ARG;
     moil_nb_ctx *h = new moil_nb_ctx();
     h->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        if (h->stream) cudaStreamDestroy(h->stream);
+        if (h->stream2) cudaStreamDestroy(h->stream2);
+        if (h->ev_fork) cudaEventDestroy(h->ev_fork);
         delete h;
         return MOIL_NB_ERR_CUDA;
     }
@@ -863,6 +886,9 @@ void moil_nb_destroy(moil_nb_ctx *h)
         if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->d_status) cudaFree(h->d_status);
+    if (h->stream2) { cudaStreamSynchronize(h->stream2); cudaStreamDestroy(h->stream2); }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -36,6 +36,8 @@ struct NbCtx {
     int device = 0;
     int nsm = 152;                // multiprocessors: grids of the rebuild-gated kernels stay one wave
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // PME branch of an evaluation, concurrent with the pair kernels
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int precision = MOIL_NB_MIXED;
     int inited = 0;
     std::string err;
