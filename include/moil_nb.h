@@ -206,7 +206,7 @@ int moil_nb_set_graph(moil_nb_ctx *h, int on);
  * accumulate them.  No counterpart in the reference (its PRESS build always does). */
 int moil_nb_set_virial(moil_nb_ctx *h, int on);
 
-/* Replica groups for the next moil_nb_init_batch: 0 automatic (two groups for batches of
+/* Replica groups for the next moil_nb_init_batch: 0 automatic (three groups for batches of
  * at least a million atoms in 8 or more replicas), 1 none, P >= 2 that many.  A grouped
  * handle evaluates contiguous replica ranges concurrently, each with its own stream, lists
  * and graph, so one group's host copies and latency-bound kernels overlap another's work;

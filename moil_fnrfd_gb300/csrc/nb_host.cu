@@ -735,6 +735,14 @@ int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bo
         }
         return rc;
     };
+    // host-buffer evaluations run on the prioritised streams (the graphs replay on any stream)
+    auto use_prio = [&](bool on) {
+        if (!host) return;
+        for (NbCtx *c : h->grp)
+            if (c->pstream) { std::swap(c->stream, c->pstream); std::swap(c->stream2, c->pstream2); }
+        (void)on;
+    };
+    use_prio(true);
     int rc = MOIL_NB_OK;
     if (h->timing) {
         // diagnostic mode: one group after the other, stage times summed
@@ -757,6 +765,7 @@ int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bo
             if (r != MOIL_NB_OK && rc == MOIL_NB_OK) rc = r;
         }
     }
+    use_prio(false);
     int64_t pairs = 0, entries = 0;
     int launches = 0;
     for (NbCtx *c : h->grp) {
@@ -788,26 +797,29 @@ void destroy_groups(NbCtx *h)
 }
 
 // groups for a batch: automatic for batches of at least a million atoms in 8 or more
-// replicas (two groups), where copy/kernel overlap pays; none for smaller ones
+// replicas (three groups), where copy/kernel overlap pays; none for smaller ones
 int choose_groups(const NbCtx *h, int nrep, int64_t natom)
 {
     if (h->want_groups == 1 || nrep < 2) return 1;
     if (h->want_groups >= 2) return std::min(h->want_groups, nrep);
-    return (nrep >= 8 && natom >= 1000000) ? 2 : 1;
+    return (nrep >= 8 && natom >= 1000000) ? 3 : 1;
 }
 
 int init_groups(moil_nb_ctx *h, int nrep, const moil_replica *reps, int P)
 {
     int64_t total = 0;
     for (int r = 0; r < nrep; ++r) total += reps[r].topo ? reps[r].topo->npt : 0;
-    // contiguous replica ranges of about total / P atoms
+    // contiguous replica ranges; with three or more groups the first and the last hold half
+    // the atoms of the others (their host copies are the ones no kernel work hides)
+    std::vector<double> cut(P + 1, 0.0);
+    for (int g = 0; g < P; ++g) cut[g + 1] = cut[g] + ((P >= 3 && (g == 0 || g == P - 1)) ? 1.0 : 2.0);
     h->grp_rep0.assign(1, 0);
     h->grp_atom0.assign(1, 0);
     int64_t acc = 0;
     for (int r = 0; r < nrep; ++r) {
         acc += reps[r].topo->npt;
         const int g = (int)h->grp_rep0.size();
-        if (g < P && r + 1 < nrep && acc >= (total * g + P - 1) / P) {
+        if (g < P && r + 1 < nrep && (double)acc >= (double)total * cut[g] / cut[P]) {
             h->grp_rep0.push_back(r + 1);
             h->grp_atom0.push_back(acc);
         }
@@ -821,6 +833,21 @@ int init_groups(moil_nb_ctx *h, int nrep, const moil_replica *reps, int P)
         c->use_graph = h->use_graph;
         c->virial = h->virial;
         c->timing = h->timing;
+        {
+            // streams for host-buffer evaluations: earlier groups at higher priority finish
+            // first, so their gradient copies overlap the later groups' kernels (device-
+            // resident evaluations keep equal priorities, which balances the kernels best)
+            int lo = 0, hi = 0;
+            cudaDeviceGetStreamPriorityRange(&lo, &hi);
+            const int prio = std::min(lo, hi + (int)g);
+            if (cudaStreamCreateWithPriority(&c->pstream, cudaStreamNonBlocking, prio) != cudaSuccess ||
+                cudaStreamCreateWithPriority(&c->pstream2, cudaStreamNonBlocking, prio) != cudaSuccess) {
+                h->err = "creating replica group streams";
+                h->grp.push_back(c);
+                destroy_groups(h);
+                return MOIL_NB_ERR_CUDA;
+            }
+        }
         h->grp.push_back(c);
         rc = init_impl(c, h->grp_rep0[g + 1] - h->grp_rep0[g], reps + h->grp_rep0[g]);
         if (rc != MOIL_NB_OK) { h->err = c->err; destroy_groups(h); return rc; }
@@ -887,6 +914,8 @@ void moil_nb_destroy(moil_nb_ctx *h)
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->d_status) cudaFree(h->d_status);
     if (h->stream2) { cudaStreamSynchronize(h->stream2); cudaStreamDestroy(h->stream2); }
+    if (h->pstream) cudaStreamDestroy(h->pstream);
+    if (h->pstream2) cudaStreamDestroy(h->pstream2);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->stream) cudaStreamDestroy(h->stream);

@@ -37,6 +37,7 @@ struct NbCtx {
     int nsm = 152;                // multiprocessors: grids of the rebuild-gated kernels stay one wave
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;   // PME branch of an evaluation, concurrent with the pair kernels
+    cudaStream_t pstream = nullptr, pstream2 = nullptr;   // replica groups: prioritised by group index
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int precision = MOIL_NB_MIXED;
     int inited = 0;
