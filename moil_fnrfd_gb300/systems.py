@@ -486,3 +486,39 @@ def make_config(idx: int):
     if idx == 3:
         return config3()
     raise ValueError(idx)
+
+
+MASS_O, MASS_H, MASS_NA, MASS_BEAD = 15.9994, 1.008, 22.98977, 12.011
+
+
+def molecules(s: MoilSystem):
+    """Covalent molecules and atom masses for the pressure analysis (analysis/pressure.f,
+    whose dmolecule groups atoms joined by bonds): here the connected components of the
+    exclusion graph (every bond is an exclusion, and every exclusion joins atoms of one
+    molecule).  Returns (mol, mass): 0-based molecule index of every atom, numbered in
+    order of first atom, and masses (TIP3P O/H, Na+ for ions, a carbon-like bead else)."""
+    n = s.npt
+    parent = np.arange(n)
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+    for i in range(n):
+        for k in range(int(s.exc1[i]), int(s.exc1[i + 1])):
+            a, b = find(i), find(int(s.exc2[k]) - 1)
+            if a != b:
+                parent[max(a, b)] = min(a, b)
+    root = np.array([find(i) for i in range(n)])
+    _, mol = np.unique(root, return_inverse=True)   # roots are first atoms: ids in atom order
+    mass = np.full(n, MASS_BEAD)
+    first = 0
+    for k in range(s.totmon):
+        last = int(s.poipt[k])
+        if s.montype[k] == MON_WATER:
+            mass[first:last] = (MASS_O, MASS_H, MASS_H)
+        elif s.montype[k] == MON_ION:
+            mass[first:last] = MASS_NA
+        first = last
+    return mol.astype(np.int32), mass

@@ -895,8 +895,12 @@ static int wrapidx(int k0, int n)
     return k % n;   /* fr == nfft exactly lands on index 0 */
 }
 
-/* PME core; phi (nullable) receives dE_rec/dq per atom: fc * sum(theta * convolved grid) */
-static int pme_core(const ora_input *in, double ewaldcof, double *dpot, double *eer, double *fpme_out, double *phi)
+/* PME core; phi (nullable) receives dE_rec/dq per atom: fc * sum(theta * convolved grid).
+ * press (nullable, with xrel): the pressure analysis terms, press[6..8] += the reciprocal
+ * virial V_PIrec (ewald_receip.f:799-807) and press[9..11] += V_PIrel = sum of the PME force
+ * times the atom's position relative to its molecule's centre of mass (:928-933). */
+static int pme_core(const ora_input *in, double ewaldcof, double *dpot, double *eer, double *fpme_out, double *phi,
+                    const double *xrel, double *press)
 {
     int n1 = in->nfft1, n2 = in->nfft2, n3 = in->nfft3, order = in->order, N = in->npt;
     size_t ng = (size_t)n1 * n2 * n3;
@@ -967,6 +971,12 @@ static int pme_core(const ora_input *in, double ewaldcof, double *dpot, double *
                     eterm = exp(-fac * msq) / denom;
                     struc2 = qr[id] * qr[id] + qi[id] * qi[id];
                     energy += eterm * struc2;
+                    if (press) {
+                        double vp = 0.5 * eterm * struc2, b = 2.0 * (1.0 + fac * msq) / msq;
+                        press[6] += vp * (1.0 - b * mh1 * mh1);
+                        press[7] += vp * (1.0 - b * mh2 * mh2);
+                        press[8] += vp * (1.0 - b * mh3 * mh3);
+                    }
                     qr[id] *= eterm;
                     qi[id] *= eterm;
                 }
@@ -997,6 +1007,11 @@ static int pme_core(const ora_input *in, double ewaldcof, double *dpot, double *
         }
         fx = rc1 * f1; fy = rc2 * f2; fz = rc3 * f3;
         dpot[3 * n] -= fx; dpot[3 * n + 1] -= fy; dpot[3 * n + 2] -= fz;
+        if (press) {
+            press[9] += fx * xrel[3 * n];
+            press[10] += fy * xrel[3 * n + 1];
+            press[11] += fz * xrel[3 * n + 2];
+        }
         if (phi) {
             double v = 0;
             k0 = (int)fr[3 * n + 2] - order;
@@ -1023,7 +1038,7 @@ static int pme_core(const ora_input *in, double ewaldcof, double *dpot, double *
 
 int ora_pme(const ora_input *in, double ewaldcof, double *dpot, double *eer, double *fpme_out)
 {
-    return pme_core(in, ewaldcof, dpot, eer, fpme_out, 0);
+    return pme_core(in, ewaldcof, dpot, eer, fpme_out, 0, 0, 0);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1184,7 +1199,9 @@ typedef struct cellgrid {
     int *head, *next;
 } cellgrid;
 
-int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
+/* Minimum-image evaluation; with xrel (positions relative to the molecules' centres of
+ * mass) it also accumulates the pressure analysis terms into press[12] (see ora_pressure_mi). */
+static int eforce_mi_core(const ora_input *in, double *dpot, ora_output *out, const double *xrel, double *press)
 {
     ctx cc, *c = &cc;
     int npt = in->npt, i, m;
@@ -1211,7 +1228,7 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
     rmax2 = rcut_el2;
     excl_corr(c, dpot, &out->e_corr, out);
     ener14(c, dpot, &out->e_vdw14, &out->e_el14, out);
-    if (in->do_pme) ora_pme(in, c->ewaldcof, dpot, &out->e_ew_receip, &out->fpme);
+    if (in->do_pme) pme_core(in, c->ewaldcof, dpot, &out->e_ew_receip, &out->fpme, 0, xrel, press);
     {
         /* cell list over atoms; cell edge >= cutoff + 2 Å (water site offsets) */
         double reach = sqrt(rmax2) + 2.2;
@@ -1338,6 +1355,14 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
                                     dpot[3 * (i - 1) + k] += df * rv[k];
                                     dpot[3 * (j - 1) + k] -= df * rv[k];
                                 }
+                                if (press)
+                                    for (k = 0; k < 3; k++) {
+                                        /* centre-of-mass separation of the two molecules, in
+                                         * the image this pair is taken in */
+                                        double rm = rv[k] - xrel[3 * (i - 1) + k] + xrel[3 * (j - 1) + k];
+                                        press[k] -= df1 * rv[k] * rm;       /* virXX..ZZ */
+                                        press[3 + k] -= df2 * rv[k] * rm;   /* V_PIdirXX..ZZ */
+                                    }
                             }
                         }
                     }
@@ -1348,6 +1373,64 @@ int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
     free(mol); free(oxy);
     ctx_free(c);
     return 0;
+}
+
+int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out)
+{
+    return eforce_mi_core(in, dpot, out, 0, 0);
+}
+
+/* Positions relative to the molecules' centres of mass (analysis/pressure.f: checkANDmove
+ * :985-1010 makes each molecule whole along its bonds, atom2molecule :419-520 forms the
+ * centres of mass).  Here each atom is placed at the minimum image of its displacement
+ * from the previous atom of its molecule in atom order, which makes the molecule whole
+ * whenever consecutive atoms of a molecule are closer than half the box. */
+static int mol_xrel(const ora_input *in, const int *mol, const double *mass, double *xrel)
+{
+    int n, k, m, nm = 0, npt = in->npt;
+    double box[3] = {in->a, in->b, in->c};
+    int *last;
+    double *msum, *mds;
+    for (n = 0; n < npt; n++) {
+        if (mol[n] < 0) return -1;
+        if (mol[n] + 1 > nm) nm = mol[n] + 1;
+    }
+    last = (int *)malloc(sizeof(int) * (nm + 1));
+    msum = (double *)calloc(nm + 1, sizeof(double));
+    mds = (double *)calloc(3 * (size_t)(nm + 1), sizeof(double));
+    for (m = 0; m < nm; m++) last[m] = -1;
+    for (n = 0; n < npt; n++) {
+        m = mol[n];
+        for (k = 0; k < 3; k++) {
+            double d = 0.0;
+            if (last[m] >= 0) {
+                double t = in->coor[3 * n + k] - in->coor[3 * last[m] + k];
+                d = xrel[3 * last[m] + k] + t - box[k] * round(t / box[k]);
+            }
+            xrel[3 * n + k] = d;
+            mds[3 * m + k] += mass[n] * d;
+        }
+        msum[m] += mass[n];
+        last[m] = n;
+    }
+    for (n = 0; n < npt; n++) {
+        m = mol[n];
+        for (k = 0; k < 3; k++) xrel[3 * n + k] -= msum[m] > 0.0 ? mds[3 * m + k] / msum[m] : 0.0;
+    }
+    free(last); free(msum); free(mds);
+    return 0;
+}
+
+int ora_pressure_mi(const ora_input *in, const int *mol, const double *mass, double *dpot, ora_output *out,
+                    double *press)
+{
+    double *xrel = (double *)malloc(sizeof(double) * 3 * (size_t)(in->npt > 0 ? in->npt : 1));
+    int k, rc;
+    for (k = 0; k < 12; k++) press[k] = 0.0;
+    rc = mol_xrel(in, mol, mass, xrel);
+    if (rc == 0) rc = eforce_mi_core(in, dpot, out, xrel, press);
+    free(xrel);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1424,7 +1507,7 @@ int ora_adjoint_mi(const ora_input *in, double *dq, double *de, double *ds)
         if (in->do_pme) {
             double eer;
             dpot = (double *)calloc(3 * (size_t)npt, sizeof(double));
-            pme_core(in, c->ewaldcof, dpot, &eer, 0, dq);
+            pme_core(in, c->ewaldcof, dpot, &eer, 0, dq, 0, 0);
             free(dpot);
         }
     }

@@ -82,6 +82,18 @@ int ora_eforce(const ora_input *in, double *dpot, ora_output *out);
  * at the given coordinates (the parity reference for the GPU path). */
 int ora_eforce_mi(const ora_input *in, double *dpot, ora_output *out);
 
+/* MOIL's pressure analysis terms (analysis/pressure.f with pressON) at the given coordinates,
+ * beside the ora_eforce_mi evaluation.  mol[n]: molecule of atom n (0-based ids), mass[n]:
+ * its mass.  press[12] = virXX, virYY, virZZ (LJ, watwat_ewald.f:163-175, cdie_ewald.f:
+ * 441-453, 555-566), V_PIdirXX..ZZ (real-space Ewald Coulomb, watwat_ewald.f:196-204,
+ * cdie_ewald.f:412-429), V_PIrecXX..ZZ (reciprocal, ewald_receip.f:799-807), V_PIrelXX..ZZ
+ * (PME force times the position relative to the centre of mass, ewald_receip.f:928-933):
+ * every pair term is F_ij,a (R_I - R_J)_a with R the molecules' centres of mass in the image
+ * the pair is taken in; pressure.f:235-238 sums vir + dir + rec - rel (V_PIcor is zero:
+ * its accumulation is commented out in cdie_ewald.f:165-170). */
+int ora_pressure_mi(const ora_input *in, const int *mol, const double *mass, double *dpot, ora_output *out,
+                    double *press);
+
 /* nevals evaluations with lists rebuilt every list_period (MOIL's '#lis'). */
 int ora_eforce_repeat(const ora_input *in, double *dpot, ora_output *out, int nevals, int list_period);
 

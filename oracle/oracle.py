@@ -92,6 +92,7 @@ def lib():
         L.ora_fft.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int]
         L.ora_pme.argtypes = [ctypes.POINTER(OraInput), ctypes.c_double, _dp, _dp, _dp]
         L.ora_adjoint_mi.argtypes = [ctypes.POINTER(OraInput), _dp, _dp, _dp]
+        L.ora_pressure_mi.argtypes = [ctypes.POINTER(OraInput), _ip, _dp, _dp, ctypes.POINTER(OraOutput), _dp]
         _lib = L
     return _lib
 
@@ -198,6 +199,26 @@ def adjoint(s, mode: str = "parity", **kw):
     if lib().ora_adjoint_mi(ctypes.byref(inp), _p(dq), _p(de), _p(ds)) != 0:
         raise RuntimeError("oracle adjoint failed")
     return dq, de, ds
+
+
+PRESS_KEYS = ("virXX", "virYY", "virZZ", "V_PIdirXX", "V_PIdirYY", "V_PIdirZZ", "V_PIrecXX", "V_PIrecYY",
+              "V_PIrecZZ", "V_PIrelXX", "V_PIrelYY", "V_PIrelZZ")
+
+
+def pressure(s, mol, mass, mode: str = "parity", **kw):
+    """MOIL's pressure analysis terms (moil_oracle.c ora_pressure_mi) at the system's
+    coordinates: returns (dpot, energies, press) with press the 12 values of PRESS_KEYS.
+    mol: molecule index of every atom (0-based), mass: atom masses."""
+    keep = _Keep()
+    inp = make_input(s, mode=mode, keep=keep, **kw)
+    dpot = np.zeros((s.npt, 3), dtype=np.float64)
+    press = np.zeros(12, dtype=np.float64)
+    out = OraOutput()
+    rc = lib().ora_pressure_mi(ctypes.byref(inp), keep.i(mol), keep.d(mass), _p(dpot), ctypes.byref(out),
+                               _p(press))
+    if rc != 0:
+        raise RuntimeError(f"oracle pressure failed ({rc})")
+    return dpot, output_dict(out), press
 
 
 def eforce_batch(systems, mode: str = "parity", nthreads: int = 0, nevals: int = 1, list_period: int = 1, **kw):
