@@ -200,6 +200,29 @@ int moil_nb_pair_stats(const moil_nb_ctx *h, int64_t *list_entries, int64_t *sit
  * with timing on always launch kernel by kernel.  No counterpart in the reference. */
 int moil_nb_set_graph(moil_nb_ctx *h, int on);
 
+/* ---- pressure analysis (analysis/pressure.f with pressON) ------------------ */
+/* Molecules of every caller atom (all replicas back to back): mol[n] = molecule index of atom
+ * n within its replica (any non-negative ids below that replica's atom count; equal ids =
+ * one molecule), mass[n] = its mass (amu).  MOIL forms them in dmolecule/atom2molecule
+ * (analysis/pressure.f:341-520).  mol = NULL switches the pressure terms off.  Molecules
+ * are made whole by placing each atom at the minimum image of its displacement from the
+ * previous atom of its molecule (consecutive atoms of a molecule must be closer than half
+ * the box).  No counterpart entry point in the reference (COMMON/PRESS.BLOCK holds pmol,
+ * patom and the masses). */
+int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass);
+/* One evaluation of coor (moil_nb_eval semantics; dpot and energies may be NULL) and MOIL's
+ * pressure analysis terms of every replica, press[12 * replica + k] =
+ *   k 0..2   virXX, virYY, virZZ     LJ molecular virial (pot/watwat_ewald.f:163-175,
+ *                                     pot/cdie_ewald.f:441-453, symm/symwat_ewald.f:161-173)
+ *   k 3..5   V_PIdirXX..ZZ           real-space Ewald Coulomb (watwat_ewald.f:196-204)
+ *   k 6..8   V_PIrecXX..ZZ           reciprocal (pot/ewald_receip.f:799-807)
+ *   k 9..11  V_PIrelXX..ZZ           PME force x position relative to the centre of mass
+ *                                     (ewald_receip.f:928-933)
+ * in kcal/mol; pressure.f:235-238 sums vir + dir + rec - rel (its V_PIcor is zero).  Every
+ * pair term is F_ij,a (R_I - R_J)_a with R the centres of mass.  Mixed path only; needs
+ * moil_nb_set_molecules. */
+int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *energies, double *press);
+
 /* Accumulate the water-water LJ virial terms (virvdw1, virvdw2 of moil_nb_get_virial) on
  * the mixed path (1), or leave them zero (0, default: the extra accumulators cost the
  * FP32 water kernel registers).  The other virial terms and the plain FP64 path always

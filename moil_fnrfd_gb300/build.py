@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmoil_nb.so")
-SOURCES = ["nb_host.cu", "nb_lists.cu", "nb_realspace.cu", "nb_pme.cu", "nb_adjoint.cu", "nb_md.cu"]
+SOURCES = ["nb_host.cu", "nb_lists.cu", "nb_realspace.cu", "nb_pme.cu", "nb_adjoint.cu", "nb_md.cu", "nb_press.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]

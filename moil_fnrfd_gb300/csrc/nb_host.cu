@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "nb_internal.h"
@@ -86,6 +87,10 @@ void release_device(NbCtx *c)
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
     free_ptr(c->d_adj); free_ptr(c->d_md_dpot);
+    free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
+    free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
+    free_ptr(c->d_press_out);
+    c->nmol = 0;
     if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
     c->h_e_rep = nullptr;
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -1009,6 +1014,105 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
         if (out[k])
             NB_CUDA_OK(h, cudaMemcpyAsync(out[k], h->d_adj + k * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
                                           h->stream));
+    NB_CUDA_OK(h, cudaStreamSynchronize(h->stream));
+    return MOIL_NB_OK;
+}
+
+int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (mol && !mass) return MOIL_NB_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (!h->grp.empty()) {
+        for (size_t g = 0; g < h->grp.size(); ++g) {
+            const int64_t a0 = h->grp_atom0[g];
+            int rc = moil_nb_set_molecules(static_cast<moil_nb_ctx *>(h->grp[g]), mol ? mol + a0 : nullptr,
+                                           mol ? mass + a0 : nullptr);
+            if (rc != MOIL_NB_OK) { h->err = h->grp[g]->err; return rc; }
+        }
+        h->nmol = mol ? 1 : 0;
+        return MOIL_NB_OK;
+    }
+    free_ptr(h->d_mol_off); free_ptr(h->d_mol_atom); free_ptr(h->d_mass); free_ptr(h->d_xrel);
+    h->nmol = 0;
+    if (!mol) return MOIL_NB_OK;
+    // CSR over caller atoms: molecules numbered in order of their first atom, atoms ascending
+    const size_t n = (size_t)h->natom;
+    std::vector<int> off(1, 0), atoms, count;
+    std::vector<int> slot(n);
+    for (int r = 0; r < h->nrep; ++r) {
+        const int a0 = h->rd[r].atom0, na = h->rd[r].natom;
+        std::vector<int> id(na, -1);
+        for (int a = a0; a < a0 + na; ++a) {
+            const int m = mol[a];
+            if (m < 0 || m >= na || !(mass[a] >= 0.0) || !std::isfinite(mass[a])) {
+                h->err = "molecule index or mass out of range at atom " + std::to_string(a);
+                return MOIL_NB_ERR_ARG;
+            }
+            if (id[m] < 0) { id[m] = (int)count.size(); count.push_back(0); }
+            slot[a] = id[m];
+            ++count[id[m]];
+        }
+    }
+    const int nmol = (int)count.size();
+    off.resize(nmol + 1);
+    off[0] = 0;
+    for (int m = 0; m < nmol; ++m) off[m + 1] = off[m] + count[m];
+    atoms.resize(n);
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (size_t a = 0; a < n; ++a) atoms[fill[slot[a]]++] = (int)a;
+    NB_CUDA_OK(h, cudaMalloc(&h->d_mol_off, sizeof(int) * (nmol + 1)));
+    NB_CUDA_OK(h, cudaMalloc(&h->d_mol_atom, sizeof(int) * std::max<size_t>(n, 1)));
+    NB_CUDA_OK(h, cudaMalloc(&h->d_mass, sizeof(double) * std::max<size_t>(n, 1)));
+    NB_CUDA_OK(h, cudaMalloc(&h->d_xrel, sizeof(double) * 3 * std::max<size_t>(n, 1)));
+    NB_CUDA_OK(h, cudaMemcpy(h->d_mol_off, off.data(), sizeof(int) * (nmol + 1), cudaMemcpyHostToDevice));
+    NB_CUDA_OK(h, cudaMemcpy(h->d_mol_atom, atoms.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    NB_CUDA_OK(h, cudaMemcpy(h->d_mass, mass, sizeof(double) * n, cudaMemcpyHostToDevice));
+    h->nmol = nmol;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *e, double *press)
+{
+    if (!h || !coor || !press) return MOIL_NB_ERR_ARG;
+    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (h->precision == MOIL_NB_FP64) {
+        h->err = "the pressure analysis terms are computed on the mixed path only";
+        return MOIL_NB_ERR_ARG;
+    }
+    if (h->nmol == 0) {
+        h->err = "no molecules: call moil_nb_set_molecules first";
+        return MOIL_NB_ERR_STATE;
+    }
+    cudaSetDevice(h->device);
+    if (!h->grp.empty()) {
+        for (size_t g = 0; g < h->grp.size(); ++g) {
+            const int64_t a0 = h->grp_atom0[g];
+            const int r0 = h->grp_rep0[g];
+            int rc = moil_nb_pressure(static_cast<moil_nb_ctx *>(h->grp[g]), coor + 3 * a0,
+                                      dpot ? dpot + 3 * a0 : nullptr, e ? e + r0 : nullptr, press + 12 * (size_t)r0);
+            if (rc != MOIL_NB_OK) { h->err = h->grp[g]->err; return rc; }
+        }
+        return MOIL_NB_OK;
+    }
+    const size_t n = (size_t)h->natom;
+    NB_CUDA_OK(h, cudaMemcpyAsync(h->d_coor, coor, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+    int rc = eval_impl(h, h->d_coor, h->d_dpot, e);   // lists, positions, PME binning and shares
+    if (rc != MOIL_NB_OK) return rc;
+    if (!h->d_press_out) {
+        NB_CUDA_OK(h, cudaMalloc(&h->d_press_unit, sizeof(double) * 6 * std::max<int64_t>(h->nW + h->nA, 1)));
+        NB_CUDA_OK(h, cudaMalloc(&h->d_press_site, sizeof(double) * 3 * std::max<int64_t>(h->nsite, 1)));
+        NB_CUDA_OK(h, cudaMalloc(&h->d_press_col, sizeof(double) * 3 * std::max<size_t>(h->cols.size(), 1)));
+        NB_CUDA_OK(h, cudaMalloc(&h->d_press_grid, sizeof(float2) * std::max<int64_t>(h->grid_elems, 1)));
+        NB_CUDA_OK(h, cudaMalloc(&h->d_press_out, sizeof(double) * 12 * h->nrep));
+    }
+    rc = nb_pressure(h, h->d_coor, h->d_press_out);
+    if (rc != MOIL_NB_OK) return rc;
+    NB_CUDA_OK(h, cudaMemcpyAsync(press, h->d_press_out, sizeof(double) * 12 * h->nrep, cudaMemcpyDeviceToHost,
+                                  h->stream));
+    if (dpot)
+        NB_CUDA_OK(h, cudaMemcpyAsync(dpot, h->d_dpot, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
     NB_CUDA_OK(h, cudaStreamSynchronize(h->stream));
     return MOIL_NB_OK;
 }

@@ -137,6 +137,17 @@ struct NbCtx {
     double *d_adj = nullptr;           // parameter derivatives, 3 x natom (allocated on first use)
     double *d_md_dpot = nullptr;       // gradient of the MD steps (moil_nb_md_step, first use)
 
+    // pressure analysis (moil_nb_set_molecules / moil_nb_pressure, nb_press.cu)
+    int nmol = 0;
+    int *d_mol_off = nullptr, *d_mol_atom = nullptr;   // molecules as CSR over caller atoms
+    double *d_mass = nullptr;          // per caller atom
+    double *d_xrel = nullptr;          // position relative to the molecule's centre of mass, 3 per atom
+    double *d_press_unit = nullptr;    // 6 per unit: LJ and real-space Coulomb terms
+    double *d_press_site = nullptr;    // 3 per site: PME force x xrel
+    double *d_press_col = nullptr;     // 3 per PME column work item: reciprocal virial
+    void *d_press_grid = nullptr;      // second half-complex grid for the reciprocal virial
+    double *d_press_out = nullptr;     // 12 per replica
+
     // device status: [0] rebuild flag, [1] error bits, [2..4] W1 / W2 / X entry totals,
     // [6] longest W1 row; all reset at the start of every evaluation
     int *d_status = nullptr;
@@ -188,6 +199,8 @@ int nb_pme_configure(NbCtx *c);
 void nb_launch_finalize(NbCtx *c, double *d_dpot);
 // parameter derivatives after an evaluation of c->d_coor (nb_adjoint.cu), mixed path
 int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds);
+// pressure analysis terms after an evaluation of d_coor (nb_press.cu), mixed path: 12 per replica
+int nb_pressure(NbCtx *c, const double *d_coor, double *d_out);
 
 #define NB_CUDA_OK(c, call)                                                         \
     do {                                                                            \

@@ -544,6 +544,71 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     }
 }
 
+// Reciprocal virial of the pressure analysis (ewald_receip.f:799-807, pressON): the z
+// transform of k_zconv_f's columns, then per m the diagonal terms
+// E(m) (1 - 2 (1 + pi^2 m^2 / alpha^2) m_a^2 / m^2) with E(m) = wgt * eterm * |S(m)|^2 as the
+// energy sum forms it; three FP64 partial sums per column work item (fixed-order reduction)
+__global__ void __launch_bounds__(256) k_press_zvir_f(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                      const FftPlanDev *__restrict__ plans,
+                                                      const int *__restrict__ rep_plan, const float2 *__restrict__ tw,
+                                                      const int2 *__restrict__ tab, const float *__restrict__ bsp_all,
+                                                      const float2 *__restrict__ grid, double *__restrict__ v_col)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[3][8];
+    const ColWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
+    const int tk = min(NB_TKF, n2 - w.ky0);
+    const float *bsp = bsp_all + R.bsp0;
+    float2 *A = (float2 *)smem, *B = A + zconv_buf_elems(n3);
+    FftCtx c3;
+    fft_ctx_load((unsigned char *)(B + zconv_buf_elems(n3)), plans + rep_plan[3 * w.rep + 2], tab, tw, c3);
+    const int sA = n3 | 1;
+    const float2 *g = grid + R.g0 + (size_t)w.kx * n2 + w.ky0;
+    const size_t zs = (size_t)n1h * n2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int kz = warp; kz < n3; kz += 8)
+        if (lane < tk) A[lane * sA + kz] = g[kz * zs + lane];
+    __syncthreads();
+    const float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0, sA, n3);
+    const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
+    const float fac2 = R.pme_fac2f, pivol = R.pivolf, fac = (float)R.pme_fac;
+    const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
+    const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
+    const float mh1 = (float)w.kx * iL0, pb1 = pivol * bsp[w.kx];
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    for (int c = warp; c < tk; c += 8) {
+        const int ky = w.ky0 + c;
+        const float mh2 = (float)(ky < nf2 ? ky : ky - n2) * iL1;
+        const float pb12 = pb1 * bsp[n1 + ky], m12 = mh1 * mh1 + mh2 * mh2;
+        for (int kz = lane; kz < n3; kz += 32) {
+            if (w.kx == 0 && ky == 0 && kz == 0) continue;
+            const float mh3 = (float)(kz < nf3 ? kz : kz - n3) * iL2;
+            const float msq = fmaf(mh3, mh3, m12);
+            const float et = nb_ex2_approx(-fac2 * msq) * nb_rcp_approx(pb12 * bsp[n1 + n2 + kz] * msq);
+            const float2 v = F[c * n3 + kz];
+            const float e = wgt * et * (v.x * v.x + v.y * v.y), b = 2.f * (1.f + fac * msq) / msq;
+            v0 += e * (1.f - b * mh1 * mh1);
+            v1 += e * (1.f - b * mh2 * mh2);
+            v2 += e * (1.f - b * mh3 * mh3);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v0 += __shfl_down_sync(0xffffffffu, v0, o);
+        v1 += __shfl_down_sync(0xffffffffu, v1, o);
+        v2 += __shfl_down_sync(0xffffffffu, v2, o);
+    }
+    if (lane == 0) { red[0][warp] = v0; red[1][warp] = v1; red[2][warp] = v2; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double sum = 0.0;
+        for (int k = 0; k < 8; ++k) sum += red[threadIdx.x][k];
+        v_col[3 * (size_t)blockIdx.x + threadIdx.x] = sum;
+    }
+}
+
 // inverse y and x transforms of plane z; the real potential plane (n1 x n2 floats) is stored
 // over the plane's own complex storage, which this block alone reads, for k_pme_gather_f
 __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
@@ -963,6 +1028,7 @@ cudaError_t raise_pme_limits(size_t sf, size_t sz, size_t si)
     if (sizeof(T) == 4) {
         if ((e = raise_smem_limit(k_plane_fwd_f, sf)) != cudaSuccess) return e;
         if ((e = raise_smem_limit(k_zconv_f, sz)) != cudaSuccess) return e;
+        if ((e = raise_smem_limit(k_press_zvir_f, sz)) != cudaSuccess) return e;
         return raise_smem_limit(k_plane_inv_f, si);
     }
     if ((e = raise_smem_limit(k_plane_fwd<T>, sf)) != cudaSuccess) return e;
@@ -1063,6 +1129,21 @@ void nb_launch_pme(NbCtx *c)
 {
     if (c->precision == MOIL_NB_FP64) pme_t<double>(c);
     else pme_t<float>(c);
+}
+
+// pressure analysis: the charge planes of the evaluation's binning spread and transformed
+// again into grid (a copy beside the handle's own grid, whose potential planes stay valid),
+// and the reciprocal virial per column work item into v_col (mixed path)
+void nb_launch_pme_virial(NbCtx *c, void *grid, double *v_col)
+{
+    cudaStream_t s = c->stream;
+    const int np = (int)c->planes.size(), nc = (int)c->cols.size();
+    k_plane_fwd_f<<<np, 256, c->smem_plane_fwd, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                       (const float2 *)c->d_tw, c->d_tab, c->d_zstart, c->d_zatoms,
+                                                       (const float4 *)c->d_fr, (float2 *)grid);
+    k_press_zvir_f<<<nc, 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                   (const float2 *)c->d_tw, c->d_tab, (const float *)c->d_bsp,
+                                                   (const float2 *)grid, v_col);
 }
 
 int nb_pme_configure(NbCtx *c)

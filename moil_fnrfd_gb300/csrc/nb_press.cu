@@ -1,0 +1,297 @@
+// nb_press.cu -- MOIL's pressure analysis terms (analysis/pressure.f, pressON) after an
+// evaluation: per replica the diagonal of the molecular virial, split as pressure.f prints it,
+//   virXX..ZZ    LJ pairs (pot/watwat_ewald.f:163-175, pot/cdie_ewald.f:441-453 and
+//                555-566, image pairs symm/symwat_ewald.f:161-173, symm/symcdie_ewald.f:151-161)
+//   V_PIdirXX..  real-space Ewald Coulomb pairs (watwat_ewald.f:196-204,
+//                cdie_ewald.f:412-429, symwat_ewald.f:193-203)
+//   V_PIrecXX..  reciprocal sum (pot/ewald_receip.f:799-807; k_press_zvir_f in nb_pme.cu)
+//   V_PIrelXX..  PME force times the atom's position relative to its molecule's centre of
+//                mass (ewald_receip.f:928-933)
+// pressure.f:235-238 adds vir + dir + rec - rel; V_PIcor stays zero (its accumulation is
+// commented out in cdie_ewald.f:165-170).
+//
+// Every pair term is F_ij,a (R_I - R_J)_a, R the centres of mass in the image the pair is
+// taken in.  R_I - R_J is formed as r_ij - xrel_i + xrel_j from the pair's own minimum-image
+// separation and the atoms' positions relative to their centres of mass (xrel), so no centre
+// of mass is imaged.  Molecules are made whole by placing each atom at the minimum image of
+// its displacement from the previous atom of its molecule (pressure.f joins them along bonds
+// with checkANDmove, :985-1010), which needs consecutive atoms of a molecule closer than half
+// the box.
+//
+// The pass reuses the evaluation's lists, site positions, PME binning and PME gradient
+// shares, with the pair predicates and FP32 pair arithmetic of the energy kernels; products
+// with the centre-of-mass separations and all sums are FP64.  Full lists hold every pair
+// twice: water-water and atom-atom terms are halved at the end, water-atom pairs are taken
+// from the atom's side only with weight two.
+#include "nb_internal.h"
+
+namespace {
+
+// positions relative to the centres of mass, per caller atom; one thread per molecule
+__global__ void k_press_xrel(int nmol, const int *__restrict__ mol_off, const int *__restrict__ mol_atom,
+                             const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
+                             const double *__restrict__ coor, const double *__restrict__ mass,
+                             double *__restrict__ xrel)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    const int b = mol_off[m], e = mol_off[m + 1];
+    const RepDev &R = reps[atom_rep[mol_atom[b]]];
+    double d[3] = {0.0, 0.0, 0.0}, sm[3] = {0.0, 0.0, 0.0}, M = 0.0;
+    int prev = mol_atom[b];
+    for (int k = b; k < e; ++k) {
+        const int a = mol_atom[k];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            if (k > b) {
+                const double t = coor[3 * (size_t)a + x] - coor[3 * (size_t)prev + x];
+                d[x] += t - R.Ld[x] * rint(t * R.invLd[x]);
+            }
+            xrel[3 * (size_t)a + x] = d[x];
+            sm[x] += mass[a] * d[x];
+        }
+        M += mass[a];
+        prev = a;
+    }
+    for (int k = b; k < e; ++k) {
+        const int a = mol_atom[k];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) xrel[3 * (size_t)a + x] -= M > 0.0 ? sm[x] / M : 0.0;
+    }
+}
+
+// water molecule per thread over its W1 row: 9 Coulomb site pairs and the O-O LJ pair of
+// every molecule inside the O-O cutoff (watwat_ewald.f semantics, water charges of RepDev)
+template <typename E>
+__global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                              const int *__restrict__ site_orig, const float4 *__restrict__ pos,
+                              const float4 *__restrict__ woff, const int2 *__restrict__ wl1_cnt,
+                              const void *__restrict__ wl1, int cap_row, const double *__restrict__ xrel,
+                              double *__restrict__ pu)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nW) return;
+    const RepDev &R = reps[site_rep[3 * i]];
+    const float4 oi = pos[3 * i], h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
+    const float hi[3][3] = {{0.f, 0.f, 0.f}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
+    const double *xi = xrel + 3 * (size_t)site_orig[3 * i];
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    const int2 c = wl1_cnt[i];
+    const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
+    const E *row = (const E *)wl1 + (size_t)i * cap_row;
+    const int base = sizeof(E) == 2 ? R.wat0 : 0;
+    for (int q = 0; q < n; ++q) {
+        const int j = base + (int)row[q < nn ? q : cap_row - 1 - (q - nn)];
+        const float4 oj = pos[3 * j];
+        float d[3] = {oi.x - oj.x, oi.y - oj.y, oi.z - oj.z};
+#pragma unroll
+        for (int x = 0; x < 3; ++x) d[x] = nb_shift(R, x, d[x], nb_rint(d[x] * R.invL[x]));
+        const float r2oo = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2oo > R.rmax2) continue;
+        const float4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
+        const float hj[3][3] = {{0.f, 0.f, 0.f}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
+        const double *xj = xrel + 3 * (size_t)site_orig[3 * j];
+        double rm[3];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) rm[x] = (double)d[x] - xi[x] + xj[x];
+        float fc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const float ex = hi[a][0] + d[0] - hj[b][0], ey = hi[a][1] + d[1] - hj[b][1],
+                            ez = hi[a][2] + d[2] - hj[b][2];
+                const float rr2 = ex * ex + ey * ey + ez * ez, rinv = nb_rsqrt_approx(rr2);
+                float exv;
+                const float erfcv = nb_erfc_ex(R.alpha * rr2 * rinv, rr2 * R.ex2c, &exv);
+                const float qq = R.qq[(a == 0 && b == 0) ? 0 : ((a == 0 || b == 0) ? 1 : 2)];
+                const float e = qq * erfcv * rinv;
+                const float mdf = (e + qq * R.c2a * exv) * rinv * rinv;   // minus dE/dr / r
+                fc[0] += mdf * ex; fc[1] += mdf * ey; fc[2] += mdf * ez;
+            }
+#pragma unroll
+        for (int x = 0; x < 3; ++x) v[3 + x] += (double)fc[x] * rm[x];
+        if (r2oo <= R.rv2) {
+            const float s2 = 1.f / r2oo, s6 = s2 * s2 * s2;
+            const float A = R.w12 * s6 * s6, B = R.w6 * s6;
+            float e1 = A - B, df1 = -6.f * s2 * (A + e1);
+            if (R.lj_switch) {
+                if (r2oo > R.ron2) {
+                    const float dd = R.rv2 - r2oo;
+                    const float sw = dd * dd * (R.rv2 + 2.f * r2oo - 3.f * R.ron2) * R.swden;
+                    const float dsw = 12.f * dd * (R.ron2 - r2oo) * R.swden;
+                    df1 = df1 * sw + e1 * dsw;
+                }
+            }
+#pragma unroll
+            for (int x = 0; x < 3; ++x) v[x] -= (double)(df1 * d[x]) * rm[x];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) pu[6 * (size_t)i + k] = v[k];
+}
+
+// non-water atom per thread over its X list (non-water atoms and water sites), the pair
+// predicate of the energy kernels' atom_pair (cdie_ewald.f list1/2/3, nbond.f:115-126)
+__global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+                             const int *__restrict__ site_orig, const float4 *__restrict__ pos,
+                             const float2 *__restrict__ lj, const unsigned *__restrict__ sflags,
+                             const int *__restrict__ xl_off, const int *__restrict__ xl, int capx,
+                             const double *__restrict__ xrel, double *__restrict__ pu)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nA) return;
+    const int si = 3 * nW + k;
+    const RepDev &R = reps[site_rep[si]];
+    const float4 xi = pos[si];
+    const float2 lji = lj[si];
+    const unsigned fi = sflags[si];
+    const double *xa = xrel + 3 * (size_t)site_orig[si];
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = min(xl_off[k], capx); q < min(xl_off[k + 1], capx); ++q) {
+        const int s = xl[q];
+        const float4 xj = pos[s];
+        float d[3] = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
+#pragma unroll
+        for (int x = 0; x < 3; ++x) d[x] = nb_shift(R, x, d[x], nb_rint(d[x] * R.invL[x]));
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const unsigned fj = sflags[s];
+        const bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < R.re2;
+        const bool do_lj = r2 < R.rv2 && !hr;
+        float qq = xi.w * xj.w;
+        const bool do_el = r2 < R.rmax2 && qq != 0.f;
+        if (!do_lj && !do_el) continue;
+        const float rinv = nb_rsqrt_approx(r2), s2 = rinv * rinv;
+        float df_el = 0.f, df_lj = 0.f;
+        if (do_el) {
+            float exv;
+            const float erfcv = nb_erfc_ex(R.alpha * r2 * rinv, r2 * R.ex2c, &exv);
+            qq *= (float)R.epstmp;
+            const float e = qq * erfcv * rinv;
+            df_el = -(e + qq * R.c2a * exv) * s2;
+        }
+        if (do_lj) {
+            const float2 ljj = lj[s];
+            const float s6 = s2 * s2 * s2;
+            float A, B;
+            if (!R.arith) {
+                A = lji.x * ljj.x * s6 * s6;
+                B = lji.y * ljj.y * s6;
+            } else {
+                const float aa = lji.x * ljj.x, sg = 0.5f * (lji.y + ljj.y);
+                float b1 = sg * sg * sg;
+                b1 = b1 * b1;
+                B = aa * b1 * s6;
+                A = aa * b1 * b1 * s6 * s6;
+            }
+            const float e1 = A - B;
+            df_lj = -6.f * s2 * (A + e1);
+            if (R.lj_switch && r2 > R.ron2) {
+                const float dd = R.rv2 - r2;
+                const float sw = dd * dd * (R.rv2 + 2.f * r2 - 3.f * R.ron2) * R.swden;
+                const float dsw = 12.f * dd * (R.ron2 - r2) * R.swden;
+                df_lj = df_lj * sw + e1 * dsw;
+            }
+        }
+        const double w = s < 3 * nW ? 2.0 : 1.0;   // water partners: this side only
+        const double *xb = xrel + 3 * (size_t)site_orig[s];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            const double rm = (double)d[x] - xa[x] + xb[x];
+            v[x] -= w * (double)(df_lj * d[x]) * rm;
+            v[3 + x] -= w * (double)(df_el * d[x]) * rm;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) pu[6 * (size_t)(nW + k) + q] = v[q];
+}
+
+// V_PIrel per site: the PME force (minus the gradient share k_final_grad adds) times xrel
+__global__ void k_press_rel(int nsite, const int *__restrict__ site_rep, const int *__restrict__ site_orig,
+                            const RepDev *__restrict__ reps, const float4 *__restrict__ part,
+                            const double *__restrict__ q, const double *__restrict__ xrel, double *__restrict__ ps)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsite) return;
+    const RepDev &R = reps[site_rep[s]];
+    const int a = site_orig[s];
+    const float4 p = part[s];
+    const double g[3] = {(double)p.x, (double)p.y, (double)p.z};
+#pragma unroll
+    for (int x = 0; x < 3; ++x) ps[3 * (size_t)s + x] = -q[a] * (double)R.pme_gs[x] * g[x] * xrel[3 * (size_t)a + x];
+}
+
+// per replica, fixed order: strided slots per thread, then a halving tree
+#define NB_PR_THREADS 256
+__global__ void __launch_bounds__(NB_PR_THREADS) k_press_reduce(int nW, const RepDev *__restrict__ reps,
+                                                               const double *__restrict__ pu,
+                                                               const double *__restrict__ ps,
+                                                               const double *__restrict__ v_col,
+                                                               const int *__restrict__ col_begin,
+                                                               double *__restrict__ out)
+{
+    __shared__ double red[12][NB_PR_THREADS];
+    const int r = blockIdx.x, t = threadIdx.x;
+    const RepDev &R = reps[r];
+    double acc[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) acc[k] = 0.0;
+    const int u0[2] = {R.wat0, nW + R.oth0}, nu[2] = {R.nwat, R.noth};
+    const int s0[2] = {3 * R.wat0, 3 * nW + R.oth0}, ns[2] = {3 * R.nwat, R.noth};
+    for (int p = 0; p < 2; ++p) {
+        for (int u = t; u < nu[p]; u += NB_PR_THREADS) {
+            const double *v = pu + 6 * (size_t)(u0[p] + u);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) acc[k] += v[k];
+        }
+        for (int u = t; u < ns[p]; u += NB_PR_THREADS) {
+            const double *v = ps + 3 * (size_t)(s0[p] + u);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc[9 + k] += v[k];
+        }
+    }
+    for (int w = col_begin[r] + t; w < col_begin[r + 1]; w += NB_PR_THREADS) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc[6 + k] += v_col[3 * (size_t)w + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 12; ++k) red[k][t] = acc[k];
+    __syncthreads();
+    for (int h = NB_PR_THREADS / 2; h > 0; h >>= 1) {
+        if (t < h)
+#pragma unroll
+            for (int k = 0; k < 12; ++k) red[k][t] += red[k][t + h];
+        __syncthreads();
+    }
+    if (t < 12) out[12 * (size_t)r + t] = (t < 9 ? 0.5 : 1.0) * red[t][0];
+}
+
+}  // namespace
+
+void nb_launch_pme_virial(NbCtx *c, void *grid, double *v_col);
+
+int nb_pressure(NbCtx *c, const double *d_coor, double *d_out)
+{
+    cudaStream_t s = c->stream;
+    const int B = 128;
+    if (c->nmol > 0)
+        k_press_xrel<<<(c->nmol + B - 1) / B, B, 0, s>>>(c->nmol, c->d_mol_off, c->d_mol_atom, c->d_atom_rep,
+                                                        c->d_reps, d_coor, c->d_mass, c->d_xrel);
+    if (c->nW > 0)
+        (c->row16 ? k_press_water<unsigned short> : k_press_water<int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
+            (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
+            (const float4 *)c->d_woff, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_xrel, c->d_press_unit);
+    if (c->nA > 0)
+        k_press_atom<<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
+            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
+            (const float2 *)c->d_site_lj, c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), c->d_xrel,
+            c->d_press_unit);
+    k_press_rel<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
+                                                            c->d_reps, (const float4 *)c->d_part, c->d_q, c->d_xrel,
+                                                            c->d_press_site);
+    nb_launch_pme_virial(c, c->d_press_grid, c->d_press_col);
+    k_press_reduce<<<c->nrep, NB_PR_THREADS, 0, s>>>((int)c->nW, c->d_reps, c->d_press_unit, c->d_press_site,
+                                                     c->d_press_col, c->d_col_begin, d_out);
+    NB_CUDA_OK(c, cudaGetLastError());
+    return MOIL_NB_OK;
+}

@@ -31,7 +31,7 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
             "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "moil_nb_md_step",
-            "moil_nb_dcd_write", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
+            "moil_nb_dcd_write", "moil_nb_set_molecules", "moil_nb_pressure", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -119,6 +119,8 @@ def load(build_if_missing: bool = True):
                                   ctypes.c_double, ctypes.c_int, _dp, ctypes.POINTER(Energies), _dp]
     L.moil_nb_dcd_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
     L.moil_nb_groups.argtypes = [ctypes.c_void_p]
+    L.moil_nb_set_molecules.argtypes = [ctypes.c_void_p, _ip, _dp]
+    L.moil_nb_pressure.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(Energies), _dp]
     _lib = L
     return L
 
@@ -295,6 +297,36 @@ class Nonbonded:
         if not self.batch:
             return tuple(out)
         return tuple([o[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))] for o in out)
+
+    def set_molecules(self, mol, mass):
+        """Molecules and masses of every atom for the pressure analysis
+        (moil_nb_set_molecules); None switches it off."""
+        if mol is None:
+            _check(self.L, self.h, self.L.moil_nb_set_molecules(self.h, None, None))
+            return
+        self._mol = np.ascontiguousarray(mol, dtype=np.int32).reshape(self.natom)
+        self._mass = np.ascontiguousarray(mass, dtype=np.float64).reshape(self.natom)
+        _check(self.L, self.h, self.L.moil_nb_set_molecules(self.h, self._mol.ctypes.data_as(_ip),
+                                                            self._mass.ctypes.data_as(_dp)))
+
+    def pressure(self, coor=None):
+        """One evaluation and MOIL's pressure analysis terms (moil_nb_pressure): (dpot,
+        energies, press), press the 12 values virXX..ZZ, V_PIdir, V_PIrec, V_PIrel; batch:
+        lists per replica."""
+        if coor is None:
+            coor = np.concatenate([s.coor for s in self.systems], axis=0)
+        elif self.batch and isinstance(coor, (list, tuple)):
+            coor = np.concatenate(coor, axis=0)
+        coor = np.ascontiguousarray(coor, dtype=np.float64).reshape(self.natom, 3)
+        dpot = np.empty_like(coor)
+        press = np.empty((len(self.systems), 12), dtype=np.float64)
+        _check(self.L, self.h, self.L.moil_nb_pressure(self.h, coor.ctypes.data_as(_dp), dpot.ctypes.data_as(_dp),
+                                                       self._e, press.ctypes.data_as(_dp)))
+        e = self.energies()
+        if not self.batch:
+            return dpot, e[0], press[0]
+        return ([dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))], e,
+                [press[k] for k in range(len(self.systems))])
 
     def eforce_device(self, d_coor_ptr: int, d_dpot_ptr: int, want_energies: bool = True):
         """Evaluate on device-resident buffers (raw CUDA pointers)."""
