@@ -15,6 +15,8 @@ roofline   : the dominant kernel against the FP32 pipe (pair math is FP32-bound)
 cpu_baseline: the oracle (a C restatement of MOIL's FP64 routines, MOIL's own list path
              and erfc table) on a bounded sample of replicas, one host thread
 plain_fp64 : the plain FP64 GPU path, one replica per launch, on a sample of replicas
+pressure_analysis: MOIL's pressure-analysis terms (molecular virial tensor, moil_nb_pressure) of
+             the whole batch, host buffers, wall clock per call (one evaluation + the pass)
 single_system_md: one 96,000-atom water box through a 1,000-step rigid-water trajectory on the
              device (lists every 10 steps, 1.5 Å skin), whole steps timed, the FP64 path beside it
 """
@@ -134,6 +136,25 @@ def cpu_baseline(reps, budget_s=12.0):
                       f"{dt:.1f} s"}
 
 
+def press_leg(nb, reps, coor, e2e_ms, calls=3):
+    """moil_nb_pressure on the whole batch (every replica a TIP3P box, one molecule per water):
+    one evaluation plus the molecular-virial pass per call, host buffers, wall clock."""
+    from moil_fnrfd_gb300.systems import MASS_H, MASS_O
+    mol = np.concatenate([np.arange(s.npt, dtype=np.int32) // 3 for s in reps])
+    mass = np.tile(np.array([MASS_O, MASS_H, MASS_H]), len(mol) // 3)
+    nb.set_molecules(mol, mass)
+    nb.pressure(coor)                      # first call allocates the pass's buffers
+    t = []
+    for _ in range(calls):
+        t0 = time.perf_counter()
+        nb.pressure(coor)
+        t.append((time.perf_counter() - t0) * 1e3)
+    nb.set_molecules(None, None)
+    ms = statistics.median(t)
+    return {"ms_per_call": ms, "eval_e2e_ms": statistics.median(e2e_ms), "pass_ms": ms - statistics.median(e2e_ms),
+            "calls": calls, "sample": "the timed batch, molecules = waters"}
+
+
 def md_leg(local, steps=1000, warmup=20):
     """One 96,000-atom water box (32,000 TIP3P, 98.6 Å, rc 10, alpha 0.32, grid 100^3) through
     a rigid-water leapfrog trajectory on the device (moil_nb_md_step: evaluation, leapfrog and
@@ -225,6 +246,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 leg")
     ap.add_argument("--replicas", type=int, default=512, help="first R replicas only (profiling captures)")
     ap.add_argument("--no-md", action="store_true", help="skip the single-system trajectory leg")
+    ap.add_argument("--no-press", action="store_true", help="skip the pressure-analysis leg")
     ap.add_argument("--groups", type=int, default=0,
                     help="replica groups evaluated concurrently (0: the library's automatic choice)")
     args = ap.parse_args()
@@ -314,6 +336,8 @@ def main():
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_value = natoms * args.steps * world / (sum(e2e_ms) / 1e3)
 
+    press = press_leg(nb, reps, hc, e2e_ms) if not args.no_press and rank == 0 else None
+
     # dominant kernel and its roofline (FP32 pipe): average over steps without a rebuild
     no_build = [t for t in stages if not t["list_rebuilt"]] or stages
     keys = ["water_ms", "atom_ms", "excl_ms", "pme_spread_fft_ms", "pme_conv_ms", "pme_gather_ms", "finalize_ms"]
@@ -394,6 +418,8 @@ def main():
         out["speedup_vs_plain_fp64"] = value / fp64_value
         out["force_err_vs_fp64"] = {"max_rel_rms": max(errs), "replicas": len(errs)}
     nb.close()
+    if press is not None:
+        out["pressure_analysis"] = press
 
     if not args.no_md and rank == 0:
         out["single_system_md"] = md_leg(local)
