@@ -88,7 +88,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
     free_ptr(c->d_adj); free_ptr(c->d_md_dpot);
     free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
-    free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
+    free_ptr(c->d_xrelf); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
     free_ptr(c->d_press_out);
     c->nmol = 0;
     if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
@@ -1035,6 +1035,7 @@ int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
         return MOIL_NB_OK;
     }
     free_ptr(h->d_mol_off); free_ptr(h->d_mol_atom); free_ptr(h->d_mass); free_ptr(h->d_xrel);
+    free_ptr(h->d_xrelf);
     h->nmol = 0;
     if (!mol) return MOIL_NB_OK;
     // CSR over caller atoms: molecules numbered in order of their first atom, atoms ascending
@@ -1066,6 +1067,7 @@ int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
     NB_CUDA_OK(h, cudaMalloc(&h->d_mol_atom, sizeof(int) * std::max<size_t>(n, 1)));
     NB_CUDA_OK(h, cudaMalloc(&h->d_mass, sizeof(double) * std::max<size_t>(n, 1)));
     NB_CUDA_OK(h, cudaMalloc(&h->d_xrel, sizeof(double) * 3 * std::max<size_t>(n, 1)));
+    NB_CUDA_OK(h, cudaMalloc(&h->d_xrelf, sizeof(float4) * std::max<size_t>(n, 1)));
     NB_CUDA_OK(h, cudaMemcpy(h->d_mol_off, off.data(), sizeof(int) * (nmol + 1), cudaMemcpyHostToDevice));
     NB_CUDA_OK(h, cudaMemcpy(h->d_mol_atom, atoms.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     NB_CUDA_OK(h, cudaMemcpy(h->d_mass, mass, sizeof(double) * n, cudaMemcpyHostToDevice));

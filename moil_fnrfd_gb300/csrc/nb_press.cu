@@ -19,19 +19,23 @@
 // the box.
 //
 // The pass reuses the evaluation's lists, site positions, PME binning and PME gradient
-// shares, with the pair predicates and FP32 pair arithmetic of the energy kernels; products
-// with the centre-of-mass separations and all sums are FP64.  Full lists hold every pair
+// shares, with the pair predicates and FP32 pair arithmetic of the energy kernels; the
+// products with the centre-of-mass separations are FP32 too, summed per thread in FP32 over
+// chunks of NB_PCHUNK list entries and in FP64 across chunks (an FP64 operation per pair
+// would cost more than the pair itself: the FP64 pipe is 1/64 of FP32).  Full lists hold every pair
 // twice: water-water and atom-atom terms are halved at the end, water-atom pairs are taken
 // from the atom's side only with weight two.
 #include "nb_internal.h"
 
 namespace {
 
+#define NB_PCHUNK 32
+
 // positions relative to the centres of mass, per caller atom; one thread per molecule
 __global__ void k_press_xrel(int nmol, const int *__restrict__ mol_off, const int *__restrict__ mol_atom,
                              const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
                              const double *__restrict__ coor, const double *__restrict__ mass,
-                             double *__restrict__ xrel)
+                             double *__restrict__ xrel, float4 *__restrict__ xrelf)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmol) return;
@@ -55,8 +59,10 @@ __global__ void k_press_xrel(int nmol, const int *__restrict__ mol_off, const in
     }
     for (int k = b; k < e; ++k) {
         const int a = mol_atom[k];
+        float f[3];
 #pragma unroll
-        for (int x = 0; x < 3; ++x) xrel[3 * (size_t)a + x] -= M > 0.0 ? sm[x] / M : 0.0;
+        for (int x = 0; x < 3; ++x) f[x] = (float)(xrel[3 * (size_t)a + x] - (M > 0.0 ? sm[x] / M : 0.0));
+        xrelf[a] = make_float4(f[0], f[1], f[2], 0.f);
     }
 }
 
@@ -66,7 +72,7 @@ template <typename E>
 __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                               const int *__restrict__ site_orig, const float4 *__restrict__ pos,
                               const float4 *__restrict__ woff, const int2 *__restrict__ wl1_cnt,
-                              const void *__restrict__ wl1, int cap_row, const double *__restrict__ xrel,
+                              const void *__restrict__ wl1, int cap_row, const float4 *__restrict__ xrel,
                               double *__restrict__ pu)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -74,13 +80,16 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
     const RepDev &R = reps[site_rep[3 * i]];
     const float4 oi = pos[3 * i], h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
     const float hi[3][3] = {{0.f, 0.f, 0.f}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
-    const double *xi = xrel + 3 * (size_t)site_orig[3 * i];
+    const float4 xi = xrel[site_orig[3 * i]];
     double v[6] = {0, 0, 0, 0, 0, 0};
+    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int cnt = 0;
     const int2 c = wl1_cnt[i];
     const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
     const E *row = (const E *)wl1 + (size_t)i * cap_row;
     const int base = sizeof(E) == 2 ? R.wat0 : 0;
     for (int q = 0; q < n; ++q) {
+        if (q + 32 < nn) nb_prefetch_l1(row + q + 32);   // the row is a DRAM stream per lane
         const int j = base + (int)row[q < nn ? q : cap_row - 1 - (q - nn)];
         const float4 oj = pos[3 * j];
         float d[3] = {oi.x - oj.x, oi.y - oj.y, oi.z - oj.z};
@@ -90,10 +99,8 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
         if (r2oo > R.rmax2) continue;
         const float4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
         const float hj[3][3] = {{0.f, 0.f, 0.f}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
-        const double *xj = xrel + 3 * (size_t)site_orig[3 * j];
-        double rm[3];
-#pragma unroll
-        for (int x = 0; x < 3; ++x) rm[x] = (double)d[x] - xi[x] + xj[x];
+        const float4 xj = xrel[site_orig[3 * j]];
+        const float rm[3] = {d[0] - xi.x + xj.x, d[1] - xi.y + xj.y, d[2] - xi.z + xj.z};
         float fc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -110,7 +117,7 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
                 fc[0] += mdf * ex; fc[1] += mdf * ey; fc[2] += mdf * ez;
             }
 #pragma unroll
-        for (int x = 0; x < 3; ++x) v[3 + x] += (double)fc[x] * rm[x];
+        for (int x = 0; x < 3; ++x) f[3 + x] = fmaf(fc[x], rm[x], f[3 + x]);
         if (r2oo <= R.rv2) {
             const float s2 = 1.f / r2oo, s6 = s2 * s2 * s2;
             const float A = R.w12 * s6 * s6, B = R.w6 * s6;
@@ -124,11 +131,16 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
                 }
             }
 #pragma unroll
-            for (int x = 0; x < 3; ++x) v[x] -= (double)(df1 * d[x]) * rm[x];
+            for (int x = 0; x < 3; ++x) f[x] = fmaf(-df1 * d[x], rm[x], f[x]);
+        }
+        if (++cnt == NB_PCHUNK) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) { v[k] += (double)f[k]; f[k] = 0.f; }
+            cnt = 0;
         }
     }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) pu[6 * (size_t)i + k] = v[k];
+    for (int k = 0; k < 6; ++k) pu[6 * (size_t)i + k] = v[k] + (double)f[k];
 }
 
 // non-water atom per thread over its X list (non-water atoms and water sites), the pair
@@ -137,7 +149,7 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
                              const int *__restrict__ site_orig, const float4 *__restrict__ pos,
                              const float2 *__restrict__ lj, const unsigned *__restrict__ sflags,
                              const int *__restrict__ xl_off, const int *__restrict__ xl, int capx,
-                             const double *__restrict__ xrel, double *__restrict__ pu)
+                             const float4 *__restrict__ xrel, double *__restrict__ pu)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nA) return;
@@ -146,8 +158,10 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
     const float4 xi = pos[si];
     const float2 lji = lj[si];
     const unsigned fi = sflags[si];
-    const double *xa = xrel + 3 * (size_t)site_orig[si];
+    const float4 xa = xrel[site_orig[si]];
     double v[6] = {0, 0, 0, 0, 0, 0};
+    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int cnt = 0;
     for (int q = min(xl_off[k], capx); q < min(xl_off[k + 1], capx); ++q) {
         const int s = xl[q];
         const float4 xj = pos[s];
@@ -193,32 +207,38 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
                 df_lj = df_lj * sw + e1 * dsw;
             }
         }
-        const double w = s < 3 * nW ? 2.0 : 1.0;   // water partners: this side only
-        const double *xb = xrel + 3 * (size_t)site_orig[s];
+        const float w = s < 3 * nW ? -2.f : -1.f;   // water partners: this side only
+        const float4 xb = xrel[site_orig[s]];
+        const float rm[3] = {d[0] - xa.x + xb.x, d[1] - xa.y + xb.y, d[2] - xa.z + xb.z};
 #pragma unroll
         for (int x = 0; x < 3; ++x) {
-            const double rm = (double)d[x] - xa[x] + xb[x];
-            v[x] -= w * (double)(df_lj * d[x]) * rm;
-            v[3 + x] -= w * (double)(df_el * d[x]) * rm;
+            f[x] = fmaf(w * df_lj * d[x], rm[x], f[x]);
+            f[3 + x] = fmaf(w * df_el * d[x], rm[x], f[3 + x]);
+        }
+        if (++cnt == NB_PCHUNK) {
+#pragma unroll
+            for (int m = 0; m < 6; ++m) { v[m] += (double)f[m]; f[m] = 0.f; }
+            cnt = 0;
         }
     }
 #pragma unroll
-    for (int q = 0; q < 6; ++q) pu[6 * (size_t)(nW + k) + q] = v[q];
+    for (int q = 0; q < 6; ++q) pu[6 * (size_t)(nW + k) + q] = v[q] + (double)f[q];
 }
 
 // V_PIrel per site: the PME force (minus the gradient share k_final_grad adds) times xrel
 __global__ void k_press_rel(int nsite, const int *__restrict__ site_rep, const int *__restrict__ site_orig,
                             const RepDev *__restrict__ reps, const float4 *__restrict__ part,
-                            const double *__restrict__ q, const double *__restrict__ xrel, double *__restrict__ ps)
+                            const double *__restrict__ q, const float4 *__restrict__ xrel, double *__restrict__ ps)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsite) return;
     const RepDev &R = reps[site_rep[s]];
     const int a = site_orig[s];
-    const float4 p = part[s];
-    const double g[3] = {(double)p.x, (double)p.y, (double)p.z};
-#pragma unroll
-    for (int x = 0; x < 3; ++x) ps[3 * (size_t)s + x] = -q[a] * (double)R.pme_gs[x] * g[x] * xrel[3 * (size_t)a + x];
+    const float4 p = part[s], x = xrel[a];
+    const float qs = -(float)q[a];
+    ps[3 * (size_t)s] = (double)(qs * R.pme_gs[0] * p.x * x.x);
+    ps[3 * (size_t)s + 1] = (double)(qs * R.pme_gs[1] * p.y * x.y);
+    ps[3 * (size_t)s + 2] = (double)(qs * R.pme_gs[2] * p.z * x.z);
 }
 
 // per replica, fixed order: strided slots per thread, then a halving tree
@@ -276,18 +296,18 @@ int nb_pressure(NbCtx *c, const double *d_coor, double *d_out)
     const int B = 128;
     if (c->nmol > 0)
         k_press_xrel<<<(c->nmol + B - 1) / B, B, 0, s>>>(c->nmol, c->d_mol_off, c->d_mol_atom, c->d_atom_rep,
-                                                        c->d_reps, d_coor, c->d_mass, c->d_xrel);
+                                                        c->d_reps, d_coor, c->d_mass, c->d_xrel, c->d_xrelf);
     if (c->nW > 0)
         (c->row16 ? k_press_water<unsigned short> : k_press_water<int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
             (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
-            (const float4 *)c->d_woff, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_xrel, c->d_press_unit);
+            (const float4 *)c->d_woff, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_xrelf, c->d_press_unit);
     if (c->nA > 0)
         k_press_atom<<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
             (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
-            (const float2 *)c->d_site_lj, c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), c->d_xrel,
+            (const float2 *)c->d_site_lj, c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), c->d_xrelf,
             c->d_press_unit);
     k_press_rel<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
-                                                            c->d_reps, (const float4 *)c->d_part, c->d_q, c->d_xrel,
+                                                            c->d_reps, (const float4 *)c->d_part, c->d_q, c->d_xrelf,
                                                             c->d_press_site);
     nb_launch_pme_virial(c, c->d_press_grid, c->d_press_col);
     k_press_reduce<<<c->nrep, NB_PR_THREADS, 0, s>>>((int)c->nW, c->d_reps, c->d_press_unit, c->d_press_site,
