@@ -88,7 +88,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
     free_ptr(c->d_adj); free_ptr(c->d_md_dpot);
     free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
-    free_ptr(c->d_xrelf); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
+    free_ptr(c->d_xrelf); free_ptr(c->d_xsite); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
     free_ptr(c->d_press_out);
     c->nmol = 0;
     if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
@@ -1105,6 +1105,7 @@ int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_ener
     if (!h->d_press_out) {
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_unit, sizeof(double) * 6 * std::max<int64_t>(h->nW + h->nA, 1)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_site, sizeof(double) * 3 * std::max<int64_t>(h->nsite, 1)));
+        NB_CUDA_OK(h, cudaMalloc(&h->d_xsite, sizeof(float4) * std::max<int64_t>(h->nsite, 1)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_col, sizeof(double) * 3 * std::max<size_t>(h->cols.size(), 1)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_grid, sizeof(float2) * std::max<int64_t>(h->grid_elems, 1)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_out, sizeof(double) * 12 * h->nrep));

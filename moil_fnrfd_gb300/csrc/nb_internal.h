@@ -142,7 +142,8 @@ struct NbCtx {
     int *d_mol_off = nullptr, *d_mol_atom = nullptr;   // molecules as CSR over caller atoms
     double *d_mass = nullptr;          // per caller atom
     double *d_xrel = nullptr;          // position relative to the molecule's centre of mass, 3 per atom
-    float4 *d_xrelf = nullptr;         // the same in FP32, one float4 per atom (pair kernels)
+    float4 *d_xrelf = nullptr;         // the same in FP32, one float4 per atom
+    float4 *d_xsite = nullptr;         // the FP32 copy in site order (pair kernels)
     double *d_press_unit = nullptr;    // 6 per unit: LJ and real-space Coulomb terms
     double *d_press_site = nullptr;    // 3 per site: PME force x xrel
     double *d_press_col = nullptr;     // 3 per PME column work item: reciprocal virial

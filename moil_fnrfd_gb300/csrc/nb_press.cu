@@ -57,30 +57,37 @@ __global__ void k_press_xrel(int nmol, const int *__restrict__ mol_off, const in
         M += mass[a];
         prev = a;
     }
+    const double im = M > 0.0 ? 1.0 / M : 0.0;
+    const double com[3] = {sm[0] * im, sm[1] * im, sm[2] * im};
     for (int k = b; k < e; ++k) {
         const int a = mol_atom[k];
-        float f[3];
-#pragma unroll
-        for (int x = 0; x < 3; ++x) f[x] = (float)(xrel[3 * (size_t)a + x] - (M > 0.0 ? sm[x] / M : 0.0));
-        xrelf[a] = make_float4(f[0], f[1], f[2], 0.f);
+        xrelf[a] = make_float4((float)(xrel[3 * (size_t)a] - com[0]), (float)(xrel[3 * (size_t)a + 1] - com[1]),
+                               (float)(xrel[3 * (size_t)a + 2] - com[2]), 0.f);
     }
+}
+
+// the same in site order, so the pair kernels read it beside the site positions
+__global__ void k_press_xrel_sites(int nsite, const int *__restrict__ site_orig, const float4 *__restrict__ xrelf,
+                                   float4 *__restrict__ xsite)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsite) xsite[s] = xrelf[site_orig[s]];
 }
 
 // water molecule per thread over its W1 row: 9 Coulomb site pairs and the O-O LJ pair of
 // every molecule inside the O-O cutoff (watwat_ewald.f semantics, water charges of RepDev)
 template <typename E>
 __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
-                              const int *__restrict__ site_orig, const float4 *__restrict__ pos,
-                              const float4 *__restrict__ woff, const int2 *__restrict__ wl1_cnt,
-                              const void *__restrict__ wl1, int cap_row, const float4 *__restrict__ xrel,
-                              double *__restrict__ pu)
+                              const float4 *__restrict__ pos, const float4 *__restrict__ woff,
+                              const int2 *__restrict__ wl1_cnt, const void *__restrict__ wl1, int cap_row,
+                              const float4 *__restrict__ xsite, double *__restrict__ pu)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nW) return;
     const RepDev &R = reps[site_rep[3 * i]];
     const float4 oi = pos[3 * i], h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
     const float hi[3][3] = {{0.f, 0.f, 0.f}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
-    const float4 xi = xrel[site_orig[3 * i]];
+    const float4 xi = xsite[3 * i];
     double v[6] = {0, 0, 0, 0, 0, 0};
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int cnt = 0;
@@ -99,7 +106,7 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
         if (r2oo > R.rmax2) continue;
         const float4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
         const float hj[3][3] = {{0.f, 0.f, 0.f}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
-        const float4 xj = xrel[site_orig[3 * j]];
+        const float4 xj = xsite[3 * j];
         const float rm[3] = {d[0] - xi.x + xj.x, d[1] - xi.y + xj.y, d[2] - xi.z + xj.z};
         float fc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -146,10 +153,10 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
 // non-water atom per thread over its X list (non-water atoms and water sites), the pair
 // predicate of the energy kernels' atom_pair (cdie_ewald.f list1/2/3, nbond.f:115-126)
 __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
-                             const int *__restrict__ site_orig, const float4 *__restrict__ pos,
+                             const float4 *__restrict__ pos,
                              const float2 *__restrict__ lj, const unsigned *__restrict__ sflags,
                              const int *__restrict__ xl_off, const int *__restrict__ xl, int capx,
-                             const float4 *__restrict__ xrel, double *__restrict__ pu)
+                             const float4 *__restrict__ xsite, double *__restrict__ pu)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nA) return;
@@ -158,7 +165,7 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
     const float4 xi = pos[si];
     const float2 lji = lj[si];
     const unsigned fi = sflags[si];
-    const float4 xa = xrel[site_orig[si]];
+    const float4 xa = xsite[si];
     double v[6] = {0, 0, 0, 0, 0, 0};
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int cnt = 0;
@@ -208,7 +215,7 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
             }
         }
         const float w = s < 3 * nW ? -2.f : -1.f;   // water partners: this side only
-        const float4 xb = xrel[site_orig[s]];
+        const float4 xb = xsite[s];
         const float rm[3] = {d[0] - xa.x + xb.x, d[1] - xa.y + xb.y, d[2] - xa.z + xb.z};
 #pragma unroll
         for (int x = 0; x < 3; ++x) {
@@ -228,13 +235,13 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
 // V_PIrel per site: the PME force (minus the gradient share k_final_grad adds) times xrel
 __global__ void k_press_rel(int nsite, const int *__restrict__ site_rep, const int *__restrict__ site_orig,
                             const RepDev *__restrict__ reps, const float4 *__restrict__ part,
-                            const double *__restrict__ q, const float4 *__restrict__ xrel, double *__restrict__ ps)
+                            const double *__restrict__ q, const float4 *__restrict__ xsite, double *__restrict__ ps)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsite) return;
     const RepDev &R = reps[site_rep[s]];
     const int a = site_orig[s];
-    const float4 p = part[s], x = xrel[a];
+    const float4 p = part[s], x = xsite[s];
     const float qs = -(float)q[a];
     ps[3 * (size_t)s] = (double)(qs * R.pme_gs[0] * p.x * x.x);
     ps[3 * (size_t)s + 1] = (double)(qs * R.pme_gs[1] * p.y * x.y);
@@ -297,17 +304,18 @@ int nb_pressure(NbCtx *c, const double *d_coor, double *d_out)
     if (c->nmol > 0)
         k_press_xrel<<<(c->nmol + B - 1) / B, B, 0, s>>>(c->nmol, c->d_mol_off, c->d_mol_atom, c->d_atom_rep,
                                                         c->d_reps, d_coor, c->d_mass, c->d_xrel, c->d_xrelf);
+    k_press_xrel_sites<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_orig, c->d_xrelf,
+                                                                   c->d_xsite);
     if (c->nW > 0)
         (c->row16 ? k_press_water<unsigned short> : k_press_water<int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
-            (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
-            (const float4 *)c->d_woff, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_xrelf, c->d_press_unit);
+            (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float4 *)c->d_woff, c->d_wl1_cnt,
+            c->d_wl1, c->cap_row1, c->d_xsite, c->d_press_unit);
     if (c->nA > 0)
         k_press_atom<<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
-            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
-            (const float2 *)c->d_site_lj, c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), c->d_xrelf,
-            c->d_press_unit);
+            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float2 *)c->d_site_lj,
+            c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), c->d_xsite, c->d_press_unit);
     k_press_rel<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
-                                                            c->d_reps, (const float4 *)c->d_part, c->d_q, c->d_xrelf,
+                                                            c->d_reps, (const float4 *)c->d_part, c->d_q, c->d_xsite,
                                                             c->d_press_site);
     nb_launch_pme_virial(c, c->d_press_grid, c->d_press_col);
     k_press_reduce<<<c->nrep, NB_PR_THREADS, 0, s>>>((int)c->nW, c->d_reps, c->d_press_unit, c->d_press_site,
