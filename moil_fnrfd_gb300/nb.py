@@ -309,24 +309,25 @@ class Nonbonded:
         _check(self.L, self.h, self.L.moil_nb_set_molecules(self.h, self._mol.ctypes.data_as(_ip),
                                                             self._mass.ctypes.data_as(_dp)))
 
-    def pressure(self, coor=None):
+    def pressure(self, coor=None, with_gradient: bool = True):
         """One evaluation and MOIL's pressure analysis terms (moil_nb_pressure): (dpot,
         energies, press), press the 12 values virXX..ZZ, V_PIdir, V_PIrec, V_PIrel; batch:
-        lists per replica."""
+        lists per replica.  with_gradient=False skips the gradient copy (dpot is None)."""
         if coor is None:
             coor = np.concatenate([s.coor for s in self.systems], axis=0)
         elif self.batch and isinstance(coor, (list, tuple)):
             coor = np.concatenate(coor, axis=0)
         coor = np.ascontiguousarray(coor, dtype=np.float64).reshape(self.natom, 3)
-        dpot = np.empty_like(coor)
+        dpot = np.empty_like(coor) if with_gradient else None
         press = np.empty((len(self.systems), 12), dtype=np.float64)
-        _check(self.L, self.h, self.L.moil_nb_pressure(self.h, coor.ctypes.data_as(_dp), dpot.ctypes.data_as(_dp),
+        _check(self.L, self.h, self.L.moil_nb_pressure(self.h, coor.ctypes.data_as(_dp),
+                                                       dpot.ctypes.data_as(_dp) if with_gradient else None,
                                                        self._e, press.ctypes.data_as(_dp)))
         e = self.energies()
         if not self.batch:
             return dpot, e[0], press[0]
-        return ([dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))], e,
-                [press[k] for k in range(len(self.systems))])
+        per = [dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))] if with_gradient else None
+        return per, e, [press[k] for k in range(len(self.systems))]
 
     def eforce_device(self, d_coor_ptr: int, d_dpot_ptr: int, want_energies: bool = True):
         """Evaluate on device-resident buffers (raw CUDA pointers)."""
