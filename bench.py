@@ -110,6 +110,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_rate(units_local: float, seconds_local: float):
+    """Whole-job throughput over the ranks of the default process group: the units every rank
+    processed, summed, over the slowest rank's time (each rank times its own GPU).  Returns
+    (units / s, slowest rank's seconds); a single process gives units / seconds."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return units_local / seconds_local, seconds_local
+    u = torch.tensor([float(units_local)], dtype=torch.float64)
+    t = torch.tensor([float(seconds_local)], dtype=torch.float64)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u[0]) / float(t[0]), float(t[0])
+
+
 def build_workload(rank=0, n_rep=512):
     """The 512-replica batch; a smaller n_rep keeps the first n_rep replicas (profiling)."""
     from moil_fnrfd_gb300 import systems
@@ -313,12 +328,7 @@ def main():
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s])
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t[0])
-    value = natoms * args.steps * world / total_s
+    value, total_s = job_rate(natoms * args.steps, sum(step_ms) / 1e3)
 
     # e2e through the public host-buffer call: H2D + evaluation + D2H every step
     h_coor = torch.from_numpy(coor).pin_memory()
@@ -335,7 +345,7 @@ def main():
         t1 = time.perf_counter()
         nb.eforce_into(hc, hd, want_energies=False)
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
-    e2e_value = natoms * args.steps * world / (sum(e2e_ms) / 1e3)
+    e2e_value, _ = job_rate(natoms * args.steps, sum(e2e_ms) / 1e3)
 
     press = press_leg(nb, reps, hc, e2e_ms) if not args.no_press and rank == 0 else None
 
