@@ -40,6 +40,9 @@ METRIC = "atom-evals/s mixed+batched vs plain FP64 on 1 GB300 at ≤1e-5 rel RMS
 F_PAIR = 50            # FP32 operations per in-cutoff site pair (FMA = 2, MUFU = 1)
 LIST_PERIOD = 10
 SKIN = 1.0
+# DRAM bytes per water molecule of one k_water_f launch (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum, 48-replica capture: 37.44 MB over 74,171 waters)
+WATER_KERNEL_DRAM_BYTES_PER_WATER = 504.9
 
 
 def log(*a):
@@ -364,8 +367,12 @@ def main():
     peak_fp32 = fp32_peak_tflops(peaks().get("sm_max_mhz", 2070.0))
     # both rooflines (the real-space kernel is the dominant one; PME by its HBM model)
     achieved = site_pairs * F_PAIR / (avg["water_ms"] + avg["atom_ms"]) / 1e9   # TFLOP/s
+    n_wat = sum(s.nwaters for s in reps)
     roof_rs = {"kernel": "k_water+k_atom (real space)", "bound": "fp32", "achieved": achieved,
-               "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
+               "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32,
+               "traffic": WATER_KERNEL_DRAM_BYTES_PER_WATER * n_wat,
+               "traffic_note": "bytes per evaluation of k_water_f (all groups): ncu DRAM read+write per water "
+                               "on a 48-replica capture x waters",
                "peak_source": "nominal FP32 FMA peak at the measured max SM clock (152 SMs x 128 lanes x 2); "
                               "MEASURED_PEAKS.json has no FP32 figure",
                "work": f"{site_pairs} unique in-cutoff site pairs x {F_PAIR} FP32 ops per launch"}
