@@ -685,6 +685,9 @@ __global__ void __launch_bounds__(256) k_pme_gather_f(int nsite, const int *__re
     int xs[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) xs[t] = pme_wrap(i1 - 3 + t, n1);
+    // without an x wrap the four stencil points of a row are contiguous: two aligned float4
+    // loads hold them (the grid allocation ends 16 bytes past its last plane for the second)
+    const bool contig = i1 >= 3;
     float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
     for (int t3 = 0; t3 < 4; ++t3) {
@@ -693,10 +696,24 @@ __global__ void __launch_bounds__(256) k_pme_gather_f(int nsite, const int *__re
 #pragma unroll
         for (int t2 = 0; t2 < 4; ++t2) {
             const float *row = P + pme_wrap(i2 - 3 + t2, n2) * n1;
+            float q4[4];
+            if (contig) {
+                const uintptr_t a = (uintptr_t)(row + i1 - 3);
+                const float4 *p4 = (const float4 *)(a & ~(uintptr_t)15);
+                const float4 c0 = __ldg(p4), c1 = __ldg(p4 + 1);
+                const int sh = (int)((a >> 2) & 3);
+                q4[0] = sh == 0 ? c0.x : (sh == 1 ? c0.y : (sh == 2 ? c0.z : c0.w));
+                q4[1] = sh == 0 ? c0.y : (sh == 1 ? c0.z : (sh == 2 ? c0.w : c1.x));
+                q4[2] = sh == 0 ? c0.z : (sh == 1 ? c0.w : (sh == 2 ? c1.x : c1.y));
+                q4[3] = sh == 0 ? c0.w : (sh == 1 ? c1.x : (sh == 2 ? c1.y : c1.z));
+            } else {
+#pragma unroll
+                for (int t1 = 0; t1 < 4; ++t1) q4[t1] = row[xs[t1]];
+            }
             float sx = 0.f, sy = 0.f;
 #pragma unroll
             for (int t1 = 0; t1 < 4; ++t1) {
-                const float q = row[xs[t1]];
+                const float q = q4[t1];
                 sx = fmaf(q, dt1[t1], sx);
                 sy = fmaf(q, th1[t1], sy);
             }
@@ -1116,7 +1133,9 @@ int configure_t(NbCtx *c)
     NB_CUDA_OK(c, cudaMalloc(&c->d_col_begin, sizeof(int) * (c->nrep + 1)));
     NB_CUDA_OK(c, cudaMemcpy(c->d_col_begin, c->col_begin.data(), sizeof(int) * (c->nrep + 1), cudaMemcpyHostToDevice));
     NB_CUDA_OK(c, cudaMalloc(&c->d_e_col, sizeof(double) * c->cols.size()));
-    NB_CUDA_OK(c, cudaMalloc(&c->d_grid, sizeof(C) * c->grid_elems));
+    // two spare elements: the FP32 gather's second aligned float4 of a row may reach 16 bytes
+    // past the last plane
+    NB_CUDA_OK(c, cudaMalloc(&c->d_grid, sizeof(C) * (c->grid_elems + 2)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_fr, sizeof(typename vec4<T>::type) * c->nsite));
     NB_CUDA_OK(c, cudaMalloc(&c->d_part, sizeof(T) * 12 * c->nsite));
     NB_CUDA_OK(c, cudaMemset(c->d_part, 0, sizeof(T) * 12 * c->nsite));
@@ -1179,7 +1198,7 @@ constexpr size_t NA_PART = NA_ZATOMS + na_up(sizeof(int) * NA_MAX_ATOMS);
 constexpr size_t NA_ZCOUNT = NA_PART + na_up(sizeof(float) * 12 * NA_MAX_ATOMS);
 constexpr size_t NA_ZSTART = NA_ZCOUNT + na_up(sizeof(int) * (NA_MAX_N + 1));
 constexpr size_t NA_GRID = NA_ZSTART + na_up(sizeof(int) * (NA_MAX_N + 1));
-constexpr size_t NA_ECOL = NA_GRID + na_up(sizeof(float2) * (NA_MAX_N / 2 + 1) * NA_MAX_N * NA_MAX_N);
+constexpr size_t NA_ECOL = NA_GRID + na_up(sizeof(float2) * ((NA_MAX_N / 2 + 1) * NA_MAX_N * NA_MAX_N + 2));
 constexpr size_t NA_PLANES = NA_ECOL + na_up(sizeof(double) * NA_MAX_COLS);
 constexpr size_t NA_COLS = NA_PLANES + na_up(sizeof(PlaneWork) * NA_MAX_N);
 constexpr size_t NA_COLBEG = NA_COLS + na_up(sizeof(ColWork) * NA_MAX_COLS);
