@@ -686,8 +686,9 @@ __global__ void __launch_bounds__(256) k_pme_gather_f(int nsite, const int *__re
 #pragma unroll
     for (int t = 0; t < 4; ++t) xs[t] = pme_wrap(i1 - 3 + t, n1);
     // without an x wrap the four stencil points of a row are contiguous: two aligned float4
-    // loads hold them (the grid allocation ends 16 bytes past its last plane for the second)
-    const bool contig = i1 >= 3;
+    // loads hold them (the grid allocation ends 16 bytes past its last plane for the second).
+    // fr1 can round to n1 itself (index n1 wraps to 0), which takes the wrapped path.
+    const bool contig = i1 >= 3 && i1 < n1;
     float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
     for (int t3 = 0; t3 < 4; ++t3) {
