@@ -54,9 +54,14 @@ def solute_system():
     return S.config1(seed=7, n_solute=60, n_ions=7, n_waters=300, box=24.0)
 
 
-@pytest.fixture(scope="module", params=["water216", "solute"])
+def geometric_system():
+    """MOIL's geometric LJ rule with tiny-epsilon hydrogens (the hvdw0 Coulomb-only pairs)."""
+    return S.config1(seed=11, n_solute=60, n_ions=7, n_waters=300, box=24.0, arith=False, tiny_h=True)
+
+
+@pytest.fixture(scope="module", params=["water216", "solute", "geometric_hydrogens"])
 def case(request, cfg0):
-    s = cfg0 if request.param == "water216" else solute_system()
+    s = {"water216": lambda: cfg0, "solute": solute_system, "geometric_hydrogens": geometric_system}[request.param]()
     mol, mass = S.molecules(s)
     return request.param, s, mol, mass
 
