@@ -81,6 +81,12 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi takes a moment to start: wait (at most 2 s) for its first row, then
+            # keep only the rows that arrive inside the timed region
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 2.0:
+                time.sleep(0.01)
+            self.rows.clear()
         except Exception:
             self.proc = None
 
@@ -258,7 +264,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # 200 steps (about 0.5 s timed) give the 200 ms clock sampler a few samples under load
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
