@@ -88,7 +88,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
     free_ptr(c->d_adj); free_ptr(c->d_md_dpot);
     free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
-    free_ptr(c->d_xrelf); free_ptr(c->d_xsite); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
+    free_ptr(c->d_xsite); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
     free_ptr(c->d_press_out);
     c->nmol = 0;
     if (c->h_e_rep) cudaFreeHost(c->h_e_rep);
@@ -1035,7 +1035,6 @@ int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
         return MOIL_NB_OK;
     }
     free_ptr(h->d_mol_off); free_ptr(h->d_mol_atom); free_ptr(h->d_mass); free_ptr(h->d_xrel);
-    free_ptr(h->d_xrelf);
     h->nmol = 0;
     if (!mol) return MOIL_NB_OK;
     // CSR over caller atoms: molecules numbered in order of their first atom, atoms ascending
@@ -1067,7 +1066,6 @@ int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
     NB_CUDA_OK(h, cudaMalloc(&h->d_mol_atom, sizeof(int) * std::max<size_t>(n, 1)));
     NB_CUDA_OK(h, cudaMalloc(&h->d_mass, sizeof(double) * std::max<size_t>(n, 1)));
     NB_CUDA_OK(h, cudaMalloc(&h->d_xrel, sizeof(double) * 3 * std::max<size_t>(n, 1)));
-    NB_CUDA_OK(h, cudaMalloc(&h->d_xrelf, sizeof(float4) * std::max<size_t>(n, 1)));
     NB_CUDA_OK(h, cudaMemcpy(h->d_mol_off, off.data(), sizeof(int) * (nmol + 1), cudaMemcpyHostToDevice));
     NB_CUDA_OK(h, cudaMemcpy(h->d_mol_atom, atoms.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     NB_CUDA_OK(h, cudaMemcpy(h->d_mass, mass, sizeof(double) * n, cudaMemcpyHostToDevice));
@@ -1079,10 +1077,6 @@ int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_ener
 {
     if (!h || !coor || !press) return MOIL_NB_ERR_ARG;
     if (!h->inited) return MOIL_NB_ERR_STATE;
-    if (h->precision == MOIL_NB_FP64) {
-        h->err = "the pressure analysis terms are computed on the mixed path only";
-        return MOIL_NB_ERR_ARG;
-    }
     if (h->nmol == 0) {
         h->err = "no molecules: call moil_nb_set_molecules first";
         return MOIL_NB_ERR_STATE;
@@ -1105,9 +1099,10 @@ int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_ener
     if (!h->d_press_out) {
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_unit, sizeof(double) * 6 * std::max<int64_t>(h->nW + h->nA, 1)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_site, sizeof(double) * 3 * std::max<int64_t>(h->nsite, 1)));
-        NB_CUDA_OK(h, cudaMalloc(&h->d_xsite, sizeof(float4) * std::max<int64_t>(h->nsite, 1)));
+        const size_t fp = h->precision == MOIL_NB_FP64 ? sizeof(double) : sizeof(float);
+        NB_CUDA_OK(h, cudaMalloc(&h->d_xsite, 4 * fp * std::max<int64_t>(h->nsite, 1)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_col, sizeof(double) * 3 * std::max<size_t>(h->cols.size(), 1)));
-        NB_CUDA_OK(h, cudaMalloc(&h->d_press_grid, sizeof(float2) * std::max<int64_t>(h->grid_elems, 1)));
+        NB_CUDA_OK(h, cudaMalloc(&h->d_press_grid, 2 * fp * (h->grid_elems + 2)));
         NB_CUDA_OK(h, cudaMalloc(&h->d_press_out, sizeof(double) * 12 * h->nrep));
     }
     rc = nb_pressure(h, h->d_coor, h->d_press_out);

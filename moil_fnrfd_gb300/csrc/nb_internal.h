@@ -142,12 +142,11 @@ struct NbCtx {
     int *d_mol_off = nullptr, *d_mol_atom = nullptr;   // molecules as CSR over caller atoms
     double *d_mass = nullptr;          // per caller atom
     double *d_xrel = nullptr;          // position relative to the molecule's centre of mass, 3 per atom
-    float4 *d_xrelf = nullptr;         // the same in FP32, one float4 per atom
-    float4 *d_xsite = nullptr;         // the FP32 copy in site order (pair kernels)
+    void *d_xsite = nullptr;           // the same in site order, float4 / double4 (pair kernels)
     double *d_press_unit = nullptr;    // 6 per unit: LJ and real-space Coulomb terms
     double *d_press_site = nullptr;    // 3 per site: PME force x xrel
     double *d_press_col = nullptr;     // 3 per PME column work item: reciprocal virial
-    void *d_press_grid = nullptr;      // second half-complex grid for the reciprocal virial
+    void *d_press_grid = nullptr;      // second half-complex grid for the reciprocal virial (float2 / double2)
     double *d_press_out = nullptr;     // 12 per replica
 
     // device status: [0] rebuild flag, [1] error bits, [2..4] W1 / W2 / X entry totals,

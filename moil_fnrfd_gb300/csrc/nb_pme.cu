@@ -869,6 +869,71 @@ __global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work,
     if (threadIdx.x == 0) e_col[blockIdx.x] = red[0];
 }
 
+// reciprocal virial of the pressure analysis on the plain path: the z transform of k_zconv's
+// columns (one warp per line), then per m the diagonal terms
+// E(m) (1 - 2 (1 + pi^2 m^2 / alpha^2) m_a^2 / m^2) (ewald_receip.f:799-807), E(m) as the
+// energy sum forms it; three FP64 sums per column work item
+template <typename T>
+__global__ void __launch_bounds__(256) k_press_zvir(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
+                                                    const FftPlanDev *__restrict__ plans,
+                                                    const int *__restrict__ rep_plan, const void *tw_v,
+                                                    const void *bsp_v, const void *grid_v, double *__restrict__ v_col)
+{
+    typedef typename cplx<T>::type C;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[3][256];
+    const ColWork w = work[blockIdx.x];
+    const RepDev &R = reps[w.rep];
+    const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
+    const int tk = min(NB_TK, n2 - w.ky0);
+    const int n3p = n3 | 1;
+    const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
+    const C *tw = (const C *)tw_v;
+    const T *bsp = (const T *)bsp_v + R.bsp0;
+    C *tile = (C *)smem;
+    C *scr = tile + NB_TK * n3p;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const C *g = (const C *)grid_v + R.g0 + (size_t)w.kx * n2 + w.ky0;
+    const size_t zs = (size_t)n1h * n2;
+    for (int idx = threadIdx.x; idx < tk * n3; idx += blockDim.x) {
+        const int kz = idx / tk, c = idx - kz * tk;
+        tile[c * n3p + kz] = g[kz * zs + c];
+    }
+    __syncthreads();
+    double v[3] = {0.0, 0.0, 0.0};
+    C *x = scr + warp * 2 * NB_MAX_FFT, *y = x + NB_MAX_FFT;
+    const double wgt = (w.kx == 0 || (2 * w.kx == n1)) ? 1.0 : 2.0;
+    const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
+    for (int c = warp; c < tk; c += nwarp) {
+        const int ky = w.ky0 + c;
+        for (int kz = lane; kz < n3; kz += 32) x[kz] = tile[c * n3p + kz];
+        __syncwarp();
+        const C *res = warp_fft<C>(x, y, p3, tw + p3.tw0, lane);
+        for (int kz = lane; kz < n3; kz += 32) {
+            if (w.kx == 0 && ky == 0 && kz == 0) continue;
+            const double mh[3] = {(double)w.kx * R.invLd[0], (double)(ky < nf2 ? ky : ky - n2) * R.invLd[1],
+                                  (double)(kz < nf3 ? kz : kz - n3) * R.invLd[2]};
+            const double msq = mh[0] * mh[0] + mh[1] * mh[1] + mh[2] * mh[2];
+            const double et = (double)eterm_of<T>(R, bsp, w.kx, ky, kz);
+            const C q = res[kz];
+            const double e = wgt * et * ((double)q.x * q.x + (double)q.y * q.y), b = 2.0 * (1.0 + R.pme_fac * msq) / msq;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) v[d] += e * (1.0 - b * mh[d] * mh[d]);
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) red[d][threadIdx.x] = v[d];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) red[d][threadIdx.x] += red[d][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) v_col[3 * (size_t)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__ work, const RepDev *__restrict__ reps,
                                                    const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
@@ -1051,6 +1116,7 @@ cudaError_t raise_pme_limits(size_t sf, size_t sz, size_t si)
     }
     if ((e = raise_smem_limit(k_plane_fwd<T>, sf)) != cudaSuccess) return e;
     if ((e = raise_smem_limit(k_zconv<T>, sz)) != cudaSuccess) return e;
+    if ((e = raise_smem_limit(k_press_zvir<T>, sz)) != cudaSuccess) return e;
     return raise_smem_limit(k_plane_inv<T>, si);
 }
 
@@ -1158,6 +1224,13 @@ void nb_launch_pme_virial(NbCtx *c, void *grid, double *v_col)
 {
     cudaStream_t s = c->stream;
     const int np = (int)c->planes.size(), nc = (int)c->cols.size();
+    if (c->precision == MOIL_NB_FP64) {
+        k_plane_fwd<double><<<np, 256, c->smem_plane_fwd, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
+                                                               c->d_tw, c->d_zstart, c->d_zatoms, c->d_fr, grid);
+        k_press_zvir<double><<<nc, 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw,
+                                                            c->d_bsp, grid, v_col);
+        return;
+    }
     k_plane_fwd_f<<<np, 256, c->smem_plane_fwd, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
                                                        (const float2 *)c->d_tw, c->d_tab, c->d_zstart, c->d_zatoms,
                                                        (const float4 *)c->d_fr, (float2 *)grid);

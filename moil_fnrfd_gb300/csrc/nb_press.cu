@@ -4,7 +4,8 @@
 //                555-566, image pairs symm/symwat_ewald.f:161-173, symm/symcdie_ewald.f:151-161)
 //   V_PIdirXX..  real-space Ewald Coulomb pairs (watwat_ewald.f:196-204,
 //                cdie_ewald.f:412-429, symwat_ewald.f:193-203)
-//   V_PIrecXX..  reciprocal sum (pot/ewald_receip.f:799-807; k_press_zvir_f in nb_pme.cu)
+//   V_PIrecXX..  reciprocal sum (pot/ewald_receip.f:799-807; k_press_zvir_f / k_press_zvir in
+//                nb_pme.cu)
 //   V_PIrelXX..  PME force times the atom's position relative to its molecule's centre of
 //                mass (ewald_receip.f:928-933)
 // pressure.f:235-238 adds vir + dir + rec - rel; V_PIcor stays zero (its accumulation is
@@ -19,23 +20,67 @@
 // the box.
 //
 // The pass reuses the evaluation's lists, site positions, PME binning and PME gradient
-// shares, with the pair predicates and FP32 pair arithmetic of the energy kernels; the
-// products with the centre-of-mass separations are FP32 too, summed per thread in FP32 over
-// chunks of NB_PCHUNK list entries and in FP64 across chunks (an FP64 operation per pair
-// would cost more than the pair itself: the FP64 pipe is 1/64 of FP32).  Full lists hold every pair
-// twice: water-water and atom-atom terms are halved at the end, water-atom pairs are taken
-// from the atom's side only with weight two.
+// shares, with the pair predicates and the arithmetic of the energy kernels of the handle's
+// precision.  On the mixed path the products with the centre-of-mass separations are FP32
+// too, summed per thread in FP32 over chunks of NB_PCHUNK list entries and in FP64 across
+// chunks (an FP64 operation per pair would cost more than the pair itself: the FP64 pipe is
+// 1/64 of FP32); the plain path is FP64 throughout.  Full lists hold every pair twice:
+// water-water and atom-atom terms are halved at the end, water-atom pairs are taken from the
+// atom's side only with weight two.
 #include "nb_internal.h"
 
 namespace {
 
 #define NB_PCHUNK 32
 
-// positions relative to the centres of mass, per caller atom; one thread per molecule
+// the pair arithmetic of each precision (as the energy kernels: MUFU rsqrt and the fitted
+// erfc in FP32, libdevice in FP64)
+template <typename T> struct PressMath;
+template <> struct PressMath<float> {
+    __device__ static float qq(const RepDev &R, int k) { return R.qq[k]; }
+    __device__ static float w12(const RepDev &R) { return R.w12; }
+    __device__ static float w6(const RepDev &R) { return R.w6; }
+    __device__ static float c2a(const RepDev &R) { return R.c2a; }
+    __device__ static float epstmp(const RepDev &R) { return (float)R.epstmp; }
+    __device__ static float rsqrt(float x) { return nb_rsqrt_approx(x); }
+    __device__ static float erfc_ex(const RepDev &R, float r2, float rinv, float *ex)
+    {
+        return nb_erfc_ex(R.alpha * r2 * rinv, r2 * R.ex2c, ex);
+    }
+};
+template <> struct PressMath<double> {
+    __device__ static double qq(const RepDev &R, int k) { return R.qqd[k]; }
+    __device__ static double w12(const RepDev &R) { return R.w12d; }
+    __device__ static double w6(const RepDev &R) { return R.w6d; }
+    __device__ static double c2a(const RepDev &R) { return NB_TWO_OVER_SQRTPI * R.alphad; }
+    __device__ static double epstmp(const RepDev &R) { return R.epstmp; }
+    __device__ static double rsqrt(double x) { return ::rsqrt(x); }
+    __device__ static double erfc_ex(const RepDev &R, double r2, double rinv, double *ex)
+    {
+        return nb_erfc_ex(R.alphad * r2 * rinv, 0.0, ex);
+    }
+};
+
+// minus (dE_LJ/dr)/r of one pair with the LJ switch extension applied
+template <typename T>
+__device__ __forceinline__ T lj_mdf(const RepDev &R, T r2, T A, T B)
+{
+    const T s2 = (T)1 / r2, e1 = A - B;
+    T df1 = (T)-6 * s2 * (A + e1);
+    if (R.lj_switch && r2 > (T)R.ron2) {
+        const T dd = (T)R.rv2 - r2;
+        const T sw = dd * dd * ((T)R.rv2 + (T)2 * r2 - (T)3 * (T)R.ron2) * (T)R.swden;
+        const T dsw = (T)12 * dd * ((T)R.ron2 - r2) * (T)R.swden;
+        df1 = df1 * sw + e1 * dsw;
+    }
+    return -df1;
+}
+
+// positions relative to the centres of mass, per caller atom (FP64); one thread per molecule
 __global__ void k_press_xrel(int nmol, const int *__restrict__ mol_off, const int *__restrict__ mol_atom,
                              const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
                              const double *__restrict__ coor, const double *__restrict__ mass,
-                             double *__restrict__ xrel, float4 *__restrict__ xrelf)
+                             double *__restrict__ xrel)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmol) return;
@@ -61,35 +106,45 @@ __global__ void k_press_xrel(int nmol, const int *__restrict__ mol_off, const in
     const double com[3] = {sm[0] * im, sm[1] * im, sm[2] * im};
     for (int k = b; k < e; ++k) {
         const int a = mol_atom[k];
-        xrelf[a] = make_float4((float)(xrel[3 * (size_t)a] - com[0]), (float)(xrel[3 * (size_t)a + 1] - com[1]),
-                               (float)(xrel[3 * (size_t)a + 2] - com[2]), 0.f);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) xrel[3 * (size_t)a + x] -= com[x];
     }
 }
 
-// the same in site order, so the pair kernels read it beside the site positions
-__global__ void k_press_xrel_sites(int nsite, const int *__restrict__ site_orig, const float4 *__restrict__ xrelf,
-                                   float4 *__restrict__ xsite)
+// the same in site order and the handle's precision, read beside the site positions
+template <typename T>
+__global__ void k_press_xrel_sites(int nsite, const int *__restrict__ site_orig, const double *__restrict__ xrel,
+                                   void *__restrict__ xsite_v)
 {
+    typedef typename vec4<T>::type T4;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < nsite) xsite[s] = xrelf[site_orig[s]];
+    if (s >= nsite) return;
+    const double *x = xrel + 3 * (size_t)site_orig[s];
+    T4 o;
+    o.x = (T)x[0]; o.y = (T)x[1]; o.z = (T)x[2]; o.w = (T)0;
+    ((T4 *)xsite_v)[s] = o;
 }
 
 // water molecule per thread over its W1 row: 9 Coulomb site pairs and the O-O LJ pair of
 // every molecule inside the O-O cutoff (watwat_ewald.f semantics, water charges of RepDev)
-template <typename E>
+template <typename T, typename E>
 __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
-                              const float4 *__restrict__ pos, const float4 *__restrict__ woff,
-                              const int2 *__restrict__ wl1_cnt, const void *__restrict__ wl1, int cap_row,
-                              const float4 *__restrict__ xsite, double *__restrict__ pu)
+                              const void *pos_v, const void *woff_v, const int2 *__restrict__ wl1_cnt,
+                              const void *__restrict__ wl1, int cap_row, const void *xsite_v,
+                              double *__restrict__ pu)
 {
+    typedef typename vec4<T>::type T4;
+    typedef PressMath<T> M;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nW) return;
+    const T4 *pos = (const T4 *)pos_v, *woff = (const T4 *)woff_v, *xsite = (const T4 *)xsite_v;
     const RepDev &R = reps[site_rep[3 * i]];
-    const float4 oi = pos[3 * i], h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
-    const float hi[3][3] = {{0.f, 0.f, 0.f}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
-    const float4 xi = xsite[3 * i];
+    const T4 oi = pos[3 * i], h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
+    const T hi[3][3] = {{(T)0, (T)0, (T)0}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
+    const T4 xi = xsite[3 * i];
+    const T rmax2 = (T)R.rmax2, rv2 = (T)R.rv2, c2a = M::c2a(R);
     double v[6] = {0, 0, 0, 0, 0, 0};
-    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    T f[6] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0};
     int cnt = 0;
     const int2 c = wl1_cnt[i];
     const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
@@ -98,51 +153,42 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
     for (int q = 0; q < n; ++q) {
         if (q + 32 < nn) nb_prefetch_l1(row + q + 32);   // the row is a DRAM stream per lane
         const int j = base + (int)row[q < nn ? q : cap_row - 1 - (q - nn)];
-        const float4 oj = pos[3 * j];
-        float d[3] = {oi.x - oj.x, oi.y - oj.y, oi.z - oj.z};
+        const T4 oj = pos[3 * j];
+        T d[3] = {oi.x - oj.x, oi.y - oj.y, oi.z - oj.z};
 #pragma unroll
-        for (int x = 0; x < 3; ++x) d[x] = nb_shift(R, x, d[x], nb_rint(d[x] * R.invL[x]));
-        const float r2oo = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if (r2oo > R.rmax2) continue;
-        const float4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
-        const float hj[3][3] = {{0.f, 0.f, 0.f}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
-        const float4 xj = xsite[3 * j];
-        const float rm[3] = {d[0] - xi.x + xj.x, d[1] - xi.y + xj.y, d[2] - xi.z + xj.z};
-        float fc[3] = {0.f, 0.f, 0.f};
+        for (int x = 0; x < 3; ++x) d[x] = nb_shift(R, x, d[x], nb_rint(d[x] * rep_invL<T>(R, x)));
+        const T r2oo = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2oo > rmax2) continue;
+        const T4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
+        const T hj[3][3] = {{(T)0, (T)0, (T)0}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
+        const T4 xj = xsite[3 * j];
+        const T rm[3] = {d[0] - xi.x + xj.x, d[1] - xi.y + xj.y, d[2] - xi.z + xj.z};
+        T fc[3] = {(T)0, (T)0, (T)0};
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
-                const float ex = hi[a][0] + d[0] - hj[b][0], ey = hi[a][1] + d[1] - hj[b][1],
-                            ez = hi[a][2] + d[2] - hj[b][2];
-                const float rr2 = ex * ex + ey * ey + ez * ez, rinv = nb_rsqrt_approx(rr2);
-                float exv;
-                const float erfcv = nb_erfc_ex(R.alpha * rr2 * rinv, rr2 * R.ex2c, &exv);
-                const float qq = R.qq[(a == 0 && b == 0) ? 0 : ((a == 0 || b == 0) ? 1 : 2)];
-                const float e = qq * erfcv * rinv;
-                const float mdf = (e + qq * R.c2a * exv) * rinv * rinv;   // minus dE/dr / r
+                const T ex = hi[a][0] + d[0] - hj[b][0], ey = hi[a][1] + d[1] - hj[b][1],
+                        ez = hi[a][2] + d[2] - hj[b][2];
+                const T rr2 = ex * ex + ey * ey + ez * ez, rinv = M::rsqrt(rr2);
+                T exv;
+                const T erfcv = M::erfc_ex(R, rr2, rinv, &exv);
+                const T qq = M::qq(R, (a == 0 && b == 0) ? 0 : ((a == 0 || b == 0) ? 1 : 2));
+                const T e = qq * erfcv * rinv;
+                const T mdf = (e + qq * c2a * exv) * rinv * rinv;   // minus dE/dr / r
                 fc[0] += mdf * ex; fc[1] += mdf * ey; fc[2] += mdf * ez;
             }
 #pragma unroll
-        for (int x = 0; x < 3; ++x) f[3 + x] = fmaf(fc[x], rm[x], f[3 + x]);
-        if (r2oo <= R.rv2) {
-            const float s2 = 1.f / r2oo, s6 = s2 * s2 * s2;
-            const float A = R.w12 * s6 * s6, B = R.w6 * s6;
-            float e1 = A - B, df1 = -6.f * s2 * (A + e1);
-            if (R.lj_switch) {
-                if (r2oo > R.ron2) {
-                    const float dd = R.rv2 - r2oo;
-                    const float sw = dd * dd * (R.rv2 + 2.f * r2oo - 3.f * R.ron2) * R.swden;
-                    const float dsw = 12.f * dd * (R.ron2 - r2oo) * R.swden;
-                    df1 = df1 * sw + e1 * dsw;
-                }
-            }
+        for (int x = 0; x < 3; ++x) f[3 + x] += fc[x] * rm[x];
+        if (r2oo <= rv2) {
+            const T s2 = (T)1 / r2oo, s6 = s2 * s2 * s2;
+            const T m1 = lj_mdf<T>(R, r2oo, M::w12(R) * s6 * s6, M::w6(R) * s6);
 #pragma unroll
-            for (int x = 0; x < 3; ++x) f[x] = fmaf(-df1 * d[x], rm[x], f[x]);
+            for (int x = 0; x < 3; ++x) f[x] += m1 * d[x] * rm[x];
         }
         if (++cnt == NB_PCHUNK) {
 #pragma unroll
-            for (int k = 0; k < 6; ++k) { v[k] += (double)f[k]; f[k] = 0.f; }
+            for (int k = 0; k < 6; ++k) { v[k] += (double)f[k]; f[k] = (T)0; }
             cnt = 0;
         }
     }
@@ -152,79 +198,77 @@ __global__ void k_press_water(int nW, const RepDev *__restrict__ reps, const int
 
 // non-water atom per thread over its X list (non-water atoms and water sites), the pair
 // predicate of the energy kernels' atom_pair (cdie_ewald.f list1/2/3, nbond.f:115-126)
+template <typename T>
 __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
-                             const float4 *__restrict__ pos,
-                             const float2 *__restrict__ lj, const unsigned *__restrict__ sflags,
-                             const int *__restrict__ xl_off, const int *__restrict__ xl, int capx,
-                             const float4 *__restrict__ xsite, double *__restrict__ pu)
+                             const void *pos_v, const void *lj_v, const unsigned *__restrict__ sflags,
+                             const int *__restrict__ xl_off, const int *__restrict__ xl, int capx, const void *xsite_v,
+                             double *__restrict__ pu)
 {
+    typedef typename vec4<T>::type T4;
+    typedef typename cplx<T>::type T2;
+    typedef PressMath<T> M;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nA) return;
+    const T4 *pos = (const T4 *)pos_v, *xsite = (const T4 *)xsite_v;
+    const T2 *lj = (const T2 *)lj_v;
     const int si = 3 * nW + k;
     const RepDev &R = reps[site_rep[si]];
-    const float4 xi = pos[si];
-    const float2 lji = lj[si];
+    const T4 xi = pos[si];
+    const T2 lji = lj[si];
     const unsigned fi = sflags[si];
-    const float4 xa = xsite[si];
+    const T4 xa = xsite[si];
+    const T rv2 = (T)R.rv2, re2 = (T)R.re2, rmax2 = (T)R.rmax2, c2a = M::c2a(R);
     double v[6] = {0, 0, 0, 0, 0, 0};
-    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    T f[6] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0};
     int cnt = 0;
     for (int q = min(xl_off[k], capx); q < min(xl_off[k + 1], capx); ++q) {
         const int s = xl[q];
-        const float4 xj = pos[s];
-        float d[3] = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
+        const T4 xj = pos[s];
+        T d[3] = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
 #pragma unroll
-        for (int x = 0; x < 3; ++x) d[x] = nb_shift(R, x, d[x], nb_rint(d[x] * R.invL[x]));
-        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        for (int x = 0; x < 3; ++x) d[x] = nb_shift(R, x, d[x], nb_rint(d[x] * rep_invL<T>(R, x)));
+        const T r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         const unsigned fj = sflags[s];
-        const bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < R.re2;
-        const bool do_lj = r2 < R.rv2 && !hr;
-        float qq = xi.w * xj.w;
-        const bool do_el = r2 < R.rmax2 && qq != 0.f;
+        const bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < re2;
+        const bool do_lj = r2 < rv2 && !hr;
+        T qq = xi.w * xj.w;
+        const bool do_el = r2 < rmax2 && qq != (T)0;
         if (!do_lj && !do_el) continue;
-        const float rinv = nb_rsqrt_approx(r2), s2 = rinv * rinv;
-        float df_el = 0.f, df_lj = 0.f;
+        const T rinv = M::rsqrt(r2), s2 = rinv * rinv;
+        T m_el = (T)0, m_lj = (T)0;   // minus (dE/dr)/r of each part
         if (do_el) {
-            float exv;
-            const float erfcv = nb_erfc_ex(R.alpha * r2 * rinv, r2 * R.ex2c, &exv);
-            qq *= (float)R.epstmp;
-            const float e = qq * erfcv * rinv;
-            df_el = -(e + qq * R.c2a * exv) * s2;
+            T exv;
+            const T erfcv = M::erfc_ex(R, r2, rinv, &exv);
+            qq *= M::epstmp(R);
+            m_el = (qq * erfcv * rinv + qq * c2a * exv) * s2;
         }
         if (do_lj) {
-            const float2 ljj = lj[s];
-            const float s6 = s2 * s2 * s2;
-            float A, B;
+            const T2 ljj = lj[s];
+            const T s6 = s2 * s2 * s2;
+            T A, B;
             if (!R.arith) {
                 A = lji.x * ljj.x * s6 * s6;
                 B = lji.y * ljj.y * s6;
             } else {
-                const float aa = lji.x * ljj.x, sg = 0.5f * (lji.y + ljj.y);
-                float b1 = sg * sg * sg;
+                const T aa = lji.x * ljj.x, sg = (T)0.5 * (lji.y + ljj.y);
+                T b1 = sg * sg * sg;
                 b1 = b1 * b1;
                 B = aa * b1 * s6;
                 A = aa * b1 * b1 * s6 * s6;
             }
-            const float e1 = A - B;
-            df_lj = -6.f * s2 * (A + e1);
-            if (R.lj_switch && r2 > R.ron2) {
-                const float dd = R.rv2 - r2;
-                const float sw = dd * dd * (R.rv2 + 2.f * r2 - 3.f * R.ron2) * R.swden;
-                const float dsw = 12.f * dd * (R.ron2 - r2) * R.swden;
-                df_lj = df_lj * sw + e1 * dsw;
-            }
+            m_lj = lj_mdf<T>(R, r2, A, B);
         }
-        const float w = s < 3 * nW ? -2.f : -1.f;   // water partners: this side only
-        const float4 xb = xsite[s];
-        const float rm[3] = {d[0] - xa.x + xb.x, d[1] - xa.y + xb.y, d[2] - xa.z + xb.z};
+        const T w = s < 3 * nW ? (T)2 : (T)1;   // water partners: this side only
+        const T4 xb = xsite[s];
+        const T rm[3] = {d[0] - xa.x + xb.x, d[1] - xa.y + xb.y, d[2] - xa.z + xb.z};
 #pragma unroll
         for (int x = 0; x < 3; ++x) {
-            f[x] = fmaf(w * df_lj * d[x], rm[x], f[x]);
-            f[3 + x] = fmaf(w * df_el * d[x], rm[x], f[3 + x]);
+            f[x] += w * m_lj * d[x] * rm[x];
+            f[3 + x] += w * m_el * d[x] * rm[x];
         }
         if (++cnt == NB_PCHUNK) {
 #pragma unroll
-            for (int m = 0; m < 6; ++m) { v[m] += (double)f[m]; f[m] = 0.f; }
+            for (int m = 0; m < 6; ++m) { v[m] += (double)f[m]; f[m] = (T)0; }
             cnt = 0;
         }
     }
@@ -233,19 +277,36 @@ __global__ void k_press_atom(int nA, int nW, const RepDev *__restrict__ reps, co
 }
 
 // V_PIrel per site: the PME force (minus the gradient share k_final_grad adds) times xrel
+template <typename T>
 __global__ void k_press_rel(int nsite, const int *__restrict__ site_rep, const int *__restrict__ site_orig,
-                            const RepDev *__restrict__ reps, const float4 *__restrict__ part,
-                            const double *__restrict__ q, const float4 *__restrict__ xsite, double *__restrict__ ps)
+                            const RepDev *__restrict__ reps, const void *part_v, const double *__restrict__ q,
+                            const void *xsite_v, double *__restrict__ ps)
 {
+    typedef typename vec4<T>::type T4;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsite) return;
     const RepDev &R = reps[site_rep[s]];
     const int a = site_orig[s];
-    const float4 p = part[s], x = xsite[s];
-    const float qs = -(float)q[a];
-    ps[3 * (size_t)s] = (double)(qs * R.pme_gs[0] * p.x * x.x);
-    ps[3 * (size_t)s + 1] = (double)(qs * R.pme_gs[1] * p.y * x.y);
-    ps[3 * (size_t)s + 2] = (double)(qs * R.pme_gs[2] * p.z * x.z);
+    const T4 x = ((const T4 *)xsite_v)[s];
+    if constexpr (sizeof(T) == 4) {
+        // one float4 per site from k_pme_gather_f, scaled by q fc n_d / L_d
+        const float4 p = ((const float4 *)part_v)[s];
+        const float qs = -(float)q[a];
+        ps[3 * (size_t)s] = (double)(qs * R.pme_gs[0] * p.x * x.x);
+        ps[3 * (size_t)s + 1] = (double)(qs * R.pme_gs[1] * p.y * x.y);
+        ps[3 * (size_t)s + 2] = (double)(qs * R.pme_gs[2] * p.z * x.z);
+    } else {
+        // four plane slots of three per site from k_plane_inv
+        const double *p = (const double *)part_v + 12 * (size_t)s;
+        const double qf = q[a] * R.fcd;
+        const double sc[3] = {qf * R.n1 * R.invLd[0], qf * R.n2 * R.invLd[1], qf * R.n3 * R.invLd[2]};
+        const double xr[3] = {x.x, x.y, x.z};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double g = p[d] + p[3 + d] + p[6 + d] + p[9 + d];
+            ps[3 * (size_t)s + d] = -sc[d] * g * xr[d];
+        }
+    }
 }
 
 // per replica, fixed order: strided slots per thread, then a halving tree
@@ -293,33 +354,40 @@ __global__ void __launch_bounds__(NB_PR_THREADS) k_press_reduce(int nW, const Re
     if (t < 12) out[12 * (size_t)r + t] = (t < 9 ? 0.5 : 1.0) * red[t][0];
 }
 
+template <typename T>
+void pressure_t(NbCtx *c, const double *d_coor, double *d_out)
+{
+    cudaStream_t s = c->stream;
+    const int B = 128;
+    if (c->nmol > 0)
+        k_press_xrel<<<(c->nmol + B - 1) / B, B, 0, s>>>(c->nmol, c->d_mol_off, c->d_mol_atom, c->d_atom_rep,
+                                                        c->d_reps, d_coor, c->d_mass, c->d_xrel);
+    k_press_xrel_sites<T><<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_orig, c->d_xrel,
+                                                                      c->d_xsite);
+    if (c->nW > 0)
+        (c->row16 ? k_press_water<T, unsigned short> : k_press_water<T, int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
+            (int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff, c->d_wl1_cnt, c->d_wl1, c->cap_row1,
+            c->d_xsite, c->d_press_unit);
+    if (c->nA > 0)
+        k_press_atom<T><<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
+            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_site_lj, c->d_site_flags, c->d_xl_off,
+            c->d_xl, cap_int(c->cap_xl), c->d_xsite, c->d_press_unit);
+    k_press_rel<T><<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
+                                                               c->d_reps, c->d_part, c->d_q, c->d_xsite,
+                                                               c->d_press_site);
+}
+
 }  // namespace
 
 void nb_launch_pme_virial(NbCtx *c, void *grid, double *v_col);
 
 int nb_pressure(NbCtx *c, const double *d_coor, double *d_out)
 {
-    cudaStream_t s = c->stream;
-    const int B = 128;
-    if (c->nmol > 0)
-        k_press_xrel<<<(c->nmol + B - 1) / B, B, 0, s>>>(c->nmol, c->d_mol_off, c->d_mol_atom, c->d_atom_rep,
-                                                        c->d_reps, d_coor, c->d_mass, c->d_xrel, c->d_xrelf);
-    k_press_xrel_sites<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_orig, c->d_xrelf,
-                                                                   c->d_xsite);
-    if (c->nW > 0)
-        (c->row16 ? k_press_water<unsigned short> : k_press_water<int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
-            (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float4 *)c->d_woff, c->d_wl1_cnt,
-            c->d_wl1, c->cap_row1, c->d_xsite, c->d_press_unit);
-    if (c->nA > 0)
-        k_press_atom<<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
-            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, (const float4 *)c->d_pos, (const float2 *)c->d_site_lj,
-            c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), c->d_xsite, c->d_press_unit);
-    k_press_rel<<<(int)((c->nsite + 255) / 256), 256, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
-                                                            c->d_reps, (const float4 *)c->d_part, c->d_q, c->d_xsite,
-                                                            c->d_press_site);
+    if (c->precision == MOIL_NB_FP64) pressure_t<double>(c, d_coor, d_out);
+    else pressure_t<float>(c, d_coor, d_out);
     nb_launch_pme_virial(c, c->d_press_grid, c->d_press_col);
-    k_press_reduce<<<c->nrep, NB_PR_THREADS, 0, s>>>((int)c->nW, c->d_reps, c->d_press_unit, c->d_press_site,
-                                                     c->d_press_col, c->d_col_begin, d_out);
+    k_press_reduce<<<c->nrep, NB_PR_THREADS, 0, c->stream>>>((int)c->nW, c->d_reps, c->d_press_unit,
+                                                             c->d_press_site, c->d_press_col, c->d_col_begin, d_out);
     NB_CUDA_OK(c, cudaGetLastError());
     return MOIL_NB_OK;
 }

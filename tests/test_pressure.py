@@ -172,6 +172,23 @@ def test_gpu_pressure_batch_and_groups(cfg0):
 
 
 @pytest.mark.gpu
+def test_gpu_pressure_plain_fp64_path(case):
+    """The plain FP64 handle: the same pass in FP64 arithmetic matches the oracle to 1e-9 of
+    the tensor's magnitude sum (the FP64 path's cutoffs are the FP32-rounded squares, so a pair
+    within rounding of the cutoff could differ; none does in these systems)."""
+    from moil_fnrfd_gb300.nb import MOIL_NB_FP64, Nonbonded
+    name, s, mol, mass = case
+    want = O.pressure(s, mol, mass, mode="mi")[2]
+    nb = Nonbonded(s, precision=MOIL_NB_FP64)
+    nb.set_molecules(mol, mass)
+    press = nb.pressure(s.coor)[2]
+    scale = float(np.abs(want).sum())
+    for k in range(12):
+        assert abs(press[k] - want[k]) <= 1e-9 * scale, (name, O.PRESS_KEYS[k], press[k], want[k])
+    nb.close()
+
+
+@pytest.mark.gpu
 def test_gpu_pressure_needs_molecules(cfg0):
     from moil_fnrfd_gb300.nb import MoilNbError, Nonbonded
     nb = Nonbonded(cfg0)
