@@ -219,7 +219,7 @@ int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass);
  *   k 9..11  V_PIrelXX..ZZ           PME force x position relative to the centre of mass
  *                                     (ewald_receip.f:928-933)
  * in kcal/mol; pressure.f:235-238 sums vir + dir + rec - rel (its V_PIcor is zero).  Every
- * pair term is F_ij,a (R_I - R_J)_a with R the centres of mass.  Mixed path only; needs
+ * pair term is F_ij,a (R_I - R_J)_a with R the centres of mass.  Both precisions; needs
  * moil_nb_set_molecules. */
 int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *energies, double *press);
 

@@ -200,7 +200,7 @@ int nb_pme_configure(NbCtx *c);
 void nb_launch_finalize(NbCtx *c, double *d_dpot);
 // parameter derivatives after an evaluation of c->d_coor (nb_adjoint.cu), mixed path
 int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds);
-// pressure analysis terms after an evaluation of d_coor (nb_press.cu), mixed path: 12 per replica
+// pressure analysis terms after an evaluation of d_coor (nb_press.cu): 12 per replica
 int nb_pressure(NbCtx *c, const double *d_coor, double *d_out);
 
 #define NB_CUDA_OK(c, call)                                                         \
