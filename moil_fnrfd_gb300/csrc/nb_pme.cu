@@ -29,10 +29,6 @@
 
 namespace {
 
-template <typename C> __device__ __forceinline__ C cmk(float r, float i);
-template <> __device__ __forceinline__ float2 cmk<float2>(float r, float i) { return make_float2(r, i); }
-template <> __device__ __forceinline__ double2 cmk<double2>(float r, float i) { return make_double2(r, i); }
-
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 template <typename C> __device__ __forceinline__ C cmul(C a, C b)
