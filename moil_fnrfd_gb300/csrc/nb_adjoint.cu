@@ -2,9 +2,10 @@
 // dE/dsigma per atom (moil_nb_adjoint).  MOIL computes none of them; the oracle's
 // ora_adjoint_mi is the reference, itself checked against finite differences.
 //
-// One evaluation (moil_nb_eval semantics) leaves the lists, the site-ordered positions and,
-// on the mixed path, the convolved PME potential grid on the device; these kernels then
-// accumulate, in FP64:
+// One evaluation (moil_nb_eval semantics) leaves the lists, the site-ordered positions and
+// the PME grid on the device (the real potential planes on the mixed path, the convolved
+// spectrum on the plain path, whose inverse plane kernel then gives each site's potential
+// shares); these kernels then accumulate, in FP64:
 //   dE/dq_i     = sum over i's real-space partners of k q_j erfc(alpha r)/r
 //               - sum over i's excluded partners of k q_j erf(alpha r)/r
 //               + 1-4 Coulomb p14(3)/(q_i r) + fc * sum(theta * potential grid)
@@ -289,26 +290,54 @@ __global__ void k_adj_pme_f(int nsite, const int *__restrict__ site_rep, const i
     dq[site_orig[s]] += R.fcd * v;
 }
 
+// PME on the plain path: fc * the four plane shares of the potential at each site
+__global__ void k_adj_pme_d(int nsite, const int *__restrict__ site_rep, const int *__restrict__ site_orig,
+                            const RepDev *__restrict__ reps, const double *__restrict__ phi4, double *__restrict__ dq)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsite) return;
+    const double *p = phi4 + 4 * (size_t)s;
+    dq[site_orig[s]] += reps[site_rep[s]].fcd * ((p[0] + p[1]) + (p[2] + p[3]));
+}
+
+template <typename T>
+void adjoint_pairs(NbCtx *c, double *d_dq, double *d_de, double *d_ds)
+{
+    cudaStream_t s = c->stream;
+    const int B = 128;
+    if (c->nW > 0)
+        (c->row16 ? k_adj_water<T, unsigned short> : k_adj_water<T, int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
+            (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_woff, c->d_site_lj,
+            c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), d_dq,
+            d_de, d_ds);
+    if (c->nA > 0)
+        k_adj_atom<T><<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
+            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_site_lj,
+            c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), d_dq, d_de, d_ds);
+}
+
 }  // namespace
+
+void nb_launch_pme_potential(NbCtx *c, double *phi4);
 
 int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds)
 {
     cudaStream_t s = c->stream;
     const int B = 128;
-    if (c->nW > 0)
-        (c->row16 ? k_adj_water<float, unsigned short> : k_adj_water<float, int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
-            (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_woff, c->d_site_lj,
-            c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), d_dq,
-            d_de, d_ds);
-    if (c->nA > 0)
-        k_adj_atom<float><<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
-            (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_site_lj,
-            c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), d_dq, d_de, d_ds);
+    if (c->precision == MOIL_NB_FP64) adjoint_pairs<double>(c, d_dq, d_de, d_ds);
+    else adjoint_pairs<float>(c, d_dq, d_de, d_ds);
     k_adj_excl14<<<(int)((c->natom + B - 1) / B), B, 0, s>>>(
         (int)c->natom, c->d_atom_rep, c->d_reps, c->d_coor, c->d_q, c->d_lj_d, c->d_ex_off, c->d_ex_j,
         c->d_p14_off, c->d_p14_j, c->d_p14_par, d_dq, d_de, d_ds);
-    k_adj_pme_f<<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig, c->d_reps,
-                                                          (const float4 *)c->d_fr, (const float2 *)c->d_grid, d_dq);
+    if (c->precision == MOIL_NB_FP64) {
+        nb_launch_pme_potential(c, c->d_adj_phi);
+        k_adj_pme_d<<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
+                                                              c->d_reps, c->d_adj_phi, d_dq);
+    } else {
+        k_adj_pme_f<<<(int)((c->nsite + B - 1) / B), B, 0, s>>>((int)c->nsite, c->d_site_rep, c->d_site_orig,
+                                                              c->d_reps, (const float4 *)c->d_fr,
+                                                              (const float2 *)c->d_grid, d_dq);
+    }
     NB_CUDA_OK(c, cudaGetLastError());
     return MOIL_NB_OK;
 }

@@ -86,7 +86,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
-    free_ptr(c->d_adj); free_ptr(c->d_md_dpot);
+    free_ptr(c->d_adj); free_ptr(c->d_adj_phi); free_ptr(c->d_md_dpot);
     free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
     free_ptr(c->d_xsite); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
     free_ptr(c->d_press_out);
@@ -987,10 +987,6 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
 {
     if (!h || !coor) return MOIL_NB_ERR_ARG;
     if (!h->inited) return MOIL_NB_ERR_STATE;
-    if (h->precision == MOIL_NB_FP64) {
-        h->err = "parameter derivatives are computed on the mixed path only";
-        return MOIL_NB_ERR_ARG;
-    }
     cudaSetDevice(h->device);
     if (!h->grp.empty()) {
         for (size_t g = 0; g < h->grp.size(); ++g) {
@@ -1007,6 +1003,8 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
     int rc = eval_impl(h, h->d_coor, h->d_dpot, e);   // lists, positions and the potential grid
     if (rc != MOIL_NB_OK) return rc;
     if (!h->d_adj) NB_CUDA_OK(h, cudaMalloc(&h->d_adj, sizeof(double) * 3 * std::max<size_t>(n, 1)));
+    if (h->precision == MOIL_NB_FP64 && !h->d_adj_phi)
+        NB_CUDA_OK(h, cudaMalloc(&h->d_adj_phi, sizeof(double) * 4 * std::max<int64_t>(h->nsite, 1)));
     rc = nb_adjoint(h, h->d_adj, h->d_adj + n, h->d_adj + 2 * n);
     if (rc != MOIL_NB_OK) return rc;
     double *out[3] = {dEdq, dEdeps, dEdsig};

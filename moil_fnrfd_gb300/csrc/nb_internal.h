@@ -135,6 +135,7 @@ struct NbCtx {
     // caller buffers used by host-pointer evaluations
     double *d_coor = nullptr, *d_dpot = nullptr;
     double *d_adj = nullptr;           // parameter derivatives, 3 x natom (allocated on first use)
+    double *d_adj_phi = nullptr;       // plain path: PME potential share of 4 planes per site (first use)
     double *d_md_dpot = nullptr;       // gradient of the MD steps (moil_nb_md_step, first use)
 
     // pressure analysis (moil_nb_set_molecules / moil_nb_pressure, nb_press.cu)

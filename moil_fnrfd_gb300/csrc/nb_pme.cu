@@ -223,7 +223,7 @@ __device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *
 template <typename T>
 __device__ __forceinline__ void gather_plane(const RepDev &R, int z, const int *__restrict__ zstart,
                                              const int *__restrict__ zatoms, const typename vec4<T>::type *fr,
-                                             const T *Rp, T *__restrict__ part)
+                                             const T *Rp, T *__restrict__ part, bool pot = false)
 {
     typedef typename vec4<T>::type T4;
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
@@ -258,6 +258,11 @@ __device__ __forceinline__ void gather_plane(const RepDev &R, int z, const int *
                 gx += sx * th2[t2];
                 gy += sy * dt2[t2];
                 gz += sy * th2[t2];
+            }
+            if (pot) {
+                // the potential share of this plane (parameter derivatives): one slot per plane
+                part[4 * (size_t)s + t3] = gz * th3[t3];
+                continue;
             }
             T *o = part + 12 * (size_t)s + 3 * t3;
             o[0] = gx * th3[t3];
@@ -935,7 +940,7 @@ __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__
                                                    const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
                                                    const void *tw_v, const int *__restrict__ zstart,
                                                    const int *__restrict__ zatoms, const void *fr_v,
-                                                   const void *grid_v, T *__restrict__ part)
+                                                   const void *grid_v, T *__restrict__ part, int pot)
 {
     typedef typename cplx<T>::type C;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -974,7 +979,7 @@ __global__ void __launch_bounds__(256) k_plane_inv(const PlaneWork *__restrict__
         __syncwarp();
     }
     __syncthreads();
-    gather_plane<T>(R, w.z, zstart, zatoms, (const typename vec4<T>::type *)fr_v, Rp, part);
+    gather_plane<T>(R, w.z, zstart, zatoms, (const typename vec4<T>::type *)fr_v, Rp, part, pot != 0);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1017,7 +1022,7 @@ void pme_t(NbCtx *c)
         if (c->timing) cudaEventRecord(c->ev[8], s);
         k_plane_inv<T><<<np, 256, c->smem_plane_inv, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw,
                                                           c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid,
-                                                          (T *)c->d_part);
+                                                          (T *)c->d_part, 0);
     }
     if (c->timing) cudaEventRecord(c->ev[9], s);
     c->launches += 6;
@@ -1233,6 +1238,15 @@ void nb_launch_pme_virial(NbCtx *c, void *grid, double *v_col)
     k_press_zvir_f<<<nc, 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan,
                                                    (const float2 *)c->d_tw, c->d_tab, (const float *)c->d_bsp,
                                                    (const float2 *)grid, v_col);
+}
+
+// parameter derivatives on the plain path: the potential share of every plane at each site
+// (4 slots per site) from the convolved grid the evaluation left in place
+void nb_launch_pme_potential(NbCtx *c, double *phi4)
+{
+    k_plane_inv<double><<<(int)c->planes.size(), 256, c->smem_plane_inv, c->stream>>>(
+        c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan, c->d_tw, c->d_zstart, c->d_zatoms, c->d_fr, c->d_grid,
+        phi4, 1);
 }
 
 int nb_pme_configure(NbCtx *c)

@@ -185,11 +185,15 @@ def test_gpu_adjoint_batch_matches_single(cfg0, neutral):
 
 
 @pytest.mark.gpu
-def test_gpu_adjoint_refused_on_fp64_handle(cfg0):
-    from moil_fnrfd_gb300.nb import MOIL_NB_FP64, MoilNbError, Nonbonded
-    nb = Nonbonded(cfg0, precision=MOIL_NB_FP64)
-    with pytest.raises(MoilNbError):
-        nb.adjoint(cfg0.coor)
+@pytest.mark.parametrize("which", ["water216", "solute"])
+def test_gpu_adjoint_plain_fp64_path(cfg0, neutral, which):
+    """The plain FP64 handle: FP64 pair arithmetic and the PME potential from the FP64 plane
+    kernels match the oracle's adjoint to 1e-9 relative RMS."""
+    from moil_fnrfd_gb300.nb import MOIL_NB_FP64, Nonbonded
+    s = cfg0 if which == "water216" else neutral
+    nb = Nonbonded(s, precision=MOIL_NB_FP64)
+    _gpu_adjoint_close(nb.adjoint(s.coor), O.adjoint(s), tol=1e-9)
+    nb.close()
 
 
 @pytest.mark.gpu
