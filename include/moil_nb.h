@@ -170,8 +170,9 @@ int moil_nb_get_virial(moil_nb_ctx *h, int replica, double *virvdw);
  * one FP64 value per atom: dE/dq (the electrostatic potential, kcal/mol/e), dE/deps and
  * dE/dsigma of the atom's LJ parameters decoded from the epsgm encoding
  * (connect/fillpt.f:136-184).  Any output may be NULL; energies as moil_nb_eval.  No
- * counterpart in the reference, which computes no parameter derivatives; mixed precision
- * handles only (MOIL_NB_ERR_ARG otherwise).  The LJ switch extension is not differentiated. */
+ * counterpart in the reference, which computes no parameter derivatives; both precisions
+ * (pair terms in the handle's arithmetic, sums in FP64).  The LJ switch extension is not
+ * differentiated. */
 int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dEdeps, double *dEdsig,
                     moil_energies *energies);
 
