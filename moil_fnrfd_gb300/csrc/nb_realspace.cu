@@ -799,19 +799,19 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
     __shared__ double part[2 * NB_EU + NB_EX + 1];   // water units, other units, atoms, columns
     const int r = blockIdx.x, t = threadIdx.x;
     const RepDev &R = reps[r];
-    // units: the replica's waters, then its other units, NB_EU doubles each; four loads in
-    // flight per thread (four partial sums, added in a fixed order)
+    // units: the replica's waters, then its other units, NB_EU doubles each; eight loads in
+    // flight per thread (eight partial sums, added in a fixed order)
     auto stream_sum = [t](const double *__restrict__ b, int n) {
-        double p[4] = {0.0, 0.0, 0.0, 0.0};
+        double p[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         int k = t;
-        for (; k + 3 * NB_FE_THREADS < n; k += 4 * NB_FE_THREADS) {
+        for (; k + 7 * NB_FE_THREADS < n; k += 8 * NB_FE_THREADS) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) p[j] += b[k + j * NB_FE_THREADS];
+            for (int j = 0; j < 8; ++j) p[j] += b[k + j * NB_FE_THREADS];
         }
-        if (k < n) p[0] += b[k];
-        if (k + NB_FE_THREADS < n) p[1] += b[k + NB_FE_THREADS];
-        if (k + 2 * NB_FE_THREADS < n) p[2] += b[k + 2 * NB_FE_THREADS];
-        return (p[0] + p[1]) + (p[2] + p[3]);
+#pragma unroll
+        for (int j = 0; j < 7; ++j)
+            if (k + j * NB_FE_THREADS < n) p[j] += b[k + j * NB_FE_THREADS];
+        return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
     };
     const double uw = stream_sum(e_unit + NB_EU * (size_t)R.wat0, NB_EU * R.nwat);
     const double uo = stream_sum(e_unit + NB_EU * ((size_t)nW + R.oth0), NB_EU * R.noth);
