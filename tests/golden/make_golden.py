@@ -29,6 +29,9 @@ def main():
             if k.startswith("e_"):
                 out[f"{mode}_{k}"] = np.float64(v)
         out[f"{mode}_site_pairs"] = np.int64(e["site_pairs"])
+    # pressure analysis terms (molecules: the waters), minimum-image evaluator
+    mol, mass = systems.molecules(s)
+    out["press_mi"] = oracle.pressure(s, mol, mass, mode="mi")[2]
     np.savez_compressed(os.path.join(HERE, "config0_oracle.npz"), **out)
     print("wrote config0_oracle.npz")
 

@@ -229,3 +229,6 @@ def test_golden_config0():
         np.testing.assert_allclose(d, g[f"dpot_{mode}"], rtol=0, atol=1e-11)
         for k in ENERGY_TERMS + ("e_total",):
             assert e[k] == pytest.approx(float(g[f"{mode}_{k}"]), rel=1e-12, abs=1e-9), (mode, k)
+    mol, mass = S.molecules(s)
+    press = O.pressure(s, mol, mass, mode="mi")[2]
+    np.testing.assert_allclose(press, g["press_mi"], rtol=1e-12, atol=1e-9)
