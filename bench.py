@@ -25,6 +25,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -45,8 +46,36 @@ SKIN = 1.0
 WATER_KERNEL_DRAM_BYTES_PER_WATER = 504.9
 
 
+ACCEL = 418.4                 # (kcal/mol/Å) / amu in Å/ps^2
+KB = 0.0019872041             # kcal/mol/K
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def host_cpu():
+    """The host's CPU model and logical core count (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith(("model name", "cpu model")):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except Exception:
+            pass
+    return {"cpu_model": model or platform.processor() or platform.machine(), "nproc": os.cpu_count(),
+            "arch": platform.machine()}
 
 
 def peaks():
@@ -157,7 +186,33 @@ def cpu_baseline(reps, budget_s=12.0):
     return {"value": done_atoms / dt, "unit": "atom-evals/s", "cores": 1, "kind": "port",
             "sample": f"{n} of {len(reps)} replicas x {LIST_PERIOD} evaluations (lists rebuilt once), "
                       f"oracle in MOIL list-path mode (13 image translations, erfc spline table, +2 Å buffers), "
-                      f"{dt:.1f} s"}
+                      f"{dt:.1f} s",
+            "note": "one host thread, as MOIL runs one serial process per system", **host_cpu()}
+
+
+def rigid_water_velocities(s, temperature, seed):
+    """Maxwell-Boltzmann velocities (Å/ps) of an all-water system with each molecule's three
+    bond-length rates removed (the velocity half of RATTLE): v_a += sum_k lambda_k d_k / m_a over
+    the O-H1, O-H2 and H1-H2 constraints d_k = x_a - x_b, lambda from the 3x3 system per water
+    that zeroes every d_k . (v_a - v_b)."""
+    from moil_fnrfd_gb300.systems import MASS_H, MASS_O
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = np.tile([MASS_O, MASS_H, MASS_H], s.npt // 3).reshape(-1, 3)
+    v = (rng.normal(size=(s.npt, 3)) * np.sqrt(KB * temperature * ACCEL / m.reshape(-1))[:, None]).reshape(-1, 3, 3)
+    x = s.coor.reshape(-1, 3, 3)
+    pairs = ((0, 1), (0, 2), (1, 2))
+    d = np.stack([x[:, a] - x[:, b] for a, b in pairs], axis=1)
+    M = np.empty((x.shape[0], 3, 3))
+    for k, (a, b) in enumerate(pairs):
+        for l, (c, e) in enumerate(pairs):
+            coef = ((a == c) - (a == e)) / m[:, a] - ((b == c) - (b == e)) / m[:, b]
+            M[:, k, l] = (d[:, k] * d[:, l]).sum(-1) * coef
+    rhs = -np.stack([(d[:, k] * (v[:, a] - v[:, b])).sum(-1) for k, (a, b) in enumerate(pairs)], axis=1)
+    lam = np.linalg.solve(M, rhs[..., None])[..., 0]
+    for k, (a, b) in enumerate(pairs):
+        v[:, a] += lam[:, k, None] * d[:, k] / m[:, a, None]
+        v[:, b] -= lam[:, k, None] * d[:, k] / m[:, b, None]
+    return v.reshape(-1, 3), m.reshape(-1)
 
 
 def press_leg(nb, reps, coor, e2e_ms, calls=3):
@@ -180,19 +235,50 @@ def press_leg(nb, reps, coor, e2e_ms, calls=3):
             "calls": calls, "sample": "the timed batch, molecules = waters, no gradient copy"}
 
 
+def accuracy_leg(nb, reps, d_coor, d_dpot, n_sample=6):
+    """One batched evaluation of the timed coordinates; for n_sample replicas spread over the
+    batch, each energy term's error relative to the term, |dE_total| / |E_total| and the
+    relative RMS gradient error against the oracle (parity mode: MOIL's predicate, FP64)."""
+    from oracle import oracle
+    energies = nb.eforce_device(d_coor.data_ptr(), d_dpot.data_ptr())
+    dp = d_dpot.cpu().numpy()
+    offs = np.cumsum([0] + [s.npt for s in reps])
+    terms = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_corr", "e_self", "e_ew_receip")
+    picks = sorted(set(int(round(k * (len(reps) - 1) / max(n_sample - 1, 1))) for k in range(n_sample)))
+    rows, worst = [], {k: 0.0 for k in terms}
+    for r in picks:
+        s = reps[r]
+        ref, eref = oracle.eforce(s, mode="parity")
+        e = energies[r]
+        rel = {k: abs(e[k] - eref[k]) / abs(eref[k]) for k in terms if eref[k] != 0}
+        for k, v in rel.items():
+            worst[k] = max(worst[k], v)
+        g = dp[offs[r]:offs[r + 1]]
+        rows.append({"replica": r, "atoms": s.npt, "e_total": eref["e_total"],
+                     "total_rel": abs(e["e_total"] - eref["e_total"]) / abs(eref["e_total"]),
+                     "force_rel_rms": float(np.sqrt(((g - ref) ** 2).sum() / (ref ** 2).sum())),
+                     "term_rel": {k: float(f"{v:.3g}") for k, v in rel.items()}})
+    return {"oracle": "parity mode (MOIL's predicate at these coordinates, FP64)",
+            "max_total_rel": max(x["total_rel"] for x in rows),
+            "max_force_rel_rms": max(x["force_rel_rms"] for x in rows),
+            "max_term_rel": {k: float(f"{v:.3g}") for k, v in worst.items()},
+            "tolerance": {"total_rel": 1e-6, "force_rel_rms": 1e-5}, "replicas": rows}
+
+
 def md_leg(local, steps=1000, warmup=20):
     """One 96,000-atom water box (32,000 TIP3P, 98.6 Å, rc 10, alpha 0.32, grid 100^3) through
     a rigid-water leapfrog trajectory on the device (moil_nb_md_step: evaluation, leapfrog and
     SETTLE each step, nothing copied to the host): 2 fs steps from 300 K, pair lists rebuilt
     every 10 steps with a 1.5 Å skin.  Timed by wall clock around the whole trajectory."""
     import torch
-    from moil_fnrfd_gb300 import dyna, systems
+    from moil_fnrfd_gb300 import systems
     from moil_fnrfd_gb300.nb import MOIL_NB_FP64, Nonbonded
     s = systems.config2()
     nb = Nonbonded(s, device=local, skin=1.5, list_period=10)
-    start = dyna.RigidWaterDynamics(nb, s, dt=0.002, temperature=300.0, seed=11)   # initial velocities
-    x, v = start.x.clone(), start.v.clone()
-    m = torch.tensor(dyna._masses(s)[0], dtype=torch.float64, device=x.device)
+    v0, m0 = rigid_water_velocities(s, 300.0, seed=11)
+    x = torch.tensor(s.coor, dtype=torch.float64, device=f"cuda:{local}")
+    v = torch.tensor(v0, dtype=torch.float64, device=x.device)
+    m = torch.tensor(m0, dtype=torch.float64, device=x.device)
     torch.cuda.synchronize()
     nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.002, warmup)
     e, ek = nb.md_step(x.data_ptr(), v.data_ptr(), m.data_ptr(), 0.002, 1)
@@ -225,6 +311,7 @@ def md_leg(local, steps=1000, warmup=20):
     tb.record(stp)
     torch.cuda.synchronize()
     out["plain_fp64_ms_per_eval"] = ta.elapsed_time(tb) / 3
+    out["plain_fp64_atom_evals_per_s"] = s.npt / (out["plain_fp64_ms_per_eval"] / 1e3)
     p.close()
     return out
 
@@ -256,7 +343,9 @@ def run_reference(args):
                        "sample_per_step": f"{len(sample)} replicas x {LIST_PERIOD} evaluations"},
             "cpu_baseline": {"value": value, "unit": "atom-evals/s", "cores": threads, "kind": "port",
                              "sample": f"{len(sample)} of {len(reps)} replicas x {LIST_PERIOD} evaluations per step, "
-                                       "OpenMP over replicas, oracle in MOIL list-path mode"},
+                                       "OpenMP over replicas, oracle in MOIL list-path mode",
+                             "label": "not MOIL: the oracle's all-core OpenMP variant (MOIL itself runs one "
+                                      "serial process per system)", **host_cpu()},
             "e2e": {"value": value, "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -410,6 +499,11 @@ def main():
                    "d2h_bytes_per_step": int(coor.nbytes + 16 * 8 * len(reps))},
            "clocks": clk, "gpu_launches": launches * args.steps}
 
+    # energy and gradient errors of the batched evaluation against the oracle (FP64, MOIL's
+    # predicate) on a sample of replicas spread over the batch
+    if not args.no_cpu and rank == 0:
+        out["accuracy_vs_oracle"] = accuracy_leg(nb, reps, d_coor, d_dpot)
+
     # accuracy and the plain FP64 path on a sample of replicas (denominator of the 20x target)
     if not args.no_fp64 and rank == 0:
         sample = reps[:24]
@@ -438,8 +532,13 @@ def main():
             p.close()
         fp64_value = fp_atoms / (fp_ms / 1e3)
         out["plain_fp64"] = {"value": fp64_value, "unit": "atom-evals/s",
-                             "sample": f"{len(sample)} replicas, one per handle/launch sequence, "
-                                       f"{LIST_PERIOD} evaluations each (one list build)"}
+                             "sample": f"{len(sample)} replicas of {min(s.npt for s in sample)}-"
+                                       f"{max(s.npt for s in sample)} atoms ({sum(s.npt for s in sample)} in all), "
+                                       f"one per handle/launch sequence, {LIST_PERIOD} evaluations each "
+                                       f"(one list build)",
+                             "note": "a ~5k-atom replica per launch sequence is dominated by fixed per-evaluation "
+                                     "costs (about 30 launches, the list check and the energy read-back); the "
+                                     "96,000-atom FP64 rate is in single_system_md.plain_fp64_atom_evals_per_s"}
         out["speedup_vs_plain_fp64"] = value / fp64_value
         out["force_err_vs_fp64"] = {"max_rel_rms": max(errs), "replicas": len(errs)}
     nb.close()
@@ -448,6 +547,7 @@ def main():
 
     if not args.no_md and rank == 0:
         out["single_system_md"] = md_leg(local)
+        out["speedup_vs_plain_fp64_96k"] = value / out["single_system_md"]["plain_fp64_atom_evals_per_s"]
 
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline(reps)

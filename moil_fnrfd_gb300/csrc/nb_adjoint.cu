@@ -265,9 +265,13 @@ __global__ void k_adj_pme_f(int nsite, const int *__restrict__ site_rep, const i
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
     const size_t zs = (size_t)R.n1h * n2 * 2;
     const float *Q = (const float *)(grid + R.g0);
-    const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+    int i1, i2, i3;
+    float w1, w2, w3;
+    pme_fr_split(f.x, i1, w1);
+    pme_fr_split(f.y, i2, w2);
+    pme_fr_split(f.z, i3, w3);
     double th[3][4];
-    const double w[3] = {(double)f.x - i1, (double)f.y - i2, (double)f.z - i3};
+    const double w[3] = {(double)w1, (double)w2, (double)w3};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double u = w[d], u2 = u * u, u3 = u2 * u, m = 1.0 - u;

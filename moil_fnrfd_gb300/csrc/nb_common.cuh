@@ -13,6 +13,7 @@
 // independent of summation order, so forces are bit-identical run to run.
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include "erfcx_coef.h"
@@ -50,6 +51,8 @@ struct RepDev {
     float qq[3];             // water qO*qO, qO*qH, qH*qH times kofdie/eps (pot/watwat_ewald.f:70-79)
     float w12, w6;           // water O-O LJ A, B (pot/watwat_ewald.f:62-68)
     double qqd[3], w12d, w6d;
+    float w12c, w6c;         // relative FP32 rounding of w12, w6: (w12d - w12) / w12, (w6d - w6) / w6
+    double pme_qcorr;        // FP32 path: sum (q fc)^2 over the sum of the squared FP32 spread charges
     double epstmp;           // kofdie / eps
     int n1, n2, n3, n1h;     // PME grid, n1h = n1/2 + 1
     long long g0;            // first complex element of this replica's half-complex grid
@@ -58,7 +61,9 @@ struct RepDev {
     float fc;                // sqrt(kofdie/eps)
     double fcd;
     float spread_scale;      // FP32 path: plane accumulation in int32 units of 1/spread_scale,
-    float spread_inv;        // a power of two chosen so one atom's contribution stays below 2^21
+    float spread_inv;        // a power of two from nb_spread_exp
+    float spread216;         // FP32 spread factor spread_scale / 216 (weights taken as 6 theta)
+    double spread216_corr;   // (spread_scale / 216) / spread216
     double pme_fac;          // pi^2 / alpha^2
     double pivol;            // pi * volume
     float pme_fac2f, pivolf; // FP32 path: pi^2 / alpha^2 * log2(e), pi * volume
@@ -66,7 +71,54 @@ struct RepDev {
     int arith, hvdw0, lj_switch, has_water;
     int wtiled;              // water-water list by tiled all-pairs (few cells per box)
     double e_self;
+    double pivol_corr;       // FP32 path: (double)pivolf / pivol, applied to the FP64 energy sums
+    float msq_c[3][2];       // FP32 path: invL_d^2 as hi + lo (accurate m^2 in the influence function)
+    float fac2_lo;           // FP32 path: pme_fac2f's rounding remainder
+    float invL_lo[3];        // FP32 path: invLd - (double)invL (PME fractional coordinates)
+    // Water exclusion energies relative to a reference water (mixed path, wref != 0): every water
+    // of the replica carries the charges of its last one, and the energy of a water's three
+    // intramolecular pairs (O-H, O-H, H-H) is wcorr0 (FP64, exact erf at the squared reference
+    // distances wt0) plus coef * (r^2 - wt0) * Q(r^2) in FP32, Q the quotient of the erf(x)/x
+    // series in r^2 by (r^2 - wt0): a small difference, so FP32 rounding stays negligible
+    int wref;
+    int wsame;               // every water has the charges (qO, qH, qH) of the last one (host check)
+    int wfirst;              // caller atom of the first water's O (the reference geometry), or -1
+    float wt0[2];            // reference r^2 of the O-H and H-H pairs (FP32 values)
+    float wcoef[2];          // -qq kofdie/eps alpha 2/sqrt(pi) of the O-H and H-H pairs
+    float wq[2][8];          // quotient polynomial coefficients, ascending powers of r^2
+    double wcorr0;           // exclusion energy of one reference water
 };
+
+// Exponent k of the int32 PME plane scale 2^k (FP32 path): one atom's largest stencil weight,
+// q fc (2/3)^3, times 2^k stays below 2^25, so a grid point holds the sum of 64 such maximal
+// contributions without overflow (the stencil weights of atoms around one grid point sum to
+// about 1 on a 1 Å grid and about 2.3 on a 1.9 Å grid) at a resolution of 2^-25 of the
+// largest contribution
+__host__ __device__ inline int nb_spread_exp(double qfc_max)
+{
+    const double contrib = qfc_max * (8.0 / 27.0);
+    int k = contrib > 0 ? (int)floor(log2(33554432.0 / contrib)) : 28;
+    return k < 8 ? 8 : (k > 28 ? 28 : k);
+}
+
+// PME fractional grid coordinates of a site.  FP64 path: fr in [0, n] as a double.  FP32 path:
+// fr as fixed point with 2^23 units per grid point (n <= 128, so below 2^30), kept in the bits
+// of a float -- a single FP32 value near n would hold the fraction to only 2^-24 n.
+__device__ __forceinline__ float pme_fr_pack(int i, float w)
+{
+    return __int_as_float((i << 23) + min(__float2int_rn(w * 8388608.f), 8388607));
+}
+__device__ __forceinline__ void pme_fr_split(float v, int &i, float &w)
+{
+    const int b = __float_as_int(v);
+    i = b >> 23;
+    w = __int2float_rn(b & 0x7fffff) * (1.f / 8388608.f);
+}
+__device__ __forceinline__ void pme_fr_split(double v, int &i, double &w)
+{
+    i = (int)v;
+    w = v - (double)i;
+}
 
 // site flags
 #define SF_CHARGED 1u        // |q| > 1e-6 (connect/chsort.f:17-24)

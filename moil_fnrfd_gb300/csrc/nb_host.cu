@@ -45,8 +45,10 @@ double find_ewaldcof(double cutoff, double dtol)
     return x;
 }
 
+}  // namespace
+
 // pot/ewald_receip.f:413-481 (load_bsp_moduli / DFTMOD) for order 4
-void bsp_moduli(int n, double *mod)
+void nb_bsp_moduli(int n, double *mod)
 {
     // B-spline values at w = 0 (fill_bspline): 1/6, 2/3, 1/6, 0 in slots 2..5
     std::vector<double> arr(n + 8, 0.0);
@@ -64,6 +66,8 @@ void bsp_moduli(int n, double *mod)
     for (int k = 1; k <= n; ++k)
         if (mod[k - 1] < 1e-7) mod[k - 1] = 0.5 * (mod[(k - 2 + n) % n] + mod[k % n]);
 }
+
+namespace {
 
 template <typename T> void free_ptr(T *&p)
 {
@@ -83,7 +87,7 @@ void release_device(NbCtx *c)
     free_ptr(c->d_p14_j); free_ptr(c->d_p14_par); free_ptr(c->d_grad_site); free_ptr(c->d_e_unit);
     free_ptr(c->d_grad_ex); free_ptr(c->d_e_ex); free_ptr(c->d_plans); free_ptr(c->d_rep_plan); free_ptr(c->d_tw);
     free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp);
-    free_ptr(c->d_bsp); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
+    free_ptr(c->d_bsp); free_ptr(c->d_etab); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
     free_ptr(c->d_adj); free_ptr(c->d_adj_phi); free_ptr(c->d_md_dpot);
@@ -284,6 +288,17 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
             }
             for (int k = 0; k < 3; ++k) R.qq[k] = (float)R.qqd[k];
             R.w12 = (float)R.w12d; R.w6 = (float)R.w6d;
+            R.w12c = R.w12 != 0.f ? (float)((R.w12d - (double)R.w12) / (double)R.w12) : 0.f;
+            R.w6c = R.w6 != 0.f ? (float)((R.w6d - (double)R.w6) / (double)R.w6) : 0.f;
+            // reference-water exclusion energies (k_wref) need every water to carry these charges
+            R.wsame = 1;
+            R.wfirst = -1;
+            for (int m = 0; m < t->totmon; ++m) {
+                if (t->montype[m] != MOIL_MON_WATER) continue;
+                const int o = m == 0 ? 0 : t->poipt[m - 1];
+                if (R.wfirst < 0) R.wfirst = (int)(atom0 + o);
+                if (t->ptchg[o] != qo || t->ptchg[o + 1] != qh || t->ptchg[o + 2] != qh) R.wsame = 0;
+            }
         }
         double s2 = 0;
         for (int i = 0; i < t->npt; ++i) s2 += t->ptchg[i] * t->ptchg[i];
@@ -305,7 +320,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
             int ns[3] = {R.n1, R.n2, R.n3};
             for (int d = 0; d < 3; ++d) {
                 std::vector<double> m(ns[d]);
-                bsp_moduli(ns[d], m.data());
+                nb_bsp_moduli(ns[d], m.data());
                 c->bsp_h.insert(c->bsp_h.end(), m.begin(), m.end());
             }
         }
@@ -315,20 +330,25 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         R.pme_gs[1] = (float)(R.fcd * R.n2 * R.invLd[1]);
         R.pme_gs[2] = (float)(R.fcd * R.n3 * R.invLd[2]);
         {
-            // int32 plane accumulation: one atom's largest stencil weight, q fc (2/3)^3, times
-            // the scale stays below 2^21 (so the FP32 rounding trick is exact); power of two
             double qmax = 0;
             for (int i = 0; i < t->npt; ++i) qmax = std::max(qmax, fabs(t->ptchg[i]));
-            double contrib = qmax * R.fcd * (8.0 / 27.0);
-            int k = contrib > 0 ? (int)floor(log2(2097152.0 / contrib)) : 24;
-            k = std::min(24, std::max(8, k));
-            R.spread_scale = (float)ldexp(1.0, k);
-            R.spread_inv = (float)ldexp(1.0, -k);
+            nb_spread_scale(qmax * R.fcd, &R);
         }
         R.pme_fac = M_PI * M_PI / (alpha * alpha);
         R.pivol = M_PI * p->a * p->b * p->c;
-        R.pme_fac2f = (float)(R.pme_fac * 1.4426950408889634);
-        R.pivolf = (float)R.pivol;
+        nb_pme_fp32_consts(&R);
+        {
+            // the FP32 path spreads fl(fl(q) fl(fc)) per site (k_pme_bin): the reciprocal energy,
+            // quadratic in the charges, is rescaled by sum (q fc)^2 / sum fl(..)^2, exact when
+            // every charge has the same relative rounding (all waters: qH = -qO/2)
+            double sd = 0.0, sf = 0.0;
+            for (int i = 0; i < t->npt; ++i) {
+                const double qd = t->ptchg[i] * R.fcd, qf = (double)((float)t->ptchg[i] * R.fc);
+                sd += qd * qd;
+                sf += qf * qf;
+            }
+            R.pme_qcorr = (sf > 0.0 ? sd / sf : 1.0) * R.spread216_corr * R.spread216_corr;
+        }
         // atoms and units
         R.wat0 = (int)wat0; R.oth0 = (int)oth0;
         int noth = 0;

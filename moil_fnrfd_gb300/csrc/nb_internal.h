@@ -112,6 +112,7 @@ struct NbCtx {
     int2 *d_tab = nullptr;             // Stockham stage tables (twiddle step, destination index)
     std::vector<double> bsp_h;
     void *d_bsp = nullptr;             // float / double moduli
+    float *d_etab = nullptr;           // FP32 path: exp(-pi^2 m^2 / (alpha L)^2) / B per dimension (bsp layout)
     int nzbin = 0;
     int *d_zcount = nullptr, *d_zstart = nullptr, *d_zslot = nullptr, *d_zatoms = nullptr;
     void *d_fr = nullptr;              // float4 / double4 per site (fr1, fr2, fr3, q*fc)
@@ -197,6 +198,15 @@ void nb_launch_excl14(NbCtx *c, const double *d_coor);
 // PME (nb_pme.cu)
 void nb_launch_pme(NbCtx *c);
 int nb_pme_configure(NbCtx *c);
+// |DFT|^2 of the order-4 B-spline (pot/ewald_receip.f:413-481), n values
+void nb_bsp_moduli(int n, double *mod);
+// int32 PME plane scale 2^nb_spread_exp(max |q| fc), its inverse and the FP32 spread factor
+void nb_spread_scale(double qfc_max, RepDev *R);
+// FP32-path constants of the influence function from pme_fac, pivol and invLd
+void nb_pme_fp32_consts(RepDev *R);
+// FP32-path influence-function table of one replica (n1 + n2 + n3 entries, bsp layout) from its
+// FP64 B-spline moduli
+void nb_pme_etab(const RepDev &R, const double *bsp, float *out);
 // finalize (nb_realspace.cu)
 void nb_launch_finalize(NbCtx *c, double *d_dpot);
 // parameter derivatives after an evaluation of c->d_coor (nb_adjoint.cu), mixed path

@@ -672,6 +672,54 @@ void nb_scan(NbCtx *c, const int *in, int *out, int n, int *total, int gate)
     c->launches += 3;
 }
 
+// Reference water of each replica for the FP32 water exclusion energies (water_intra_f):
+// squared O-H and H-H distances t0 of the replica's first water (rounded to FP32), its three
+// exclusion energies -qq erf(alpha r)/r in FP64 (cdie_ewald.f:117-199), and the quotient of
+// the erf(x)/x series in r^2, sum_n (-1)^n (alpha^2 r^2)^n / (n! (2n+1)) to n = 8, by
+// (r^2 - t0).  Runs with the list build; needs every water to carry the replica's water
+// charges (wsame) and (alpha 2.2 Å)^2 <= 1, where 2.2 Å bounds H-H of a water whose sites
+// lie within rwat of its oxygen (the series then converges to 1e-8).
+__global__ void k_wref(int nrep, RepDev *__restrict__ reps, const double *__restrict__ coor, const int *st)
+{
+    if (rebuild_off(st)) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrep) return;
+    RepDev &R = reps[r];
+    R.wref = 0;
+    const double al = R.alphad;
+    if (!R.has_water || !R.wsame || R.wfirst < 0 || al * al * 4.84 > 1.0) return;
+    const double *x = coor + 3 * (size_t)R.wfirst;
+    double t[2] = {0.0, 0.0};
+    for (int d = 0; d < 3; ++d) {
+        t[0] += (x[3 + d] - x[d]) * (x[3 + d] - x[d]);
+        t[1] += (x[6 + d] - x[3 + d]) * (x[6 + d] - x[3 + d]);
+    }
+    if (!(t[0] > 1e-4 && t[1] > 1e-4 && al * al * t[1] <= 1.0 && al * al * t[0] <= 1.0)) return;
+    double e0 = 0.0;
+    for (int ty = 0; ty < 2; ++ty) {
+        const float t0 = (float)t[ty];
+        const double td = (double)t0, rr = sqrt(td), qq = R.qqd[1 + ty];
+        e0 += (ty == 0 ? 2.0 : 1.0) * (-qq * erf(al * rr) / rr);
+        // series coefficients in r^2: a_n = (-1)^n alpha^(2n) / (n! (2n+1))
+        double a[9], f = 1.0, p = 1.0;
+        for (int n = 0; n <= 8; ++n) {
+            if (n > 0) { f *= n; p *= -al * al; }
+            a[n] = p / (f * (2 * n + 1));
+        }
+        // synthetic division by (r^2 - t0): b_7 = a_8, b_(m-1) = a_m + t0 b_m
+        double b = a[8];
+        R.wq[ty][7] = (float)b;
+        for (int m = 7; m >= 1; --m) {
+            b = a[m] + td * b;
+            R.wq[ty][m - 1] = (float)b;
+        }
+        R.wt0[ty] = t0;
+        R.wcoef[ty] = (float)(-qq * al * NB_TWO_OVER_SQRTPI);
+    }
+    R.wcorr0 = e0;
+    R.wref = 1;
+}
+
 template <typename T>
 void build_lists_t(NbCtx *c, const double *d_coor)
 {
@@ -722,6 +770,10 @@ void build_lists_t(NbCtx *c, const double *d_coor)
     };
     if (c->row16) water_lists((unsigned short)0);
     else water_lists(0);
+    if (sizeof(T) == 4 && c->nW > 0 && c->water_excl_fast) {
+        k_wref<<<(c->nrep + 127) / 128, 128, 0, s>>>(c->nrep, c->d_reps, d_coor, c->d_status);
+        c->launches++;
+    }
     if (c->nA > 0) {
         const int ga = grid(c->nA, 128);
         k_xlist<T, 0><<<ga, 128, 0, s>>>((int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos,

@@ -110,15 +110,42 @@ __global__ void k_pme_bin(int nsite, const int *__restrict__ site_rep, const Rep
     typedef typename vec4<T>::type T4;
     const RepDev &R = reps[site_rep[s]];
     T4 p = ((const T4 *)pos_v)[s];
-    T w, f1, f2, f3;
-    w = p.x * rep_invL<T>(R, 0); f1 = (T)R.n1 * (w - nb_round(w) + (T)0.5);
-    w = p.y * rep_invL<T>(R, 1); f2 = (T)R.n2 * (w - nb_round(w) + (T)0.5);
-    w = p.z * rep_invL<T>(R, 2); f3 = (T)R.n3 * (w - nb_round(w) + (T)0.5);
     T4 o;
-    o.x = f1; o.y = f2; o.z = f3;
-    o.w = ((const T *)q_v)[s] * (sizeof(T) == 4 ? (T)R.fc : (T)R.fcd);
+    int zb;
+    if constexpr (sizeof(T) == 4) {
+        // fr = n (u - anint(u) + 1/2), u = x / L, carried as hi + lo through every step (1/L as
+        // hi + lo, the product's rounding error by an FMA, the + 1/2 by Fast2Sum) so the
+        // fraction within the grid cell keeps 2^-23 of a grid spacing
+        const float xs[3] = {p.x, p.y, p.z};
+        const int ns[3] = {R.n1, R.n2, R.n3};
+        float out[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float x = xs[d], ih = R.invL[d];
+            const float uh = x * ih, ul = fmaf(x, ih, -uh) + x * R.invL_lo[d];
+            const float a = uh - rintf(uh);              // exact (Sterbenz)
+            const float th = a + 0.5f, tl = (a - (th - 0.5f)) + ul;
+            const float n = (float)ns[d];
+            int i = (int)floorf(n * th);
+            float w = fmaf(n, th, -(float)i) + n * tl;
+            if (w < 0.f) { --i; w += 1.f; }
+            if (w >= 1.f) { ++i; w -= 1.f; }
+            if (i < 0) { i = 0; w = 0.f; }
+            out[d] = pme_fr_pack(i, w);
+            if (d == 2) zb = i;
+        }
+        o.x = out[0]; o.y = out[1]; o.z = out[2];
+        o.w = ((const T *)q_v)[s] * (T)R.fc;
+    } else {
+        T w, f1, f2, f3;
+        w = p.x * rep_invL<T>(R, 0); f1 = (T)R.n1 * (w - nb_round(w) + (T)0.5);
+        w = p.y * rep_invL<T>(R, 1); f2 = (T)R.n2 * (w - nb_round(w) + (T)0.5);
+        w = p.z * rep_invL<T>(R, 2); f3 = (T)R.n3 * (w - nb_round(w) + (T)0.5);
+        o.x = f1; o.y = f2; o.z = f3;
+        o.w = ((const T *)q_v)[s] * (T)R.fcd;
+        zb = (int)f3;
+    }
     ((T4 *)fr_v)[s] = o;
-    int zb = (int)f3;
     zb = zb >= R.n3 ? zb - R.n3 : (zb < 0 ? 0 : zb);
     // one atomic per distinct bin of the warp (a warp's sites are neighbours in space)
     const int key = R.zb0 + zb, lane = threadIdx.x & 31;
@@ -137,20 +164,21 @@ __global__ void k_pme_scatter(int nsite, const int *__restrict__ site_rep, const
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsite) return;
     const RepDev &R = reps[site_rep[s]];
-    double f3 = is_double ? ((const double4 *)fr_v)[s].z : (double)((const float4 *)fr_v)[s].z;
-    int zb = (int)f3;
+    int zb;
+    if (is_double) zb = (int)((const double4 *)fr_v)[s].z;
+    else zb = __float_as_int(((const float4 *)fr_v)[s].z) >> 23;   // pme_fr_split
     zb = zb >= R.n3 ? zb - R.n3 : (zb < 0 ? 0 : zb);
     zatoms[zstart[R.zb0 + zb] + zslot[s]] = s;
 }
 
 // plane accumulation.  FP32: int32 fixed point; the caller pre-multiplies by the replica's
-// spread_scale so |x| < 2^21, and x + 1.5*2^23 rounds x to an integer whose bits sit in the
-// low mantissa -- a float-to-int conversion without a conversion instruction.  Integer
-// addition makes the plane independent of the order of the atomics.  FP64: FP64 atomics.
+// spread_scale (nb_spread_exp) so one contribution stays below 2^25 and rounds it to the
+// nearest integer.  Integer addition makes the plane independent of the order of the
+// atomics.  FP64: FP64 atomics.
 template <typename T> struct Acc;
 template <> struct Acc<float> {
     typedef int type;
-    __device__ static void add(type *p, float x) { atomicAdd(p, __float_as_int(x + 12582912.0f) - 0x4B400000); }
+    __device__ static void add(type *p, float x) { atomicAdd(p, __float2int_rn(x)); }
     __device__ static float get(type v, float inv) { return __int2float_rn(v) * inv; }
 };
 template <> struct Acc<double> {
@@ -171,6 +199,17 @@ __device__ __forceinline__ void bsp4_th(T w, T th[4])
     th[1] = s * ((T)4 - (T)6 * w2 + (T)3 * w3);
     th[2] = s * ((T)1 + (T)3 * (w + w2 - w3));
     th[3] = s * w3;
+}
+// 6 th: the same weights without the factor 1/6, whose FP32 rounding (2.98e-8 high) would
+// raise every spread charge by 9e-8 and the reciprocal energy by 1.8e-7; the FP32 spread
+// applies 1/216 once per site (spread216)
+__device__ __forceinline__ void bsp4_th6(float w, float th[4])
+{
+    const float w2 = w * w, w3 = w2 * w, m = 1.f - w;
+    th[0] = m * m * m;
+    th[1] = 4.f - 6.f * w2 + 3.f * w3;
+    th[2] = 1.f + 3.f * (w + w2 - w3);
+    th[3] = w3;
 }
 template <typename T>
 __device__ __forceinline__ void bsp4_dth(T w, T d[4])
@@ -199,11 +238,21 @@ __device__ __forceinline__ void spread_plane(const RepDev &R, int z, const int *
         const int t3 = 3 - tp;
         for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
             const T4 f = fr[zatoms[idx]];
-            const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            int i1, i2, i3;
+            T w1, w2, w3;
+            pme_fr_split(f.x, i1, w1);
+            pme_fr_split(f.y, i2, w2);
+            pme_fr_split(f.z, i3, w3);
             T th1[4], th2[4], th3[4];
-            bsp4_th<T>(f.x - (T)i1, th1);
-            bsp4_th<T>(f.y - (T)i2, th2);
-            bsp4_th<T>(f.z - (T)i3, th3);
+            if constexpr (sizeof(T) == 4) {
+                bsp4_th6(w1, th1);
+                bsp4_th6(w2, th2);
+                bsp4_th6(w3, th3);
+            } else {
+                bsp4_th<T>(w1, th1);
+                bsp4_th<T>(w2, th2);
+                bsp4_th<T>(w3, th3);
+            }
             const T qz = th3[t3] * (f.w * scale);
             int xs[4];
 #pragma unroll
@@ -235,9 +284,12 @@ __device__ __forceinline__ void gather_plane(const RepDev &R, int z, const int *
         for (int idx = b0 + threadIdx.x; idx < b1; idx += blockDim.x) {
             const int s = zatoms[idx];
             const T4 f = fr[s];
-            const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+            int i1, i2, i3;
+            T w1, w2, w3;
+            pme_fr_split(f.x, i1, w1);
+            pme_fr_split(f.y, i2, w2);
+            pme_fr_split(f.z, i3, w3);
             T th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
-            const T w1 = f.x - (T)i1, w2 = f.y - (T)i2, w3 = f.z - (T)i3;
             bsp4_th<T>(w1, th1); bsp4_dth<T>(w1, dt1);
             bsp4_th<T>(w2, th2); bsp4_dth<T>(w2, dt2);
             bsp4_th<T>(w3, th3); bsp4_dth<T>(w3, dt3);
@@ -451,7 +503,7 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
     fft_ctx_load(ctx, plans + rep_plan[3 * w.rep + 1], tab, tw, c2);
     for (int k = threadIdx.x; k < n1 * n2; k += blockDim.x) acc[k] = 0;
     __syncthreads();
-    spread_plane<float>(R, w.z, zstart, zatoms, fr, acc, R.spread_scale);
+    spread_plane<float>(R, w.z, zstart, zatoms, fr, acc, R.spread216);
     __syncthreads();
     // x transform of real rows two at a time: line p carries row 2p as its real part and
     // row 2p+1 as its imaginary part
@@ -485,7 +537,7 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
 __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
                                                  const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
                                                  const float2 *__restrict__ tw, const int2 *__restrict__ tab,
-                                                 const float *__restrict__ bsp_all, float2 *__restrict__ grid,
+                                                 const float *__restrict__ etab_all, float2 *__restrict__ grid,
                                                  double *__restrict__ e_col)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -494,7 +546,7 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
     const int tk = min(NB_TKF, n2 - w.ky0);
-    const float *bsp = bsp_all + R.bsp0;
+    const float *etab = etab_all + R.bsp0;
     float2 *A = (float2 *)smem, *B = A + zconv_buf_elems(n3);
     FftCtx c3;
     fft_ctx_load((unsigned char *)(B + zconv_buf_elems(n3)), plans + rep_plan[3 * w.rep + 2], tab, tw, c3);
@@ -508,22 +560,29 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0, sA, n3);
     float2 *Fo = F == A ? B : A;
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
-    // influence function: exp(-pi^2 m^2 / alpha^2) = 2^(-fac2 m^2), fac2 = pi^2 / alpha^2 * log2(e)
-    const float fac2 = R.pme_fac2f, pivol = R.pivolf;
+    // influence function exp(-pi^2 m^2 / alpha^2) / (pi V B(m) m^2): the exponential and the
+    // B-spline moduli factor per dimension, so they come from a per-dimension table
+    // etab[k] = exp(-pi^2 m_k^2 / (alpha^2 L^2)) / B(k) formed in FP64 (no approximate
+    // exponential in the energy); m^2 = sum_d k_d^2 / L_d^2 from exact integer squares and
+    // 1/L_d^2 as hi + lo, and one correctly rounded division
+    const float pivol = R.pivolf;
     const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
-    const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
-    const float mh1 = (float)w.kx * iL0, pb1 = pivol * bsp[w.kx];
+    const float m1s = (float)(w.kx * w.kx), t1 = etab[w.kx];
+    const float c2h = R.msq_c[2][0], c2l = R.msq_c[2][1];
     float en = 0.f;
     for (int c = warp; c < tk; c += 8) {
         const int ky = w.ky0 + c;
-        const float mh2 = (float)(ky < nf2 ? ky : ky - n2) * iL1;
-        const float pb12 = pb1 * bsp[n1 + ky], m12 = mh1 * mh1 + mh2 * mh2;
+        const int m2 = ky < nf2 ? ky : ky - n2;
+        const float m2s = (float)(m2 * m2);
+        const float t12 = t1 * etab[n1 + ky];
+        const float m12 = fmaf(m1s, R.msq_c[0][0], fmaf(m2s, R.msq_c[1][0], fmaf(m1s, R.msq_c[0][1], m2s * R.msq_c[1][1])));
         for (int kz = lane; kz < n3; kz += 32) {
-            const float mh3 = (float)(kz < nf3 ? kz : kz - n3) * iL2;
-            const float msq = fmaf(mh3, mh3, m12);
+            const int m3 = kz < nf3 ? kz : kz - n3;
+            const float m3s = (float)(m3 * m3);
+            const float msq = fmaf(m3s, c2h, fmaf(m3s, c2l, m12));
             float et = (w.kx == 0 && ky == 0 && kz == 0)
                            ? 0.f
-                           : nb_ex2_approx(-fac2 * msq) * nb_rcp_approx(pb12 * bsp[n1 + n2 + kz] * msq);
+                           : __fdiv_rn(t12 * etab[n1 + n2 + kz], pivol * msq);
             float2 v = F[c * n3 + kz];
             en += wgt * et * (v.x * v.x + v.y * v.y);
             F[c * n3 + kz] = make_float2(v.x * et, -v.y * et);    // conj: the inverse runs forward
@@ -533,15 +592,18 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     float2 *I = fft_lines<0, true>(c3, F, Fo, nullptr, tk, 0, n3, sA);
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) g[kz * zs + lane] = I[lane * sA + kz];
-    // fixed-order reduction: FP32 within each warp, FP64 over the 8 warp sums
+    // fixed-order reduction: each thread's few terms in FP32, then FP64 across the warp and
+    // over the 8 warp sums; pivol_corr and pme_qcorr remove the FP32 rounding of pi V and of the
+    // spread charges from the sum
+    double ed = (double)en;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) en += __shfl_down_sync(0xffffffffu, en, o);
-    if (lane == 0) red[warp] = (double)en;
+    for (int o = 16; o > 0; o >>= 1) ed += __shfl_down_sync(0xffffffffu, ed, o);
+    if (lane == 0) red[warp] = ed;
     __syncthreads();
     if (threadIdx.x == 0) {
         double sum = 0.0;
         for (int k = 0; k < 8; ++k) sum += red[k];
-        e_col[blockIdx.x] = sum;
+        e_col[blockIdx.x] = sum * (R.pivol_corr * R.pme_qcorr);
     }
 }
 
@@ -677,9 +739,12 @@ __global__ void __launch_bounds__(256) k_pme_gather_f(int nsite, const int *__re
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3;
     const size_t zs = (size_t)R.n1h * n2 * 2;    // floats per plane
     const float *Q = (const float *)(grid + R.g0);
-    const int i1 = (int)f.x, i2 = (int)f.y, i3 = (int)f.z;
+    int i1, i2, i3;
+    float w1, w2, w3;
+    pme_fr_split(f.x, i1, w1);
+    pme_fr_split(f.y, i2, w2);
+    pme_fr_split(f.z, i3, w3);
     float th1[4], dt1[4], th2[4], dt2[4], th3[4], dt3[4];
-    const float w1 = f.x - (float)i1, w2 = f.y - (float)i2, w3 = f.z - (float)i3;
     bsp4_th<float>(w1, th1); bsp4_dth<float>(w1, dt1);
     bsp4_th<float>(w2, th2); bsp4_dth<float>(w2, dt2);
     bsp4_th<float>(w3, th3); bsp4_dth<float>(w3, dt3);
@@ -1004,7 +1069,7 @@ void pme_t(NbCtx *c)
                                                            c->d_zatoms, (const float4 *)c->d_fr, (float2 *)c->d_grid);
         if (c->timing) cudaEventRecord(c->ev[7], s);
         k_zconv_f<<<nc, 256, c->smem_zconv, s>>>(c->d_cols, c->d_reps, c->d_plans, c->d_rep_plan,
-                                                  (const float2 *)c->d_tw, c->d_tab, (const float *)c->d_bsp,
+                                                  (const float2 *)c->d_tw, c->d_tab, c->d_etab,
                                                   (float2 *)c->d_grid, c->d_e_col);
         if (c->timing) cudaEventRecord(c->ev[8], s);
         k_plane_inv_f<<<np, 256, c->smem_plane_inv, s>>>(c->d_planes, c->d_reps, c->d_plans, c->d_rep_plan,
@@ -1166,6 +1231,15 @@ int configure_t(NbCtx *c)
     for (size_t k = 0; k < bsp.size(); ++k) bsp[k] = (T)c->bsp_h[k];
     NB_CUDA_OK(c, cudaMalloc(&c->d_bsp, sizeof(T) * bsp.size()));
     NB_CUDA_OK(c, cudaMemcpy(c->d_bsp, bsp.data(), sizeof(T) * bsp.size(), cudaMemcpyHostToDevice));
+    if (sizeof(T) == 4) {
+        std::vector<float> et(c->bsp_h.size());
+        for (int r = 0; r < c->nrep; ++r) {
+            const RepDev &R = c->rd[r];
+            nb_pme_etab(R, c->bsp_h.data() + R.bsp0, et.data() + R.bsp0);
+        }
+        NB_CUDA_OK(c, cudaMalloc(&c->d_etab, sizeof(float) * et.size()));
+        NB_CUDA_OK(c, cudaMemcpy(c->d_etab, et.data(), sizeof(float) * et.size(), cudaMemcpyHostToDevice));
+    }
     // work lists: planes (replica, z) and z columns (replica, kx, ky run)
     c->planes.clear();
     c->cols.clear();
@@ -1254,6 +1328,43 @@ int nb_pme_configure(NbCtx *c)
     return c->precision == MOIL_NB_FP64 ? configure_t<double>(c) : configure_t<float>(c);
 }
 
+void nb_spread_scale(double qfc_max, RepDev *R)
+{
+    const int k = nb_spread_exp(qfc_max);
+    R->spread_scale = (float)ldexp(1.0, k);
+    R->spread_inv = (float)ldexp(1.0, -k);
+    const double s216 = ldexp(1.0, k) / 216.0;
+    R->spread216 = (float)s216;
+    R->spread216_corr = s216 / (double)R->spread216;
+}
+
+void nb_pme_etab(const RepDev &R, const double *bsp, float *out)
+{
+    const int ns[3] = {R.n1, R.n2, R.n3};
+    for (int d = 0, o = 0; d < 3; o += ns[d], ++d)
+        for (int k = 0; k < ns[d]; ++k) {
+            // MOIL's m folding (pot/ewald_receip.f:723-812): k > ceil(n/2) - 1 -> k - n
+            const int m = k < (ns[d] + 1) / 2 ? k : k - ns[d];
+            const double mh = m * R.invLd[d];
+            out[o + k] = (float)(exp(-R.pme_fac * mh * mh) / bsp[o + k]);
+        }
+}
+
+void nb_pme_fp32_consts(RepDev *R)
+{
+    const double fac2 = R->pme_fac * 1.4426950408889634;
+    R->pme_fac2f = (float)fac2;
+    R->fac2_lo = (float)(fac2 - (double)R->pme_fac2f);
+    R->pivolf = (float)R->pivol;
+    R->pivol_corr = (double)R->pivolf / R->pivol;
+    for (int d = 0; d < 3; ++d) R->invL_lo[d] = (float)(R->invLd[d] - (double)R->invL[d]);
+    for (int d = 0; d < 3; ++d) {
+        const double c = R->invLd[d] * R->invLd[d];
+        R->msq_c[d][0] = (float)c;
+        R->msq_c[d][1] = (float)(c - (double)R->msq_c[d][0]);
+    }
+}
+
 // ---------------------------------------------------------------------------------
 // Allocation-free PME reciprocal sum (moil_nb_pme_noalloc).
 //
@@ -1291,7 +1402,8 @@ constexpr size_t NA_REPPLAN = NA_PLANS + na_up(sizeof(FftPlanDev) * 3);
 constexpr size_t NA_TW = NA_REPPLAN + na_up(sizeof(int) * 3);
 constexpr size_t NA_TAB = NA_TW + na_up(sizeof(float2) * 3 * NA_MAX_N);
 constexpr size_t NA_BSP = NA_TAB + na_up(sizeof(int2) * NA_MAX_TAB);
-constexpr size_t NA_REPS = NA_BSP + na_up(sizeof(float) * 3 * NA_MAX_N);
+constexpr size_t NA_ETAB = NA_BSP + na_up(sizeof(float) * 3 * NA_MAX_N);
+constexpr size_t NA_REPS = NA_ETAB + na_up(sizeof(float) * 3 * NA_MAX_N);
 constexpr size_t NA_EOUT = NA_REPS + na_up(sizeof(RepDev));
 constexpr size_t NA_STATUS = NA_EOUT + na_up(sizeof(double));
 constexpr size_t NA_BYTES = NA_STATUS + na_up(sizeof(int) * 8);
@@ -1325,11 +1437,13 @@ __global__ void k_na_scale(int natom, const double *__restrict__ q, RepDev *__re
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double contrib = sh[0] * reps[0].fcd * (8.0 / 27.0);
-        int k = contrib > 0 ? (int)floor(log2(2097152.0 / contrib)) : 24;
-        k = min(24, max(8, k));
+        const int k = nb_spread_exp(sh[0] * reps[0].fcd);
         reps[0].spread_scale = (float)ldexp(1.0, k);
         reps[0].spread_inv = (float)ldexp(1.0, -k);
+        const double s216 = ldexp(1.0, k) / 216.0;
+        reps[0].spread216 = (float)s216;
+        const double c = s216 / (double)reps[0].spread216;
+        reps[0].pme_qcorr = c * c;
     }
 }
 
@@ -1360,26 +1474,6 @@ __global__ void k_na_energy(int ncol, const double *__restrict__ e_col, double *
         __syncthreads();
     }
     if (threadIdx.x == 0) *out = 0.5 * sh[0];
-}
-
-// |DFT|^2 of the order-4 B-spline at w = 0 (pot/ewald_receip.f:413-481)
-void na_bsp_moduli(int n, float *mod)
-{
-    const double th[4] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 0.0};
-    std::vector<double> m(n);
-    for (int k = 0; k < n; ++k) {
-        double s1 = 0, s2 = 0;
-        for (int j = 1; j <= 4 && j < n; ++j) {
-            double arg = 2.0 * M_PI * k * j / n;
-            s1 += th[j - 1] * cos(arg);
-            s2 += th[j - 1] * sin(arg);
-        }
-        m[k] = s1 * s1 + s2 * s2;
-    }
-    for (int k = 0; k < n; ++k) {
-        if (m[k] < 1e-7) m[k] = 0.5 * (m[(k - 1 + n) % n] + m[(k + 1) % n]);
-        mod[k] = (float)m[k];
-    }
 }
 
 }  // namespace
@@ -1433,8 +1527,8 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     R.alphad = alpha;
     R.pme_fac = M_PI * M_PI / (alpha * alpha);
     R.pivol = M_PI * box[0] * box[1] * box[2];
-    R.pme_fac2f = (float)(R.pme_fac * 1.4426950408889634);
-    R.pivolf = (float)R.pivol;
+    nb_pme_fp32_consts(&R);
+    R.pme_qcorr = 1.0;    // the charges stay on the device: no rounding correction
     R.natom = natom;
     FftPlanDev plans[3];
     int rep_plan[3];
@@ -1454,9 +1548,13 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
         rep_plan[d] = d;
     }
     if ((int)tab.size() > NA_MAX_TAB) return MOIL_NB_ERR_GRID;
-    na_bsp_moduli(n1, bsp);
-    na_bsp_moduli(n2, bsp + n1);
-    na_bsp_moduli(n3, bsp + n1 + n2);
+    double bspd[3 * NA_MAX_N];
+    nb_bsp_moduli(n1, bspd);
+    nb_bsp_moduli(n2, bspd + n1);
+    nb_bsp_moduli(n3, bspd + n1 + n2);
+    for (int k = 0; k < n1 + n2 + n3; ++k) bsp[k] = (float)bspd[k];
+    float etab[3 * NA_MAX_N];
+    nb_pme_etab(R, bspd, etab);
     NbCtx tmp;
     tmp.stream = stream;
     tmp.nrep = 1;
@@ -1488,6 +1586,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     tmp.d_tw = base + NA_TW;
     tmp.d_tab = (int2 *)(base + NA_TAB);
     tmp.d_bsp = base + NA_BSP;
+    tmp.d_etab = (float *)(base + NA_ETAB);
     tmp.d_reps = (RepDev *)(base + NA_REPS);
     tmp.d_status = (int *)(base + NA_STATUS);
     double *d_eout = (double *)(base + NA_EOUT);
@@ -1500,6 +1599,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     NA_CP(tmp.d_tw, tw, sizeof(float2) * ntw);
     NA_CP(tmp.d_tab, tab.data(), sizeof(int2) * tab.size());
     NA_CP(tmp.d_bsp, bsp, sizeof(float) * (n1 + n2 + n3));
+    NA_CP(tmp.d_etab, etab, sizeof(float) * (n1 + n2 + n3));
     NA_CP(tmp.d_planes, tmp.planes.data(), sizeof(PlaneWork) * tmp.planes.size());
     NA_CP(tmp.d_cols, tmp.cols.data(), sizeof(ColWork) * tmp.cols.size());
     NA_CP(tmp.d_col_begin, col_begin, sizeof(col_begin));

@@ -72,6 +72,10 @@ __device__ __forceinline__ T atom_pair(const RepDev &R, T r2, T qi, T qj, T e12i
         eel += e;
     }
     if (lj) {
+        // r^-6 and r^-12 amplify the approximate FP32 rsqrt's error 6 and 12 times: one
+        // Newton step (FP32) first
+        const T rl = sizeof(T) == 4 ? fma((T)-0.5 * rinv, fma(r2, s2, (T)-1), rinv) : rinv;
+        s2 = rl * rl;
         T s6 = s2 * s2 * s2, A, B;
         if (!R.arith) {
             A = e12i * e12j * s6 * s6;
@@ -309,7 +313,10 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
 // one rigid water): the three intramolecular displacements come from the FP64-formed H
 // offsets h1, h2, so no absolute FP32 coordinate enters; erf(x)/x from its Taylor series in
 // u = x^2 (9 terms, truncation below 6e-9 for u <= 0.5), erff beyond.  Adds the gradient of
-// the three sites to g[3 * site + axis] and returns the energy.
+// the three sites to g[3 * site + axis] and returns the energy.  With R.wref the returned
+// energy is the difference from the replica's reference water (wcorr0, added in FP64 by the
+// energy reduction): coef * (r^2 - t0) * Q(r^2) per pair, Q the quotient of the series by
+// (r^2 - t0), which keeps the FP32 error a fraction of a small difference.
 __device__ __forceinline__ float water_intra_f(const RepDev &R, float4 h1, float4 h2, const float q[3], float g[9])
 {
     // displacement x_a - x_b for the pairs (O,H1), (O,H2), (H1,H2)
@@ -322,22 +329,32 @@ __device__ __forceinline__ float water_intra_f(const RepDev &R, float4 h1, float
         const float rx = d[k][0], ry = d[k][1], rz = d[k][2];
         const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz)), u = al * al * r2;
         const float qq = q[pa[k]] * q[pb[k]] * ke;
-        float e, df;
+        float e = 0.f, df;
         if (u <= 0.5f) {
-            float s = 1.f / 685440.f, ds = 8.f / 685440.f;
-            s = fmaf(s, u, -1.f / 75600.f); s = fmaf(s, u, 1.f / 9360.f); s = fmaf(s, u, -1.f / 1320.f);
-            s = fmaf(s, u, 1.f / 216.f); s = fmaf(s, u, -1.f / 42.f); s = fmaf(s, u, 0.1f);
-            s = fmaf(s, u, -1.f / 3.f); s = fmaf(s, u, 1.f);
+            float ds = 8.f / 685440.f;
             ds = fmaf(ds, u, -7.f / 75600.f); ds = fmaf(ds, u, 6.f / 9360.f); ds = fmaf(ds, u, -5.f / 1320.f);
             ds = fmaf(ds, u, 4.f / 216.f); ds = fmaf(ds, u, -3.f / 42.f); ds = fmaf(ds, u, 0.2f);
             ds = fmaf(ds, u, -1.f / 3.f);
-            e = -qq * al * c2 * s;
+            if (!R.wref) {
+                float s = 1.f / 685440.f;
+                s = fmaf(s, u, -1.f / 75600.f); s = fmaf(s, u, 1.f / 9360.f); s = fmaf(s, u, -1.f / 1320.f);
+                s = fmaf(s, u, 1.f / 216.f); s = fmaf(s, u, -1.f / 42.f); s = fmaf(s, u, 0.1f);
+                s = fmaf(s, u, -1.f / 3.f); s = fmaf(s, u, 1.f);
+                e = -qq * al * c2 * s;
+            }
             df = -qq * 2.f * al * al * al * c2 * ds;
         } else {
             const float rij = sqrtf(r2), sinv = 1.f / rij, x = al * rij;
             const float erfv = erff(x), derfc = c2 * expf(-x * x);
-            e = -qq * sinv * erfv;
+            if (!R.wref) e = -qq * sinv * erfv;
             df = qq * sinv * (sinv * sinv * erfv - sinv * al * derfc);
+        }
+        if (R.wref) {
+            const int ty = k == 2 ? 1 : 0;    // O-H, O-H, H-H
+            float qv = R.wq[ty][7];
+#pragma unroll
+            for (int m = 6; m >= 0; --m) qv = fmaf(qv, r2, R.wq[ty][m]);
+            e = R.wcoef[ty] * ((r2 - R.wt0[ty]) * qv);
         }
         ecorr += e;
         const int a = pa[k], b = pb[k];
@@ -421,6 +438,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     const float rmax2 = R.rmax2, rv2 = R.rv2;
     const float2 palpha = f2(ERFCX_P * R.alpha), ex2c = f2(R.ex2c);
     const float2 w12 = f2(R.w12), nw6 = f2(-R.w6);
+    const float2 c12 = f2(R.w12c), c6 = f2(R.w6c);
     const float qqv[3] = {R.qq[0], R.qq[1], R.qq[2]};
     const float c2a = R.c2a;
     const W1Row<E> L1(wl1_cnt, wl1, cap_row, i, R.wat0);
@@ -497,11 +515,19 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
                     // minus dE/dr / r
                     float2 mdf = __fmul2_rn(__ffma2_rn(f2(qq * c2a), ex, e), s2);
                     if (a == 0 && b == 0) {
-                        const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+                        // LJ powers from a Newton-refined 1/r (r^-12 amplifies rsqrt's error 12 times)
+                        // rinv - rinv (r^2 rinv^2 - 1) / 2: the correction is formed as a small
+                        // number, so the result keeps round-to-nearest's lack of bias
+                        const float2 ri = __ffma2_rn(__fmul2_rn(f2(-0.5f), rinv), __ffma2_rn(rr2, s2, f2(-1.f)), rinv);
+                        const float2 sl = __fmul2_rn(ri, ri);
+                        const float2 s6 = __fmul2_rn(__fmul2_rn(sl, sl), sl);
                         const float2 A = __fmul2_rn(__fmul2_rn(w12, s6), s6);
-                        float2 e1 = __ffma2_rn(nw6, s6, A);   // A - B
-                        // -df1 = 6 s2 (A + e1)
-                        float2 m1 = __fmul2_rn(__fmul2_rn(f2(6.f), s2), __fadd2_rn(A, e1));
+                        // energy A (1 + c12) - B (1 + c6): c12, c6 restore the FP32 rounding of the
+                        // coefficients, whose relative error would otherwise bias every pair alike
+                        // (the force keeps A and B)
+                        float2 e1 = __ffma2_rn(nw6, __ffma2_rn(s6, c6, s6), __ffma2_rn(A, c12, A));
+                        // -df1 = 6 s2 (2A - B)
+                        float2 m1 = __fmul2_rn(__fmul2_rn(f2(6.f), sl), __ffma2_rn(nw6, s6, __fadd2_rn(A, A)));
                         if (R.lj_switch) {
                             float d0 = -m1.x, d1 = -m1.y;
                             lj_switch_apply<float>(R, rr2.x, e1.x, d0);
@@ -848,7 +874,9 @@ __global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const Re
         const double elp = 0.5 * (pw[0] + po[0]), eli = 0.5 * (pw[1] + po[1]);
         const double eep = 0.5 * (pw[2] + po[2]), eei = 0.5 * (pw[3] + po[3]);
         const double npairs = 0.5 * (pw[4] + po[4]);
-        const double ecorr = px[0] + pw[5] + po[5], eel14 = px[1], evdw14 = px[2];
+        // waters relative to the reference water (k_wref) add their reference energy here
+        const double ecorr = px[0] + pw[5] + po[5] + (R.wref ? (double)R.nwat * R.wcorr0 : 0.0);
+        const double eel14 = px[1], evdw14 = px[2];
         const double erec = 0.5 * part[2 * NB_EU + NB_EX];
         double *o = e_rep + NB_EREP * (size_t)r;
         o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym

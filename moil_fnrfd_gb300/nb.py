@@ -148,12 +148,19 @@ class _Keep:
         return a.ctypes.data_as(_ip)
 
 
-def make_params(s, precision=MOIL_NB_MIXED, skin=1.0, list_period=0, lj_switch=False, alpha=None) -> Params:
+def make_params(s, precision=MOIL_NB_MIXED, skin=1.0, list_period=0, lj_switch=False, alpha=None,
+                dtol=None) -> Params:
+    """moil_nb_params of system s.  dtol (> 0) selects MOIL's route to the Ewald coefficient,
+    alpha from erfc(alpha relx) / relx = dtol by bisection (symm/ewald_init.f:298-335);
+    otherwise alpha (default s.alpha) is passed as is."""
     p = Params()
     p.rvmx, p.relx, p.eps = float(s.rvmx), float(s.relx), float(s.eps)
     p.a, p.b, p.c = (float(x) for x in s.box)
-    p.dtol = 0.0
-    p.alpha = float(s.alpha if alpha is None else alpha)
+    if dtol is not None:
+        p.dtol, p.alpha = float(dtol), 0.0
+    else:
+        p.dtol = 0.0
+        p.alpha = float(s.alpha if alpha is None else alpha)
     p.nfft1, p.nfft2, p.nfft3 = (int(x) for x in s.nfft)
     p.order = int(s.order)
     p.arith, p.hvdw0 = int(s.arith), int(s.hvdw0)
@@ -182,7 +189,7 @@ class Nonbonded:
     """One device handle over one system or a batch of independent replicas."""
 
     def __init__(self, systems, precision=MOIL_NB_MIXED, device=0, skin=1.0, list_period=0,
-                 lj_switch=False, timing=False, groups=0):
+                 lj_switch=False, timing=False, groups=0, dtol=None):
         self.L = load()
         h = ctypes.c_void_p()
         _check(self.L, None, self.L.moil_nb_create(ctypes.byref(h), int(device)))
@@ -191,7 +198,7 @@ class Nonbonded:
         self.batch = isinstance(systems, (list, tuple))
         self.systems = list(systems) if self.batch else [systems]
         keep = _Keep()
-        self._params = [make_params(s, precision, skin, list_period, lj_switch) for s in self.systems]
+        self._params = [make_params(s, precision, skin, list_period, lj_switch, dtol=dtol) for s in self.systems]
         self._topos = [make_topology(s, keep) for s in self.systems]
         reps = (Replica * len(self.systems))()
         for k in range(len(self.systems)):

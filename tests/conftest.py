@@ -38,3 +38,16 @@ ENERGY_TERMS = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_el14", "e_vdw14", "e_cor
 def energy_scale(e):
     """Sum of the magnitudes of the nonbonded energy terms."""
     return sum(abs(e[k]) for k in ENERGY_TERMS)
+
+
+def energy_report(e, eref):
+    """Energy errors against the oracle: each term's error relative to its own size (None
+    for a term the oracle gives as exactly zero) and |dE_total| / |E_total|."""
+    terms = {k: (abs(e[k] - eref[k]) / abs(eref[k]) if eref[k] != 0 else None) for k in ENERGY_TERMS}
+    total = abs(e["e_total"] - eref["e_total"]) / abs(eref["e_total"])
+    return terms, total
+
+
+def format_energy_report(terms, total):
+    parts = " ".join(f"{k[2:]} {v:.1e}" for k, v in terms.items() if v is not None)
+    return f"|dE_total|/|E_total| {total:.2e}; per term (relative to the term): {parts}"

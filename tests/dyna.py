@@ -26,7 +26,7 @@ import math
 
 import numpy as np
 
-from .systems import MON_WATER, TIP3_HOH_DEG, TIP3_ROH
+from moil_fnrfd_gb300.systems import MON_WATER, TIP3_HOH_DEG, TIP3_ROH
 
 ACCEL = 418.4                 # (kcal/mol/Å) / amu in Å/ps^2
 MASS_O, MASS_H = 15.9994, 1.008
