@@ -564,7 +564,8 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     // B-spline moduli factor per dimension, so they come from a per-dimension table
     // etab[k] = exp(-pi^2 m_k^2 / (alpha^2 L^2)) / B(k) formed in FP64 (no approximate
     // exponential in the energy); m^2 = sum_d k_d^2 / L_d^2 from exact integer squares and
-    // 1/L_d^2 as hi + lo, and one correctly rounded division
+    // 1/L_d^2 as hi + lo, and the reciprocal of pi V m^2 to within an ulp (one Newton step on
+    // the approximate reciprocal, its residual formed exactly by an FMA)
     const float pivol = R.pivolf;
     const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
     const float m1s = (float)(w.kx * w.kx), t1 = etab[w.kx];
@@ -580,9 +581,10 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
             const int m3 = kz < nf3 ? kz : kz - n3;
             const float m3s = (float)(m3 * m3);
             const float msq = fmaf(m3s, c2h, fmaf(m3s, c2l, m12));
-            float et = (w.kx == 0 && ky == 0 && kz == 0)
-                           ? 0.f
-                           : __fdiv_rn(t12 * etab[n1 + n2 + kz], pivol * msq);
+            const float den = pivol * msq;
+            float rd = nb_rcp_approx(den);
+            rd = fmaf(rd, fmaf(-den, rd, 1.f), rd);
+            const float et = (w.kx == 0 && ky == 0 && kz == 0) ? 0.f : (t12 * etab[n1 + n2 + kz]) * rd;
             float2 v = F[c * n3 + kz];
             en += wgt * et * (v.x * v.x + v.y * v.y);
             F[c * n3 + kz] = make_float2(v.x * et, -v.y * et);    // conj: the inverse runs forward
