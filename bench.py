@@ -19,6 +19,8 @@ pressure_analysis: MOIL's pressure-analysis terms (molecular virial tensor, moil
              the whole batch, host buffers, wall clock per call (one evaluation + the pass)
 single_system_md: one 96,000-atom water box through a 1,000-step rigid-water trajectory on the
              device (lists every 10 steps, 1.5 Å skin), whole steps timed, the FP64 path beside it
+adjoint_64 : dE/dq, dE/deps, dE/dsigma per atom (moil_nb_adjoint) for 64 perturbed copies of the
+             23,558-atom solute system in one batch, wall clock per call, the evaluation beside it
 """
 from __future__ import annotations
 
@@ -235,6 +237,46 @@ def press_leg(nb, reps, coor, e2e_ms, calls=3):
             "calls": calls, "sample": "the timed batch, molecules = waters, no gradient copy"}
 
 
+def adjoint_leg(local, calls=5):
+    """Parameter derivatives (moil_nb_adjoint) of the sensitivity workload: 64 seeded +-1%
+    perturbed copies of the 23,558-atom solute system in one batch.  One call is an evaluation
+    (lists, positions, the PME grid recomputed) plus the adjoint kernels, pinned host
+    coordinates in and the three per-atom derivative arrays out, wall clock (median of
+    `calls`); moil_nb_eval of the same batch and buffers beside it."""
+    import torch
+    from moil_fnrfd_gb300 import systems as S
+    from moil_fnrfd_gb300.nb import Nonbonded
+    t0 = time.perf_counter()
+    copies = S.perturbed_copies(S.config1(), 64)
+    nb = Nonbonded(copies, device=local, skin=SKIN, list_period=LIST_PERIOD)
+    natoms = sum(s.npt for s in copies)
+    log(f"adjoint workload: {len(copies)} copies, {natoms} atoms, set up in {time.perf_counter() - t0:.1f} s")
+    hc = torch.from_numpy(np.ascontiguousarray(np.concatenate([s.coor for s in copies]))).pin_memory().numpy()
+    hd = torch.empty((natoms, 3), dtype=torch.float64).pin_memory().numpy()
+    outs = [torch.empty(natoms, dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        t = []
+        for _ in range(calls):
+            t1 = time.perf_counter()
+            fn()
+            t.append((time.perf_counter() - t1) * 1e3)
+        return statistics.median(t)
+
+    adj_ms = timed(lambda: nb.adjoint_into(hc, *outs))
+    eval_ms = timed(lambda: nb.eforce_into(hc, hd, want_energies=False))
+    groups = nb.groups()
+    nb.close()
+    return {"workload": f"{len(copies)} perturbed copies (eps, sigma per LJ type and solute charges, +-1%) "
+                        f"of the {copies[0].npt}-atom solute system, {natoms} atoms",
+            "value": natoms / (adj_ms / 1e3), "unit": "atom-evals/s (dE/dq, dE/deps, dE/dsigma per atom)",
+            "ms_per_call": adj_ms, "eval_ms": eval_ms, "cost_vs_eval": adj_ms / eval_ms, "calls": calls,
+            "replica_groups": groups,
+            "timing": "wall clock per call, pinned host buffers: H2D coordinates, D2H three derivative arrays"}
+
+
 def accuracy_leg(nb, reps, d_coor, d_dpot, n_sample=6):
     """One batched evaluation of the timed coordinates; for n_sample replicas spread over the
     batch, each energy term's error relative to the term, |dE_total| / |E_total| and the
@@ -364,6 +406,11 @@ def main():
     ap.add_argument("--no-press", action="store_true", help="skip the pressure-analysis leg")
     ap.add_argument("--groups", type=int, default=0,
                     help="replica groups evaluated concurrently (0: the library's automatic choice)")
+    ap.add_argument("--water-kernel", default="auto", choices=["auto", "full", "half"],
+                    help="water-water kernel shape (moil_nb_set_shape; auto: the library's choice)")
+    ap.add_argument("--half-block", type=int, default=0, choices=[0, 128, 256],
+                    help="waters per block of the half-list water kernel (0: the library's default)")
+    ap.add_argument("--no-adj", action="store_true", help="skip the parameter-derivative (adjoint) leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -384,8 +431,9 @@ def main():
     reps = build_workload(rank, args.replicas)
     natoms = sum(s.npt for s in reps)
     log(f"workload: {len(reps)} replicas, {natoms} atoms, generated in {time.perf_counter() - t0:.1f} s")
+    shape = {"water_kernel": {"auto": 0, "full": 1, "half": 2}[args.water_kernel], "half_block": args.half_block}
     nb = Nonbonded(reps, precision=MOIL_NB_MIXED, device=local, skin=SKIN, list_period=LIST_PERIOD,
-                   groups=args.groups)
+                   groups=args.groups, shape=shape)
     stream = torch.cuda.ExternalStream(nb.stream())
     coor = np.ascontiguousarray(np.concatenate([s.coor for s in reps]), dtype=np.float64)
     d_coor = torch.from_numpy(coor).to(f"cuda:{local}")
@@ -488,7 +536,7 @@ def main():
            "config": {"workload": "512 batched uneven TIP3P boxes (config 3 shape): 1500-12000 atoms each, "
                                   "rc 9 Å, alpha 0.35, PME order 4 on 2/3/5-smooth grids >= 1 pt/Å",
                       "replicas": len(reps), "atoms": natoms, "list_period": LIST_PERIOD, "skin": SKIN,
-                      "replica_groups": nb.groups(),
+                      "replica_groups": nb.groups(), "shape": nb.shape(),
                       "l2": "256 MB buffer written between timed steps (untimed)",
                       "precision": "FP32 pair/spline/FFT math, int64 fixed-point forces, FP64 energies and corrections"},
            "stage_ms": {k: round(v, 4) for k, v in avg.items()},
@@ -544,6 +592,9 @@ def main():
     nb.close()
     if press is not None:
         out["pressure_analysis"] = press
+
+    if not args.no_adj and rank == 0:
+        out["adjoint_64"] = adjoint_leg(local)
 
     if not args.no_md and rank == 0:
         out["single_system_md"] = md_leg(local)

@@ -239,6 +239,34 @@ int moil_nb_set_virial(moil_nb_ctx *h, int on);
 int moil_nb_set_groups(moil_nb_ctx *h, int groups);
 int moil_nb_groups(const moil_nb_ctx *h);
 
+/* Kernel and list shapes of a handle: the search space of the autotuner
+ * (moil_fnrfd_gb300/tune.py).  No counterpart in the reference, whose list scheme is fixed
+ * (pot/nbondm.f:143-210, pot/nbond.f:54-157).  Every shape gives the same pair set and
+ * results within the mixed path's tolerances; each is deterministic run to run. */
+enum {
+    MOIL_NB_WATER_AUTO = 0,       /* half lists where they apply, else full lists */
+    MOIL_NB_WATER_FULL = 1,       /* one water per thread over its full row (both directions) */
+    MOIL_NB_WATER_HALF = 2        /* each water pair once; the partner's share summed per block in
+                                     shared memory (mixed path, replicas below 65,536 waters) */
+};
+enum {
+    MOIL_NB_TILED_AUTO = 0,       /* all-pairs tiles where the 27-cell stencil covers >= 40% of a box */
+    MOIL_NB_TILED_OFF = 1,        /* cell search for every replica */
+    MOIL_NB_TILED_ALL = 2         /* all-pairs tiles for every replica of at most 16,384 waters */
+};
+typedef struct {
+    int water_kernel;             /* MOIL_NB_WATER_* */
+    int half_block;               /* waters per block of the half-list kernel: 128 or 256 (0: 256) */
+    int tiled;                    /* MOIL_NB_TILED_*: how the water-water rows are built */
+    int groups;                   /* replica groups, as moil_nb_set_groups (next moil_nb_init_batch) */
+} moil_nb_shape;
+
+/* Set the shapes.  water_kernel, half_block and tiled apply to the current handle at once
+ * (the lists are rebuilt at the next evaluation); groups applies at the next init.
+ * moil_nb_get_shape returns the shapes in use, automatic choices resolved. */
+int moil_nb_set_shape(moil_nb_ctx *h, const moil_nb_shape *s);
+int moil_nb_get_shape(const moil_nb_ctx *h, moil_nb_shape *s);
+
 /* ---- PME reciprocal sum without device allocation -------------------------
  * No counterpart in the reference (MOIL's ewald_receip() works on static COMMON
  * arrays and never allocates).  This entry point is for callers that cannot call

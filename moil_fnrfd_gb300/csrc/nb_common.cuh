@@ -242,6 +242,19 @@ __device__ __forceinline__ double nb_fix2d(long long x)
 __device__ __forceinline__ long long nb_fix(float v) { return __float2ll_rn(v * NB_FIX_SCALE_F); }
 __device__ __forceinline__ long long nb_fix(double v) { return __double2ll_rn(v * NB_FIX_SCALE); }
 
+// Owner of the water pair (a, b) in the half lists (indices relative to the replica's first
+// water): the lower index when a + b is odd, the higher one when it is even.  Each water owns
+// about half of its partners whatever its position in the sorted order.
+__host__ __device__ __forceinline__ int nb_half_owner(int a, int b)
+{
+    return ((a ^ b) & 1) ? min(a, b) : max(a, b);
+}
+
+// Half-list water kernel: j-side gradients are summed per block in int32 at 2^(24 - log2 HB)
+// units per kcal/mol/Å, so HB contributions of magnitude below NB_HALF_CAP cannot overflow;
+// a larger contribution goes straight to the int64 site gradient
+#define NB_HALF_CAP 127.0f
+
 // bounded-status helpers
 #define NB_DEV_ERR_OVERFLOW 1
 #define NB_DEV_ERR_NAN 2

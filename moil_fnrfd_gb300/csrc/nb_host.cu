@@ -87,6 +87,9 @@ void release_device(NbCtx *c)
     free_ptr(c->d_p14_j); free_ptr(c->d_p14_par); free_ptr(c->d_grad_site); free_ptr(c->d_e_unit);
     free_ptr(c->d_grad_ex); free_ptr(c->d_e_ex); free_ptr(c->d_plans); free_ptr(c->d_rep_plan); free_ptr(c->d_tw);
     free_ptr(c->d_tab); free_ptr(c->d_wtiles); free_ptr(c->d_scan_tmp);
+    free_ptr(c->d_hblocks); free_ptr(c->d_hrow); free_ptr(c->d_hcnt); free_ptr(c->d_jset); free_ptr(c->d_jn);
+    c->hblocks.clear();
+    c->whalf = 0;
     free_ptr(c->d_bsp); free_ptr(c->d_etab); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
@@ -156,6 +159,78 @@ template <typename V> int upload(NbCtx *c, V *&dst, const std::vector<V> &src)
         if (rc_ != MOIL_NB_OK) return rc_; \
     } while (0)
 
+// Water-water rows by all-pairs tiles (k_wlist_tiled) or by cell search (k_wlist).  By
+// default the tiles take replicas where the 27-cell stencil already covers at least 40% of
+// the box (2-4 cells per side); moil_nb_set_shape can switch them off or on everywhere.
+int tiled_choice(const NbCtx *c, const RepDev &R)
+{
+    if (R.nwat <= 0 || R.nwat > 16384 || c->want_tiled == MOIL_NB_TILED_OFF) return 0;
+    if (c->want_tiled == MOIL_NB_TILED_ALL) return 1;
+    double frac = 1.0;
+    for (int d = 0; d < 3; ++d) frac *= (double)std::min(R.nc[d], 3) / R.nc[d];
+    return frac >= 0.4 ? 1 : 0;
+}
+
+// the tile work list of the replicas built by tiles (NB_WTILE waters per block)
+int setup_tiles(NbCtx *c)
+{
+    free_ptr(c->d_wtiles);
+    c->wtiles.clear();
+    for (int r = 0; r < c->nrep; ++r) {
+        const RepDev &R = c->rd[r];
+        if (!R.wtiled) continue;
+        for (int i0 = 0; i0 < R.nwat; i0 += NB_WTILE) c->wtiles.push_back(make_int2(r, R.wat0 + i0));
+    }
+    if (!c->wtiles.empty()) NB_TRY(upload(c, c->d_wtiles, c->wtiles));
+    return MOIL_NB_OK;
+}
+
+// Half water rows and j-sets at the current capacities.  When the j-set of the largest
+// block no longer fits the device's shared memory, the handle goes back to full lists.
+int alloc_half(NbCtx *c)
+{
+    free_ptr(c->d_hrow);
+    free_ptr(c->d_jset);
+    if (!c->whalf) return MOIL_NB_OK;
+    if (nb_half_configure(c) != MOIL_NB_OK) {
+        c->whalf = 0;
+        c->need_rebuild = 1;
+        return MOIL_NB_OK;
+    }
+    const int64_t nb = (int64_t)c->hblocks.size();
+    NB_CUDA_OK(c, cudaMalloc(&c->d_hrow, sizeof(unsigned) * std::max<int64_t>(nb * c->hb * c->caph, 1)));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_jset, sizeof(int) * std::max<int64_t>(nb * c->jcap, 1)));
+    return MOIL_NB_OK;
+}
+
+// Half-list set-up for the current shape: on for FP32 handles whose replicas all have fewer
+// than 65,536 waters (16-bit rows) unless full lists were asked for; blocks of hb waters
+// never straddle replicas.  Capacities start from the full rows and the replica sizes and
+// are regrown from the build's maxima.
+int setup_half(NbCtx *c)
+{
+    free_ptr(c->d_hblocks); free_ptr(c->d_hcnt); free_ptr(c->d_jn);
+    free_ptr(c->d_hrow); free_ptr(c->d_jset);
+    c->hblocks.clear();
+    c->whalf = c->precision != MOIL_NB_FP64 && c->row16 && c->nW > 0 && c->want_whalf != MOIL_NB_WATER_FULL;
+    if (!c->whalf) return MOIL_NB_OK;
+    int maxw = 0;
+    for (int r = 0; r < c->nrep; ++r) {
+        const RepDev &R = c->rd[r];
+        maxw = std::max(maxw, R.nwat);
+        for (int i0 = 0; i0 < R.nwat; i0 += c->hb) c->hblocks.push_back(make_int2(r, R.wat0 + i0));
+    }
+    NB_TRY(upload(c, c->d_hblocks, c->hblocks));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_hcnt, sizeof(int2) * c->nW));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_jn, sizeof(int) * c->hblocks.size()));
+    NB_CUDA_OK(c, cudaMemset(c->d_hcnt, 0, sizeof(int2) * c->nW));
+    NB_CUDA_OK(c, cudaMemset(c->d_jn, 0, sizeof(int) * c->hblocks.size()));
+    c->caph = ((c->cap_row1 * 5 / 8 + 32) + 31) & ~31;
+    c->jcap = std::min(maxw, 7 * c->hb);
+    c->need_rebuild = 1;
+    return alloc_half(c);
+}
+
 int alloc_lists(NbCtx *c)
 {
     free_ptr(c->d_wl1);
@@ -166,7 +241,7 @@ int alloc_lists(NbCtx *c)
     NB_CUDA_OK(c, cudaMalloc(&c->d_wl2, sizeof(int) * std::max<int64_t>(c->cap_wl2, 1)));
     NB_CUDA_OK(c, cudaMalloc(&c->d_xl, sizeof(int) * std::max<int64_t>(c->cap_xl, 1)));
     c->list_gen++;   // a captured evaluation graph refers to the old buffers
-    return MOIL_NB_OK;
+    return alloc_half(c);
 }
 
 int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
@@ -367,13 +442,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         }
         R.nwat = nwat; R.noth = noth;
         wat0 += nwat; oth0 += noth;
-        // water-water list by tiled all-pairs when the 27-cell stencil already covers at
-        // least 40% of the box (small replicas: 2-4 cells per side)
-        {
-            double frac = 1.0;
-            for (int d = 0; d < 3; ++d) frac *= (double)std::min(R.nc[d], 3) / R.nc[d];
-            R.wtiled = (nwat > 0 && nwat <= 16384 && frac >= 0.4) ? 1 : 0;
-        }
+        R.wtiled = tiled_choice(c, R);
         for (int i = 0; i < t->npt; ++i) {
             q.push_back(t->ptchg[i]);
             lj_e12.push_back(t->epsgm12[i]);
@@ -459,13 +528,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
         NB_TRY(upload(c, c->d_p14_par, pp));
     }
     NB_TRY(upload(c, c->d_reps, c->rd));
-    c->wtiles.clear();
-    for (int r = 0; r < nrep; ++r) {
-        const RepDev &R = c->rd[r];
-        if (!R.wtiled) continue;
-        for (int i0 = 0; i0 < R.nwat; i0 += NB_WTILE) c->wtiles.push_back(make_int2(r, R.wat0 + i0));
-    }
-    if (!c->wtiles.empty()) NB_TRY(upload(c, c->d_wtiles, c->wtiles));
+    NB_TRY(setup_tiles(c));
     const size_t ts = c->precision == MOIL_NB_FP64 ? 8 : 4;
     int64_t nu = c->nunit, ns = c->nsite;
     NB_CUDA_OK(c, cudaMalloc(&c->d_unit_key, sizeof(int) * nu));
@@ -519,6 +582,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     }
     c->cap_row1 = ((int)row1 + 31) & ~31;
     NB_TRY(alloc_lists(c));
+    NB_TRY(setup_half(c));
     NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * NB_EREP * nrep));
     memset(c->h_e_rep, 0, sizeof(double) * NB_EREP * nrep);
     NB_TRY(nb_pme_configure(c));
@@ -698,6 +762,11 @@ int eval_retry(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e,
         c->cap_row1 = std::max<int>(c->cap_row1, (int)((need1 + need1 / 8 + 32 + 31) & ~31));
         c->cap_wl2 = std::max<int64_t>(c->cap_wl2, need2 + need2 / 8 + 64);
         c->cap_xl = std::max<int64_t>(c->cap_xl, need3 + need3 / 8 + 64);
+        if (c->whalf) {
+            const int64_t needj = c->h_status[5], needh = c->h_status[7];
+            c->caph = std::max<int>(c->caph, (int)((needh + needh / 8 + 32 + 31) & ~31));
+            c->jcap = std::max<int>(c->jcap, (int)std::min<int64_t>(needj + needj / 16 + 64, 65535));
+        }
         int a = alloc_lists(c);
         if (a != MOIL_NB_OK) return a;
         c->need_rebuild = 1;
@@ -858,6 +927,9 @@ int init_groups(moil_nb_ctx *h, int nrep, const moil_replica *reps, int P)
         c->use_graph = h->use_graph;
         c->virial = h->virial;
         c->timing = h->timing;
+        c->want_whalf = h->want_whalf;
+        c->hb = h->hb;
+        c->want_tiled = h->want_tiled;
         {
             // streams for host-buffer evaluations: earlier groups at higher priority finish
             // first, so their gradient copies overlap the later groups' kernels (device-
@@ -1251,6 +1323,51 @@ int moil_nb_set_groups(moil_nb_ctx *h, int groups)
 int moil_nb_groups(const moil_nb_ctx *h)
 {
     return h ? std::max<int>(1, (int)h->grp.size()) : 0;
+}
+
+int moil_nb_set_shape(moil_nb_ctx *h, const moil_nb_shape *sp)
+{
+    if (!h || !sp) return MOIL_NB_ERR_ARG;
+    if (sp->water_kernel < MOIL_NB_WATER_AUTO || sp->water_kernel > MOIL_NB_WATER_HALF ||
+        (sp->half_block != 0 && sp->half_block != 128 && sp->half_block != 256) ||
+        sp->tiled < MOIL_NB_TILED_AUTO || sp->tiled > MOIL_NB_TILED_ALL || sp->groups < 0) {
+        h->err = "moil_nb_set_shape: a field out of range";
+        return MOIL_NB_ERR_ARG;
+    }
+    cudaSetDevice(h->device);
+    h->want_groups = sp->groups;
+    auto apply = [&](NbCtx *c) -> int {
+        c->want_whalf = sp->water_kernel;
+        c->hb = sp->half_block ? sp->half_block : 256;
+        c->want_tiled = sp->tiled;
+        if (!c->inited || !c->grp.empty()) return MOIL_NB_OK;   // a group parent holds no lists
+        NB_CUDA_OK(c, cudaStreamSynchronize(c->stream));
+        drop_graph(c);
+        for (int r = 0; r < c->nrep; ++r) c->rd[r].wtiled = tiled_choice(c, c->rd[r]);
+        NB_CUDA_OK(c, cudaMemcpy(c->d_reps, c->rd.data(), sizeof(RepDev) * c->nrep, cudaMemcpyHostToDevice));
+        NB_TRY(setup_tiles(c));
+        NB_TRY(setup_half(c));
+        c->list_gen++;
+        c->need_rebuild = 1;
+        return MOIL_NB_OK;
+    };
+    NB_TRY(apply(h));
+    for (NbCtx *c : h->grp) {
+        const int rc = apply(c);
+        if (rc != MOIL_NB_OK) { h->err = c->err; return rc; }
+    }
+    return MOIL_NB_OK;
+}
+
+int moil_nb_get_shape(const moil_nb_ctx *h, moil_nb_shape *sp)
+{
+    if (!h || !sp) return MOIL_NB_ERR_ARG;
+    const NbCtx *c = h->grp.empty() ? h : h->grp[0];
+    sp->water_kernel = c->inited ? ((c->whalf && !c->virial) ? MOIL_NB_WATER_HALF : MOIL_NB_WATER_FULL) : c->want_whalf;
+    sp->half_block = c->hb;
+    sp->tiled = c->want_tiled;
+    sp->groups = h->inited ? moil_nb_groups(h) : h->want_groups;
+    return MOIL_NB_OK;
 }
 
 // ---- Fortran entry points --------------------------------------------------------

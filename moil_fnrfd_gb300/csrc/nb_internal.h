@@ -91,6 +91,18 @@ struct NbCtx {
     long long *d_scan_tmp = nullptr;   // tile sums of the three-phase scan
     std::vector<int2> wtiles;     // (replica, first sorted water) of each tiled water-list block
     int2 *d_wtiles = nullptr;
+    // half water rows (FP32 path with 16-bit rows: k_whalf builds them, k_water_h reads them)
+    int whalf = 0;                // the half-list water kernel is in use
+    int want_whalf = 0;           // MOIL_NB_WATER_*: 0 automatic, 1 full lists, 2 half lists
+    int hb = 256;                 // waters per half-list block (128 or 256)
+    int want_tiled = 0;           // MOIL_NB_TILED_*
+    std::vector<int2> hblocks;    // (replica, first sorted water) of each half-list block
+    int2 *d_hblocks = nullptr;
+    unsigned *d_hrow = nullptr;   // caph entries per lane, entry k of lane t at k * hb + t per block
+    int2 *d_hcnt = nullptr;       // per water: owned in-cutoff entries, owned entries
+    int *d_jset = nullptr;        // per block: jcap sorted water indices (the block's partners)
+    int *d_jn = nullptr;          // per block: j-set size
+    int caph = 0, jcap = 0;
 
     // exclusion / 1-4 lists per caller atom (both directions)
     int *d_ex_off = nullptr, *d_ex_j = nullptr;
@@ -152,7 +164,8 @@ struct NbCtx {
     double *d_press_out = nullptr;     // 12 per replica
 
     // device status: [0] rebuild flag, [1] error bits, [2..4] W1 / W2 / X entry totals,
-    // [6] longest W1 row; all reset at the start of every evaluation
+    // [5] largest half-list j-set, [6] longest W1 row, [7] longest half row; all reset at the
+    // start of every evaluation
     int *d_status = nullptr;
     int *h_status = nullptr;           // pinned: [0..7] mirror, [8..9] initial words of an evaluation
     int need_rebuild = 1;
@@ -194,6 +207,8 @@ void nb_launch_prepare(NbCtx *c, const double *d_coor, int check);
 void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_total);
 // real space + corrections (nb_realspace.cu)
 void nb_launch_realspace(NbCtx *c);
+// half-list water kernel: dynamic shared memory for c->jcap; MOIL_NB_OK if it fits the device
+int nb_half_configure(NbCtx *c);
 void nb_launch_excl14(NbCtx *c, const double *d_coor);
 // PME (nb_pme.cu)
 void nb_launch_pme(NbCtx *c);

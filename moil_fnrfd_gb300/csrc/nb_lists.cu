@@ -492,6 +492,105 @@ __global__ void __launch_bounds__(NB_WTILE) k_wlist_tiled(int ntile, const int2 
         wlist_tile<T, E>(work[b], sj, sbb, reps, pos_v, wcnt, l1, cap_row, st);
 }
 
+// 4c. Half water rows for the FP32 half-list water kernel (k_water_h).  Every water-water
+// pair of the full W1 rows is kept once, under its owner (nb_half_owner: an index-parity
+// rule that gives every water about half of its partners, so lanes stay balanced).  One
+// block = HB consecutive sorted waters of one replica (the k_water_h block); its j-set is
+// the sorted set of partners its rows own, found with a bitmap over the replica's waters
+// and a block scan of the word popcounts.  Row entry k of lane t sits at k * HB + t (the
+// kernel's loads coalesce) and packs (j-set index << 16) | (j's offset from the replica's
+// first water); owned in-cutoff partners first, as in the full row.  The block's longest
+// row and its j-set size go to st[7] and st[5] (capacity regrowth).
+#define NB_HB_WORDS 2048     // bitmap words: replicas of up to 65,536 waters (16-bit rows)
+template <int HB>
+__global__ void __launch_bounds__(HB) k_whalf(int nblk, const int2 *__restrict__ blocks,
+                                              const RepDev *__restrict__ reps, const int2 *__restrict__ wcnt,
+                                              const unsigned short *__restrict__ wl1, int cap_row,
+                                              unsigned *__restrict__ hrow, int caph, int2 *__restrict__ hcnt,
+                                              int *__restrict__ jset, int *__restrict__ jn, int jcap, int *st)
+{
+    if (rebuild_off(st)) return;
+    __shared__ unsigned bits[NB_HB_WORDS];
+    __shared__ int pre[NB_HB_WORDS];
+    __shared__ int wsum[HB / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int b = blockIdx.x; b < nblk; b += gridDim.x) {
+        const int2 w = blocks[b];
+        const RepDev &R = reps[w.x];
+        const int nwords = (R.nwat + 31) >> 5;
+        __syncthreads();    // the previous block's bitmap and prefix are no longer read
+        for (int k = t; k < nwords; k += HB) bits[k] = 0u;
+        __syncthreads();
+        const int i = w.y + t, il = i - R.wat0;
+        const bool act = il < R.nwat;
+        const int2 c = act ? wcnt[i] : make_int2(0, 0);
+        // an overflowed row is read within its capacity (the evaluation is redone)
+        const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
+        const unsigned short *row = wl1 + (size_t)i * cap_row;
+        for (int v = 0; v < n; ++v) {
+            const int jl = row[v < nn ? v : cap_row - 1 - (v - nn)];
+            if (nb_half_owner(il, jl) == il) atomicOr(&bits[jl >> 5], 1u << (jl & 31));
+        }
+        __syncthreads();
+        // exclusive prefix of the word popcounts: each thread a contiguous chunk of words
+        const int per = (nwords + HB - 1) / HB, k0 = min(t * per, nwords), k1 = min(k0 + per, nwords);
+        int s = 0;
+        for (int k = k0; k < k1; ++k) s += __popc(bits[k]);
+        int x = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        int base = 0, total = 0;
+#pragma unroll
+        for (int q = 0; q < HB / 32; ++q) {
+            base += q < warp ? wsum[q] : 0;
+            total += wsum[q];
+        }
+        int run = base + x - s;
+        for (int k = k0; k < k1; ++k) {
+            pre[k] = run;
+            run += __popc(bits[k]);
+        }
+        __syncthreads();
+        // the j-set in ascending water order
+        for (int k = t; k < nwords; k += HB) {
+            unsigned m = bits[k];
+            int p = pre[k];
+            while (m) {
+                const int bb = __ffs(m) - 1;
+                m &= m - 1u;
+                if (p < jcap) jset[(size_t)b * jcap + p] = R.wat0 + 32 * k + bb;
+                ++p;
+            }
+        }
+        // the owned entries, in the full row's order (in-cutoff partners first)
+        unsigned *hr = hrow + (size_t)b * caph * HB + t;
+        int kin = 0, kt = 0;
+        for (int v = 0; v < n; ++v) {
+            const int jl = row[v < nn ? v : cap_row - 1 - (v - nn)];
+            if (nb_half_owner(il, jl) != il) continue;
+            const int loc = pre[jl >> 5] + __popc(bits[jl >> 5] & ((1u << (jl & 31)) - 1u));
+            if (kt < caph) hr[(size_t)kt * HB] = ((unsigned)loc << 16) | (unsigned)jl;
+            ++kt;
+            kin += v < nn;
+        }
+        // a j-set beyond its capacity leaves the block's rows empty (the evaluation is redone
+        // with a larger one), so no entry indexes past the kernel's accumulators
+        if (act) hcnt[i] = total > jcap ? make_int2(0, 0) : make_int2(min(kin, caph), min(kt, caph));
+        const int mx = __reduce_max_sync(0xffffffffu, kt);
+        if (lane == 0) atomicMax(&st[7], mx);
+        if (t == 0) {
+            jn[b] = min(total, jcap);
+            atomicMax(&st[5], total);
+        }
+        if (kt > caph || (t == 0 && total > jcap)) atomicOr(&st[1], NB_DEV_ERR_OVERFLOW);
+    }
+}
+
 // 5. non-water list X: every site j within reach, exclusions removed
 template <typename T, int FILL>
 __device__ __forceinline__ void xlist_one(int k, int nW, const RepDev *__restrict__ reps,
@@ -770,6 +869,13 @@ void build_lists_t(NbCtx *c, const double *d_coor)
     };
     if (c->row16) water_lists((unsigned short)0);
     else water_lists(0);
+    if (sizeof(T) == 4 && c->whalf && c->row16) {
+        const int nb = (int)c->hblocks.size(), g = std::min(nb, c->nsm * 4);
+        (c->hb == 128 ? k_whalf<128> : k_whalf<256>)<<<g, c->hb, 0, s>>>(
+            nb, c->d_hblocks, c->d_reps, c->d_wl1_cnt, (const unsigned short *)c->d_wl1, c->cap_row1, c->d_hrow,
+            c->caph, c->d_hcnt, c->d_jset, c->d_jn, c->jcap, c->d_status);
+        c->launches++;
+    }
     if (sizeof(T) == 4 && c->nW > 0 && c->water_excl_fast) {
         k_wref<<<(c->nrep + 127) / 128, 128, 0, s>>>(c->nrep, c->d_reps, d_coor, c->d_status);
         c->launches++;

@@ -573,6 +573,243 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
     eu[7] = VIR ? (double)sE[5][t].x + (double)sE[5][t].y : 0.0;
 }
 
+// ---------------------------------------------------------------------------------
+// FP32 water kernel over half lists (k_whalf): every water-water pair is evaluated once, by
+// its owner, with the pair arithmetic of k_water_f.  The owner keeps its own gradient as in
+// k_water_f; the partner's side of each pair (per partner site, summed over the owner's three
+// sites) goes to an int32 accumulator in shared memory indexed by the partner's place in the
+// block's j-set, at 2^S units per kcal/mol/Å (S = 24 - log2 HB: HB contributions below
+// NB_HALF_CAP in magnitude fit); larger contributions go directly to the int64 gradient.
+// At the end the block adds its j-set sums and its own waters' gradients to the int64 site
+// gradient with atomics (integer sums: the result does not depend on their order).  The
+// site gradient of the waters is cleared before the launch.  Water-water energies and pair
+// counts are doubled, as the energy reduction halves the full-list sums.
+template <int HB> struct HalfScale;
+template <> struct HalfScale<128> { static constexpr int S = 17; };
+template <> struct HalfScale<256> { static constexpr int S = 16; };
+
+template <int HB>
+__global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict__ blocks, const RepDev *__restrict__ reps,
+                                                          const float4 *__restrict__ pos, const float4 *__restrict__ woff,
+                                                          const void *lj_v, const unsigned *__restrict__ sflags,
+                                                          const unsigned *__restrict__ hrow, int caph,
+                                                          const int2 *__restrict__ hcnt, const int *__restrict__ jset,
+                                                          const int *__restrict__ jn, int jcap,
+                                                          const int *__restrict__ wl2_off, const int *__restrict__ wl2,
+                                                          int cap2, long long *__restrict__ grad,
+                                                          double *__restrict__ e_unit, int intra)
+{
+    constexpr int S = HalfScale<HB>::S;
+    constexpr float SC = (float)(1 << S);
+    __shared__ long long sG[9][HB];
+    __shared__ float2 sE[4][HB];
+    extern __shared__ int sJ[];      // [9][jcap]: partner-site gradients, 2^S units
+    const int t = threadIdx.x, b = blockIdx.x;
+    const int2 w = blocks[b];
+    const RepDev &R = reps[w.x];
+    const int nJ = jn[b];
+    for (int k = t; k < nJ; k += HB)
+#pragma unroll
+        for (int c = 0; c < 9; ++c) sJ[c * jcap + k] = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) sG[k][t] = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sE[k][t] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const int i = w.y + t;
+    if (i - R.wat0 < R.nwat) {
+        const float4 oi0 = woff[3 * i];
+        const float4 oi1 = woff[3 * i + 1], oi2 = woff[3 * i + 2];
+        const float2 hi[2][3] = {{f2(oi1.x), f2(oi1.y), f2(oi1.z)}, {f2(oi2.x), f2(oi2.y), f2(oi2.z)}};
+        float2 G[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) G[k] = f2(0.f);
+        float g[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) g[k] = 0.f;
+        float e4[4] = {0.f, 0.f, 0.f, 0.f};   // LJ prim, LJ img, Coulomb prim, Coulomb img
+        double *eu = e_unit + NB_EU * (size_t)i;
+        {
+            // the molecule's own exclusion corrections, flushed at once (fewer live registers
+            // in the pair loop)
+            float ecorr = 0.f;
+            if (intra) {
+                const float qs[3] = {oi0.w, pos[3 * i + 1].w, pos[3 * i + 2].w};
+                ecorr = water_intra_f(R, oi1, oi2, qs, g);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) { sG[k][t] += nb_fix(g[k]); g[k] = 0.f; }
+            }
+            eu[5] = (double)ecorr;
+        }
+        // ef: 2 for the water-water energies (each pair once), 1 for the W2 part (full list)
+        auto flush = [&](float ef) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                sG[k][t] += nb_fix(g[k] - (G[k].x + G[k].y));   // G holds minus the gradient
+                g[k] = 0.f;
+                G[k] = f2(0.f);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 a = sE[k][t];
+                const float v = ef * e4[k];
+                const float sm = a.x + v, bb = sm - a.x, err = (a.x - (sm - bb)) + (v - bb);
+                sE[k][t] = make_float2(sm, a.y + err);
+                e4[k] = 0.f;
+            }
+        };
+        auto flush1 = [&]() { flush(1.f); };
+        // a partner site's gradient share (fx, fy, fz) of one pair
+        auto jadd = [&](int loc, int jg, int site, float fx, float fy, float fz) {
+            const float f[3] = {fx, fy, fz};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (fabsf(f[d]) < NB_HALF_CAP) atomicAdd(&sJ[(3 * site + d) * jcap + loc], __float2int_rn(f[d] * SC));
+                else atomicAdd((unsigned long long *)&grad[9 * (size_t)jg + 3 * site + d], (unsigned long long)nb_fix(f[d]));
+            }
+        };
+        int npair = 0;
+        const float iL0 = R.invL[0], iL1 = R.invL[1], iL2 = R.invL[2];
+        const float rmax2 = R.rmax2, rv2 = R.rv2;
+        const float2 palpha = f2(ERFCX_P * R.alpha), ex2c = f2(R.ex2c);
+        const float2 w12 = f2(R.w12), nw6 = f2(-R.w6);
+        const float2 c12 = f2(R.w12c), c6 = f2(R.w6c);
+        const float qqv[3] = {R.qq[0], R.qq[1], R.qq[2]};
+        const float c2a = R.c2a;
+        const unsigned *hr = hrow + (size_t)b * caph * HB + t;
+        const int k1 = hcnt[i].y, wat0 = R.wat0;
+        int cnt = 0;
+        // next pair of entries, loaded one iteration ahead
+        unsigned ea = k1 > 0 ? hr[0] : 0u;
+        unsigned eb = k1 > 1 ? hr[HB] : ea;
+        float4 oa = woff[3 * (wat0 + (int)(ea & 0xffffu))], ob = woff[3 * (wat0 + (int)(eb & 0xffffu))];
+        for (int k = 0; k < k1; k += 2) {
+            const bool hasb = k + 1 < k1;
+            const unsigned e0 = ea, e1 = eb;
+            const int j0 = wat0 + (int)(e0 & 0xffffu), j1 = wat0 + (int)(e1 & 0xffffu);
+            const int l0 = (int)(e0 >> 16), l1 = (int)(e1 >> 16);
+            const float4 o0 = oa, o1 = ob;
+            if (k + 2 < k1) {
+                ea = hr[(size_t)(k + 2) * HB];
+                eb = k + 3 < k1 ? hr[(size_t)(k + 3) * HB] : ea;
+                oa = woff[3 * (wat0 + (int)(ea & 0xffffu))];
+                ob = woff[3 * (wat0 + (int)(eb & 0xffffu))];
+            }
+            float dx0 = oi0.x - o0.x, dy0 = oi0.y - o0.y, dz0 = oi0.z - o0.z;
+            float dx1 = oi0.x - o1.x, dy1 = oi0.y - o1.y, dz1 = oi0.z - o1.z;
+            const float nx0 = fmaf(dx0, iL0, 12582912.f) - 12582912.f, ny0 = fmaf(dy0, iL1, 12582912.f) - 12582912.f, nz0 = fmaf(dz0, iL2, 12582912.f) - 12582912.f;
+            const float nx1 = fmaf(dx1, iL0, 12582912.f) - 12582912.f, ny1 = fmaf(dy1, iL1, 12582912.f) - 12582912.f, nz1 = fmaf(dz1, iL2, 12582912.f) - 12582912.f;
+            dx0 = nb_shift(R, 0, dx0, nx0); dy0 = nb_shift(R, 1, dy0, ny0); dz0 = nb_shift(R, 2, dz0, nz0);
+            dx1 = nb_shift(R, 0, dx1, nx1); dy1 = nb_shift(R, 1, dy1, ny1); dz1 = nb_shift(R, 2, dz1, nz1);
+            const float r0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0, r1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
+            const bool in0 = r0 <= rmax2, in1 = hasb && r1 <= rmax2;
+            if (in0 || in1) {
+                const float4 a1 = woff[3 * j0 + 1], a2 = woff[3 * j0 + 2];
+                const float4 b1 = woff[3 * j1 + 1], b2 = woff[3 * j1 + 2];
+                if (!in0) { dx0 = 1.0e4f; dy0 = 0.f; dz0 = 0.f; }
+                if (!in1) { dx1 = 1.0e4f; dy1 = 0.f; dz1 = 0.f; }
+                float2 eel = f2(0.f), elj = f2(0.f);
+#pragma unroll
+                for (int bs = 0; bs < 3; ++bs) {
+                    float2 q[3];
+                    if (bs == 0) {
+                        q[0] = f2(dx0, dx1); q[1] = f2(dy0, dy1); q[2] = f2(dz0, dz1);
+                    } else if (bs == 1) {
+                        q[0] = f2(dx0 - a1.x, dx1 - b1.x); q[1] = f2(dy0 - a1.y, dy1 - b1.y);
+                        q[2] = f2(dz0 - a1.z, dz1 - b1.z);
+                    } else {
+                        q[0] = f2(dx0 - a2.x, dx1 - b2.x); q[1] = f2(dy0 - a2.y, dy1 - b2.y);
+                        q[2] = f2(dz0 - a2.z, dz1 - b2.z);
+                    }
+                    float2 H[3] = {f2(0.f), f2(0.f), f2(0.f)};    // partner site bs: its gradient share
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const float2 ddx = a ? __fadd2_rn(hi[a - 1][0], q[0]) : q[0];
+                        const float2 ddy = a ? __fadd2_rn(hi[a - 1][1], q[1]) : q[1];
+                        const float2 ddz = a ? __fadd2_rn(hi[a - 1][2], q[2]) : q[2];
+                        const float2 rr2 = __ffma2_rn(ddx, ddx, __ffma2_rn(ddy, ddy, __fmul2_rn(ddz, ddz)));
+                        const float2 rinv = f2(nb_rsqrt_approx(rr2.x), nb_rsqrt_approx(rr2.y));
+                        const float2 s2 = __fmul2_rn(rinv, rinv);
+                        const float2 arg = __fmul2_rn(rr2, ex2c);
+                        const float2 den = __ffma2_rn(palpha, __fmul2_rn(rr2, rinv), f2(1.f));
+                        const float2 tt = f2(nb_rcp_approx(den.x), nb_rcp_approx(den.y));
+                        const float2 u = __ffma2_rn(f2(ERFCX_A), tt, f2(ERFCX_B));
+                        const float C[ERFCX_NC] = ERFCX_COEFS;
+                        float2 p = f2(C[ERFCX_NC - 1]);
+#pragma unroll
+                        for (int m = ERFCX_NC - 2; m >= 0; --m) p = __ffma2_rn(p, u, f2(C[m]));
+                        const float2 ex = f2(nb_ex2_approx(-arg.x), nb_ex2_approx(-arg.y));
+                        const float2 erfcv = __fmul2_rn(ex, __fmul2_rn(tt, p));
+                        const float qq = (a == 0 && bs == 0) ? qqv[0] : ((a == 0 || bs == 0) ? qqv[1] : qqv[2]);
+                        const float2 e = __fmul2_rn(__fmul2_rn(f2(qq), erfcv), rinv);
+                        float2 mdf = __fmul2_rn(__ffma2_rn(f2(qq * c2a), ex, e), s2);
+                        if (a == 0 && bs == 0) {
+                            const float2 ri = __ffma2_rn(__fmul2_rn(f2(-0.5f), rinv), __ffma2_rn(rr2, s2, f2(-1.f)), rinv);
+                            const float2 sl = __fmul2_rn(ri, ri);
+                            const float2 s6 = __fmul2_rn(__fmul2_rn(sl, sl), sl);
+                            const float2 A = __fmul2_rn(__fmul2_rn(w12, s6), s6);
+                            float2 e1 = __ffma2_rn(nw6, __ffma2_rn(s6, c6, s6), __ffma2_rn(A, c12, A));
+                            float2 m1 = __fmul2_rn(__fmul2_rn(f2(6.f), sl), __ffma2_rn(nw6, s6, __fadd2_rn(A, A)));
+                            if (R.lj_switch) {
+                                float d0 = -m1.x, d1 = -m1.y;
+                                lj_switch_apply<float>(R, rr2.x, e1.x, d0);
+                                lj_switch_apply<float>(R, rr2.y, e1.y, d1);
+                                m1 = f2(-d0, -d1);
+                            }
+                            const bool lj0 = rr2.x <= rv2, lj1 = rr2.y <= rv2;
+                            e1 = f2(lj0 ? e1.x : 0.f, lj1 ? e1.y : 0.f);
+                            m1 = f2(lj0 ? m1.x : 0.f, lj1 ? m1.y : 0.f);
+                            elj = __fadd2_rn(elj, e1);
+                            mdf = __fadd2_rn(mdf, m1);
+                        }
+                        eel = __fadd2_rn(eel, e);
+                        G[3 * a] = __ffma2_rn(mdf, ddx, G[3 * a]);
+                        G[3 * a + 1] = __ffma2_rn(mdf, ddy, G[3 * a + 1]);
+                        G[3 * a + 2] = __ffma2_rn(mdf, ddz, G[3 * a + 2]);
+                        H[0] = __ffma2_rn(mdf, ddx, H[0]);
+                        H[1] = __ffma2_rn(mdf, ddy, H[1]);
+                        H[2] = __ffma2_rn(mdf, ddz, H[2]);
+                    }
+                    if (in0) jadd(l0, j0, bs, H[0].x, H[1].x, H[2].x);
+                    if (in1) jadd(l1, j1, bs, H[0].y, H[1].y, H[2].y);
+                }
+                const bool img0 = (nx0 != 0.f) | (ny0 != 0.f) | (nz0 != 0.f);
+                const bool img1 = (nx1 != 0.f) | (ny1 != 0.f) | (nz1 != 0.f);
+                e4[img0 ? 1 : 0] += elj.x;
+                e4[img0 ? 3 : 2] += eel.x;
+                e4[img1 ? 1 : 0] += elj.y;
+                e4[img1 ? 3 : 2] += eel.y;
+                npair += 18 * ((int)in0 + (int)in1);
+            }
+            cnt += 2;
+            if (cnt >= CHUNK) { flush(2.f); cnt = 0; }
+        }
+        flush(2.f);
+        water_vs_atoms<float>(R, i, pos, lj_v, sflags, wl2_off, wl2, cap2, g, e4, npair, flush1);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) eu[k] = (double)sE[k][t].x + (double)sE[k][t].y;
+        eu[4] = (double)npair;
+        eu[6] = 0.0;
+        eu[7] = 0.0;
+    }
+    __syncthreads();
+    // the block's sums: its own waters' gradients and the partner shares of its j-set
+    if (i - R.wat0 < R.nwat) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            if (sG[k][t] != 0) atomicAdd((unsigned long long *)&grad[9 * (size_t)i + k], (unsigned long long)sG[k][t]);
+    }
+    const int *js = jset + (size_t)b * jcap;
+    for (int l = t; l < nJ; l += HB) {
+        const size_t jg = (size_t)js[l];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            const int v = sJ[c * jcap + l];
+            if (v != 0) atomicAdd((unsigned long long *)&grad[9 * jg + c], (unsigned long long)((long long)v * (1LL << (32 - S))));
+        }
+    }
+}
+
 // non-water atom per thread over its full site list
 template <typename T>
 __global__ void __launch_bounds__(128) k_atom(int nA, int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
@@ -895,7 +1132,15 @@ void realspace_t(NbCtx *c)
 {
     cudaStream_t s = c->stream;
     if (c->timing) cudaEventRecord(c->ev[2], s);
-    if (c->nW > 0) {
+    if (sizeof(T) == 4 && c->nW > 0 && c->whalf && !c->virial) {
+        // the water sites' gradients are sums of atomics: cleared first
+        cudaMemsetAsync(c->d_grad_site, 0, sizeof(long long) * 9 * (size_t)c->nW, s);
+        (c->hb == 128 ? k_water_h<128> : k_water_h<256>)<<<(int)c->hblocks.size(), c->hb, (size_t)36 * c->jcap, s>>>(
+            c->d_hblocks, c->d_reps, (const float4 *)c->d_pos, (const float4 *)c->d_woff, c->d_site_lj,
+            c->d_site_flags, c->d_hrow, c->caph, c->d_hcnt, c->d_jset, c->d_jn, c->jcap, c->d_wl2_off, c->d_wl2,
+            cap_int(c->cap_wl2), c->d_grad_site, c->d_e_unit, c->water_excl_fast);
+        c->launches++;
+    } else if (c->nW > 0) {
         const int nb = (int)((c->nW + WBLOCK - 1) / WBLOCK);
         if constexpr (sizeof(T) == 4)
             (c->virial ? (c->row16 ? k_water_f<true, unsigned short> : k_water_f<true, int>)
@@ -926,6 +1171,19 @@ void nb_launch_realspace(NbCtx *c)
 {
     if (c->precision == MOIL_NB_FP64) realspace_t<double>(c);
     else realspace_t<float>(c);
+}
+
+int nb_half_configure(NbCtx *c)
+{
+    int optin = 0;
+    NB_CUDA_OK(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    const void *fn = c->hb == 128 ? (const void *)k_water_h<128> : (const void *)k_water_h<256>;
+    cudaFuncAttributes fa;
+    NB_CUDA_OK(c, cudaFuncGetAttributes(&fa, fn));
+    const size_t dyn = (size_t)36 * c->jcap;
+    if (c->jcap > 65535 || dyn + fa.sharedSizeBytes > (size_t)optin) return MOIL_NB_ERR_OVERFLOW;
+    NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    return MOIL_NB_OK;
 }
 
 void nb_launch_excl14(NbCtx *c, const double *d_coor)

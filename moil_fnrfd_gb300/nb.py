@@ -31,6 +31,7 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
             "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "moil_nb_md_step",
+            "moil_nb_set_shape", "moil_nb_get_shape",
             "moil_nb_dcd_write", "moil_nb_set_molecules", "moil_nb_pressure", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -66,6 +67,15 @@ class Timing(ctypes.Structure):
                                                "pme_spread_fft_ms", "pme_conv_ms", "pme_gather_ms",
                                                "finalize_ms", "total_ms")] + [
         ("list_rebuilt", ctypes.c_int), ("launches", ctypes.c_int)]
+
+
+WATER_AUTO, WATER_FULL, WATER_HALF = 0, 1, 2
+TILED_AUTO, TILED_OFF, TILED_ALL = 0, 1, 2
+SHAPE_KEYS = ("water_kernel", "half_block", "tiled", "groups")
+
+
+class Shape(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in SHAPE_KEYS]
 
 
 class MoilNbError(RuntimeError):
@@ -115,6 +125,8 @@ def load(build_if_missing: bool = True):
     L.moil_nb_get_virial.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     L.moil_nb_set_virial.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.moil_nb_set_groups.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.moil_nb_set_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(Shape)]
+    L.moil_nb_get_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(Shape)]
     L.moil_nb_md_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                   ctypes.c_double, ctypes.c_int, _dp, ctypes.POINTER(Energies), _dp]
     L.moil_nb_dcd_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
@@ -189,12 +201,14 @@ class Nonbonded:
     """One device handle over one system or a batch of independent replicas."""
 
     def __init__(self, systems, precision=MOIL_NB_MIXED, device=0, skin=1.0, list_period=0,
-                 lj_switch=False, timing=False, groups=0, dtol=None):
+                 lj_switch=False, timing=False, groups=0, dtol=None, shape=None):
         self.L = load()
         h = ctypes.c_void_p()
         _check(self.L, None, self.L.moil_nb_create(ctypes.byref(h), int(device)))
         self.h = h
         _check(self.L, self.h, self.L.moil_nb_set_groups(self.h, int(groups)))
+        if shape is not None:
+            self.set_shape(**dict(shape, groups=shape.get("groups", groups)))
         self.batch = isinstance(systems, (list, tuple))
         self.systems = list(systems) if self.batch else [systems]
         keep = _Keep()
@@ -254,6 +268,17 @@ class Nonbonded:
         """Number of concurrently evaluated replica groups (1: none)."""
         return int(self.L.moil_nb_groups(self.h))
 
+    def set_shape(self, water_kernel=WATER_AUTO, half_block=0, tiled=TILED_AUTO, groups=0):
+        """Kernel and list shapes (moil_nb_set_shape); the lists are rebuilt at the next call."""
+        sh = Shape(int(water_kernel), int(half_block), int(tiled), int(groups))
+        _check(self.L, self.h, self.L.moil_nb_set_shape(self.h, ctypes.byref(sh)))
+
+    def shape(self) -> dict:
+        """The shapes in use, automatic choices resolved (moil_nb_get_shape)."""
+        sh = Shape()
+        _check(self.L, self.h, self.L.moil_nb_get_shape(self.h, ctypes.byref(sh)))
+        return {k: getattr(sh, k) for k in SHAPE_KEYS}
+
     def set_virial(self, on=True):
         """Accumulate the water-water LJ virial terms on the mixed path (off by default)."""
         _check(self.L, self.h, self.L.moil_nb_set_virial(self.h, int(on)))
@@ -289,6 +314,15 @@ class Nonbonded:
         if not self.batch:
             return dpot, e[0]
         return [dpot[self.offsets[k]:self.offsets[k + 1]] for k in range(len(self.systems))], e
+
+    def adjoint_into(self, coor: np.ndarray, dq: np.ndarray, de: np.ndarray, ds: np.ndarray):
+        """moil_nb_adjoint into caller-owned arrays: coor (natom,3), dq/de/ds (natom,) float64."""
+        assert coor.dtype == np.float64 and coor.flags.c_contiguous and coor.size == 3 * self.natom
+        for o in (dq, de, ds):
+            assert o.dtype == np.float64 and o.flags.c_contiguous and o.size == self.natom
+        _check(self.L, self.h, self.L.moil_nb_adjoint(self.h, coor.ctypes.data_as(_dp), dq.ctypes.data_as(_dp),
+                                                      de.ctypes.data_as(_dp), ds.ctypes.data_as(_dp), self._e))
+        return self.energies()
 
     def adjoint(self, coor=None):
         """Per-atom dE/dq, dE/deps, dE/dsigma (moil_nb_adjoint).  Single system: three
