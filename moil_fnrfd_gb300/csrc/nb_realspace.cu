@@ -1182,7 +1182,10 @@ int nb_half_configure(NbCtx *c)
     NB_CUDA_OK(c, cudaFuncGetAttributes(&fa, fn));
     const size_t dyn = (size_t)36 * c->jcap;
     if (c->jcap > 65535 || dyn + fa.sharedSizeBytes > (size_t)optin) return MOIL_NB_ERR_OVERFLOW;
-    NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    // the limit belongs to the kernel, not to the handle: other handles (replica groups) may
+    // launch it with larger j-sets, so it only ever grows
+    if ((int)dyn > fa.maxDynamicSharedSizeBytes)
+        NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     return MOIL_NB_OK;
 }
 

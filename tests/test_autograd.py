@@ -87,7 +87,7 @@ def grads(base, precision):
     s_t = torch.tensor(sig_t, requires_grad=True)
     E = NonbondedEnergy.apply(q, e_t, s_t, base, tid, precision)
     E.backward()
-    return tid, eps_t, sig_t, q.grad.numpy(), e_t.grad.numpy(), s_t.grad.numpy(), float(E)
+    return tid, eps_t, sig_t, q.grad.numpy(), e_t.grad.numpy(), s_t.grad.numpy(), float(E.detach())
 
 
 def solute_direction(base, seed):
