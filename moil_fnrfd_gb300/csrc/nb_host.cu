@@ -1363,7 +1363,7 @@ int moil_nb_get_shape(const moil_nb_ctx *h, moil_nb_shape *sp)
 {
     if (!h || !sp) return MOIL_NB_ERR_ARG;
     const NbCtx *c = h->grp.empty() ? h : h->grp[0];
-    sp->water_kernel = c->inited ? ((c->whalf && !c->virial) ? MOIL_NB_WATER_HALF : MOIL_NB_WATER_FULL) : c->want_whalf;
+    sp->water_kernel = c->inited ? (c->whalf ? MOIL_NB_WATER_HALF : MOIL_NB_WATER_FULL) : c->want_whalf;
     sp->half_block = c->hb;
     sp->tiled = c->want_tiled;
     sp->groups = h->inited ? moil_nb_groups(h) : h->want_groups;

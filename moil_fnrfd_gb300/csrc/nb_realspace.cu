@@ -588,7 +588,8 @@ template <int HB> struct HalfScale;
 template <> struct HalfScale<128> { static constexpr int S = 17; };
 template <> struct HalfScale<256> { static constexpr int S = 16; };
 
-template <int HB>
+// VIR: also the water-water LJ virial terms (as k_water_f<true>)
+template <int HB, bool VIR>
 __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict__ blocks, const RepDev *__restrict__ reps,
                                                           const float4 *__restrict__ pos, const float4 *__restrict__ woff,
                                                           const void *lj_v, const unsigned *__restrict__ sflags,
@@ -601,8 +602,9 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
 {
     constexpr int S = HalfScale<HB>::S;
     constexpr float SC = (float)(1 << S);
+    constexpr int NE = VIR ? 6 : 4;
     __shared__ long long sG[9][HB];
-    __shared__ float2 sE[4][HB];
+    __shared__ float2 sE[NE][HB];
     extern __shared__ int sJ[];      // [9][jcap]: partner-site gradients, 2^S units
     const int t = threadIdx.x, b = blockIdx.x;
     const int2 w = blocks[b];
@@ -614,7 +616,7 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
 #pragma unroll
     for (int k = 0; k < 9; ++k) sG[k][t] = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) sE[k][t] = make_float2(0.f, 0.f);
+    for (int k = 0; k < NE; ++k) sE[k][t] = make_float2(0.f, 0.f);
     __syncthreads();
     const int i = w.y + t;
     if (i - R.wat0 < R.nwat) {
@@ -627,7 +629,10 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
         float g[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) g[k] = 0.f;
-        float e4[4] = {0.f, 0.f, 0.f, 0.f};   // LJ prim, LJ img, Coulomb prim, Coulomb img
+        // LJ prim, LJ img, Coulomb prim, Coulomb img (, LJ virial prim, LJ virial img)
+        float e4[NE];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) e4[k] = 0.f;
         double *eu = e_unit + NB_EU * (size_t)i;
         {
             // the molecule's own exclusion corrections, flushed at once (fewer live registers
@@ -650,7 +655,7 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
                 G[k] = f2(0.f);
             }
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < NE; ++k) {
                 const float2 a = sE[k][t];
                 const float v = ef * e4[k];
                 const float sm = a.x + v, bb = sm - a.x, err = (a.x - (sm - bb)) + (v - bb);
@@ -708,7 +713,7 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
                 const float4 b1 = woff[3 * j1 + 1], b2 = woff[3 * j1 + 2];
                 if (!in0) { dx0 = 1.0e4f; dy0 = 0.f; dz0 = 0.f; }
                 if (!in1) { dx1 = 1.0e4f; dy1 = 0.f; dz1 = 0.f; }
-                float2 eel = f2(0.f), elj = f2(0.f);
+                float2 eel = f2(0.f), elj = f2(0.f), vlj = f2(0.f);
 #pragma unroll
                 for (int bs = 0; bs < 3; ++bs) {
                     float2 q[3];
@@ -760,6 +765,7 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
                             e1 = f2(lj0 ? e1.x : 0.f, lj1 ? e1.y : 0.f);
                             m1 = f2(lj0 ? m1.x : 0.f, lj1 ? m1.y : 0.f);
                             elj = __fadd2_rn(elj, e1);
+                            if (VIR) vlj = __fmul2_rn(m1, rr2);   // -df1 r^2 (watwat_ewald_press.f:146-152)
                             mdf = __fadd2_rn(mdf, m1);
                         }
                         eel = __fadd2_rn(eel, e);
@@ -777,8 +783,10 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
                 const bool img1 = (nx1 != 0.f) | (ny1 != 0.f) | (nz1 != 0.f);
                 e4[img0 ? 1 : 0] += elj.x;
                 e4[img0 ? 3 : 2] += eel.x;
+                if (VIR) e4[img0 ? NE - 1 : NE - 2] += vlj.x;
                 e4[img1 ? 1 : 0] += elj.y;
                 e4[img1 ? 3 : 2] += eel.y;
+                if (VIR) e4[img1 ? NE - 1 : NE - 2] += vlj.y;
                 npair += 18 * ((int)in0 + (int)in1);
             }
             cnt += 2;
@@ -789,8 +797,8 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
 #pragma unroll
         for (int k = 0; k < 4; ++k) eu[k] = (double)sE[k][t].x + (double)sE[k][t].y;
         eu[4] = (double)npair;
-        eu[6] = 0.0;
-        eu[7] = 0.0;
+        eu[6] = VIR ? (double)sE[NE - 2][t].x + (double)sE[NE - 2][t].y : 0.0;
+        eu[7] = VIR ? (double)sE[NE - 1][t].x + (double)sE[NE - 1][t].y : 0.0;
     }
     __syncthreads();
     // the block's sums: its own waters' gradients and the partner shares of its j-set
@@ -1132,10 +1140,11 @@ void realspace_t(NbCtx *c)
 {
     cudaStream_t s = c->stream;
     if (c->timing) cudaEventRecord(c->ev[2], s);
-    if (sizeof(T) == 4 && c->nW > 0 && c->whalf && !c->virial) {
+    if (sizeof(T) == 4 && c->nW > 0 && c->whalf) {
         // the water sites' gradients are sums of atomics: cleared first
         cudaMemsetAsync(c->d_grad_site, 0, sizeof(long long) * 9 * (size_t)c->nW, s);
-        (c->hb == 128 ? k_water_h<128> : k_water_h<256>)<<<(int)c->hblocks.size(), c->hb, (size_t)36 * c->jcap, s>>>(
+        (c->hb == 128 ? (c->virial ? k_water_h<128, true> : k_water_h<128, false>)
+                      : (c->virial ? k_water_h<256, true> : k_water_h<256, false>))<<<(int)c->hblocks.size(), c->hb, (size_t)36 * c->jcap, s>>>(
             c->d_hblocks, c->d_reps, (const float4 *)c->d_pos, (const float4 *)c->d_woff, c->d_site_lj,
             c->d_site_flags, c->d_hrow, c->caph, c->d_hcnt, c->d_jset, c->d_jn, c->jcap, c->d_wl2_off, c->d_wl2,
             cap_int(c->cap_wl2), c->d_grad_site, c->d_e_unit, c->water_excl_fast);
@@ -1177,15 +1186,18 @@ int nb_half_configure(NbCtx *c)
 {
     int optin = 0;
     NB_CUDA_OK(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-    const void *fn = c->hb == 128 ? (const void *)k_water_h<128> : (const void *)k_water_h<256>;
-    cudaFuncAttributes fa;
-    NB_CUDA_OK(c, cudaFuncGetAttributes(&fa, fn));
+    const void *fns[2] = {c->hb == 128 ? (const void *)k_water_h<128, false> : (const void *)k_water_h<256, false>,
+                          c->hb == 128 ? (const void *)k_water_h<128, true> : (const void *)k_water_h<256, true>};
     const size_t dyn = (size_t)36 * c->jcap;
-    if (c->jcap > 65535 || dyn + fa.sharedSizeBytes > (size_t)optin) return MOIL_NB_ERR_OVERFLOW;
-    // the limit belongs to the kernel, not to the handle: other handles (replica groups) may
-    // launch it with larger j-sets, so it only ever grows
-    if ((int)dyn > fa.maxDynamicSharedSizeBytes)
-        NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    for (const void *fn : fns) {
+        cudaFuncAttributes fa;
+        NB_CUDA_OK(c, cudaFuncGetAttributes(&fa, fn));
+        if (c->jcap > 65535 || dyn + fa.sharedSizeBytes > (size_t)optin) return MOIL_NB_ERR_OVERFLOW;
+        // the limit belongs to the kernel, not to the handle: other handles (replica groups)
+        // may launch it with larger j-sets, so it only ever grows
+        if ((int)dyn > fa.maxDynamicSharedSizeBytes)
+            NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    }
     return MOIL_NB_OK;
 }
 
