@@ -525,12 +525,29 @@ __global__ void __launch_bounds__(HB) k_whalf(int nblk, const int2 *__restrict__
         const bool act = il < R.nwat;
         const int2 c = act ? wcnt[i] : make_int2(0, 0);
         // an overflowed row is read within its capacity (the evaluation is redone)
-        const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
+        const int nn = min(c.x, cap_row), nf = min(c.x + c.y, cap_row) - nn;
         const unsigned short *row = wl1 + (size_t)i * cap_row;
-        for (int v = 0; v < n; ++v) {
-            const int jl = row[v < nn ? v : cap_row - 1 - (v - nn)];
+        // the row's entries, eight at a time (16-byte loads; rows start 64-byte aligned): the
+        // in-cutoff ones [0, nn), then the skin ones [cap_row - nf, cap_row)
+        auto for_row = [&](auto fn) {
+            for (int v0 = 0; v0 < nn; v0 += 8) {
+                const uint4 q = *reinterpret_cast<const uint4 *>(row + v0);
+                const unsigned u[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int e = 0; e < 8; ++e)
+                    if (v0 + e < nn) fn((int)((u[e >> 1] >> (16 * (e & 1))) & 0xffffu), true);
+            }
+            for (int v0 = (cap_row - nf) & ~7; v0 < cap_row; v0 += 8) {
+                const uint4 q = *reinterpret_cast<const uint4 *>(row + v0);
+                const unsigned u[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int e = 0; e < 8; ++e)
+                    if (v0 + e >= cap_row - nf) fn((int)((u[e >> 1] >> (16 * (e & 1))) & 0xffffu), false);
+            }
+        };
+        for_row([&](int jl, bool) {
             if (nb_half_owner(il, jl) == il) atomicOr(&bits[jl >> 5], 1u << (jl & 31));
-        }
+        });
         __syncthreads();
         // exclusive prefix of the word popcounts: each thread a contiguous chunk of words
         const int per = (nwords + HB - 1) / HB, k0 = min(t * per, nwords), k1 = min(k0 + per, nwords);
@@ -570,14 +587,13 @@ __global__ void __launch_bounds__(HB) k_whalf(int nblk, const int2 *__restrict__
         // the owned entries, in the full row's order (in-cutoff partners first)
         unsigned *hr = hrow + (size_t)b * caph * HB + t;
         int kin = 0, kt = 0;
-        for (int v = 0; v < n; ++v) {
-            const int jl = row[v < nn ? v : cap_row - 1 - (v - nn)];
-            if (nb_half_owner(il, jl) != il) continue;
+        for_row([&](int jl, bool near) {
+            if (nb_half_owner(il, jl) != il) return;
             const int loc = pre[jl >> 5] + __popc(bits[jl >> 5] & ((1u << (jl & 31)) - 1u));
             if (kt < caph) hr[(size_t)kt * HB] = ((unsigned)loc << 16) | (unsigned)jl;
             ++kt;
-            kin += v < nn;
-        }
+            kin += near;
+        });
         // a j-set beyond its capacity leaves the block's rows empty (the evaluation is redone
         // with a larger one), so no entry indexes past the kernel's accumulators
         if (act) hcnt[i] = total > jcap ? make_int2(0, 0) : make_int2(min(kin, caph), min(kt, caph));

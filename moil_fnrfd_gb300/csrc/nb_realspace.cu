@@ -664,13 +664,31 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
             }
         };
         auto flush1 = [&]() { flush(1.f); };
-        // a partner site's gradient share (fx, fy, fz) of one pair
-        auto jadd = [&](int loc, int jg, int site, float fx, float fy, float fz) {
-            const float f[3] = {fx, fy, fz};
+        // partner site `site` of both entries: its gradient shares H (x: entry 0, y: entry 1).
+        // A parked entry's share is exactly zero, so it is added without a test; a share at or
+        // above NB_HALF_CAP (rare) takes the int64 path for that entry and component.
+        auto jadd = [&](int l0, int l1, int j0, int j1, int site, const float2 H[3]) {
+            bool big = false;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                if (fabsf(f[d]) < NB_HALF_CAP) atomicAdd(&sJ[(3 * site + d) * jcap + loc], __float2int_rn(f[d] * SC));
-                else atomicAdd((unsigned long long *)&grad[9 * (size_t)jg + 3 * site + d], (unsigned long long)nb_fix(f[d]));
+            for (int d = 0; d < 3; ++d) big |= (fabsf(H[d].x) >= NB_HALF_CAP) | (fabsf(H[d].y) >= NB_HALF_CAP);
+            if (!big) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    atomicAdd(&sJ[(3 * site + d) * jcap + l0], __float2int_rn(H[d].x * SC));
+                    atomicAdd(&sJ[(3 * site + d) * jcap + l1], __float2int_rn(H[d].y * SC));
+                }
+            } else {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float fe[2] = {H[d].x, H[d].y};
+                    const int le[2] = {l0, l1}, je[2] = {j0, j1};
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        if (fabsf(fe[q]) < NB_HALF_CAP) atomicAdd(&sJ[(3 * site + d) * jcap + le[q]], __float2int_rn(fe[q] * SC));
+                        else atomicAdd((unsigned long long *)&grad[9 * (size_t)je[q] + 3 * site + d],
+                                       (unsigned long long)nb_fix(fe[q]));
+                    }
+                }
             }
         };
         int npair = 0;
@@ -694,6 +712,8 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
             const int j0 = wat0 + (int)(e0 & 0xffffu), j1 = wat0 + (int)(e1 & 0xffffu);
             const int l0 = (int)(e0 >> 16), l1 = (int)(e1 >> 16);
             const float4 o0 = oa, o1 = ob;
+            // the warp's row lines (one 128-byte line per entry) eight iterations ahead
+            nb_prefetch_l1(hr + (size_t)min(k + 16, k1 - 1) * HB);
             if (k + 2 < k1) {
                 ea = hr[(size_t)(k + 2) * HB];
                 eb = k + 3 < k1 ? hr[(size_t)(k + 3) * HB] : ea;
@@ -776,8 +796,7 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
                         H[1] = __ffma2_rn(mdf, ddy, H[1]);
                         H[2] = __ffma2_rn(mdf, ddz, H[2]);
                     }
-                    if (in0) jadd(l0, j0, bs, H[0].x, H[1].x, H[2].x);
-                    if (in1) jadd(l1, j1, bs, H[0].y, H[1].y, H[2].y);
+                    jadd(l0, l1, j0, j1, bs, H);
                 }
                 const bool img0 = (nx0 != 0.f) | (ny0 != 0.f) | (nz0 != 0.f);
                 const bool img1 = (nx1 != 0.f) | (ny1 != 0.f) | (nz1 != 0.f);
