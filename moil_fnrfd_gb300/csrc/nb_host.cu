@@ -599,6 +599,53 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     return MOIL_NB_OK;
 }
 
+// While an evaluation is captured: the list rebuild goes into the body of a conditional IF
+// node that a one-thread kernel sets from the device rebuild flag, so evaluations without a
+// rebuild launch none of the rebuild kernels.  Returns false (the gated kernels are then
+// captured in line) if the stream is not capturing or a graph call fails before the node is
+// added.
+bool enqueue_lists_conditional(NbCtx *c, const double *d_coor)
+{
+    cudaStream_t s = c->stream;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+        return false;
+    cudaGraphConditionalHandle hc;
+    if (cudaGraphConditionalHandleCreate(&hc, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return false;
+    if (!c->sbody && cudaStreamCreateWithFlags(&c->sbody, cudaStreamNonBlocking) != cudaSuccess) {
+        c->sbody = nullptr;
+        return false;
+    }
+    nb_launch_rebuild_cond(c, hc);
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) return false;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hc;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &np) != cudaSuccess) return false;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(c->sbody, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+        cudaSuccess) {
+        // an empty body: the gated kernels are captured after the node instead
+        cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        return false;
+    }
+    std::swap(c->stream, c->sbody);
+    nb_launch_build_lists(c, d_coor);
+    std::swap(c->stream, c->sbody);
+    cudaGraph_t done = nullptr;
+    cudaStreamEndCapture(c->sbody, &done);
+    // the rest of the evaluation follows the conditional node (errors surface at EndCapture)
+    cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    return true;
+}
+
 // The device part of one evaluation, in stream order.  The sequence does not depend on host
 // state beyond the handle's fixed buffers and the two caller pointers: the rebuild decision
 // travels through the pinned word h_status[8], read by the first copy.  That makes it
@@ -610,10 +657,27 @@ void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
     if (c->timing) cudaEventRecord(c->ev[0], s);
     cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 8, cudaMemcpyHostToDevice, s);
     nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
-    nb_launch_build_lists(c, d_coor);  // every kernel here is gated by the flag
+    // every rebuild kernel is gated by the flag; a captured evaluation also skips their
+    // launches through a conditional node
+    if (c->timing) {
+        // stage timing (kernel by kernel): the host reads the flag and launches the rebuild
+        // only when it is set, as the conditional node of a replayed evaluation does
+        // (the stage ends at the flag's read-back unless the rebuild runs: the event is then
+        // recorded again after it, so the host's wait is not counted)
+        cudaMemcpyAsync(c->h_status + 16, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaEventRecord(c->ev[1], s);
+        cudaStreamSynchronize(s);
+        if (c->h_status[16]) {
+            nb_launch_build_lists(c, d_coor);
+            cudaEventRecord(c->ev[1], s);
+        }
+    } else if (!(c->capturing && !c->on_prio && enqueue_lists_conditional(c, d_coor))) {
+        // (on the prioritised streams of host-buffer group evaluations the conditional node
+        // cost the copy/kernel overlap more than the skipped launches save: gated kernels)
+        nb_launch_build_lists(c, d_coor);
+    }
     if (c->timing) {
         // stage timing: one stream, stage after stage
-        cudaEventRecord(c->ev[1], s);
         nb_launch_realspace(c);
         nb_launch_excl14(c, d_coor);
         cudaEventRecord(c->ev[5], s);
@@ -650,7 +714,8 @@ void drop_graph(NbCtx *c)
 bool launch_graph(NbCtx *c, const double *d_coor, double *d_dpot)
 {
     cudaStream_t s = c->stream;
-    if (!c->gexec || c->g_coor != d_coor || c->g_dpot != d_dpot || c->g_gen != c->list_gen) {
+    if (!c->gexec || c->g_coor != d_coor || c->g_dpot != d_dpot || c->g_gen != c->list_gen ||
+        c->g_prio != c->on_prio) {
         drop_graph(c);
         cudaGraph_t g = nullptr;
         if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
@@ -658,7 +723,9 @@ bool launch_graph(NbCtx *c, const double *d_coor, double *d_dpot)
             c->use_graph = 0;
             return false;
         }
+        c->capturing = 1;
         enqueue_eval(c, d_coor, d_dpot);
+        c->capturing = 0;
         cudaError_t e1 = cudaStreamEndCapture(s, &g);
         cudaError_t e2 = e1 == cudaSuccess ? cudaGraphInstantiate(&c->gexec, g, 0) : e1;
         if (g) cudaGraphDestroy(g);
@@ -670,6 +737,7 @@ bool launch_graph(NbCtx *c, const double *d_coor, double *d_dpot)
         }
         c->g_coor = d_coor;
         c->g_dpot = d_dpot;
+        c->g_prio = c->on_prio;
         c->g_gen = c->list_gen;
         c->graph_launches = c->launches;
     }
@@ -833,8 +901,11 @@ int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bo
     auto use_prio = [&](bool on) {
         if (!host) return;
         for (NbCtx *c : h->grp)
-            if (c->pstream) { std::swap(c->stream, c->pstream); std::swap(c->stream2, c->pstream2); }
-        (void)on;
+            if (c->pstream) {
+                std::swap(c->stream, c->pstream);
+                std::swap(c->stream2, c->pstream2);
+                c->on_prio = on ? 1 : 0;
+            }
     };
     use_prio(true);
     int rc = MOIL_NB_OK;
@@ -990,7 +1061,7 @@ int moil_nb_create(moil_nb_ctx **out, int device)
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
     if (h->nsm <= 0) h->nsm = 1;
     for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
-    if (cudaMallocHost(&h->h_status, sizeof(int) * 16) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
+    if (cudaMallocHost(&h->h_status, sizeof(int) * 24) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
         moil_nb_destroy(h);
         return MOIL_NB_ERR_CUDA;
     }
@@ -1011,6 +1082,7 @@ void moil_nb_destroy(moil_nb_ctx *h)
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->d_status) cudaFree(h->d_status);
     if (h->stream2) { cudaStreamSynchronize(h->stream2); cudaStreamDestroy(h->stream2); }
+    if (h->sbody) cudaStreamDestroy(h->sbody);
     if (h->pstream) cudaStreamDestroy(h->pstream);
     if (h->pstream2) cudaStreamDestroy(h->pstream2);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);

@@ -37,6 +37,8 @@ struct NbCtx {
     int nsm = 152;                // multiprocessors: grids of the rebuild-gated kernels stay one wave
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;   // PME branch of an evaluation, concurrent with the pair kernels
+    cudaStream_t sbody = nullptr;     // captures the list rebuild into the conditional node's body
+    int capturing = 0;                // the evaluation is being captured into the handle's graph
     cudaStream_t pstream = nullptr, pstream2 = nullptr;   // replica groups: prioritised by group index
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int precision = MOIL_NB_MIXED;
@@ -167,7 +169,8 @@ struct NbCtx {
     // [5] largest half-list j-set, [6] longest W1 row, [7] longest half row; all reset at the
     // start of every evaluation
     int *d_status = nullptr;
-    int *h_status = nullptr;           // pinned: [0..7] mirror, [8..9] initial words of an evaluation
+    int *h_status = nullptr;           // pinned: [0..7] mirror, [8..15] initial words of an evaluation,
+                                       // [16] the rebuild flag read back in stage-timing mode
     int need_rebuild = 1;
     int evals_since_build = 0;
     int64_t last_list_entries = 0, last_water_pairs = 0, last_atom_pairs = 0, last_site_pairs = 0;
@@ -192,6 +195,7 @@ struct NbCtx {
     const double *g_coor = nullptr;
     double *g_dpot = nullptr;
     int g_gen = -1, list_gen = 0, graph_launches = 0;
+    int on_prio = 0, g_prio = 0;       // running on the prioritised group streams (now / when captured)
 };
 
 // the public handle is the context itself
@@ -203,6 +207,8 @@ inline int cap_int(int64_t cap) { return cap > 0x7fffffff ? 0x7fffffff : (int)ca
 // ---- launchers implemented in the kernel files -------------------------------------
 // lists (nb_lists.cu)
 void nb_launch_build_lists(NbCtx *c, const double *d_coor);
+// one thread sets the conditional node of a captured evaluation to the device rebuild flag
+void nb_launch_rebuild_cond(NbCtx *c, cudaGraphConditionalHandle h);
 void nb_launch_prepare(NbCtx *c, const double *d_coor, int check);
 void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_total);
 // real space + corrections (nb_realspace.cu)

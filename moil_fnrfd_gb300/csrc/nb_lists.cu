@@ -924,6 +924,21 @@ void prepare_t(NbCtx *c, const double *d_coor, int check)
 
 }  // namespace
 
+namespace {
+// the rebuild decision of a captured evaluation: the IF node around the list rebuild runs its
+// body only when the coordinate preparation (or the host) set the device rebuild flag
+__global__ void k_rebuild_cond(cudaGraphConditionalHandle h, const int *st)
+{
+    cudaGraphSetConditional(h, st[0] != 0 ? 1u : 0u);
+}
+}  // namespace
+
+void nb_launch_rebuild_cond(NbCtx *c, cudaGraphConditionalHandle h)
+{
+    k_rebuild_cond<<<1, 1, 0, c->stream>>>(h, c->d_status);
+    c->launches++;
+}
+
 void nb_launch_build_lists(NbCtx *c, const double *d_coor)
 {
     if (c->precision == MOIL_NB_FP64) build_lists_t<double>(c, d_coor);
