@@ -411,6 +411,8 @@ def main():
     ap.add_argument("--half-block", type=int, default=0, choices=[0, 128, 256],
                     help="waters per block of the half-list water kernel (0: the library's default)")
     ap.add_argument("--no-adj", action="store_true", help="skip the parameter-derivative (adjoint) leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (it runs unless a shape is forced by --groups/--water-kernel/--half-block)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -432,8 +434,12 @@ def main():
     natoms = sum(s.npt for s in reps)
     log(f"workload: {len(reps)} replicas, {natoms} atoms, generated in {time.perf_counter() - t0:.1f} s")
     shape = {"water_kernel": {"auto": 0, "full": 1, "half": 2}[args.water_kernel], "half_block": args.half_block}
+    forced = args.groups != 0 or args.water_kernel != "auto" or args.half_block != 0
+    cache = os.path.join(ROOT, "moil_fnrfd_gb300", "_build", "tune_cache.tsv")
+    t0 = time.perf_counter()
     nb = Nonbonded(reps, precision=MOIL_NB_MIXED, device=local, skin=SKIN, list_period=LIST_PERIOD,
-                   groups=args.groups, shape=shape)
+                   groups=args.groups, shape=shape, tune_cache=None if forced else cache)
+    log(f"handle built in {time.perf_counter() - t0:.1f} s")
     stream = torch.cuda.ExternalStream(nb.stream())
     coor = np.ascontiguousarray(np.concatenate([s.coor for s in reps]), dtype=np.float64)
     d_coor = torch.from_numpy(coor).to(f"cuda:{local}")
@@ -443,6 +449,16 @@ def main():
 
     def step_device():
         nb.eforce_device(d_coor.data_ptr(), d_dpot.data_ptr(), want_energies=False)
+
+    # kernel and list shapes chosen on this batch by the library's autotuner (coordinate
+    # descent over replica groups, water kernel and row build; 2 list periods per candidate)
+    tune = None
+    if not forced and not args.no_tune:
+        t0 = time.perf_counter()
+        tune = nb.autotune(d_coor.data_ptr(), d_dpot.data_ptr(), evals=2 * LIST_PERIOD)
+        tune["seconds"] = time.perf_counter() - t0
+        log(f"autotune: {tune['best']} in {tune['seconds']:.1f} s")
+        stream = torch.cuda.ExternalStream(nb.stream())
 
     for _ in range(args.warmup):
         step_device()
@@ -546,6 +562,8 @@ def main():
            "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": int(coor.nbytes),
                    "d2h_bytes_per_step": int(coor.nbytes + 16 * 8 * len(reps))},
            "clocks": clk, "gpu_launches": launches * args.steps}
+    if tune is not None:
+        out["autotune"] = tune
 
     # energy and gradient errors of the batched evaluation against the oracle (FP64, MOIL's
     # predicate) on a sample of replicas spread over the batch

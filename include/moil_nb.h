@@ -267,6 +267,27 @@ typedef struct {
 int moil_nb_set_shape(moil_nb_ctx *h, const moil_nb_shape *s);
 int moil_nb_get_shape(const moil_nb_ctx *h, moil_nb_shape *s);
 
+/* One timed candidate of moil_nb_autotune. */
+typedef struct {
+    moil_nb_shape shape;          /* as resolved by the handle */
+    double ms_per_eval;           /* wall clock per device-resident evaluation */
+} moil_nb_tune_trial;
+
+/* Autotuner (no counterpart in the reference).  Times `evals` device-resident evaluations
+ * (0: one list period) of each candidate shape on the handle's batch -- the same replicas as
+ * the last moil_nb_init_batch, passed again because the handle is rebuilt for each replica-
+ * group count -- by coordinate descent: groups 1..4, then the water kernel (full lists, half
+ * lists in blocks of 128 or 256 waters), then the water-row build (automatic, cell search,
+ * all-pairs tiles).  d_coor / d_dpot are device buffers of the batch.  The fastest shape
+ * stays applied and is returned in *best; trials (up to max_trials, may be NULL) receive every
+ * candidate timed, *ntrials their number.  With a cache file set (moil_nb_set_tune_cache) the
+ * result is stored under a key made of the GPU model, its multiprocessor count, the
+ * precision, the replica count and the replica-size histogram (power-of-two atom bins), and
+ * moil_nb_init_batch applies a stored shape for a matching batch. */
+int moil_nb_set_tune_cache(moil_nb_ctx *h, const char *path);
+int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const double *d_coor, double *d_dpot,
+                     int evals, moil_nb_shape *best, moil_nb_tune_trial *trials, int max_trials, int *ntrials);
+
 /* ---- PME reciprocal sum without device allocation -------------------------
  * No counterpart in the reference (MOIL's ewald_receip() works on static COMMON
  * arrays and never allocates).  This entry point is for callers that cannot call

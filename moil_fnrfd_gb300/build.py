@@ -1,6 +1,6 @@
 """Build the in-tree CUDA library ``_build/libmoil_nb.so`` for sm_103a with nvcc.
 
-Four translation units are compiled in parallel and linked into one shared
+The translation units are compiled in parallel and linked into one shared
 library that exports the C ABI of ``include/moil_nb.h``.
 """
 from __future__ import annotations
@@ -15,7 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmoil_nb.so")
-SOURCES = ["nb_host.cu", "nb_lists.cu", "nb_realspace.cu", "nb_pme.cu", "nb_adjoint.cu", "nb_md.cu", "nb_press.cu"]
+SOURCES = ["nb_host.cu", "nb_lists.cu", "nb_realspace.cu", "nb_pme.cu", "nb_adjoint.cu", "nb_md.cu", "nb_press.cu",
+           "nb_tune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -1110,6 +1110,7 @@ int moil_nb_init_batch(moil_nb_ctx *h, int nrep, const moil_replica *reps)
         if (!reps[r].params || !reps[r].topo) { h->err = "replica without parameters or topology"; return MOIL_NB_ERR_ARG; }
         natom += reps[r].topo->npt;
     }
+    if (reps) nb_tune_cached_shape(h, nrep, reps);
     const int P = reps ? choose_groups(h, nrep, natom) : 1;
     if (P <= 1) return init_impl(h, nrep, reps);
     if (h->inited) release_device(h);

@@ -191,6 +191,8 @@ struct NbCtx {
     std::vector<int> grp_rep0;         // first replica of each group, then nrep
     std::vector<int64_t> grp_atom0;    // first caller atom of each group, then natom
     int want_groups = 0;               // 0: automatic, 1: none, P: P groups (next init)
+    std::string tune_cache;            // autotuner cache file read by moil_nb_init_batch ("" none)
+    int tuning = 0;                    // moil_nb_autotune is re-initialising the handle
     cudaGraphExec_t gexec = nullptr;
     const double *g_coor = nullptr;
     double *g_dpot = nullptr;
@@ -200,6 +202,9 @@ struct NbCtx {
 
 // the public handle is the context itself
 struct moil_nb_ctx : NbCtx {};
+
+// a cached shape for this batch (nb_tune.cu), applied to h's requested shapes; 1 if found
+int nb_tune_cached_shape(moil_nb_ctx *h, int nrep, const moil_replica *reps);
 
 // list capacity as the int the kernels compare CSR offsets against
 inline int cap_int(int64_t cap) { return cap > 0x7fffffff ? 0x7fffffff : (int)cap; }

@@ -31,7 +31,7 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
             "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "moil_nb_md_step",
-            "moil_nb_set_shape", "moil_nb_get_shape",
+            "moil_nb_set_shape", "moil_nb_get_shape", "moil_nb_set_tune_cache", "moil_nb_autotune",
             "moil_nb_dcd_write", "moil_nb_set_molecules", "moil_nb_pressure", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -76,6 +76,10 @@ SHAPE_KEYS = ("water_kernel", "half_block", "tiled", "groups")
 
 class Shape(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in SHAPE_KEYS]
+
+
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("shape", Shape), ("ms_per_eval", ctypes.c_double)]
 
 
 class MoilNbError(RuntimeError):
@@ -127,6 +131,10 @@ def load(build_if_missing: bool = True):
     L.moil_nb_set_groups.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.moil_nb_set_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(Shape)]
     L.moil_nb_get_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(Shape)]
+    L.moil_nb_set_tune_cache.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    L.moil_nb_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Replica), ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Shape), ctypes.POINTER(TuneTrial),
+                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.moil_nb_md_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                   ctypes.c_double, ctypes.c_int, _dp, ctypes.POINTER(Energies), _dp]
     L.moil_nb_dcd_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
@@ -201,7 +209,7 @@ class Nonbonded:
     """One device handle over one system or a batch of independent replicas."""
 
     def __init__(self, systems, precision=MOIL_NB_MIXED, device=0, skin=1.0, list_period=0,
-                 lj_switch=False, timing=False, groups=0, dtol=None, shape=None):
+                 lj_switch=False, timing=False, groups=0, dtol=None, shape=None, tune_cache=None):
         self.L = load()
         h = ctypes.c_void_p()
         _check(self.L, None, self.L.moil_nb_create(ctypes.byref(h), int(device)))
@@ -209,6 +217,8 @@ class Nonbonded:
         _check(self.L, self.h, self.L.moil_nb_set_groups(self.h, int(groups)))
         if shape is not None:
             self.set_shape(**dict(shape, groups=shape.get("groups", groups)))
+        if tune_cache is not None:
+            _check(self.L, self.h, self.L.moil_nb_set_tune_cache(self.h, str(tune_cache).encode()))
         self.batch = isinstance(systems, (list, tuple))
         self.systems = list(systems) if self.batch else [systems]
         keep = _Keep()
@@ -219,7 +229,8 @@ class Nonbonded:
             reps[k].params = ctypes.pointer(self._params[k])
             reps[k].topo = ctypes.pointer(self._topos[k])
         _check(self.L, self.h, self.L.moil_nb_init_batch(self.h, len(self.systems), reps))
-        del keep
+        # the replica descriptions stay alive: the autotuner rebuilds the handle from them
+        self._reps, self._keep = reps, keep
         self.natom = sum(s.npt for s in self.systems)
         self.offsets = np.cumsum([0] + [s.npt for s in self.systems])
         self._e = (Energies * len(self.systems))()
@@ -278,6 +289,20 @@ class Nonbonded:
         sh = Shape()
         _check(self.L, self.h, self.L.moil_nb_get_shape(self.h, ctypes.byref(sh)))
         return {k: getattr(sh, k) for k in SHAPE_KEYS}
+
+    def autotune(self, d_coor_ptr: int, d_dpot_ptr: int, evals: int = 0) -> dict:
+        """moil_nb_autotune on device buffers of the batch: the chosen shape (applied) and
+        every candidate timed, {"best": shape, "trials": [(shape, ms per evaluation), ...]}."""
+        best = Shape()
+        trials = (TuneTrial * 32)()
+        n = ctypes.c_int()
+        _check(self.L, self.h, self.L.moil_nb_autotune(
+            self.h, len(self.systems), self._reps, ctypes.c_void_p(d_coor_ptr), ctypes.c_void_p(d_dpot_ptr),
+            int(evals), ctypes.byref(best), trials, 32, ctypes.byref(n)))
+        as_dict = lambda sh: {k: getattr(sh, k) for k in SHAPE_KEYS}
+        return {"best": as_dict(best),
+                "trials": [{"shape": as_dict(trials[k].shape), "ms_per_eval": trials[k].ms_per_eval}
+                           for k in range(min(n.value, 32))]}
 
     def set_virial(self, on=True):
         """Accumulate the water-water LJ virial terms on the mixed path (off by default)."""
