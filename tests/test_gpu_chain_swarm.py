@@ -10,8 +10,9 @@ replica of the same topology); e0, sener and dv per image are checked against th
 Swarm of trajectories (dim/dim_sample_MD.f:113-264 runs many short trajectories from one
 milestone): one batch handle steps six uneven water boxes together on the device
 (moil_nb_md_step: evaluation, leapfrog, SETTLE); every replica's final frame is evaluated
-and checked against the oracle, the constraints are held, and each replica's trajectory is
-bit-identical to the same replica stepped alone (the batch couples nothing).
+and checked against the oracle, the constraints are held, and a replica stepped alone follows
+the same trajectory (to 1e-3 Å over 30 steps: only the list-rebuild steps, decided per handle,
+differ).
 
 Tolerances: the mixed path's (relative RMS gradient error <= 1e-5, |dE_total|/|E_total|
 <= 1e-6, each term within 1e-6 of the energy-term scale).
@@ -96,7 +97,10 @@ def test_swarm_final_frames_match_oracle():
         oh = np.linalg.norm(t.coor[1::3] - t.coor[0::3], axis=1)
         assert np.abs(oh - S.TIP3_ROH).max() < 1e-9
     nb.close()
-    # replica 3 stepped alone from the same state ends where it ended in the swarm
+    # replica 3 stepped alone from the same state ends where it ended in the swarm.  Not bit
+    # for bit: a handle rebuilds all its replicas' lists when any site moved more than half
+    # the skin, so the swarm rebuilds at other steps than the lone replica; the pair set is
+    # the same, the FP32 summation order is not
     k = 3
     one = Nonbonded(reps[k], skin=1.5, list_period=10)
     xs = x0[offs[k]:offs[k + 1]].clone()
@@ -104,5 +108,5 @@ def test_swarm_final_frames_match_oracle():
     ms = m[offs[k]:offs[k + 1]].clone()
     torch.cuda.synchronize()
     one.md_step(xs.data_ptr(), vs.data_ptr(), ms.data_ptr(), 0.002, 30)
-    assert torch.equal(xs, x[offs[k]:offs[k + 1]]) and torch.equal(vs, v[offs[k]:offs[k + 1]])
+    assert float((xs - x[offs[k]:offs[k + 1]]).abs().max()) < 1e-3
     one.close()
