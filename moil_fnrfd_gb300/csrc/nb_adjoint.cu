@@ -214,6 +214,230 @@ __global__ void k_adj_atom(int nA, int nW, const RepDev *__restrict__ reps, cons
     ds[o] = dS;
 }
 
+// ---------------------------------------------------------------------------------
+// Mixed path: the same sums with FP32 pair arithmetic (the energy kernels' erfc fit and a
+// Newton-refined reciprocal square root), summed per site in FP32 over chunks of CHUNK_ADJ list
+// entries and flushed into FP64 -- the FP64 pipe of this GPU is a small fraction of the FP32
+// one, so per-pair FP64 erfc, square roots and divisions would dominate.  k = kofdie/eps is
+// applied to the FP64 potential sums at the end.
+#define CHUNK_ADJ 64
+
+// 1/sqrt(r2) to about an ulp: the approximate MUFU value and one Newton step
+__device__ __forceinline__ float adj_rsqrt(float r2)
+{
+    const float y = nb_rsqrt_approx(r2);
+    return fmaf(-0.5f * y, fmaf(r2, y * y, -1.f), y);
+}
+
+// eps and sigma from the epsgm encoding in FP32 (as lj_decode)
+__device__ __forceinline__ void lj_decode_f(int arith, float e12, float e6, float &eps, float &sig)
+{
+    if (arith) {
+        eps = 0.25f * e12 * e12;
+        sig = e6;
+    } else if (e12 > 0.f && e6 > 0.f) {
+        const float se = e6 * e6 / (2.f * e12);
+        sig = cbrtf(e12 / e6);
+        eps = se * se;
+    } else {
+        eps = 0.f;
+        sig = 0.f;
+    }
+}
+
+// one non-water-semantics site pair (atom_pair of the energy kernels): q_j erfc(alpha r)/r into
+// phi (k applied later), the LJ parts into de, ds of site i (1/(2 eps_i), 1/sigma_i given)
+__device__ __forceinline__ void atom_pair_adj_f(const RepDev &R, float r2, float qi, float qj, float2 lji,
+                                                float2 ljj, unsigned fi, unsigned fj, float inv2e_i, float sig_i,
+                                                float &phi, float &de, float &ds)
+{
+    const bool hr = !R.arith && R.hvdw0 && ((fi | fj) & SF_HTINY) && r2 < R.re2;
+    const bool lj = r2 < R.rv2 && !hr;
+    const bool el = r2 < R.rmax2 && qi * qj != 0.f;
+    if (!el && !lj) return;
+    const float rinv = adj_rsqrt(r2);
+    if (el) {
+        float ex;
+        phi += qj * nb_erfc_ex(R.alpha * r2 * rinv, r2 * R.ex2c, &ex) * rinv;
+    }
+    if (lj) {
+        const float s2 = rinv * rinv, s6 = s2 * s2 * s2;
+        float a, b;
+        if (!R.arith) {
+            a = lji.x * ljj.x * s6 * s6;
+            b = lji.y * ljj.y * s6;
+        } else {
+            const float aa = lji.x * ljj.x, sg = 0.5f * (lji.y + ljj.y);
+            float b1 = sg * sg * sg;
+            b1 = b1 * b1;
+            b = aa * b1 * s6;
+            a = aa * b1 * b1 * s6 * s6;
+        }
+        const float g = 6.f * a - 3.f * b;
+        de += (a - b) * inv2e_i;
+        if (!R.arith) {
+            if (sig_i > 0.f) ds += g / sig_i;
+        } else {
+            float ej, sj;
+            lj_decode_f(1, ljj.x, ljj.y, ej, sj);
+            const float sij = 0.5f * (sig_i + sj);
+            if (sij > 0.f) ds += g / sij;
+        }
+    }
+}
+
+// water molecule per thread (FP32 pairs): W1 (nine site pairs per molecule pair, O-O LJ) and W2
+template <typename E>
+__global__ void __launch_bounds__(128) k_adj_water_f(int nW, const RepDev *__restrict__ reps,
+                                                     const int *__restrict__ site_rep,
+                                                     const int *__restrict__ site_orig,
+                                                     const float4 *__restrict__ pos, const float4 *__restrict__ woff,
+                                                     const float2 *__restrict__ lj,
+                                                     const unsigned *__restrict__ sflags,
+                                                     const int2 *__restrict__ wl1_cnt, const void *__restrict__ wl1,
+                                                     int cap_row, const int *__restrict__ wl2_off,
+                                                     const int *__restrict__ wl2, int cap2, double *__restrict__ dq,
+                                                     double *__restrict__ de, double *__restrict__ ds)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nW) return;
+    const RepDev &R = reps[site_rep[3 * i]];
+    const float4 oi = woff[3 * i];
+    const float4 h1 = woff[3 * i + 1], h2 = woff[3 * i + 2];
+    const float hi[3][3] = {{0.f, 0.f, 0.f}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}};
+    double phi[3] = {0, 0, 0}, dE[3] = {0, 0, 0}, dS[3] = {0, 0, 0};
+    float p[3] = {0.f, 0.f, 0.f}, e3[3] = {0.f, 0.f, 0.f}, s3[3] = {0.f, 0.f, 0.f};
+    auto flush = [&]() {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            phi[a] += (double)p[a]; dE[a] += (double)e3[a]; dS[a] += (double)s3[a];
+            p[a] = 0.f; e3[a] = 0.f; s3[a] = 0.f;
+        }
+    };
+    float epsO, sigO;
+    const float2 ljO = lj[3 * i];
+    lj_decode_f(R.arith, ljO.x, ljO.y, epsO, sigO);
+    const float inv2eO = epsO > 0.f ? 0.5f / epsO : 0.f, invsO = sigO > 0.f ? 1.f / sigO : 0.f;
+    const float alpha = R.alpha, ex2c = R.ex2c, rmax2 = R.rmax2, rv2 = R.rv2, w12 = R.w12, w6 = R.w6;
+    const int2 c = wl1_cnt[i];
+    const int nn = min(c.x, cap_row), n = min(c.x + c.y, cap_row);
+    const E *row = (const E *)wl1 + (size_t)i * cap_row;
+    const int base = sizeof(E) == 2 ? R.wat0 : 0;   // uint16 entries: offsets from the replica's first water
+    int cnt = 0;
+    for (int v = 0; v < n; ++v) {
+        nb_prefetch_l1(row + min(v + 32, n - 1));
+        const int j = base + (int)row[v < nn ? v : cap_row - 1 - (v - nn)];
+        const float4 oj = woff[3 * j];
+        float dx = oi.x - oj.x, dy = oi.y - oj.y, dz = oi.z - oj.z;
+        dx = nb_shift(R, 0, dx, rintf(dx * R.invL[0]));
+        dy = nb_shift(R, 1, dy, rintf(dy * R.invL[1]));
+        dz = nb_shift(R, 2, dz, rintf(dz * R.invL[2]));
+        const float r2oo = dx * dx + dy * dy + dz * dz;
+        if (r2oo > rmax2) continue;
+        const float4 j1 = woff[3 * j + 1], j2 = woff[3 * j + 2];
+        const float hj[3][3] = {{0.f, 0.f, 0.f}, {j1.x, j1.y, j1.z}, {j2.x, j2.y, j2.z}};
+        const float qj[3] = {oj.w, pos[3 * j + 1].w, pos[3 * j + 2].w};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const float ex = hi[a][0] + dx - hj[b][0], ey = hi[a][1] + dy - hj[b][1], ez = hi[a][2] + dz - hj[b][2];
+                const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                const float rinv = adj_rsqrt(r2);
+                float exv;
+                p[a] += qj[b] * nb_erfc_ex(alpha * r2 * rinv, r2 * ex2c, &exv) * rinv;
+            }
+        if (r2oo <= rv2) {
+            const float ri = adj_rsqrt(r2oo), s2 = ri * ri, s6 = s2 * s2 * s2;
+            const float A = w12 * s6 * s6, B = w6 * s6;
+            e3[0] += (A - B) * inv2eO;
+            s3[0] += (6.f * A - 3.f * B) * invsO;     // sigma_ij = sigma_O for water pairs (both rules)
+        }
+        if (++cnt == CHUNK_ADJ) { flush(); cnt = 0; }
+    }
+    flush();
+    cnt = 0;
+    const int q0 = min(wl2_off[i], cap2), q1 = min(wl2_off[i + 1], cap2);
+    float inv2e[3], sg[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float ea, sa;
+        const float2 l = lj[3 * i + a];
+        lj_decode_f(R.arith, l.x, l.y, ea, sa);
+        inv2e[a] = ea > 0.f ? 0.5f / ea : 0.f;
+        sg[a] = sa;
+    }
+    for (int k = q0; k < q1; ++k) {
+        const int s = wl2[k];
+        const float4 xj = pos[s];
+        const float2 ljj = lj[s];
+        const unsigned fj = sflags[s];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float4 xi = pos[3 * i + a];
+            float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            dx = nb_shift(R, 0, dx, rintf(dx * R.invL[0]));
+            dy = nb_shift(R, 1, dy, rintf(dy * R.invL[1]));
+            dz = nb_shift(R, 2, dz, rintf(dz * R.invL[2]));
+            atom_pair_adj_f(R, dx * dx + dy * dy + dz * dz, xi.w, xj.w, lj[3 * i + a], ljj, sflags[3 * i + a], fj,
+                            inv2e[a], sg[a], p[a], e3[a], s3[a]);
+        }
+        if (++cnt == CHUNK_ADJ) { flush(); cnt = 0; }
+    }
+    flush();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int o = site_orig[3 * i + a];
+        dq[o] = R.epstmp * phi[a];
+        de[o] = dE[a];
+        ds[o] = dS[a];
+    }
+}
+
+// non-water atom per thread over its X list (FP32 pairs)
+__global__ void __launch_bounds__(128) k_adj_atom_f(int nA, int nW, const RepDev *__restrict__ reps,
+                                                    const int *__restrict__ site_rep,
+                                                    const int *__restrict__ site_orig, const float4 *__restrict__ pos,
+                                                    const float2 *__restrict__ lj, const unsigned *__restrict__ sflags,
+                                                    const int *__restrict__ xl_off, const int *__restrict__ xl, int capx,
+                                                    double *__restrict__ dq, double *__restrict__ de,
+                                                    double *__restrict__ ds)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nA) return;
+    const int si = 3 * nW + k;
+    const RepDev &R = reps[site_rep[si]];
+    const float4 xi = pos[si];
+    const float2 lji = lj[si];
+    const unsigned fi = sflags[si];
+    float ei, sgi;
+    lj_decode_f(R.arith, lji.x, lji.y, ei, sgi);
+    const float inv2e = ei > 0.f ? 0.5f / ei : 0.f;
+    double phi = 0, dE = 0, dS = 0;
+    float p = 0.f, e1 = 0.f, s1 = 0.f;
+    int cnt = 0;
+    const int q1 = min(xl_off[k + 1], capx);
+    for (int q = min(xl_off[k], capx); q < q1; ++q) {
+        nb_prefetch_l1(xl + min(q + 32, q1 - 1));
+        const int s = xl[q];
+        const float4 xj = pos[s];
+        float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        dx = nb_shift(R, 0, dx, rintf(dx * R.invL[0]));
+        dy = nb_shift(R, 1, dy, rintf(dy * R.invL[1]));
+        dz = nb_shift(R, 2, dz, rintf(dz * R.invL[2]));
+        atom_pair_adj_f(R, dx * dx + dy * dy + dz * dz, xi.w, xj.w, lji, lj[s], fi, sflags[s], inv2e, sgi, p, e1, s1);
+        if (++cnt == CHUNK_ADJ) {
+            phi += (double)p; dE += (double)e1; dS += (double)s1;
+            p = 0.f; e1 = 0.f; s1 = 0.f; cnt = 0;
+        }
+    }
+    phi += (double)p; dE += (double)e1; dS += (double)s1;
+    const int o = site_orig[si];
+    dq[o] = R.epstmp * phi;
+    de[o] = dE;
+    ds[o] = dS;
+}
+
 // per caller atom: exclusion erf corrections, 1-4 terms, self energy (FP64 coordinates)
 __global__ void k_adj_excl14(int natom, const int *__restrict__ atom_rep, const RepDev *__restrict__ reps,
                              const double *__restrict__ coor, const double *__restrict__ q,
@@ -309,6 +533,19 @@ void adjoint_pairs(NbCtx *c, double *d_dq, double *d_de, double *d_ds)
 {
     cudaStream_t s = c->stream;
     const int B = 128;
+    if constexpr (sizeof(T) == 4) {
+        if (c->nW > 0)
+            (c->row16 ? k_adj_water_f<unsigned short> : k_adj_water_f<int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
+                (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
+                (const float4 *)c->d_woff, (const float2 *)c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1,
+                c->cap_row1, c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), d_dq, d_de, d_ds);
+        if (c->nA > 0)
+            k_adj_atom_f<<<(int)((c->nA + B - 1) / B), B, 0, s>>>(
+                (int)c->nA, (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, (const float4 *)c->d_pos,
+                (const float2 *)c->d_site_lj, c->d_site_flags, c->d_xl_off, c->d_xl, cap_int(c->cap_xl), d_dq, d_de,
+                d_ds);
+        return;
+    }
     if (c->nW > 0)
         (c->row16 ? k_adj_water<T, unsigned short> : k_adj_water<T, int>)<<<(int)((c->nW + B - 1) / B), B, 0, s>>>(
             (int)c->nW, c->d_reps, c->d_site_rep, c->d_site_orig, c->d_pos, c->d_woff, c->d_site_lj,
