@@ -43,9 +43,15 @@ METRIC = "atom-evals/s mixed+batched vs plain FP64 on 1 GB300 at ≤1e-5 rel RMS
 F_PAIR = 50            # FP32 operations per in-cutoff site pair (FMA = 2, MUFU = 1)
 LIST_PERIOD = 10
 SKIN = 1.0
-# DRAM bytes per water molecule of one k_water_f launch (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum, 48-replica capture: 37.44 MB over 74,171 waters)
-WATER_KERNEL_DRAM_BYTES_PER_WATER = 504.9
+# DRAM bytes per water molecule of one water-kernel launch (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum, 48-replica captures over 74,171 waters): k_water_f (full lists)
+# 37.44 MB, k_water_h (half lists, 256-water blocks) 38.48 MB
+WATER_KERNEL_DRAM_BYTES_PER_WATER = {1: 504.9, 2: 518.8}
+WATER_KERNEL_NAME = {1: "k_water_f (full lists)", 2: "k_water_h (half lists)"}
+# DRAM bytes per atom of one evaluation's PME kernels (k_pme_bin, k_plane_fwd_f, k_zconv_f,
+# k_plane_inv_f, k_pme_gather_f: 5.37 + 4.55 + 10.86 + 10.82 + 15.00 MB, 48-replica capture over
+# 222,513 atoms, caches flushed before each launch, so an upper bound)
+PME_DRAM_BYTES_PER_ATOM = 209.5
 
 
 ACCEL = 418.4                 # (kcal/mol/Å) / amu in Å/ps^2
@@ -528,11 +534,12 @@ def main():
     # both rooflines (the real-space kernel is the dominant one; PME by its HBM model)
     achieved = site_pairs * F_PAIR / (avg["water_ms"] + avg["atom_ms"]) / 1e9   # TFLOP/s
     n_wat = sum(s.nwaters for s in reps)
-    roof_rs = {"kernel": "k_water+k_atom (real space)", "bound": "fp32", "achieved": achieved,
+    wk = nb.shape()["water_kernel"]
+    roof_rs = {"kernel": f"{WATER_KERNEL_NAME[wk]} + k_atom (real space)", "bound": "fp32", "achieved": achieved,
                "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32,
-               "traffic": WATER_KERNEL_DRAM_BYTES_PER_WATER * n_wat,
-               "traffic_note": "bytes per evaluation of k_water_f (all groups): ncu DRAM read+write per water "
-                               "on a 48-replica capture x waters",
+               "traffic": WATER_KERNEL_DRAM_BYTES_PER_WATER[wk] * n_wat,
+               "traffic_note": "bytes per evaluation of the water kernel (all groups): ncu DRAM read+write per "
+                               "water on a 48-replica capture x waters",
                "peak_source": "nominal FP32 FMA peak at the measured max SM clock (152 SMs x 128 lanes x 2); "
                               "MEASURED_PEAKS.json has no FP32 figure",
                "work": f"{site_pairs} unique in-cutoff site pairs x {F_PAIR} FP32 ops per launch"}
@@ -540,9 +547,14 @@ def main():
     ng = sum(s.nfft[0] * s.nfft[1] * s.nfft[2] for s in reps)
     b = 56 * natoms + 64 * ng
     t_pme = (avg["pme_spread_fft_ms"] + avg["pme_conv_ms"] + avg["pme_gather_ms"]) / 1e3
+    traffic_pme = PME_DRAM_BYTES_PER_ATOM * natoms
     roof_pme = {"kernel": "PME (bin+spread+FFT, convolution, gather)", "bound": "hbm",
                 "achieved": b / t_pme / 1e9, "peak": hbm, "unit": "GB/s", "frac": b / t_pme / 1e9 / hbm,
-                "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                "traffic": traffic_pme,
+                "traffic_note": "ncu DRAM read+write of the five PME kernels per atom on a 48-replica capture "
+                                "(cold caches) x atoms; measured DRAM rate at the stage times: "
+                                f"{traffic_pme / t_pme / 1e9:.0f} GB/s",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                 "work": f"56 N + 64 Ng bytes per evaluation = {b} B"}
     roof = roof_rs if dom in ("water_ms", "atom_ms") else roof_pme
 

@@ -305,8 +305,14 @@ int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const d
  *   host     box[3], grid[3] (nfft1..3), *e_recip (energy, kcal/mol)
  *   stream   cudaStream_t as void* (0: the default stream); the call returns after
  *            synchronising it
- * The first call on a device looks up the device address of the array (set-up);
- * make that first call before any stream capture.  Every call reuses the same array
+ * The first call on a device looks up the device address of the array (set-up) and
+ * keeps it for the life of the process: resetting the device afterwards is not
+ * supported.  Make that first call before any stream capture.  No call may be made on
+ * a stream that is being captured into a CUDA graph: every call synchronises its
+ * stream and copies the energy into host memory.  A CUDA error pending when the call
+ * starts, or raised by its launches, is returned as MOIL_NB_ERR_CUDA and left pending;
+ * a grid whose planes do not fit in shared memory is refused with MOIL_NB_ERR_GRID.
+ * Every call reuses the same array
  * and leaves the last call's contents in it (the bin counters are cleared each call,
  * all other regions are rewritten before they are read), so calls that overlap on
  * the GPU -- from two streams or two host threads -- race: serialise them. */

@@ -1492,6 +1492,8 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
             return MOIL_NB_ERR_GRID;
     }
     cudaStream_t stream = (cudaStream_t)stream_v;
+    // an error the caller's own earlier work left pending is reported and left in place
+    if (cudaPeekAtLastError() != cudaSuccess) return MOIL_NB_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return MOIL_NB_ERR_CUDA;
     unsigned char *base = nullptr;
@@ -1507,6 +1509,15 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
         base = g_na_base[dev];
     }
     const int n1 = grid[0], n2 = grid[1], n3 = grid[2];
+    {
+        // the planes of this grid must fit the device's shared memory per block
+        int optin = 0;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+            return MOIL_NB_ERR_CUDA;
+        if (plane_fwd_smem<float>(n1, n2) > (size_t)optin || plane_inv_smem<float>(n1, n2) > (size_t)optin ||
+            zconv_smem<float>(n3) > (size_t)optin)
+            return MOIL_NB_ERR_GRID;
+    }
     // shared-memory limits for this grid (raise only; other handles may need more)
     if (raise_pme_limits<float>(plane_fwd_smem<float>(n1, n2), zconv_smem<float>(n3),
                                 plane_inv_smem<float>(n1, n2)) != cudaSuccess)
@@ -1612,8 +1623,11 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     pme_t<float>(&tmp);
     k_na_grad<<<(natom + 255) / 256, 256, 0, stream>>>(natom, tmp.d_reps, d_q, (const float *)tmp.d_part, d_dpot);
     k_na_energy<<<1, 256, 0, stream>>>((int)tmp.cols.size(), tmp.d_e_col, d_eout);
+    // a launch that failed is reported before waiting for the stream (the error stays pending
+    // for the caller to read)
+    if (cudaPeekAtLastError() != cudaSuccess) return MOIL_NB_ERR_CUDA;
     if (cudaMemcpyAsync(e_recip, d_eout, sizeof(double), cudaMemcpyDeviceToHost, stream) != cudaSuccess)
         return MOIL_NB_ERR_CUDA;
-    if (cudaStreamSynchronize(stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) return MOIL_NB_ERR_CUDA;
+    if (cudaStreamSynchronize(stream) != cudaSuccess || cudaPeekAtLastError() != cudaSuccess) return MOIL_NB_ERR_CUDA;
     return MOIL_NB_OK;
 }

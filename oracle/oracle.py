@@ -190,6 +190,18 @@ def eforce(s, mode: str = "parity", **kw):
     return dpot, output_dict(out)
 
 
+def pme(s, alpha: float, mode: str = "parity", **kw):
+    """PME reciprocal energy and gradient alone (moil_oracle.c ora_pme, ewald_receip's
+    do_pmesh_kspace with the exact FFT): (dpot, e_recip)."""
+    keep = _Keep()
+    inp = make_input(s, mode=mode, keep=keep, **kw)
+    dpot = np.zeros((s.npt, 3), dtype=np.float64)
+    e, f = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    if lib().ora_pme(ctypes.byref(inp), float(alpha), _p(dpot), ctypes.byref(e), ctypes.byref(f)) != 0:
+        raise RuntimeError("oracle pme failed")
+    return dpot, e.value
+
+
 def adjoint(s, mode: str = "parity", **kw):
     """Parameter derivatives of the energy (moil_oracle.c ora_adjoint_mi): per atom dE/dq,
     dE/deps and dE/dsigma, the LJ parameters decoded from the epsgm encoding."""

@@ -1,4 +1,4 @@
-"""The allocation-free PME entry point (moil_nb_pme_noalloc) against the handle path.
+"""The allocation-free PME entry point (moil_nb_pme_noalloc) against the handle path and the oracle.
 
 Some callers cannot allocate device memory (their device memory belongs to another
 runtime's pool, or they cannot take the synchronisation an allocation may cause), so
@@ -37,6 +37,28 @@ def sparse_ion_lattice(seed=5):
                         spec2=np.zeros(0, np.int32), p14=np.zeros((0, 3)),
                         poipt=np.arange(1, n + 1, dtype=np.int32), montype=np.full(n, S.MON_ION, np.int32),
                         box=(L, L, L), rvmx=10.0, relx=10.0, alpha=0.35, nfft=(48, 48, 48))
+
+
+def noalloc_rc(torch, s, natom=None, grid=None):
+    """Status of one call with the given (possibly invalid) sizes, and whether the gradient
+    buffer was left untouched (still NaN)."""
+    L = NB.load()
+    fn = L.moil_nb_pme_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(ctypes.c_int), ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                   ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    n = s.npt if natom is None else natom
+    dc = torch.zeros((max(n, s.npt), 3), dtype=torch.float64, device="cuda")
+    dc[:s.npt] = torch.tensor(s.coor, dtype=torch.float64)
+    dq = torch.zeros(max(n, s.npt), dtype=torch.float64, device="cuda")
+    dd = torch.full_like(dc, float("nan"))
+    torch.cuda.synchronize()
+    box = (ctypes.c_double * 3)(*s.box)
+    g = (ctypes.c_int * 3)(*(grid or s.nfft))
+    e = ctypes.c_double(float("nan"))
+    rc = fn(dc.data_ptr(), dq.data_ptr(), n, box, g, s.alpha, s.eps, dd.data_ptr(), ctypes.byref(e), None)
+    torch.cuda.synchronize()
+    return rc, bool(torch.isnan(dd).all())
 
 
 def noalloc(torch, s):
@@ -81,3 +103,30 @@ def test_noalloc_pme_energy_matches_handle_path_for_water():
     for _ in range(2):
         _, e = noalloc(torch, s)
         assert abs(e - e_ref["e_ew_receip"]) <= 1e-6 * energy_scale(e_ref)
+
+
+def test_noalloc_pme_matches_the_oracle_twice():
+    """The 216-water box against the oracle's reciprocal sum alone (ewald_receip with an exact
+    FFT), on two calls in a row: relative RMS gradient error <= 1e-5 and the energy within 1e-6
+    relative (the mixed path's tolerances)."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as O
+    s = S.config0()
+    ref, e_ref = O.pme(s, s.alpha)
+    for _ in range(2):
+        dpot, e = noalloc(torch, s)
+        assert rel_rms(dpot, ref) <= 1e-5
+        assert abs(e - e_ref) <= 1e-6 * abs(e_ref)
+
+
+def test_noalloc_rejects_sizes_beyond_its_array():
+    """Sizes the fixed array cannot hold are refused before anything runs: the gradient
+    buffer is left as it was."""
+    torch = pytest.importorskip("torch")
+    s = sparse_ion_lattice()
+    ERR_ARG, ERR_GRID = 1, 4          # MOIL_NB_ERR_ARG, MOIL_NB_ERR_GRID (include/moil_nb.h)
+    for kw, want in ((dict(natom=65537), ERR_ARG), (dict(grid=(65, 48, 48)), ERR_GRID),
+                     (dict(grid=(48, 7, 48)), ERR_GRID), (dict(grid=(48, 48, 3)), ERR_GRID)):
+        rc, untouched = noalloc_rc(torch, s, **kw)
+        assert rc == want, (kw, rc)
+        assert untouched, kw
