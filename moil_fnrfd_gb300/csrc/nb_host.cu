@@ -582,6 +582,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     }
     c->cap_row1 = ((int)row1 + 31) & ~31;
     NB_TRY(alloc_lists(c));
+    NB_TRY(nb_realspace_configure(c));
     NB_TRY(setup_half(c));
     NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * NB_EREP * nrep));
     memset(c->h_e_rep, 0, sizeof(double) * NB_EREP * nrep);

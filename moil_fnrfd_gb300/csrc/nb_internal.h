@@ -220,6 +220,8 @@ void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_tota
 void nb_launch_realspace(NbCtx *c);
 // half-list water kernel: dynamic shared memory for c->jcap; MOIL_NB_OK if it fits the device
 int nb_half_configure(NbCtx *c);
+// shared-memory carveouts of the full-list water kernels
+int nb_realspace_configure(NbCtx *c);
 void nb_launch_excl14(NbCtx *c, const double *d_coor);
 // PME (nb_pme.cu)
 void nb_launch_pme(NbCtx *c);

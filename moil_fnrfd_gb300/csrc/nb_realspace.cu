@@ -1201,6 +1201,30 @@ void nb_launch_realspace(NbCtx *c)
     else realspace_t<float>(c);
 }
 
+// shared-memory carveout (percent of the per-SM maximum) for `bytes` of resident blocks
+static int carveout_pct(NbCtx *c, size_t bytes)
+{
+    int smax = 0;
+    if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device) != cudaSuccess || smax <= 0)
+        return 100;
+    return (int)std::min<size_t>(100, (100 * bytes + smax - 1) / smax);
+}
+
+int nb_realspace_configure(NbCtx *c)
+{
+    // full-list FP32 water kernels: four resident blocks of static shared memory each; the
+    // smallest carveout that holds them leaves the most L1 for the partner-record gathers
+    const void *fns[4] = {(const void *)k_water_f<false, unsigned short>, (const void *)k_water_f<false, int>,
+                          (const void *)k_water_f<true, unsigned short>, (const void *)k_water_f<true, int>};
+    for (const void *fn : fns) {
+        cudaFuncAttributes fa;
+        NB_CUDA_OK(c, cudaFuncGetAttributes(&fa, fn));
+        NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                           carveout_pct(c, 4 * fa.sharedSizeBytes)));
+    }
+    return MOIL_NB_OK;
+}
+
 int nb_half_configure(NbCtx *c)
 {
     int optin = 0;
@@ -1216,6 +1240,10 @@ int nb_half_configure(NbCtx *c)
         // may launch it with larger j-sets, so it only ever grows
         if ((int)dyn > fa.maxDynamicSharedSizeBytes)
             NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        // the smallest shared-memory carveout that holds the resident blocks (512 / hb per SM):
+        // the rest of the SM's unified memory stays L1 for the partner-record gathers
+        NB_CUDA_OK(c, cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                           carveout_pct(c, (512 / c->hb) * (dyn + fa.sharedSizeBytes))));
     }
     return MOIL_NB_OK;
 }
