@@ -614,9 +614,12 @@ def main():
                                        f"{max(s.npt for s in sample)} atoms ({sum(s.npt for s in sample)} in all), "
                                        f"one per handle/launch sequence, {LIST_PERIOD} evaluations each "
                                        f"(one list build)",
-                             "note": "a ~5k-atom replica per launch sequence is dominated by fixed per-evaluation "
-                                     "costs (about 30 launches, the list check and the energy read-back); the "
-                                     "96,000-atom FP64 rate is in single_system_md.plain_fp64_atom_evals_per_s"}
+                             "note": "the FP64 water kernel takes 93% of a small replica's evaluation (launch "
+                                     "list of a 2,151-atom replica: 3.4 of 3.7 ms): one water per thread runs "
+                                     "its ~900 FP64 site pairs (erfc, square root, division) in series, and "
+                                     "spreading a replica over 4x more multiprocessors gained 6%, so it is "
+                                     "latency-bound per thread, not launch-bound; the 96,000-atom FP64 rate is "
+                                     "in single_system_md.plain_fp64_atom_evals_per_s"}
         out["speedup_vs_plain_fp64"] = value / fp64_value
         out["force_err_vs_fp64"] = {"max_rel_rms": max(errs), "replicas": len(errs)}
     nb.close()

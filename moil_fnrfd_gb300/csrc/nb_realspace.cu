@@ -195,8 +195,12 @@ struct W1Row {
     __device__ int at(int v) const { return base + (int)*addr(v); }
 };
 
+// Plain FP64 path: one water per thread in blocks of WBLOCK64 (the FP64 pipe of this GPU is a
+// small fraction of the FP32 one, so a replica of a few hundred waters needs every
+// multiprocessor it can get: 32-thread blocks spread it over four times more SMs than 128)
+#define WBLOCK64 32
 template <typename T, typename E>
-__global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
+__global__ void __launch_bounds__(WBLOCK64) k_water(int nW, const RepDev *__restrict__ reps, const int *__restrict__ site_rep,
                                                      const void *pos_v, const void *woff_v, const void *lj_v,
                                                      const unsigned *__restrict__ sflags,
                                                      const int2 *__restrict__ wl1_cnt, const void *__restrict__ wl1,
@@ -204,10 +208,10 @@ __global__ void __launch_bounds__(WBLOCK, sizeof(T) == 4 ? 4 : 2) k_water(int nW
                                                      const int *__restrict__ wl2, int cap2, long long *__restrict__ grad,
                                                      double *__restrict__ e_unit)
 {
-    __shared__ long long sG[9][WBLOCK];
-    __shared__ double sE[6][WBLOCK];
+    __shared__ long long sG[9][WBLOCK64];
+    __shared__ double sE[6][WBLOCK64];
     const int t = threadIdx.x;
-    int i = blockIdx.x * WBLOCK + t;
+    int i = blockIdx.x * WBLOCK64 + t;
     if (i >= nW) return;
     typedef typename vec4<T>::type T4;
     typedef typename cplx<T>::type T2;
@@ -1177,7 +1181,7 @@ void realspace_t(NbCtx *c)
                 c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1, c->d_wl2_off, c->d_wl2,
                 cap_int(c->cap_wl2), c->d_grad_site, c->d_e_unit, c->water_excl_fast);
         else
-            (c->row16 ? k_water<T, unsigned short> : k_water<T, int>)<<<nb, WBLOCK, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
+            (c->row16 ? k_water<T, unsigned short> : k_water<T, int>)<<<(int)((c->nW + WBLOCK64 - 1) / WBLOCK64), WBLOCK64, 0, s>>>((int)c->nW, c->d_reps, c->d_site_rep, c->d_pos, c->d_woff,
                                              c->d_site_lj, c->d_site_flags, c->d_wl1_cnt, c->d_wl1, c->cap_row1,
                                              c->d_wl2_off, c->d_wl2, cap_int(c->cap_wl2), c->d_grad_site,
                                              c->d_e_unit);
