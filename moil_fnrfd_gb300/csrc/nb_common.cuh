@@ -125,6 +125,11 @@ __device__ __forceinline__ void pme_fr_split(double v, int &i, double &w)
 #define SF_WATER 2u
 #define SF_HTINY 4u          // geometric rule: epsgm12 < 1e-3 (pot/nbond.f:115-126)
 
+// a chunk of one replica's per-unit, per-atom or per-column energy partials (the energy
+// reduction): kind 0 water units, 1 other units, 2 atoms, 3 PME column items; [begin, end)
+struct EChunk { int rep, kind, begin, end; };
+#define NB_FE_SEG 4096
+
 // work descriptors for the PME plane / column kernels
 struct PlaneWork { int rep, z; };
 struct ColWork { int rep, kx, ky0; };   // z columns at fixed kx for ky in [ky0, ky0 + tile)

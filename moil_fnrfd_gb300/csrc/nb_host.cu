@@ -92,7 +92,9 @@ void release_device(NbCtx *c)
     c->whalf = 0;
     free_ptr(c->d_bsp); free_ptr(c->d_etab); free_ptr(c->d_zcount); free_ptr(c->d_zstart); free_ptr(c->d_zslot); free_ptr(c->d_zatoms);
     free_ptr(c->d_fr); free_ptr(c->d_grid); free_ptr(c->d_part); free_ptr(c->d_planes); free_ptr(c->d_cols);
-    free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep); free_ptr(c->d_coor); free_ptr(c->d_dpot);
+    free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep);
+    free_ptr(c->d_echunks); free_ptr(c->d_echunk_begin); free_ptr(c->d_epart);
+    c->echunks.clear(); free_ptr(c->d_coor); free_ptr(c->d_dpot);
     free_ptr(c->d_adj); free_ptr(c->d_adj_phi); free_ptr(c->d_md_dpot);
     free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
     free_ptr(c->d_xsite); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
@@ -229,6 +231,34 @@ int setup_half(NbCtx *c)
     c->jcap = std::min(maxw, 7 * c->hb);
     c->need_rebuild = 1;
     return alloc_half(c);
+}
+
+// The energy reduction's fixed partition: per replica its water units, other units, atoms
+// (skipped on the mixed path for a replica of waters whose corrections the water kernel adds)
+// and PME column items, in chunks of NB_FE_SEG counted from the replica's own start (so a
+// replica reduces in the same order alone, in a batch or in a replica group).
+int setup_energy_chunks(NbCtx *c, int water_fast)
+{
+    c->echunks.clear();
+    std::vector<int> begin(c->nrep + 1, 0);
+    auto add = [&](int r, int kind, int64_t b, int64_t e) {
+        for (int64_t x = b; x < e; x += NB_FE_SEG)
+            c->echunks.push_back(EChunk{r, kind, (int)x, (int)std::min<int64_t>(x + NB_FE_SEG, e)});
+    };
+    const bool skip_ex = c->precision != MOIL_NB_FP64 && water_fast;
+    for (int r = 0; r < c->nrep; ++r) {
+        const RepDev &R = c->rd[r];
+        begin[r] = (int)c->echunks.size();
+        add(r, 0, R.wat0, (int64_t)R.wat0 + R.nwat);
+        add(r, 1, c->nW + R.oth0, c->nW + (int64_t)R.oth0 + R.noth);
+        if (!(skip_ex && R.noth == 0 && R.nwat > 0)) add(r, 2, R.atom0, (int64_t)R.atom0 + R.natom);
+        add(r, 3, c->col_begin[r], c->col_begin[r + 1]);
+    }
+    begin[c->nrep] = (int)c->echunks.size();
+    NB_TRY(upload(c, c->d_echunks, c->echunks));
+    NB_TRY(upload(c, c->d_echunk_begin, begin));
+    NB_CUDA_OK(c, cudaMalloc(&c->d_epart, sizeof(double) * NB_EU * std::max<size_t>(c->echunks.size(), 1)));
+    return MOIL_NB_OK;
 }
 
 int alloc_lists(NbCtx *c)
@@ -587,6 +617,7 @@ int init_impl(NbCtx *c, int nrep, const moil_replica *reps)
     NB_CUDA_OK(c, cudaMallocHost(&c->h_e_rep, sizeof(double) * NB_EREP * nrep));
     memset(c->h_e_rep, 0, sizeof(double) * NB_EREP * nrep);
     NB_TRY(nb_pme_configure(c));
+    NB_TRY(setup_energy_chunks(c, water_fast));
     {
         // tile sums for every scan: bins, per-water and per-atom counts, PME z-bins
         int64_t nmax = std::max<int64_t>({2 * (int64_t)c->ncell, c->nW, c->nA, (int64_t)c->nzbin, 1});

@@ -144,6 +144,10 @@ struct NbCtx {
     int max_n1 = 0, max_n2 = 0, max_n3 = 0;
 
     // energies
+    std::vector<EChunk> echunks;       // fixed partition of the energy partials (k_energy_part)
+    EChunk *d_echunks = nullptr;
+    int *d_echunk_begin = nullptr;     // first chunk of each replica, then the count
+    double *d_epart = nullptr;         // NB_EU slot sums per chunk
     double *d_e_rep = nullptr;         // nrep * 16
     double *h_e_rep = nullptr;         // pinned mirror
 

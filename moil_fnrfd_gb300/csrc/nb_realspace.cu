@@ -1076,86 +1076,90 @@ __global__ void k_final_grad(int natom, const int *__restrict__ site_of, const i
     if (bad) atomicOr(&st[1], NB_DEV_ERR_NAN);
 }
 
-// Per-replica energies, one block of NB_FE_THREADS (a multiple of 32, of NB_EU and of 3) per
-// replica: every thread streams the replica's flat per-unit and per-atom arrays with a stride
-// that keeps its slot fixed, so the reads are coalesced and each thread adds one slot; the
-// slots are then summed in a fixed order (deterministic).
-#define NB_FE_THREADS 384
-__global__ void __launch_bounds__(NB_FE_THREADS) k_final_energy(int nW, const RepDev *__restrict__ reps,
-                                                                const double *__restrict__ e_unit,
-                                                                const double *__restrict__ e_ex,
-                                                                const double *__restrict__ e_col,
-                                                                const int *__restrict__ col_begin,
-                                                                int water_ex_zero, double *__restrict__ e_rep)
+// Per-replica energies in two passes with a fixed partition, so large replicas spread over
+// many blocks and the sums stay in a fixed order (deterministic):
+//  k_energy_part: one block per chunk (EChunk: up to NB_FE_SEG consecutive units, atoms or PME
+//    column items of one replica); every thread streams the chunk's flat array with a stride
+//    that keeps its slot fixed (coalesced reads), the slots are summed by a halving tree;
+//  k_energy_final: one thread per replica adds its chunks' slot sums in chunk order and forms
+//    MOIL's energy names (pot/eforce.f:122-204).
+#define NB_FE_THREADS 256
+static_assert(NB_FE_THREADS % NB_EU == 0 && NB_FE_THREADS % NB_EX == 0, "slot-preserving stride");
+__global__ void __launch_bounds__(NB_FE_THREADS) k_energy_part(const EChunk *__restrict__ chunks,
+                                                               const double *__restrict__ e_unit,
+                                                               const double *__restrict__ e_ex,
+                                                               const double *__restrict__ e_col,
+                                                               double *__restrict__ part)
 {
-    static_assert(NB_FE_THREADS % NB_EU == 0 && NB_FE_THREADS % NB_EX == 0, "slot-preserving stride");
     __shared__ double sh[NB_FE_THREADS];
-    __shared__ double part[2 * NB_EU + NB_EX + 1];   // water units, other units, atoms, columns
-    const int r = blockIdx.x, t = threadIdx.x;
-    const RepDev &R = reps[r];
-    // units: the replica's waters, then its other units, NB_EU doubles each; eight loads in
-    // flight per thread (eight partial sums, added in a fixed order)
-    auto stream_sum = [t](const double *__restrict__ b, int n) {
-        double p[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        int k = t;
-        for (; k + 7 * NB_FE_THREADS < n; k += 8 * NB_FE_THREADS) {
+    const int t = threadIdx.x;
+    const EChunk ch = chunks[blockIdx.x];
+    const int width = ch.kind <= 1 ? NB_EU : (ch.kind == 2 ? NB_EX : 1);
+    const double *b = ch.kind <= 1 ? e_unit + (size_t)NB_EU * ch.begin
+                                   : (ch.kind == 2 ? e_ex + (size_t)NB_EX * ch.begin : e_col + ch.begin);
+    const int n = width * (ch.end - ch.begin);
+    // four loads in flight per thread, four partial sums added in a fixed order
+    double p[4] = {0.0, 0.0, 0.0, 0.0};
+    int k = t;
+    for (; k + 3 * NB_FE_THREADS < n; k += 4 * NB_FE_THREADS) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) p[j] += b[k + j * NB_FE_THREADS];
-        }
-#pragma unroll
-        for (int j = 0; j < 7; ++j)
-            if (k + j * NB_FE_THREADS < n) p[j] += b[k + j * NB_FE_THREADS];
-        return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
-    };
-    const double uw = stream_sum(e_unit + NB_EU * (size_t)R.wat0, NB_EU * R.nwat);
-    const double uo = stream_sum(e_unit + NB_EU * ((size_t)nW + R.oth0), NB_EU * R.noth);
-    // per-atom corrections: none in a replica of waters whose corrections the water kernel added
-    double x = (water_ex_zero && R.noth == 0) ? 0.0 : stream_sum(e_ex + NB_EX * (size_t)R.atom0, NB_EX * R.natom);
-    double cl = 0.0;
-    for (int w = col_begin[r] + t; w < col_begin[r + 1]; w += NB_FE_THREADS) cl += e_col[w];
-    // slot sums by halving trees (fixed order): while the live range halves into a multiple
-    // of the slot count, thread k adds k + half, which holds the same slot; the few left
-    // are added serially
-    auto tree = [&](double v, int width, double *out) {
-        sh[t] = v;
-        __syncthreads();
-        int live = NB_FE_THREADS;
-        while (live % 2 == 0 && (live / 2) % width == 0) {
-            const int h = live / 2;
-            if (t < h) sh[t] += sh[t + h];
-            __syncthreads();
-            live = h;
-        }
-        if (t < width) {
-            double w = 0.0;
-            for (int k = t; k < live; k += width) w += sh[k];
-            out[t] = w;
-        }
-        __syncthreads();
-    };
-    tree(uw, NB_EU, part);
-    tree(uo, NB_EU, part + NB_EU);
-    tree(x, NB_EX, part + 2 * NB_EU);
-    tree(cl, 1, part + 2 * NB_EU + NB_EX);
-    if (t == 0) {
-        const double *pw = part, *po = part + NB_EU, *px = part + 2 * NB_EU;
-        const double elp = 0.5 * (pw[0] + po[0]), eli = 0.5 * (pw[1] + po[1]);
-        const double eep = 0.5 * (pw[2] + po[2]), eei = 0.5 * (pw[3] + po[3]);
-        const double npairs = 0.5 * (pw[4] + po[4]);
-        // waters relative to the reference water (k_wref) add their reference energy here
-        const double ecorr = px[0] + pw[5] + po[5] + (R.wref ? (double)R.nwat * R.wcorr0 : 0.0);
-        const double eel14 = px[1], evdw14 = px[2];
-        const double erec = 0.5 * part[2 * NB_EU + NB_EX];
-        double *o = e_rep + NB_EREP * (size_t)r;
-        o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym
-        o[4] = eel14; o[5] = evdw14; o[6] = ecorr; o[7] = R.e_self; o[8] = erec;
-        o[9] = elp + eep + eli + eei + eel14 + evdw14 + ecorr + R.e_self + erec;
-        o[10] = eep + eei;
-        o[11] = npairs;                                           // in-cutoff site pairs
-        // LJ virial terms virvdw1..5 (MOIL's PRESS build): water-water primary and images,
-        // other pairs primary and images, 1-4
-        o[12] = 0.5 * pw[6]; o[13] = 0.5 * pw[7]; o[14] = 0.5 * po[6]; o[15] = 0.5 * po[7]; o[16] = px[3];
+        for (int j = 0; j < 4; ++j) p[j] += b[k + j * NB_FE_THREADS];
     }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+        if (k + j * NB_FE_THREADS < n) p[j] += b[k + j * NB_FE_THREADS];
+    sh[t] = (p[0] + p[1]) + (p[2] + p[3]);
+    __syncthreads();
+    // halving tree while the live range halves into a multiple of the slot width (thread k
+    // adds k + half, which holds the same slot)
+    int live = NB_FE_THREADS;
+    while (live % 2 == 0 && (live / 2) % width == 0) {
+        const int h = live / 2;
+        if (t < h) sh[t] += sh[t + h];
+        __syncthreads();
+        live = h;
+    }
+    if (t < NB_EU) {
+        double w = 0.0;
+        if (t < width)
+            for (int q = t; q < live; q += width) w += sh[q];
+        part[(size_t)NB_EU * blockIdx.x + t] = w;
+    }
+}
+
+__global__ void k_energy_final(int nrep, const RepDev *__restrict__ reps, const EChunk *__restrict__ chunks,
+                               const int *__restrict__ chunk_begin, const double *__restrict__ part,
+                               double *__restrict__ e_rep)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrep) return;
+    const RepDev &R = reps[r];
+    double pw[NB_EU] = {0, 0, 0, 0, 0, 0, 0, 0}, po[NB_EU] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double px[NB_EX] = {0, 0, 0, 0}, cl = 0.0;
+    for (int c = chunk_begin[r]; c < chunk_begin[r + 1]; ++c) {
+        const double *q = part + (size_t)NB_EU * c;
+        const int kind = chunks[c].kind;
+        if (kind == 0) { for (int k = 0; k < NB_EU; ++k) pw[k] += q[k]; }
+        else if (kind == 1) { for (int k = 0; k < NB_EU; ++k) po[k] += q[k]; }
+        else if (kind == 2) { for (int k = 0; k < NB_EX; ++k) px[k] += q[k]; }
+        else cl += q[0];
+    }
+    const double elp = 0.5 * (pw[0] + po[0]), eli = 0.5 * (pw[1] + po[1]);
+    const double eep = 0.5 * (pw[2] + po[2]), eei = 0.5 * (pw[3] + po[3]);
+    const double npairs = 0.5 * (pw[4] + po[4]);
+    // waters relative to the reference water (k_wref) add their reference energy here
+    const double ecorr = px[0] + pw[5] + po[5] + (R.wref ? (double)R.nwat * R.wcorr0 : 0.0);
+    const double eel14 = px[1], evdw14 = px[2];
+    const double erec = 0.5 * cl;
+    double *o = e_rep + NB_EREP * (size_t)r;
+    o[0] = elp; o[1] = eep; o[2] = eli; o[3] = eei;          // e_vdw, e_el, e_vsym, e_lsym
+    o[4] = eel14; o[5] = evdw14; o[6] = ecorr; o[7] = R.e_self; o[8] = erec;
+    o[9] = elp + eep + eli + eei + eel14 + evdw14 + ecorr + R.e_self + erec;
+    o[10] = eep + eei;
+    o[11] = npairs;                                           // in-cutoff site pairs
+    // LJ virial terms virvdw1..5 (MOIL's PRESS build): water-water primary and images,
+    // other pairs primary and images, 1-4
+    o[12] = 0.5 * pw[6]; o[13] = 0.5 * pw[7]; o[14] = 0.5 * po[6]; o[15] = 0.5 * po[7]; o[16] = px[3];
 }
 
 template <typename T>
@@ -1280,8 +1284,9 @@ void nb_launch_finalize(NbCtx *c, double *d_dpot)
         k_final_grad<float><<<(int)((c->natom + 255) / 256), 256, 0, s>>>(
             (int)c->natom, c->d_site_of, c->d_atom_rep, c->d_reps, c->d_grad_site, c->d_grad_ex,
             (const float *)c->d_part, c->d_q, c->water_excl_fast ? (int)(3 * c->nW) : 0, d_dpot, c->d_status);
-    k_final_energy<<<c->nrep, NB_FE_THREADS, 0, s>>>(
-        (int)c->nW, c->d_reps, c->d_e_unit, c->d_e_ex, c->d_e_col, c->d_col_begin,
-        c->precision != MOIL_NB_FP64 && c->water_excl_fast, c->d_e_rep);
-    c->launches += 2;
+    k_energy_part<<<(int)c->echunks.size(), NB_FE_THREADS, 0, s>>>(c->d_echunks, c->d_e_unit, c->d_e_ex, c->d_e_col,
+                                                                    c->d_epart);
+    k_energy_final<<<(c->nrep + 127) / 128, 128, 0, s>>>(c->nrep, c->d_reps, c->d_echunks, c->d_echunk_begin,
+                                                         c->d_epart, c->d_e_rep);
+    c->launches += 3;
 }
