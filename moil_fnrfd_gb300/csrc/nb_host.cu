@@ -95,7 +95,8 @@ void release_device(NbCtx *c)
     free_ptr(c->d_col_begin); free_ptr(c->d_e_col); free_ptr(c->d_e_rep);
     free_ptr(c->d_echunks); free_ptr(c->d_echunk_begin); free_ptr(c->d_epart);
     c->echunks.clear(); free_ptr(c->d_coor); free_ptr(c->d_dpot);
-    free_ptr(c->d_adj); free_ptr(c->d_adj_phi); free_ptr(c->d_md_dpot);
+    free_ptr(c->d_adj); free_ptr(c->d_adj_phi); free_ptr(c->d_md_dpot); free_ptr(c->d_mdctl);
+    free_ptr(c->d_md_save);
     free_ptr(c->d_mol_off); free_ptr(c->d_mol_atom); free_ptr(c->d_mass); free_ptr(c->d_xrel);
     free_ptr(c->d_xsite); free_ptr(c->d_press_unit); free_ptr(c->d_press_site); free_ptr(c->d_press_col); free_ptr(c->d_press_grid);
     free_ptr(c->d_press_out);
@@ -104,6 +105,8 @@ void release_device(NbCtx *c)
     c->h_e_rep = nullptr;
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
+    if (c->gexec_md) cudaGraphExecDestroy(c->gexec_md);
+    c->gexec_md = nullptr;
     c->inited = 0;
 }
 
@@ -682,12 +685,11 @@ bool enqueue_lists_conditional(NbCtx *c, const double *d_coor)
 // state beyond the handle's fixed buffers and the two caller pointers: the rebuild decision
 // travels through the pinned word h_status[8], read by the first copy.  That makes it
 // capturable as a CUDA graph.
-void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
+// The evaluation between its status words: coordinate preparation, list rebuild, pair, PME
+// and correction kernels, gradient and energy assembly.
+void enqueue_core(NbCtx *c, const double *d_coor, double *d_dpot)
 {
     cudaStream_t s = c->stream;
-    c->launches = 0;
-    if (c->timing) cudaEventRecord(c->ev[0], s);
-    cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 8, cudaMemcpyHostToDevice, s);
     nb_launch_prepare(c, d_coor, 1);   // sets the rebuild flag when a site moved > skin/2
     // every rebuild kernel is gated by the flag; a captured evaluation also skips their
     // launches through a conditional node
@@ -730,15 +732,39 @@ void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
         cudaStreamWaitEvent(s, c->ev_join, 0);
     }
     nb_launch_finalize(c, d_dpot);
+}
+
+void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
+{
+    cudaStream_t s = c->stream;
+    c->launches = 0;
+    if (c->timing) cudaEventRecord(c->ev[0], s);
+    cudaMemcpyAsync(c->d_status, c->h_status + 8, sizeof(int) * 8, cudaMemcpyHostToDevice, s);
+    enqueue_core(c, d_coor, d_dpot);
     if (c->timing) cudaEventRecord(c->ev[10], s);
     cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(c->h_e_rep, c->d_e_rep, sizeof(double) * NB_EREP * c->nrep, cudaMemcpyDeviceToHost, s);
+}
+
+// one whole MD step of a context, as captured into its step graph: the step-control kernel,
+// the evaluation, the error bits and rebuild counter, the leapfrog + SETTLE integrator
+void enqueue_md_step(NbCtx *c, double *coor, double *vel, const double *mass, double *dpot, double dt, double doh,
+                     double dhh)
+{
+    cudaStream_t s = c->stream;
+    c->launches = 0;
+    nb_launch_md_begin(c, s);
+    enqueue_core(c, coor, dpot);
+    nb_launch_md_end(c, s);
+    nb_launch_integrate(c, s, coor, vel, mass, dpot, dt, doh, dhh);
 }
 
 void drop_graph(NbCtx *c)
 {
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
+    if (c->gexec_md) cudaGraphExecDestroy(c->gexec_md);
+    c->gexec_md = nullptr;
 }
 
 // replay the captured evaluation, capturing it first when the caller pointers or the list
@@ -1546,3 +1572,49 @@ void eforce_nb_press_gpu_(const int *npt, const double *coor, double *dpot, doub
 }
 
 }  // extern "C"
+
+// ---- device-side MD step loop (moil_nb_md_step) -----------------------------------------
+void read_energies_of(NbCtx *c, moil_energies *e) { read_energies(c, e); }
+
+int nb_md_loop(NbCtx *c, double *coor, double *vel, const double *mass, double *dpot, double dt, double doh,
+               double dhh, int nsteps)
+{
+    cudaStream_t s = c->stream;
+    if (!c->d_mdctl) NB_CUDA_OK(c, cudaMalloc(&c->d_mdctl, sizeof(int) * 4));
+    // the host's list schedule goes to the device once per call
+    c->h_status[17] = c->evals_since_build;
+    c->h_status[18] = c->need_rebuild ? 1 : 0;
+    c->h_status[19] = 0;
+    NB_CUDA_OK(c, cudaMemcpyAsync(c->d_mdctl, c->h_status + 17, sizeof(int) * 3, cudaMemcpyHostToDevice, s));
+    const bool same = c->gexec_md && c->gmd_key[0] == coor && c->gmd_key[1] == vel && c->gmd_key[2] == mass &&
+                      c->gmd_dt == dt && c->gmd_doh == doh && c->gmd_dhh == dhh && c->gmd_gen == c->list_gen &&
+                      c->gmd_dpot == dpot;
+    if (!same) {
+        if (c->gexec_md) cudaGraphExecDestroy(c->gexec_md);
+        c->gexec_md = nullptr;
+        cudaGraph_t g = nullptr;
+        NB_CUDA_OK(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        c->capturing = 1;
+        enqueue_md_step(c, coor, vel, mass, dpot, dt, doh, dhh);
+        c->capturing = 0;
+        cudaError_t e1 = cudaStreamEndCapture(s, &g);
+        cudaError_t e2 = e1 == cudaSuccess ? cudaGraphInstantiate(&c->gexec_md, g, 0) : e1;
+        if (g) cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) {
+            c->gexec_md = nullptr;
+            c->err = std::string("capturing the MD step graph: ") + cudaGetErrorString(e2);
+            return MOIL_NB_ERR_CUDA;
+        }
+        c->gmd_key[0] = coor; c->gmd_key[1] = vel; c->gmd_key[2] = mass;
+        c->gmd_dpot = dpot;
+        c->gmd_dt = dt; c->gmd_doh = doh; c->gmd_dhh = dhh;
+        c->gmd_gen = c->list_gen;
+    }
+    for (int k = 0; k < nsteps; ++k) NB_CUDA_OK(c, cudaGraphLaunch(c->gexec_md, s));
+    // the last step's status words and energies, and the step control, in one wait
+    NB_CUDA_OK(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
+    NB_CUDA_OK(c, cudaMemcpyAsync(c->h_e_rep, c->d_e_rep, sizeof(double) * NB_EREP * c->nrep,
+                                  cudaMemcpyDeviceToHost, s));
+    NB_CUDA_OK(c, cudaMemcpyAsync(c->h_status + 20, c->d_mdctl, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+    return MOIL_NB_OK;
+}

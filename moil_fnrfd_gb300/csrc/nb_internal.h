@@ -156,6 +156,17 @@ struct NbCtx {
     double *d_adj = nullptr;           // parameter derivatives, 3 x natom (allocated on first use)
     double *d_adj_phi = nullptr;       // plain path: PME potential share of 4 planes per site (first use)
     double *d_md_dpot = nullptr;       // gradient of the MD steps (moil_nb_md_step, first use)
+    // device-side MD step loop (moil_nb_md_step): one graph per context holds a whole step
+    // (evaluation, then leapfrog + SETTLE); d_mdctl = {evaluations since the last rebuild,
+    // rebuild requested, sticky error bits}, read back once per call
+    cudaGraphExec_t gexec_md = nullptr;
+    const void *gmd_key[3] = {nullptr, nullptr, nullptr};
+    double gmd_dt = 0.0, gmd_doh = 0.0, gmd_dhh = 0.0;
+    int gmd_gen = -1;
+    double *gmd_dpot = nullptr;
+    int *d_mdctl = nullptr;
+    double *d_md_save = nullptr;       // the call's starting coordinates and velocities (the
+                                       // per-step path redoes the call from them after an error)
 
     // pressure analysis (moil_nb_set_molecules / moil_nb_pressure, nb_press.cu)
     int nmol = 0;
@@ -174,7 +185,8 @@ struct NbCtx {
     // start of every evaluation
     int *d_status = nullptr;
     int *h_status = nullptr;           // pinned: [0..7] mirror, [8..15] initial words of an evaluation,
-                                       // [16] the rebuild flag read back in stage-timing mode
+                                       // [16] the rebuild flag read back in stage-timing mode,
+                                       // [17..19] / [20..22] MD step control written / read back
     int need_rebuild = 1;
     int evals_since_build = 0;
     int64_t last_list_entries = 0, last_water_pairs = 0, last_atom_pairs = 0, last_site_pairs = 0;
@@ -241,6 +253,16 @@ void nb_pme_fp32_consts(RepDev *R);
 void nb_pme_etab(const RepDev &R, const double *bsp, float *out);
 // finalize (nb_realspace.cu)
 void nb_launch_finalize(NbCtx *c, double *d_dpot);
+// MD step loop (nb_md.cu / nb_host.cu): the step-control kernels around an evaluation, the
+// integrator of one context, and the graph replay of nsteps whole steps (no host wait)
+void nb_launch_md_begin(NbCtx *c, cudaStream_t s);
+void nb_launch_md_end(NbCtx *c, cudaStream_t s);
+int nb_launch_integrate(NbCtx *c, cudaStream_t s, double *coor, double *vel, const double *mass, const double *dpot,
+                        double dt, double doh, double dhh);
+int nb_md_loop(NbCtx *c, double *coor, double *vel, const double *mass, double *dpot, double dt, double doh,
+               double dhh, int nsteps);
+// per-replica energies and pair count of the last completed evaluation (e may be NULL)
+void read_energies_of(NbCtx *c, moil_energies *e);
 // parameter derivatives after an evaluation of c->d_coor (nb_adjoint.cu), mixed path
 int nb_adjoint(NbCtx *c, double *d_dq, double *d_de, double *d_ds);
 // pressure analysis terms after an evaluation of d_coor (nb_press.cu): 12 per replica

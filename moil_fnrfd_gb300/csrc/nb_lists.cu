@@ -185,9 +185,12 @@ __global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, con
             double x[3][3];
 #pragma unroll
             for (int m = 0; m < 3; ++m) load_atom(coor, a + m, x[m], st);
+            // only the oxygen's displacement counts: every water list is built from oxygen
+            // distances with radii that include the hydrogens' reach (rwat, checked below)
 #pragma unroll
             for (int m = 0; m < 3; ++m)
-                prepare_site<T>(3 * u + m, x[m], site_flags, site_q, pos_v, posb, half_skin2, snapshot, moved);
+                prepare_site<T>(3 * u + m, x[m], site_flags, site_q, pos_v, posb, m == 0 ? half_skin2 : 3.0e38f,
+                                snapshot, moved);
             // the molecule record of the water kernel: O position (and charge), then the offsets
             ((T4 *)woff_v)[3 * u] = ((const T4 *)pos_v)[3 * u];
 #pragma unroll

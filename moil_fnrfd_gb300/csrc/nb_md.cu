@@ -138,6 +138,24 @@ __global__ void __launch_bounds__(256) k_kinetic(int natom, const double *__rest
     if (threadIdx.x == 0) part[blockIdx.x] = sh[0] / kAccel;
 }
 
+// Step control of the device-side step loop (d_mdctl = {evaluations since the last rebuild,
+// rebuild requested, sticky error bits}).  Before an evaluation: the status words the host
+// writes before a normal evaluation, with the rebuild forced when the list period is reached
+// or a rebuild was requested (the skin check of the coordinate preparation adds its own).
+__global__ void k_md_begin(int *__restrict__ st, int *__restrict__ ctl, int list_period)
+{
+    st[0] = (ctl[1] || (list_period > 0 && ctl[0] >= list_period)) ? 1 : 0;
+    for (int k = 1; k < 8; ++k) st[k] = 0;
+    ctl[1] = 0;
+}
+// after it: the error bits kept across steps, the rebuild counter advanced
+__global__ void k_md_end(const int *__restrict__ st, int *__restrict__ ctl)
+{
+    if (st[0]) ctl[0] = 0;
+    ctl[0] += 1;
+    ctl[2] |= st[1];
+}
+
 // the integrator kernels of one (ungrouped) context over its caller-atom range
 int integrate(NbCtx *c, cudaStream_t s, double *coor, double *vel, const double *mass, const double *dpot,
               double dt, double doh, double dhh)
@@ -151,6 +169,28 @@ int integrate(NbCtx *c, cudaStream_t s, double *coor, double *vel, const double 
     NB_CUDA_OK(c, cudaGetLastError());
     return MOIL_NB_OK;
 }
+
+}  // namespace
+
+void nb_launch_md_begin(NbCtx *c, cudaStream_t s)
+{
+    k_md_begin<<<1, 1, 0, s>>>(c->d_status, c->d_mdctl, c->list_period);
+    c->launches++;
+}
+
+void nb_launch_md_end(NbCtx *c, cudaStream_t s)
+{
+    k_md_end<<<1, 1, 0, s>>>(c->d_status, c->d_mdctl);
+    c->launches++;
+}
+
+int nb_launch_integrate(NbCtx *c, cudaStream_t s, double *coor, double *vel, const double *mass, const double *dpot,
+                        double dt, double doh, double dhh)
+{
+    return integrate(c, s, coor, vel, mass, dpot, dt, doh, dhh);
+}
+
+namespace {
 
 void put_record(FILE *f, const void *data, uint32_t bytes)
 {
@@ -174,7 +214,65 @@ int moil_nb_md_step(moil_nb_ctx *h, double *d_coor, double *d_vel, const double 
     const double dhh = water_geom ? water_geom[1] : 2.0 * 0.9572 * sin(104.52 * M_PI / 360.0);
     const size_t n = (size_t)h->natom;
     if (!h->d_md_dpot) NB_CUDA_OK(h, cudaMalloc(&h->d_md_dpot, sizeof(double) * 3 * std::max<size_t>(n, 1)));
-    for (int step = 0; step < nsteps; ++step) {
+    // Device-side loop: every context replays a graph of whole steps nsteps times with no host
+    // wait between them; the error bits are read once at the end.  Any error (a list overflow
+    // to regrow, a non-finite coordinate) sends the call back to the saved state and through
+    // the per-step path below, which handles it as a single evaluation does.
+    int first = 0;
+    const bool loop = nsteps > 1 && h->use_graph && !h->timing;
+    if (loop) {
+        if (!h->d_md_save) NB_CUDA_OK(h, cudaMalloc(&h->d_md_save, sizeof(double) * 6 * std::max<size_t>(n, 1)));
+        NB_CUDA_OK(h, cudaMemcpyAsync(h->d_md_save, d_coor, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, h->stream));
+        NB_CUDA_OK(h, cudaMemcpyAsync(h->d_md_save + 3 * n, d_vel, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice,
+                                      h->stream));
+        std::vector<NbCtx *> ctxs;
+        if (h->grp.empty()) ctxs.push_back(h);
+        else for (NbCtx *c : h->grp) ctxs.push_back(c);
+        int rc = MOIL_NB_OK;
+        for (size_t g = 0; g < ctxs.size() && rc == MOIL_NB_OK; ++g) {
+            NbCtx *c = ctxs[g];
+            const int64_t a0 = h->grp.empty() ? 0 : h->grp_atom0[g];
+            if (c != h) {
+                NB_CUDA_OK(h, cudaEventRecord(h->ev[11], h->stream));            // the snapshot copies
+                NB_CUDA_OK(h, cudaStreamWaitEvent(c->stream, h->ev[11], 0));
+            }
+            rc = nb_md_loop(c, d_coor + 3 * a0, d_vel + 3 * a0, d_mass + a0, h->d_md_dpot + 3 * a0, dt, doh, dhh,
+                            nsteps);
+        }
+        int err = 0;
+        for (NbCtx *c : ctxs) {
+            NB_CUDA_OK(h, cudaStreamSynchronize(c->stream));
+            if (rc == MOIL_NB_OK) {
+                err |= c->h_status[22];
+                if (!c->h_status[22]) {
+                    // the host's view of the list schedule, pair counts and energies
+                    c->evals_since_build = c->h_status[20];
+                    c->need_rebuild = 0;
+                    read_energies_of(c, nullptr);
+                }
+            }
+        }
+        if (rc == MOIL_NB_OK && !err) {
+            if (!h->grp.empty()) {
+                h->last_site_pairs = 0;
+                for (NbCtx *c : ctxs) h->last_site_pairs += c->last_site_pairs;
+            }
+            if (energies) {
+                for (size_t g = 0; g < ctxs.size(); ++g)
+                    read_energies_of(ctxs[g], energies + (h->grp.empty() ? 0 : h->grp_rep0[g]));
+            }
+            first = nsteps;
+        } else {
+            NB_CUDA_OK(h, cudaMemcpyAsync(d_coor, h->d_md_save, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice,
+                                          h->stream));
+            NB_CUDA_OK(h, cudaMemcpyAsync(d_vel, h->d_md_save + 3 * n, sizeof(double) * 3 * n,
+                                          cudaMemcpyDeviceToDevice, h->stream));
+            NB_CUDA_OK(h, cudaStreamSynchronize(h->stream));
+            for (NbCtx *c : ctxs) c->need_rebuild = 1;
+            if (rc != MOIL_NB_OK) cudaGetLastError();
+        }
+    }
+    for (int step = first; step < nsteps; ++step) {
         int rc = moil_nb_eval_device(h, d_coor, h->d_md_dpot, step + 1 == nsteps ? energies : nullptr);
         if (rc != MOIL_NB_OK) return rc;
         if (h->grp.empty()) {
