@@ -197,7 +197,8 @@ int alloc_half(NbCtx *c)
     free_ptr(c->d_hrow);
     free_ptr(c->d_jset);
     if (!c->whalf) return MOIL_NB_OK;
-    if (nb_half_configure(c) != MOIL_NB_OK) {
+    if (nb_half_configure(c) != MOIL_NB_OK || (c->want_whalf == MOIL_NB_WATER_AUTO && !nb_half_two_blocks(c))) {
+        // the j-sets no longer fit (at two blocks per SM for the automatic choice): full lists
         c->whalf = 0;
         c->need_rebuild = 1;
         return MOIL_NB_OK;
@@ -746,17 +747,50 @@ void enqueue_eval(NbCtx *c, const double *d_coor, double *d_dpot)
     cudaMemcpyAsync(c->h_e_rep, c->d_e_rep, sizeof(double) * NB_EREP * c->nrep, cudaMemcpyDeviceToHost, s);
 }
 
-// one whole MD step of a context, as captured into its step graph: the step-control kernel,
-// the evaluation, the error bits and rebuild counter, the leapfrog + SETTLE integrator
-void enqueue_md_step(NbCtx *c, double *coor, double *vel, const double *mass, double *dpot, double dt, double doh,
+// one whole MD step of a context, as captured into its step graph: a gate kernel sets an IF
+// node that runs the step only while no error has been raised in the call; the step is the
+// step-control kernel, the evaluation, the error bits and rebuild counter, the leapfrog +
+// SETTLE integrator.  Returns false if the gate could not be built (nothing captured then).
+bool enqueue_md_step(NbCtx *c, double *coor, double *vel, const double *mass, double *dpot, double dt, double doh,
                      double dhh)
 {
     cudaStream_t s = c->stream;
     c->launches = 0;
-    nb_launch_md_begin(c, s);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+        return false;
+    cudaGraphConditionalHandle hc;
+    if (cudaGraphConditionalHandleCreate(&hc, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return false;
+    if (!c->sstep && cudaStreamCreateWithFlags(&c->sstep, cudaStreamNonBlocking) != cudaSuccess) {
+        c->sstep = nullptr;
+        return false;
+    }
+    nb_launch_md_gate(c, s, hc);
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) return false;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hc;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &np) != cudaSuccess) return false;
+    if (cudaStreamBeginCaptureToGraph(c->sstep, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return false;
+    std::swap(c->stream, c->sstep);
+    nb_launch_md_begin(c, c->stream);
     enqueue_core(c, coor, dpot);
-    nb_launch_md_end(c, s);
-    nb_launch_integrate(c, s, coor, vel, mass, dpot, dt, doh, dhh);
+    nb_launch_md_end(c, c->stream);
+    nb_launch_integrate(c, c->stream, coor, vel, mass, dpot, dt, doh, dhh);
+    std::swap(c->stream, c->sstep);
+    cudaGraph_t done = nullptr;
+    cudaStreamEndCapture(c->sstep, &done);
+    cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    return true;
 }
 
 void drop_graph(NbCtx *c)
@@ -891,7 +925,7 @@ int eval_retry(NbCtx *c, const double *d_coor, double *d_dpot, moil_energies *e,
         if (c->whalf) {
             const int64_t needj = c->h_status[5], needh = c->h_status[7];
             c->caph = std::max<int>(c->caph, (int)((needh + needh / 8 + 32 + 31) & ~31));
-            c->jcap = std::max<int>(c->jcap, (int)std::min<int64_t>(needj + needj / 16 + 64, 65535));
+            c->jcap = std::max<int>(c->jcap, (int)std::min<int64_t>(needj + needj / 8 + 64, 65535));
         }
         int a = alloc_lists(c);
         if (a != MOIL_NB_OK) return a;
@@ -1141,6 +1175,7 @@ void moil_nb_destroy(moil_nb_ctx *h)
     if (h->d_status) cudaFree(h->d_status);
     if (h->stream2) { cudaStreamSynchronize(h->stream2); cudaStreamDestroy(h->stream2); }
     if (h->sbody) cudaStreamDestroy(h->sbody);
+    if (h->sstep) cudaStreamDestroy(h->sstep);
     if (h->pstream) cudaStreamDestroy(h->pstream);
     if (h->pstream2) cudaStreamDestroy(h->pstream2);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -1595,10 +1630,10 @@ int nb_md_loop(NbCtx *c, double *coor, double *vel, const double *mass, double *
         cudaGraph_t g = nullptr;
         NB_CUDA_OK(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         c->capturing = 1;
-        enqueue_md_step(c, coor, vel, mass, dpot, dt, doh, dhh);
+        const bool built = enqueue_md_step(c, coor, vel, mass, dpot, dt, doh, dhh);
         c->capturing = 0;
         cudaError_t e1 = cudaStreamEndCapture(s, &g);
-        cudaError_t e2 = e1 == cudaSuccess ? cudaGraphInstantiate(&c->gexec_md, g, 0) : e1;
+        cudaError_t e2 = e1 == cudaSuccess ? (built ? cudaGraphInstantiate(&c->gexec_md, g, 0) : cudaErrorNotSupported) : e1;
         if (g) cudaGraphDestroy(g);
         if (e2 != cudaSuccess) {
             c->gexec_md = nullptr;

@@ -38,6 +38,7 @@ struct NbCtx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;   // PME branch of an evaluation, concurrent with the pair kernels
     cudaStream_t sbody = nullptr;     // captures the list rebuild into the conditional node's body
+    cudaStream_t sstep = nullptr;     // captures an MD step into its gate node's body
     int capturing = 0;                // the evaluation is being captured into the handle's graph
     cudaStream_t pstream = nullptr, pstream2 = nullptr;   // replica groups: prioritised by group index
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -236,6 +237,8 @@ void nb_exclusive_scan(NbCtx *c, const int *d_in, int *d_out, int n, int *d_tota
 void nb_launch_realspace(NbCtx *c);
 // half-list water kernel: dynamic shared memory for c->jcap; MOIL_NB_OK if it fits the device
 int nb_half_configure(NbCtx *c);
+// the half-list kernel still fits its two (256-water) or four (128) resident blocks per SM
+bool nb_half_two_blocks(NbCtx *c);
 // shared-memory carveouts of the full-list water kernels
 int nb_realspace_configure(NbCtx *c);
 void nb_launch_excl14(NbCtx *c, const double *d_coor);
@@ -256,6 +259,7 @@ void nb_launch_finalize(NbCtx *c, double *d_dpot);
 // MD step loop (nb_md.cu / nb_host.cu): the step-control kernels around an evaluation, the
 // integrator of one context, and the graph replay of nsteps whole steps (no host wait)
 void nb_launch_md_begin(NbCtx *c, cudaStream_t s);
+void nb_launch_md_gate(NbCtx *c, cudaStream_t s, cudaGraphConditionalHandle h);
 void nb_launch_md_end(NbCtx *c, cudaStream_t s);
 int nb_launch_integrate(NbCtx *c, cudaStream_t s, double *coor, double *vel, const double *mass, const double *dpot,
                         double dt, double doh, double dhh);

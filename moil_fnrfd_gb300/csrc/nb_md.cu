@@ -148,6 +148,12 @@ __global__ void k_md_begin(int *__restrict__ st, int *__restrict__ ctl, int list
     for (int k = 1; k < 8; ++k) st[k] = 0;
     ctl[1] = 0;
 }
+// the gate of a step: its body runs only while no step of the call has raised an error (after
+// one, the call is redone from its starting state by the per-step path)
+__global__ void k_md_gate(cudaGraphConditionalHandle h, const int *__restrict__ ctl)
+{
+    cudaGraphSetConditional(h, ctl[2] == 0 ? 1u : 0u);
+}
 // after it: the error bits kept across steps, the rebuild counter advanced
 __global__ void k_md_end(const int *__restrict__ st, int *__restrict__ ctl)
 {
@@ -175,6 +181,12 @@ int integrate(NbCtx *c, cudaStream_t s, double *coor, double *vel, const double 
 void nb_launch_md_begin(NbCtx *c, cudaStream_t s)
 {
     k_md_begin<<<1, 1, 0, s>>>(c->d_status, c->d_mdctl, c->list_period);
+    c->launches++;
+}
+
+void nb_launch_md_gate(NbCtx *c, cudaStream_t s, cudaGraphConditionalHandle h)
+{
+    k_md_gate<<<1, 1, 0, s>>>(h, c->d_mdctl);
     c->launches++;
 }
 

@@ -1233,6 +1233,20 @@ int nb_realspace_configure(NbCtx *c)
     return MOIL_NB_OK;
 }
 
+// the half-list kernel keeps two resident blocks per SM (its register budget) with the
+// current j-set capacity
+bool nb_half_two_blocks(NbCtx *c)
+{
+    int smax = 0;
+    cudaFuncAttributes fa;
+    const void *fn = c->hb == 128 ? (const void *)k_water_h<128, false> : (const void *)k_water_h<256, false>;
+    if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, fn) != cudaSuccess)
+        return false;
+    const int per_sm = 512 / c->hb;
+    return (size_t)per_sm * ((size_t)36 * c->jcap + fa.sharedSizeBytes + 1024) <= (size_t)smax;
+}
+
 int nb_half_configure(NbCtx *c)
 {
     int optin = 0;
