@@ -185,3 +185,29 @@ def test_native_steps_grouped_batch_is_bit_identical():
         out.append((x, v, e, ek))
     assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
     assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
+
+
+@pytest.mark.gpu
+def test_device_step_loop_matches_the_per_step_path():
+    """moil_nb_md_step(n) replays a captured graph of whole steps n times on the device (one
+    wait per call); n calls of one step run the per-step path (an evaluation and the
+    integrator per call).  Both apply the same kernels and the same list schedule, so the
+    trajectories are bit-identical -- over 25 steps with thermal velocities, list rebuilds by
+    the list period and by the skin on the way, on a three-replica batch."""
+    from moil_fnrfd_gb300.nb import Nonbonded
+    reps = S.config3(3, seed=91)
+    m = torch.tensor(np.concatenate([_masses_of(r) for r in reps]), dtype=torch.float64, device="cuda")
+    loop = Nonbonded(reps, skin=1.0, list_period=10)
+    md = D.RigidWaterDynamics(loop, reps, dt=0.002, temperature=300.0, seed=4)
+    x0, v0 = md.x.clone(), md.v.clone()
+    torch.cuda.synchronize()
+    xa, va = x0.clone(), v0.clone()
+    ea, ka = loop.md_step(xa.data_ptr(), va.data_ptr(), m.data_ptr(), 0.002, 25)
+    step = Nonbonded(reps, skin=1.0, list_period=10)
+    xb, vb = x0.clone(), v0.clone()
+    for _ in range(25):
+        eb, kb = step.md_step(xb.data_ptr(), vb.data_ptr(), m.data_ptr(), 0.002, 1)
+    assert torch.equal(xa, xb) and torch.equal(va, vb)
+    assert ea == eb and ka == kb
+    loop.close()
+    step.close()
