@@ -607,7 +607,6 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
     constexpr int S = HalfScale<HB>::S;
     constexpr float SC = (float)(1 << S);
     constexpr int NE = VIR ? 6 : 4;
-    __shared__ long long sG[9][HB];
     __shared__ float2 sE[NE][HB];
     extern __shared__ int sJ[];      // [9][jcap]: partner-site gradients, 2^S units
     const int t = threadIdx.x, b = blockIdx.x;
@@ -617,8 +616,6 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
     for (int k = t; k < nJ; k += HB)
 #pragma unroll
         for (int c = 0; c < 9; ++c) sJ[c * jcap + k] = 0;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) sG[k][t] = 0;
 #pragma unroll
     for (int k = 0; k < NE; ++k) sE[k][t] = make_float2(0.f, 0.f);
     __syncthreads();
@@ -630,6 +627,9 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
         float2 G[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) G[k] = f2(0.f);
+        // the owner's gradient goes to the int64 site gradient with one atomic per component
+        // and flush (no shared-memory slots: they would take the L1 that the gathers use)
+        unsigned long long *gi = (unsigned long long *)(grad + 9 * (size_t)i);
         float g[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) g[k] = 0.f;
@@ -646,7 +646,11 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
                 const float qs[3] = {oi0.w, pos[3 * i + 1].w, pos[3 * i + 2].w};
                 ecorr = water_intra_f(R, oi1, oi2, qs, g);
 #pragma unroll
-                for (int k = 0; k < 9; ++k) { sG[k][t] += nb_fix(g[k]); g[k] = 0.f; }
+                for (int k = 0; k < 9; ++k) {
+                    const long long v = nb_fix(g[k]);
+                    if (v != 0) atomicAdd(gi + k, (unsigned long long)v);
+                    g[k] = 0.f;
+                }
             }
             eu[5] = (double)ecorr;
         }
@@ -654,7 +658,8 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
         auto flush = [&](float ef) {
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                sG[k][t] += nb_fix(g[k] - (G[k].x + G[k].y));   // G holds minus the gradient
+                const long long v = nb_fix(g[k] - (G[k].x + G[k].y));   // G holds minus the gradient
+                if (v != 0) atomicAdd(gi + k, (unsigned long long)v);
                 g[k] = 0.f;
                 G[k] = f2(0.f);
             }
@@ -824,12 +829,7 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
         eu[7] = VIR ? (double)sE[NE - 1][t].x + (double)sE[NE - 1][t].y : 0.0;
     }
     __syncthreads();
-    // the block's sums: its own waters' gradients and the partner shares of its j-set
-    if (i - R.wat0 < R.nwat) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k)
-            if (sG[k][t] != 0) atomicAdd((unsigned long long *)&grad[9 * (size_t)i + k], (unsigned long long)sG[k][t]);
-    }
+    // the block's partner shares of its j-set
     const int *js = jset + (size_t)b * jcap;
     for (int l = t; l < nJ; l += HB) {
         const size_t jg = (size_t)js[l];
