@@ -696,16 +696,16 @@ void enqueue_core(NbCtx *c, const double *d_coor, double *d_dpot)
     // launches through a conditional node
     if (c->timing) {
         // stage timing (kernel by kernel): the host reads the flag and launches the rebuild
-        // only when it is set, as the conditional node of a replayed evaluation does
-        // (the stage ends at the flag's read-back unless the rebuild runs: the event is then
-        // recorded again after it, so the host's wait is not counted)
+        // only when it is set, as the conditional node of a replayed evaluation does.  The
+        // preparation stage (status upload, coordinate conversion with the skin check) ends
+        // before the read-back; the rebuild stage starts after the host's decision, so
+        // neither counts the round trip a replayed evaluation does not make
+        cudaEventRecord(c->ev[12], s);
         cudaMemcpyAsync(c->h_status + 16, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
-        cudaEventRecord(c->ev[1], s);
         cudaStreamSynchronize(s);
-        if (c->h_status[16]) {
-            nb_launch_build_lists(c, d_coor);
-            cudaEventRecord(c->ev[1], s);
-        }
+        cudaEventRecord(c->ev[13], s);
+        if (c->h_status[16]) nb_launch_build_lists(c, d_coor);
+        cudaEventRecord(c->ev[1], s);
     } else if (!(c->capturing && !c->on_prio && enqueue_lists_conditional(c, d_coor))) {
         // (on the prioritised streams of host-buffer group evaluations the conditional node
         // cost the copy/kernel overlap more than the skipped launches save: gated kernels)
@@ -867,8 +867,8 @@ int eval_complete(NbCtx *c)
             cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]);
             return ms;
         };
-        t.list_ms = el(0, 1);
-        t.prepare_ms = 0;
+        t.prepare_ms = el(0, 12);
+        t.list_ms = el(13, 1);
         t.water_ms = el(2, 3);
         t.atom_ms = el(3, 4);
         t.excl_ms = el(4, 5);
@@ -1152,7 +1152,7 @@ int moil_nb_create(moil_nb_ctx **out, int device)
     }
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
     if (h->nsm <= 0) h->nsm = 1;
-    for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
+    for (int k = 0; k < NB_NEV; ++k) cudaEventCreate(&h->ev[k]);
     if (cudaMallocHost(&h->h_status, sizeof(int) * 24) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int) * 8) != cudaSuccess) {
         moil_nb_destroy(h);
         return MOIL_NB_ERR_CUDA;
@@ -1169,7 +1169,7 @@ void moil_nb_destroy(moil_nb_ctx *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     destroy_groups(h);
     release_device(h);
-    for (int k = 0; k < 12; ++k)
+    for (int k = 0; k < NB_NEV; ++k)
         if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->d_status) cudaFree(h->d_status);

@@ -194,7 +194,10 @@ struct NbCtx {
 
     // instrumentation
     int timing = 0;
-    cudaEvent_t ev[12];
+    // stage events: 0 start, 12 prepared, 13 rebuild decided, 1 lists, 2..5 pair kernels,
+    // 6..9 PME, 10 end; 11 orders the replica groups after their shared input copies
+#define NB_NEV 14
+    cudaEvent_t ev[NB_NEV];
     moil_nb_timing last_timing{};
     int launches = 0;
 

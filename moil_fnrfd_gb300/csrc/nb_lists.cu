@@ -129,10 +129,11 @@ __global__ void k_site_build(int nunit, int nW, const int *__restrict__ sorted, 
 // 3. per-evaluation coordinate conversion into site order; displacement check.  One thread
 // per sorted water (its three consecutive caller atoms, 72 contiguous bytes) or non-water
 // site, so every site-order array is read and written coalesced.
+// Sites that do not track (water hydrogens) neither read nor write their build position.
 template <typename T>
 __device__ __forceinline__ void prepare_site(int s, const double *x, const unsigned *__restrict__ site_flags,
                                              const T *__restrict__ site_q, void *pos_v, float4 *__restrict__ posb,
-                                             float half_skin2, int snapshot, bool &moved)
+                                             float half_skin2, int snapshot, bool track, bool &moved)
 {
     typedef typename vec4<T>::type T4;
     const unsigned f = site_flags[s];
@@ -140,6 +141,7 @@ __device__ __forceinline__ void prepare_site(int s, const double *x, const unsig
     p.x = (T)x[0]; p.y = (T)x[1]; p.z = (T)x[2];
     p.w = (f & SF_CHARGED) ? site_q[s] : (T)0;
     ((T4 *)pos_v)[s] = p;
+    if (!track) return;
     const float4 pf = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
     if (snapshot) {
         posb[s] = pf;
@@ -189,8 +191,8 @@ __global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, con
             // distances with radii that include the hydrogens' reach (rwat, checked below)
 #pragma unroll
             for (int m = 0; m < 3; ++m)
-                prepare_site<T>(3 * u + m, x[m], site_flags, site_q, pos_v, posb, m == 0 ? half_skin2 : 3.0e38f,
-                                snapshot, moved);
+                prepare_site<T>(3 * u + m, x[m], site_flags, site_q, pos_v, posb, half_skin2, snapshot, m == 0,
+                                moved);
             // the molecule record of the water kernel: O position (and charge), then the offsets
             ((T4 *)woff_v)[3 * u] = ((const T4 *)pos_v)[3 * u];
 #pragma unroll
@@ -208,7 +210,7 @@ __global__ void k_prepare(int nW, int nA, const int *__restrict__ site_orig, con
             const int s = 3 * nW + (u - nW);
             double x[3];
             load_atom(coor, site_orig[s], x, st);
-            prepare_site<T>(s, x, site_flags, site_q, pos_v, posb, half_skin2, snapshot, moved);
+            prepare_site<T>(s, x, site_flags, site_q, pos_v, posb, half_skin2, snapshot, true, moved);
         }
     }
     if (moved) atomicOr(&st[0], 1);

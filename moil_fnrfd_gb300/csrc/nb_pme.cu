@@ -16,7 +16,8 @@
 //   plane_inv      one CTA per (replica, z plane): inverse C2C along y, C2R along x in shared
 //                  memory, then each atom's share of the gradient from this plane (grad_sum,
 //                  :815-970) into its own slot -- four planes, four slots, summed at the end
-// FFTs (FP32 path): Stockham autosort with radices 4/2/3/5; every pass transforms all lines
+// FFTs (FP32 path): Stockham autosort with radices 2..5 (plane kernels) or up to 10 (z
+// columns, two passes per line: the composite codelets of nb_fft.cuh); every pass transforms all lines
 // of a tile at once, the block's threads spread over (line, butterfly) pairs, with the
 // index arithmetic (twiddle step, destination) read from per-stage tables built on the host
 // and the line number obtained by a multiply-high by a precomputed magic constant.  The
@@ -25,72 +26,10 @@
 // Inverse transforms are conj(FFT(conj(x))), unnormalised like FFTPACK's cfftb.
 #include <mutex>
 
+#include "nb_fft.cuh"
 #include "nb_internal.h"
 
 namespace {
-
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
-template <typename C> __device__ __forceinline__ C cmul(C a, C b)
-{
-    C r;
-    r.x = a.x * b.x - a.y * b.y;
-    r.y = a.x * b.y + a.y * b.x;
-    return r;
-}
-template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
-// multiply by -i
-template <typename C> __device__ __forceinline__ C cmi(C a) { C r; r.x = a.y; r.y = -a.x; return r; }
-
-// forward DFT butterflies, W_R = exp(-2 pi i / R)
-template <typename C> __device__ __forceinline__ void bfly2(C *v)
-{
-    C a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
-}
-template <typename C> __device__ __forceinline__ void bfly4(C *v)
-{
-    C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]), t2 = cadd(v[1], v[3]), t3 = cmi(csub(v[1], v[3]));
-    v[0] = cadd(t0, t2);
-    v[2] = csub(t0, t2);
-    v[1] = cadd(t1, t3);
-    v[3] = csub(t1, t3);
-}
-template <typename C> __device__ __forceinline__ void bfly3(C *v)
-{
-    typedef decltype(v[0].x) T;
-    const T h = (T)0.86602540378443864676;   // sqrt(3)/2
-    C s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
-    C m;
-    m.x = v[0].x - (T)0.5 * s.x;
-    m.y = v[0].y - (T)0.5 * s.y;
-    C r0 = cadd(v[0], s);
-    C r1, r2;
-    r1.x = m.x + h * d.y; r1.y = m.y - h * d.x;
-    r2.x = m.x - h * d.y; r2.y = m.y + h * d.x;
-    v[0] = r0; v[1] = r1; v[2] = r2;
-}
-template <typename C> __device__ __forceinline__ void bfly5(C *v)
-{
-    typedef decltype(v[0].x) T;
-    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;   // cos(2pi/5), cos(4pi/5)
-    const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;    // sin(2pi/5), sin(4pi/5)
-    C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]), a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
-    C x0 = v[0];
-    C p1, p2;
-    p1.x = x0.x + c1 * a1.x + c2 * a2.x; p1.y = x0.y + c1 * a1.y + c2 * a2.y;
-    p2.x = x0.x + c2 * a1.x + c1 * a2.x; p2.y = x0.y + c2 * a1.y + c1 * a2.y;
-    C q1, q2;   // the sine combinations; results are p -/+ i q
-    q1.x = s1 * b1.x + s2 * b2.x; q1.y = s1 * b1.y + s2 * b2.y;
-    q2.x = s2 * b1.x - s1 * b2.x; q2.y = s2 * b1.y - s1 * b2.y;
-    v[0].x = x0.x + a1.x + a2.x; v[0].y = x0.y + a1.y + a2.y;
-    C mq1 = cmi(q1), mq2 = cmi(q2);
-    v[1] = cadd(p1, mq1);
-    v[4] = csub(p1, mq1);
-    v[2] = cadd(p2, mq2);
-    v[3] = csub(p2, mq2);
-}
 
 __device__ __forceinline__ float nb_round(float x) { return roundf(x); }
 __device__ __forceinline__ double nb_round(double x) { return round(x); }
@@ -373,10 +312,7 @@ __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float
         for (int r = 0; r < RADIX; ++r) v[r] = src[SW_IN ? swz(s0 + r * nb) : s0 + r * nb];
 #pragma unroll
         for (int r = 1; r < RADIX; ++r) v[r] = cmul(v[r], tw[r * e.x]);
-        if (RADIX == 4) bfly4(v);
-        else if (RADIX == 2) bfly2(v);
-        else if (RADIX == 3) bfly3(v);
-        else bfly5(v);
+        bfly<RADIX>(v);
 #pragma unroll
         for (int r = 0; r < RADIX; ++r) {
             float2 o = CONJ_OUT ? cconj(v[r]) : v[r];
@@ -389,7 +325,9 @@ __device__ __forceinline__ void fft_pass_r(const float2 *__restrict__ src, float
     __syncthreads();
 }
 
-template <int MODE, bool CONJ_OUT, bool SW_IN, bool SW_OUT>
+// WIDE: the radix set of a wide plan (2..10); otherwise 2, 3, 4, 5 only, so the kernel keeps
+// the register count of the small butterflies
+template <int MODE, bool CONJ_OUT, bool SW_IN, bool SW_OUT, bool WIDE>
 __device__ __forceinline__ void fft_pass(int R, const float2 *src, float2 *dst, float *rdst, int L, int ss, int ds,
                                          int keep, int Ns, int nb, unsigned magic, const int2 *tab, const float2 *tw)
 {
@@ -397,7 +335,17 @@ __device__ __forceinline__ void fft_pass(int R, const float2 *src, float2 *dst, 
     case 4: fft_pass_r<4, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
     case 2: fft_pass_r<2, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
     case 3: fft_pass_r<3, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
-    default: fft_pass_r<5, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    case 5: fft_pass_r<5, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+    default:
+        if constexpr (WIDE) {
+            switch (R) {
+            case 6: fft_pass_r<6, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+            case 8: fft_pass_r<8, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+            case 9: fft_pass_r<9, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+            default: fft_pass_r<10, MODE, CONJ_OUT, SW_IN, SW_OUT>(src, dst, rdst, L, ss, ds, keep, Ns, nb, magic, tab, tw); break;
+            }
+        }
+        break;
     }
 }
 
@@ -410,7 +358,7 @@ struct FftCtx {
 };
 
 // shared-memory bytes of one staged plan of length n
-size_t fft_ctx_bytes(int n);
+size_t fft_ctx_bytes(int n, bool wide);
 
 __device__ __forceinline__ unsigned char *fft_ctx_load(unsigned char *dst, const FftPlanDev *__restrict__ gp,
                                                        const int2 *__restrict__ gtab, const float2 *__restrict__ gtw,
@@ -435,7 +383,7 @@ __device__ __forceinline__ unsigned char *fft_ctx_load(unsigned char *dst, const
 // last pass is stored in the mode given with stride out_ds (MODE 1: the transposed row
 // stride); the stages between keep the spread layout.  Returns the buffer holding the
 // result; CONJ_LAST conjugates the final output (second half of an inverse transform).
-template <int LAST_MODE, bool CONJ_LAST>
+template <int LAST_MODE, bool CONJ_LAST, bool WIDE = false>
 __device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst, int L, int keep, int in_ss,
                              int out_ds)
 {
@@ -446,16 +394,16 @@ __device__ float2 *fft_lines(const FftCtx &c, float2 *a, float2 *b, float *rdst,
         const int2 *t = c.tab + p.off[s];
         if (s + 1 < nst) {
             if (s == 0)
-                fft_pass<0, false, false, true>(p.rad[s], src, dst, nullptr, L, in_ss, n, 0, p.ns[s], p.nb[s],
+                fft_pass<0, false, false, true, WIDE>(p.rad[s], src, dst, nullptr, L, in_ss, n, 0, p.ns[s], p.nb[s],
                                                 p.magic[s], t, c.tw);
             else
-                fft_pass<0, false, true, true>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s],
+                fft_pass<0, false, true, true, WIDE>(p.rad[s], src, dst, nullptr, L, n, n, 0, p.ns[s], p.nb[s], p.magic[s],
                                                t, c.tw);
         } else if (s == 0) {
-            fft_pass<LAST_MODE, CONJ_LAST, false, false>(p.rad[s], src, dst, rdst, L, in_ss, out_ds, keep, p.ns[s],
+            fft_pass<LAST_MODE, CONJ_LAST, false, false, WIDE>(p.rad[s], src, dst, rdst, L, in_ss, out_ds, keep, p.ns[s],
                                                          p.nb[s], p.magic[s], t, c.tw);
         } else {
-            fft_pass<LAST_MODE, CONJ_LAST, true, false>(p.rad[s], src, dst, rdst, L, n, out_ds, keep, p.ns[s],
+            fft_pass<LAST_MODE, CONJ_LAST, true, false, WIDE>(p.rad[s], src, dst, rdst, L, n, out_ds, keep, p.ns[s],
                                                         p.nb[s], p.magic[s], t, c.tw);
         }
         float2 *x = src; src = dst; dst = x;
@@ -534,7 +482,7 @@ __global__ void __launch_bounds__(256) k_plane_fwd_f(const PlaneWork *__restrict
     for (int k = threadIdx.x; k < n1h * n2; k += blockDim.x) g[k] = Y[k];
 }
 
-__global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
+__global__ void __launch_bounds__(256, 6) k_zconv_f(const ColWork *__restrict__ work, const RepDev *__restrict__ reps,
                                                  const FftPlanDev *__restrict__ plans, const int *__restrict__ rep_plan,
                                                  const float2 *__restrict__ tw, const int2 *__restrict__ tab,
                                                  const float *__restrict__ etab_all, float2 *__restrict__ grid,
@@ -557,7 +505,7 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) A[lane * sA + kz] = g[kz * zs + lane];
     __syncthreads();
-    float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0, sA, n3);
+    float2 *F = fft_lines<0, false, true>(c3, A, B, nullptr, tk, 0, sA, n3);
     float2 *Fo = F == A ? B : A;
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
     // influence function exp(-pi^2 m^2 / alpha^2) / (pi V B(m) m^2): the exponential and the
@@ -591,7 +539,7 @@ __global__ void __launch_bounds__(256) k_zconv_f(const ColWork *__restrict__ wor
         }
     }
     __syncthreads();
-    float2 *I = fft_lines<0, true>(c3, F, Fo, nullptr, tk, 0, n3, sA);
+    float2 *I = fft_lines<0, true, true>(c3, F, Fo, nullptr, tk, 0, n3, sA);
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) g[kz * zs + lane] = I[lane * sA + kz];
     // fixed-order reduction: each thread's few terms in FP32, then FP64 across the warp and
@@ -636,7 +584,7 @@ __global__ void __launch_bounds__(256) k_press_zvir_f(const ColWork *__restrict_
     for (int kz = warp; kz < n3; kz += 8)
         if (lane < tk) A[lane * sA + kz] = g[kz * zs + lane];
     __syncthreads();
-    const float2 *F = fft_lines<0, false>(c3, A, B, nullptr, tk, 0, sA, n3);
+    const float2 *F = fft_lines<0, false, true>(c3, A, B, nullptr, tk, 0, sA, n3);
     const float wgt = (w.kx == 0 || 2 * w.kx == n1) ? 1.f : 2.f;
     const float fac2 = R.pme_fac2f, pivol = R.pivolf, fac = (float)R.pme_fac;
     const int nf2 = (n2 + 1) / 2, nf3 = (n3 + 1) / 2;
@@ -729,7 +677,7 @@ __global__ void __launch_bounds__(256) k_plane_inv_f(const PlaneWork *__restrict
 // ewald_receip.f:815-970): order-4 weights and derivatives once per site, the 4x4x4 stencil
 // read from the grid planes k_plane_inv_f left in place; result (x, y, z) per site, to be
 // scaled by q * fc * n_d / L_d in the finalize
-__global__ void __launch_bounds__(256) k_pme_gather_f(int nsite, const int *__restrict__ site_rep,
+__global__ void __launch_bounds__(256, 4) k_pme_gather_f(int nsite, const int *__restrict__ site_rep,
                                                       const RepDev *__restrict__ reps, const float4 *__restrict__ fr,
                                                       const float2 *__restrict__ grid, float4 *__restrict__ part)
 {
@@ -1095,18 +1043,46 @@ void pme_t(NbCtx *c)
     c->launches += 6;
 }
 
-// radix plan and Stockham tables: 4s first, then 2, 3, 5; returns 0 if n is not
-// 2/3/5-smooth or too long.  tab receives (twiddle step, destination index) per butterfly.
-int make_plan(int n, FftPlanDev *p, std::vector<int2> *tab)
+// radix plan and Stockham tables; returns 0 if n is not 2/3/5-smooth or too long.  Narrow
+// plans (the plane kernels and the FP64 one-warp-per-line transform) take 4s first, then 2, 3,
+// 5.  Wide plans (the FP32 z columns) also have the composite codelets 6, 8, 9, 10 and take
+// the fewest passes (a line of up to 100 points in two), larger radices first on ties.  tab
+// receives (twiddle step, destination index) per butterfly.
+// fewest factors of m from the wide radix set, at most `left` of them (-1: none)
+int wide_factors(int m, int left, int *out)
+{
+    static const int R[8] = {10, 9, 8, 6, 5, 4, 3, 2};
+    if (m == 1) return 0;
+    if (left == 0) return -1;
+    int best = -1, tmp[8];
+    for (int k = 0; k < 8; ++k) {
+        if (m % R[k]) continue;
+        const int f = wide_factors(m / R[k], best < 0 ? left - 1 : best - 2, tmp);
+        if (f < 0) continue;
+        best = f + 1;
+        out[0] = R[k];
+        for (int q = 0; q < f; ++q) out[1 + q] = tmp[q];
+        if (best == 1) break;
+    }
+    return best;
+}
+
+int make_plan(int n, FftPlanDev *p, std::vector<int2> *tab, bool wide)
 {
     memset(p, 0, sizeof(*p));
     p->n = n;
     int m = n, k = 0;
     if (n < 2 || n > NB_MAX_FFT) return 0;
-    while (m % 4 == 0) { p->rad[k++] = 4; m /= 4; }
-    while (m % 2 == 0) { p->rad[k++] = 2; m /= 2; }
-    while (m % 3 == 0) { p->rad[k++] = 3; m /= 3; }
-    while (m % 5 == 0) { p->rad[k++] = 5; m /= 5; }
+    if (wide) {
+        k = wide_factors(n, 8, p->rad);
+        if (k < 0) return 0;
+        m = 1;
+    } else {
+        while (m % 4 == 0) { p->rad[k++] = 4; m /= 4; }
+        while (m % 2 == 0) { p->rad[k++] = 2; m /= 2; }
+        while (m % 3 == 0) { p->rad[k++] = 3; m /= 3; }
+        while (m % 5 == 0) { p->rad[k++] = 5; m /= 5; }
+    }
     if (m != 1 || k > 8) return 0;
     p->nst = k;
     int Ns = 1, off = 0;
@@ -1128,10 +1104,10 @@ int make_plan(int n, FftPlanDev *p, std::vector<int2> *tab)
     return 1;
 }
 
-size_t fft_ctx_bytes(int n)
+size_t fft_ctx_bytes(int n, bool wide)
 {
     FftPlanDev p;
-    if (!make_plan(n, &p, nullptr)) return 0;
+    if (!make_plan(n, &p, nullptr, wide)) return 0;
     size_t ntab = (size_t)p.off[p.nst - 1] + p.nb[p.nst - 1];
     return align16(sizeof(FftPlanDev)) + align16(ntab * sizeof(int2)) + align16(n * sizeof(float2));
 }
@@ -1139,7 +1115,7 @@ size_t fft_ctx_bytes(int n)
 template <typename T>
 size_t plane_fwd_smem(int n1, int n2)
 {
-    if (sizeof(T) == 4) return (size_t)2 * plane_buf_elems(n1, n2) * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
+    if (sizeof(T) == 4) return (size_t)2 * plane_buf_elems(n1, n2) * sizeof(float2) + fft_ctx_bytes(n1, false) + fft_ctx_bytes(n2, false);
     typedef typename cplx<T>::type C;
     size_t acc = (sizeof(typename Acc<T>::type) * n1 * n2 + 15) & ~(size_t)15;
     return acc + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -1147,7 +1123,7 @@ size_t plane_fwd_smem(int n1, int n2)
 template <typename T>
 size_t plane_inv_smem(int n1, int n2)
 {
-    if (sizeof(T) == 4) return (size_t)2 * plane_buf_elems(n1, n2) * sizeof(float2) + fft_ctx_bytes(n1) + fft_ctx_bytes(n2);
+    if (sizeof(T) == 4) return (size_t)2 * plane_buf_elems(n1, n2) * sizeof(float2) + fft_ctx_bytes(n1, false) + fft_ctx_bytes(n2, false);
     typedef typename cplx<T>::type C;
     size_t r = (sizeof(T) * n1 * n2 + 15) & ~(size_t)15;
     return r + sizeof(C) * n2 * ((n1 / 2 + 1) | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
@@ -1155,7 +1131,7 @@ size_t plane_inv_smem(int n1, int n2)
 template <typename T>
 size_t zconv_smem(int n3)
 {
-    if (sizeof(T) == 4) return (size_t)2 * zconv_buf_elems(n3) * sizeof(float2) + fft_ctx_bytes(n3);
+    if (sizeof(T) == 4) return (size_t)2 * zconv_buf_elems(n3) * sizeof(float2) + fft_ctx_bytes(n3, true);
     typedef typename cplx<T>::type C;
     return sizeof(C) * NB_TK * (n3 | 1) + sizeof(C) * 8 * 2 * NB_MAX_FFT;
 }
@@ -1196,16 +1172,18 @@ int configure_t(NbCtx *c)
     c->rep_plan.assign(3 * c->nrep, 0);
     std::vector<double> twr, twi;
     std::vector<int2> tab;
+    std::vector<char> wide_of;     // per plan: wide radix set (the FP32 z columns)
     for (int r = 0; r < c->nrep; ++r) {
         int ns[3] = {c->rd[r].n1, c->rd[r].n2, c->rd[r].n3};
         for (int d = 0; d < 3; ++d) {
+            const bool wide = sizeof(T) == 4 && d == 2;
             int found = -1;
             for (size_t k = 0; k < c->plans.size(); ++k)
-                if (c->plans[k].n == ns[d]) found = (int)k;
+                if (c->plans[k].n == ns[d] && (bool)wide_of[k] == wide) found = (int)k;
             if (found < 0) {
                 FftPlanDev p;
                 int tab0 = (int)tab.size();
-                if (!make_plan(ns[d], &p, &tab)) return MOIL_NB_ERR_GRID;
+                if (!make_plan(ns[d], &p, &tab, wide)) return MOIL_NB_ERR_GRID;
                 p.tab0 = tab0;
                 p.tw0 = (int)twr.size();
                 for (int t = 0; t < ns[d]; ++t) {
@@ -1214,6 +1192,7 @@ int configure_t(NbCtx *c)
                     twi.push_back(sin(ang));
                 }
                 c->plans.push_back(p);
+                wide_of.push_back(wide);
                 found = (int)c->plans.size() - 1;
             }
             c->rep_plan[3 * r + d] = found;
@@ -1488,7 +1467,8 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     if (natom < 1 || natom > NA_MAX_ATOMS || !(alpha > 0) || !(eps > 0)) return MOIL_NB_ERR_ARG;
     for (int d = 0; d < 3; ++d) {
         FftPlanDev p;
-        if (!(box[d] > 0) || grid[d] < 4 || grid[d] > NA_MAX_N || !make_plan(grid[d], &p, nullptr))
+        if (!(box[d] > 0) || grid[d] < 4 || grid[d] > NA_MAX_N || !make_plan(grid[d], &p, nullptr, false) ||
+            !make_plan(grid[d], &p, nullptr, true))
             return MOIL_NB_ERR_GRID;
     }
     cudaStream_t stream = (cudaStream_t)stream_v;
@@ -1551,7 +1531,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     int ntw = 0;
     for (int d = 0; d < 3; ++d) {
         int tab0 = (int)tab.size();
-        make_plan(grid[d], &plans[d], &tab);
+        make_plan(grid[d], &plans[d], &tab, d == 2);     // the z columns take the wide radix set
         plans[d].tab0 = tab0;
         plans[d].tw0 = ntw;
         for (int t = 0; t < grid[d]; ++t) {
