@@ -51,7 +51,7 @@ WATER_KERNEL_NAME = {1: "k_water_f (full lists)", 2: "k_water_h (half lists)"}
 # DRAM bytes per atom of one evaluation's PME kernels (k_pme_bin, k_plane_fwd_f, k_zconv_f,
 # k_plane_inv_f, k_pme_gather_f: 5.37 + 4.55 + 10.86 + 10.82 + 15.00 MB, 48-replica capture over
 # 222,513 atoms, caches flushed before each launch, so an upper bound)
-PME_DRAM_BYTES_PER_ATOM = 209.5
+PME_DRAM_BYTES_PER_ATOM = 209.8
 
 
 ACCEL = 418.4                 # (kcal/mol/Å) / amu in Å/ps^2
