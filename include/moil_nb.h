@@ -154,6 +154,18 @@ int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies
  * (device pointers, same layout); energies still go to host memory. */
 int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *energies);
 
+/* moil_nb_eval_device in two halves, so the caller's host work overlaps the GPU: the first
+ * queues the evaluation on the handle's streams and returns at once (after d_coor has been
+ * read on the handle's stream, see moil_nb_stream, nothing orders the caller's later work);
+ * the second waits for it, regrows and redoes it if a list overflowed, and returns its status
+ * and energies.  One evaluation may be pending per handle: until moil_nb_eval_wait returns, the
+ * caller leaves d_coor and d_dpot alone and calls nothing else on the handle but
+ * moil_nb_eval_wait (other calls return MOIL_NB_ERR_STATE); moil_nb_eval_wait without a
+ * pending evaluation returns MOIL_NB_ERR_STATE.  With stage timing on, the first half runs the
+ * whole evaluation. */
+int moil_nb_eval_device_async(moil_nb_ctx *h, const double *d_coor, double *d_dpot);
+int moil_nb_eval_wait(moil_nb_ctx *h, moil_energies *energies);
+
 /* LJ virial terms of the last evaluation for one replica, as MOIL's PRESS build accumulates
  * them into COMMON/ENERGY.BLOCK:94-96 (virvdw1..virvdw5): virvdw = -sum df1 r^2 over the
  * LJ pairs, df1 = (dE_LJ/dr)/r, for water-water pairs in the primary box

@@ -955,7 +955,8 @@ int group_of(const NbCtx *h, int r)
     return g;
 }
 
-int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bool host)
+// phase 1 queues the groups' evaluations, phase 2 completes them (3: both)
+int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bool host, int phase = 3)
 {
     const int P = (int)h->grp.size();
     // device-resident callers may have queued their coordinates on the handle's stream
@@ -1016,7 +1017,12 @@ int eval_groups(NbCtx *h, const double *coor, double *dpot, moil_energies *e, bo
         }
         h->last_timing = sum;
     } else {
-        for (int g = 0; g < P && rc == MOIL_NB_OK; ++g) rc = launch(g);
+        if (phase & 1)
+            for (int g = 0; g < P && rc == MOIL_NB_OK; ++g) rc = launch(g);
+        if (phase == 1) {
+            use_prio(false);
+            return rc;
+        }
         for (int g = 0; g < P; ++g) {
             int r = finish(g);
             if (r != MOIL_NB_OK && rc == MOIL_NB_OK) rc = r;
@@ -1196,6 +1202,7 @@ int moil_nb_init(moil_nb_ctx *h, const moil_nb_params *p, const moil_topology *t
 int moil_nb_init_batch(moil_nb_ctx *h, int nrep, const moil_replica *reps)
 {
     if (!h) return MOIL_NB_ERR_ARG;
+    if (h->pending) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
     destroy_groups(h);
     int64_t natom = 0;
@@ -1225,7 +1232,7 @@ int moil_nb_get_alpha(const moil_nb_ctx *h, int r, double *alpha)
 int moil_nb_eval(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *e)
 {
     if (!h || !coor || !dpot) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
     if (!h->grp.empty()) return eval_groups(h, coor, dpot, e, true);
     // staged through device copies even for pinned buffers: on GB300 the finalize kernel
@@ -1244,7 +1251,7 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
                     moil_energies *e)
 {
     if (!h || !coor) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
     if (!h->grp.empty()) {
         for (size_t g = 0; g < h->grp.size(); ++g) {
@@ -1277,7 +1284,7 @@ int moil_nb_adjoint(moil_nb_ctx *h, const double *coor, double *dEdq, double *dE
 int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
 {
     if (!h) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     if (mol && !mass) return MOIL_NB_ERR_ARG;
     cudaSetDevice(h->device);
     if (!h->grp.empty()) {
@@ -1332,7 +1339,7 @@ int moil_nb_set_molecules(moil_nb_ctx *h, const int *mol, const double *mass)
 int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_energies *e, double *press)
 {
     if (!h || !coor || !press) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     if (h->nmol == 0) {
         h->err = "no molecules: call moil_nb_set_molecules first";
         return MOIL_NB_ERR_STATE;
@@ -1374,7 +1381,7 @@ int moil_nb_pressure(moil_nb_ctx *h, const double *coor, double *dpot, moil_ener
 int moil_nb_get_virial(moil_nb_ctx *h, int replica, double *virvdw)
 {
     if (!h || !virvdw) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     if (replica < 0 || replica >= h->nrep) {
         h->err = "replica index out of range";
         return MOIL_NB_ERR_ARG;
@@ -1391,15 +1398,59 @@ int moil_nb_get_virial(moil_nb_ctx *h, int replica, double *virvdw)
 int moil_nb_eval_device(moil_nb_ctx *h, const double *d_coor, double *d_dpot, moil_energies *e)
 {
     if (!h || !d_coor || !d_dpot) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
     if (!h->grp.empty()) return eval_groups(h, d_coor, d_dpot, e, false);
     return eval_impl(h, d_coor, d_dpot, e);
 }
 
+int moil_nb_eval_device_async(moil_nb_ctx *h, const double *d_coor, double *d_dpot)
+{
+    if (!h || !d_coor || !d_dpot) return MOIL_NB_ERR_ARG;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
+    cudaSetDevice(h->device);
+    int rc = MOIL_NB_OK;
+    if (h->timing) {
+        // diagnostic mode runs stage after stage: the whole evaluation here, its status kept
+        rc = h->grp.empty() ? eval_impl(h, d_coor, d_dpot, nullptr)
+                            : eval_groups(h, d_coor, d_dpot, nullptr, false);
+    } else if (!h->grp.empty()) {
+        rc = eval_groups(h, d_coor, d_dpot, nullptr, false, 1);
+        if (rc != MOIL_NB_OK) return rc;
+    } else {
+        eval_launch(h, d_coor, d_dpot);
+        NB_CUDA_OK(h, cudaPeekAtLastError());
+    }
+    h->pending = 1;
+    h->pend_rc = rc;
+    h->pend_coor = d_coor;
+    h->pend_dpot = d_dpot;
+    return MOIL_NB_OK;
+}
+
+int moil_nb_eval_wait(moil_nb_ctx *h, moil_energies *e)
+{
+    if (!h) return MOIL_NB_ERR_ARG;
+    if (!h->pending) return MOIL_NB_ERR_STATE;
+    cudaSetDevice(h->device);
+    h->pending = 0;
+    if (h->timing) {
+        if (h->pend_rc == MOIL_NB_OK) {
+            if (h->grp.empty()) read_energies(h, e);
+            else
+                for (size_t g = 0; g < h->grp.size(); ++g) read_energies(h->grp[g], e ? e + h->grp_rep0[g] : nullptr);
+        }
+        return h->pend_rc;
+    }
+    if (!h->grp.empty()) return eval_groups(h, h->pend_coor, h->pend_dpot, e, false, 2);
+    const int first = eval_complete(h);
+    return eval_retry(h, h->pend_coor, h->pend_dpot, e, first, true);
+}
+
 int moil_nb_request_rebuild(moil_nb_ctx *h)
 {
     if (!h) return MOIL_NB_ERR_ARG;
+    if (h->pending) return MOIL_NB_ERR_STATE;
     h->need_rebuild = 1;
     for (NbCtx *c : h->grp) c->need_rebuild = 1;
     return MOIL_NB_OK;
@@ -1472,6 +1523,7 @@ int moil_nb_set_graph(moil_nb_ctx *h, int on)
 int moil_nb_set_virial(moil_nb_ctx *h, int on)
 {
     if (!h) return MOIL_NB_ERR_ARG;
+    if (h->pending) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
     h->virial = on ? 1 : 0;
     drop_graph(h);
@@ -1482,6 +1534,7 @@ int moil_nb_set_virial(moil_nb_ctx *h, int on)
 int moil_nb_set_groups(moil_nb_ctx *h, int groups)
 {
     if (!h || groups < 0) return MOIL_NB_ERR_ARG;
+    if (h->pending) return MOIL_NB_ERR_STATE;
     h->want_groups = groups;
     return MOIL_NB_OK;
 }
@@ -1494,6 +1547,7 @@ int moil_nb_groups(const moil_nb_ctx *h)
 int moil_nb_set_shape(moil_nb_ctx *h, const moil_nb_shape *sp)
 {
     if (!h || !sp) return MOIL_NB_ERR_ARG;
+    if (h->pending) return MOIL_NB_ERR_STATE;
     if (sp->water_kernel < MOIL_NB_WATER_AUTO || sp->water_kernel > MOIL_NB_WATER_HALF ||
         (sp->half_block != 0 && sp->half_block != 128 && sp->half_block != 256) ||
         sp->tiled < MOIL_NB_TILED_AUTO || sp->tiled > MOIL_NB_TILED_ALL || sp->groups < 0) {

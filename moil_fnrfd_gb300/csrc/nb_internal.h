@@ -217,6 +217,10 @@ struct NbCtx {
     const double *g_coor = nullptr;
     double *g_dpot = nullptr;
     int g_gen = -1, list_gen = 0, graph_launches = 0;
+    // an asynchronous evaluation queued by moil_nb_eval_device_async and not yet waited for
+    int pending = 0, pend_rc = 0;
+    const double *pend_coor = nullptr;
+    double *pend_dpot = nullptr;
     int on_prio = 0, g_prio = 0;       // running on the prioritised group streams (now / when captured)
 };
 

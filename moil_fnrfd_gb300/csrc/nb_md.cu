@@ -219,7 +219,7 @@ int moil_nb_md_step(moil_nb_ctx *h, double *d_coor, double *d_vel, const double 
                     const double *water_geom, moil_energies *energies, double *ekin)
 {
     if (!h || !d_coor || !d_vel || !d_mass || !(dt > 0.0) || nsteps < 0) return MOIL_NB_ERR_ARG;
-    if (!h->inited) return MOIL_NB_ERR_STATE;
+    if (!h->inited || h->pending) return MOIL_NB_ERR_STATE;
     cudaSetDevice(h->device);
     // TIP3P: O-H 0.9572 Å, H-O-H 104.52 degrees
     const double doh = water_geom ? water_geom[0] : 0.9572;

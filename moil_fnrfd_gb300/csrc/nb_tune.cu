@@ -125,6 +125,7 @@ int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const d
                      int evals, moil_nb_shape *best, moil_nb_tune_trial *trials, int max_trials, int *ntrials)
 {
     if (!h || nrep <= 0 || !reps || !d_coor || !d_dpot) return MOIL_NB_ERR_ARG;
+    if (h->pending) return MOIL_NB_ERR_STATE;
     for (int r = 0; r < nrep; ++r)
         if (!reps[r].params || !reps[r].topo) return MOIL_NB_ERR_ARG;
     if (ntrials) *ntrials = 0;

@@ -27,7 +27,8 @@ ENERGY_KEYS = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_el14", "e_vdw14", "e_corr
                "e_ew_receip", "e_total", "e_dir")
 
 EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_last_error", "moil_nb_init",
-            "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device", "moil_nb_adjoint",
+            "moil_nb_init_batch", "moil_nb_get_alpha", "moil_nb_eval", "moil_nb_eval_device",
+            "moil_nb_eval_device_async", "moil_nb_eval_wait", "moil_nb_adjoint",
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
             "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "moil_nb_md_step",
@@ -116,6 +117,8 @@ def load(build_if_missing: bool = True):
     L.moil_nb_get_alpha.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     L.moil_nb_eval.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(Energies)]
     L.moil_nb_eval_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Energies)]
+    L.moil_nb_eval_device_async.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.moil_nb_eval_wait.argtypes = [ctypes.c_void_p, ctypes.POINTER(Energies)]
     L.moil_nb_adjoint.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.POINTER(Energies)]
     L.moil_nb_request_rebuild.argtypes = [ctypes.c_void_p]
     L.moil_nb_squeeze.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Topology), _dp]
@@ -399,6 +402,18 @@ class Nonbonded:
         """Evaluate on device-resident buffers (raw CUDA pointers)."""
         _check(self.L, self.h, self.L.moil_nb_eval_device(self.h, ctypes.c_void_p(d_coor_ptr),
                                                           ctypes.c_void_p(d_dpot_ptr), self._e))
+        return self.energies() if want_energies else None
+
+    def eforce_device_async(self, d_coor_ptr: int, d_dpot_ptr: int):
+        """Queue an evaluation on device-resident buffers and return at once; ``eval_wait``
+        completes it.  The buffers stay untouched until then."""
+        _check(self.L, self.h, self.L.moil_nb_eval_device_async(self.h, ctypes.c_void_p(d_coor_ptr),
+                                                                ctypes.c_void_p(d_dpot_ptr)))
+
+    def eval_wait(self, want_energies: bool = True):
+        """Wait for the evaluation queued by ``eforce_device_async`` (regrowing lists and redoing
+        it after an overflow); its energies per replica."""
+        _check(self.L, self.h, self.L.moil_nb_eval_wait(self.h, self._e))
         return self.energies() if want_energies else None
 
     def set_timing(self, on=True):

@@ -36,6 +36,13 @@ def test_status_strings():
     assert L.moil_nb_strerror(999) == b"unknown status"
 
 
+def test_async_evaluation_rejects_bad_arguments():
+    """The asynchronous evaluation pair checks its arguments before any CUDA call."""
+    L = nb.load()
+    assert L.moil_nb_eval_device_async(None, None, None) == 1       # MOIL_NB_ERR_ARG
+    assert L.moil_nb_eval_wait(None, None) == 1
+
+
 def test_create_without_gpu_fails_cleanly():
     """With no visible GPU the handle constructor reports a CUDA error instead of aborting."""
     L = nb.load()
