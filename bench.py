@@ -499,12 +499,22 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in ev]
     value, total_s = job_rate(natoms * args.steps, sum(step_ms) / 1e3)
 
-    # e2e through the public host-buffer call: H2D + evaluation + D2H every step
+    # e2e through the public host-buffer call: H2D + evaluation + D2H every step, on a handle
+    # tuned for that call (the tuner's host objective: more replica groups hide more of the
+    # copies) unless the shape is forced
+    nbe, tune_host = nb, None
+    if not forced and not args.no_tune:
+        t0 = time.perf_counter()
+        nbe = Nonbonded(reps, precision=MOIL_NB_MIXED, device=local, skin=SKIN, list_period=LIST_PERIOD,
+                        shape=shape, tune_cache=cache, tune_host=True)
+        tune_host = nbe.autotune(d_coor.data_ptr(), d_dpot.data_ptr(), evals=2 * LIST_PERIOD)
+        tune_host["seconds"] = time.perf_counter() - t0
+        log(f"autotune (host buffers): {tune_host['best']} in {tune_host['seconds']:.1f} s")
     h_coor = torch.from_numpy(coor).pin_memory()
     h_dpot = torch.empty_like(h_coor).pin_memory()
     hc, hd = h_coor.numpy(), h_dpot.numpy()
     for _ in range(3):
-        nb.eforce_into(hc, hd, want_energies=False)
+        nbe.eforce_into(hc, hd, want_energies=False)
     torch.cuda.synchronize()
     e2e_ms = []
     for _ in range(args.steps):
@@ -512,11 +522,14 @@ def main():
             flush.zero_()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        nb.eforce_into(hc, hd, want_energies=False)
+        nbe.eforce_into(hc, hd, want_energies=False)
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_value, _ = job_rate(natoms * args.steps, sum(e2e_ms) / 1e3)
+    e2e_shape = nbe.shape()
 
-    press = press_leg(nb, reps, hc, e2e_ms) if not args.no_press and rank == 0 else None
+    press = press_leg(nbe, reps, hc, e2e_ms) if not args.no_press and rank == 0 else None
+    if nbe is not nb:
+        nbe.close()
 
     # dominant kernel and its roofline (FP32 pipe): average over steps without a rebuild
     no_build = [t for t in stages if not t["list_rebuilt"]] or stages
@@ -575,10 +588,12 @@ def main():
            "roofline": roof,
            "roofline_pme": roof_pme,
            "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": int(coor.nbytes),
-                   "d2h_bytes_per_step": int(coor.nbytes + 16 * 8 * len(reps))},
+                   "d2h_bytes_per_step": int(coor.nbytes + 16 * 8 * len(reps)), "shape": e2e_shape},
            "clocks": clk, "gpu_launches": launches * args.steps}
     if tune is not None:
         out["autotune"] = tune
+    if tune_host is not None:
+        out["autotune_host"] = tune_host
 
     # energy and gradient errors of the batched evaluation against the oracle (FP64, MOIL's
     # predicate) on a sample of replicas spread over the batch

@@ -252,7 +252,7 @@ int moil_nb_set_groups(moil_nb_ctx *h, int groups);
 int moil_nb_groups(const moil_nb_ctx *h);
 
 /* Kernel and list shapes of a handle: the search space of the autotuner
- * (moil_fnrfd_gb300/tune.py).  No counterpart in the reference, whose list scheme is fixed
+ * (moil_nb_autotune).  No counterpart in the reference, whose list scheme is fixed
  * (pot/nbondm.f:143-210, pot/nbond.f:54-157).  Every shape gives the same pair set and
  * results within the mixed path's tolerances; each is deterministic run to run. */
 enum {
@@ -282,11 +282,12 @@ int moil_nb_get_shape(const moil_nb_ctx *h, moil_nb_shape *s);
 /* One timed candidate of moil_nb_autotune. */
 typedef struct {
     moil_nb_shape shape;          /* as resolved by the handle */
-    double ms_per_eval;           /* wall clock per device-resident evaluation */
+    double ms_per_eval;           /* wall clock per evaluation (device-resident or host buffers) */
 } moil_nb_tune_trial;
 
-/* Autotuner (no counterpart in the reference).  Times `evals` device-resident evaluations
- * (0: one list period) of each candidate shape on the handle's batch -- the same replicas as
+/* Autotuner (no counterpart in the reference).  Times `evals` evaluations (0: one list
+ * period; device-resident, or through host buffers after moil_nb_set_tune_mode) of each
+ * candidate shape on the handle's batch -- the same replicas as
  * the last moil_nb_init_batch, passed again because the handle is rebuilt for each replica-
  * group count -- by coordinate descent: groups 1..4, then the water kernel (full lists, half
  * lists in blocks of 128 or 256 waters), then the water-row build (automatic, cell search,
@@ -297,6 +298,13 @@ typedef struct {
  * precision, the replica count and the replica-size histogram (power-of-two atom bins), and
  * moil_nb_init_batch applies a stored shape for a matching batch. */
 int moil_nb_set_tune_cache(moil_nb_ctx *h, const char *path);
+
+/* What the autotuner times: device-resident evaluations (MOIL_NB_TUNE_DEVICE, the default) or
+ * evaluations through host buffers (MOIL_NB_TUNE_HOST: moil_nb_eval on page-locked copies of
+ * the batch that the tuner allocates for the search), whose copies more replica groups hide
+ * better.  The mode is part of the cache key. */
+enum { MOIL_NB_TUNE_DEVICE = 0, MOIL_NB_TUNE_HOST = 1 };
+int moil_nb_set_tune_mode(moil_nb_ctx *h, int mode);
 int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const double *d_coor, double *d_dpot,
                      int evals, moil_nb_shape *best, moil_nb_tune_trial *trials, int max_trials, int *ntrials);
 

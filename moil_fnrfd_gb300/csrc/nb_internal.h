@@ -213,6 +213,7 @@ struct NbCtx {
     int want_groups = 0;               // 0: automatic, 1: none, P: P groups (next init)
     std::string tune_cache;            // autotuner cache file read by moil_nb_init_batch ("" none)
     int tuning = 0;                    // moil_nb_autotune is re-initialising the handle
+    int tune_mode = 0;                 // MOIL_NB_TUNE_DEVICE / MOIL_NB_TUNE_HOST
     cudaGraphExec_t gexec = nullptr;
     const double *g_coor = nullptr;
     double *g_dpot = nullptr;

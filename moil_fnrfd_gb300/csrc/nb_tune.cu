@@ -22,9 +22,9 @@
 
 namespace {
 
-// GPU model, multiprocessors, precision, replica count and the replica-size histogram over
-// power-of-two atom-count bins
-std::string tune_key(int device, int nrep, const moil_replica *reps)
+// GPU model, multiprocessors, precision, replica count, the replica-size histogram over
+// power-of-two atom-count bins, and the timed call (device-resident or host buffers)
+std::string tune_key(int device, int nrep, const moil_replica *reps, int mode)
 {
     cudaDeviceProp prop;
     std::string gpu = "unknown";
@@ -45,6 +45,7 @@ std::string tune_key(int device, int nrep, const moil_replica *reps)
     k << gpu << "|sm" << nsm << "|prec" << (nrep > 0 ? reps[0].params->precision : 0) << "|nrep" << nrep << "|hist";
     for (int b = 0; b < 32; ++b)
         if (hist[b]) k << ":" << b << "=" << hist[b];
+    if (mode == MOIL_NB_TUNE_HOST) k << "|host";
     return k.str();
 }
 
@@ -104,7 +105,7 @@ int nb_tune_cached_shape(moil_nb_ctx *h, int nrep, const moil_replica *reps)
 {
     if (h->tune_cache.empty() || h->tuning || nrep <= 0 || !reps) return 0;
     moil_nb_shape s;
-    if (!cache_lookup(h->tune_cache, tune_key(h->device, nrep, reps), &s)) return 0;
+    if (!cache_lookup(h->tune_cache, tune_key(h->device, nrep, reps, h->tune_mode), &s)) return 0;
     h->want_whalf = s.water_kernel;
     h->hb = s.half_block ? s.half_block : 256;
     h->want_tiled = s.tiled;
@@ -121,6 +122,13 @@ int moil_nb_set_tune_cache(moil_nb_ctx *h, const char *path)
     return MOIL_NB_OK;
 }
 
+int moil_nb_set_tune_mode(moil_nb_ctx *h, int mode)
+{
+    if (!h || (mode != MOIL_NB_TUNE_DEVICE && mode != MOIL_NB_TUNE_HOST)) return MOIL_NB_ERR_ARG;
+    h->tune_mode = mode;
+    return MOIL_NB_OK;
+}
+
 int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const double *d_coor, double *d_dpot,
                      int evals, moil_nb_shape *best, moil_nb_tune_trial *trials, int max_trials, int *ntrials)
 {
@@ -131,6 +139,22 @@ int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const d
     if (ntrials) *ntrials = 0;
     if (evals <= 0) evals = reps[0].params->list_period > 0 ? reps[0].params->list_period : 10;
     evals = std::max(evals, 3);
+    // host mode: page-locked copies of the batch for moil_nb_eval (freed on every return path)
+    struct Pinned {
+        double *c = nullptr, *d = nullptr;
+        ~Pinned() { if (c) cudaFreeHost(c); if (d) cudaFreeHost(d); }
+    } hb;
+    if (h->tune_mode == MOIL_NB_TUNE_HOST) {
+        int64_t natom = 0;
+        for (int r = 0; r < nrep; ++r) natom += reps[r].topo->npt;
+        const size_t bytes = sizeof(double) * 3 * (size_t)natom;
+        NB_CUDA_OK(h, cudaMallocHost(&hb.c, bytes));
+        NB_CUDA_OK(h, cudaMallocHost(&hb.d, bytes));
+        NB_CUDA_OK(h, cudaMemcpy(hb.c, d_coor, bytes, cudaMemcpyDeviceToHost));
+    }
+    auto one_eval = [&]() -> int {
+        return hb.c ? moil_nb_eval(h, hb.c, hb.d, nullptr) : moil_nb_eval_device(h, d_coor, d_dpot, nullptr);
+    };
     h->tuning = 1;
     std::vector<moil_nb_tune_trial> log;
     int inited_groups = -1;        // the group count the handle was last built with here
@@ -145,12 +169,12 @@ int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const d
             if (rc != MOIL_NB_OK) return rc;
         }
         for (int k = 0; k < 2; ++k) {          // list build, graph capture
-            rc = moil_nb_eval_device(h, d_coor, d_dpot, nullptr);
+            rc = one_eval();
             if (rc != MOIL_NB_OK) return rc;
         }
         const auto t0 = std::chrono::steady_clock::now();
         for (int k = 0; k < evals; ++k) {
-            rc = moil_nb_eval_device(h, d_coor, d_dpot, nullptr);
+            rc = one_eval();
             if (rc != MOIL_NB_OK) return rc;
         }
         *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count() / evals;
@@ -208,7 +232,8 @@ int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const d
     }
     h->tuning = 0;
     if (rc != MOIL_NB_OK) return rc;
-    if (!h->tune_cache.empty() && !cache_store(h->tune_cache, tune_key(h->device, nrep, reps), best_s, best_ms)) {
+    if (!h->tune_cache.empty() &&
+        !cache_store(h->tune_cache, tune_key(h->device, nrep, reps, h->tune_mode), best_s, best_ms)) {
         h->err = "moil_nb_autotune: cannot write the cache file " + h->tune_cache;
         return MOIL_NB_ERR_ARG;
     }

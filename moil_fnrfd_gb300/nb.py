@@ -22,6 +22,7 @@ import numpy as np
 
 from . import build as _build
 
+TUNE_DEVICE, TUNE_HOST = 0, 1
 MOIL_NB_MIXED, MOIL_NB_FP64 = 0, 1
 ENERGY_KEYS = ("e_vdw", "e_el", "e_vsym", "e_lsym", "e_el14", "e_vdw14", "e_corr", "e_self",
                "e_ew_receip", "e_total", "e_dir")
@@ -32,7 +33,8 @@ EXPORTED = ("moil_nb_create", "moil_nb_destroy", "moil_nb_strerror", "moil_nb_la
             "moil_nb_request_rebuild", "moil_nb_squeeze", "moil_nb_natoms", "moil_nb_stream",
             "moil_nb_set_timing", "moil_nb_get_timing", "moil_nb_pair_stats", "moil_nb_set_graph",
             "moil_nb_get_virial", "moil_nb_set_virial", "moil_nb_set_groups", "moil_nb_groups", "moil_nb_md_step",
-            "moil_nb_set_shape", "moil_nb_get_shape", "moil_nb_set_tune_cache", "moil_nb_autotune",
+            "moil_nb_set_shape", "moil_nb_get_shape", "moil_nb_set_tune_cache", "moil_nb_set_tune_mode",
+            "moil_nb_autotune",
             "moil_nb_dcd_write", "moil_nb_set_molecules", "moil_nb_pressure", "ewald_init_gpu_", "nblist_gpu_", "eforce_nb_gpu_", "eforce_nb_press_gpu_")
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -135,6 +137,7 @@ def load(build_if_missing: bool = True):
     L.moil_nb_set_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(Shape)]
     L.moil_nb_get_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(Shape)]
     L.moil_nb_set_tune_cache.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    L.moil_nb_set_tune_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.moil_nb_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Replica), ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Shape), ctypes.POINTER(TuneTrial),
                                    ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
@@ -212,7 +215,8 @@ class Nonbonded:
     """One device handle over one system or a batch of independent replicas."""
 
     def __init__(self, systems, precision=MOIL_NB_MIXED, device=0, skin=1.0, list_period=0,
-                 lj_switch=False, timing=False, groups=0, dtol=None, shape=None, tune_cache=None):
+                 lj_switch=False, timing=False, groups=0, dtol=None, shape=None, tune_cache=None,
+                 tune_host=False):
         self.L = load()
         h = ctypes.c_void_p()
         _check(self.L, None, self.L.moil_nb_create(ctypes.byref(h), int(device)))
@@ -222,6 +226,9 @@ class Nonbonded:
             self.set_shape(**dict(shape, groups=shape.get("groups", groups)))
         if tune_cache is not None:
             _check(self.L, self.h, self.L.moil_nb_set_tune_cache(self.h, str(tune_cache).encode()))
+        if tune_host:
+            # the tuner (and the cached shape) for callers that pass host buffers (eforce_into)
+            _check(self.L, self.h, self.L.moil_nb_set_tune_mode(self.h, TUNE_HOST))
         self.batch = isinstance(systems, (list, tuple))
         self.systems = list(systems) if self.batch else [systems]
         keep = _Keep()

@@ -4,7 +4,8 @@ The tuner times every candidate shape on the handle's own batch and leaves the f
 applied; whatever it picks, the evaluation stays within the mixed path's tolerances against
 the oracle (parity mode).  Its cache file holds one line per (GPU, precision, replica count,
 replica-size histogram): a new handle over the same batch starts with the cached shape, one
-over another batch does not.
+over another batch does not.  The host-buffer objective (MOIL_NB_TUNE_HOST) has a cache line
+of its own.
 """
 import numpy as np
 import pytest
@@ -52,3 +53,29 @@ def test_autotune_picks_a_timed_shape_that_matches_the_oracle(batch, tmp_path):
     other = Nonbonded(batch[:3], skin=1.0, list_period=10, tune_cache=cache)
     assert other.groups() == 1           # no entry for a 3-replica batch: the automatic choice
     other.close()
+
+
+def test_host_objective_has_its_own_cache_line(batch, tmp_path):
+    """MOIL_NB_TUNE_HOST times moil_nb_eval on page-locked copies of the batch; its result is
+    stored under its own key, which device-mode handles do not read."""
+    cache = tmp_path / "tune.tsv"
+    nb = Nonbonded(batch, skin=1.0, list_period=10, tune_cache=cache, tune_host=True)
+    coor = np.concatenate([s.coor for s in batch])
+    dc = torch.from_numpy(coor).cuda()
+    dd = torch.empty_like(dc)
+    res = nb.autotune(dc.data_ptr(), dd.data_ptr(), evals=4)
+    best = res["best"]
+    assert nb.shape() == best
+    hd = np.zeros_like(coor)
+    es = nb.eforce_into(coor, hd)
+    ref, eref = O.eforce(batch[0], mode="parity")
+    check(hd[:batch[0].npt], es[0], ref, eref, 0, "host-tuned replica 0")
+    nb.close()
+    lines = cache.read_text().strip().splitlines()
+    assert len(lines) == 1 and lines[0].split("\t")[0].endswith("|host")
+    again = Nonbonded(batch, skin=1.0, list_period=10, tune_cache=cache, tune_host=True)
+    assert again.shape() == best
+    again.close()
+    dev = Nonbonded(batch, skin=1.0, list_period=10, tune_cache=cache)
+    assert dev.groups() == 1            # no device-mode entry: the automatic choice (1 for 10 replicas)
+    dev.close()
