@@ -414,7 +414,7 @@ def main():
                     help="replica groups evaluated concurrently (0: the library's automatic choice)")
     ap.add_argument("--water-kernel", default="auto", choices=["auto", "full", "half"],
                     help="water-water kernel shape (moil_nb_set_shape; auto: the library's choice)")
-    ap.add_argument("--half-block", type=int, default=0, choices=[0, 128, 256],
+    ap.add_argument("--half-block", type=int, default=0, choices=[0, 128, 256, 512],
                     help="waters per block of the half-list water kernel (0: the library's default)")
     ap.add_argument("--no-adj", action="store_true", help="skip the parameter-derivative (adjoint) leg")
     ap.add_argument("--no-tune", action="store_true",

@@ -268,7 +268,7 @@ enum {
 };
 typedef struct {
     int water_kernel;             /* MOIL_NB_WATER_* */
-    int half_block;               /* waters per block of the half-list kernel: 128 or 256 (0: 256) */
+    int half_block;               /* waters per block of the half-list kernel: 128, 256 or 512 (0: 256) */
     int tiled;                    /* MOIL_NB_TILED_*: how the water-water rows are built */
     int groups;                   /* replica groups, as moil_nb_set_groups (next moil_nb_init_batch) */
 } moil_nb_shape;
@@ -290,7 +290,7 @@ typedef struct {
  * candidate shape on the handle's batch -- the same replicas as
  * the last moil_nb_init_batch, passed again because the handle is rebuilt for each replica-
  * group count -- by coordinate descent: groups 1..4, then the water kernel (full lists, half
- * lists in blocks of 128 or 256 waters), then the water-row build (automatic, cell search,
+ * lists in blocks of 128, 256 or 512 waters), then the water-row build (automatic, cell search,
  * all-pairs tiles).  d_coor / d_dpot are device buffers of the batch.  The fastest shape
  * stays applied and is returned in *best; trials (up to max_trials, may be NULL) receive every
  * candidate timed, *ntrials their number.  With a cache file set (moil_nb_set_tune_cache) the

@@ -1549,7 +1549,7 @@ int moil_nb_set_shape(moil_nb_ctx *h, const moil_nb_shape *sp)
     if (!h || !sp) return MOIL_NB_ERR_ARG;
     if (h->pending) return MOIL_NB_ERR_STATE;
     if (sp->water_kernel < MOIL_NB_WATER_AUTO || sp->water_kernel > MOIL_NB_WATER_HALF ||
-        (sp->half_block != 0 && sp->half_block != 128 && sp->half_block != 256) ||
+        (sp->half_block != 0 && sp->half_block != 128 && sp->half_block != 256 && sp->half_block != 512) ||
         sp->tiled < MOIL_NB_TILED_AUTO || sp->tiled > MOIL_NB_TILED_ALL || sp->groups < 0) {
         h->err = "moil_nb_set_shape: a field out of range";
         return MOIL_NB_ERR_ARG;

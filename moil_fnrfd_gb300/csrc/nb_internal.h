@@ -97,7 +97,7 @@ struct NbCtx {
     // half water rows (FP32 path with 16-bit rows: k_whalf builds them, k_water_h reads them)
     int whalf = 0;                // the half-list water kernel is in use
     int want_whalf = 0;           // MOIL_NB_WATER_*: 0 automatic, 1 full lists, 2 half lists
-    int hb = 256;                 // waters per half-list block (128 or 256)
+    int hb = 256;                 // waters per half-list block (128, 256 or 512)
     int want_tiled = 0;           // MOIL_NB_TILED_*
     std::vector<int2> hblocks;    // (replica, first sorted water) of each half-list block
     int2 *d_hblocks = nullptr;

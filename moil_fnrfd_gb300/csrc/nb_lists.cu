@@ -892,7 +892,7 @@ void build_lists_t(NbCtx *c, const double *d_coor)
     else water_lists(0);
     if (sizeof(T) == 4 && c->whalf && c->row16) {
         const int nb = (int)c->hblocks.size(), g = std::min(nb, c->nsm * 4);
-        (c->hb == 128 ? k_whalf<128> : k_whalf<256>)<<<g, c->hb, 0, s>>>(
+        (c->hb == 128 ? k_whalf<128> : (c->hb == 512 ? k_whalf<512> : k_whalf<256>))<<<g, c->hb, 0, s>>>(
             nb, c->d_hblocks, c->d_reps, c->d_wl1_cnt, (const unsigned short *)c->d_wl1, c->cap_row1, c->d_hrow,
             c->caph, c->d_hcnt, c->d_jset, c->d_jn, c->jcap, c->d_status);
         c->launches++;

@@ -591,6 +591,7 @@ __global__ void __launch_bounds__(WBLOCK, 4) k_water_f(int nW, const RepDev *__r
 template <int HB> struct HalfScale;
 template <> struct HalfScale<128> { static constexpr int S = 17; };
 template <> struct HalfScale<256> { static constexpr int S = 16; };
+template <> struct HalfScale<512> { static constexpr int S = 15; };
 
 // VIR: also the water-water LJ virial terms (as k_water_f<true>)
 template <int HB, bool VIR>
@@ -1162,6 +1163,17 @@ __global__ void k_energy_final(int nrep, const RepDev *__restrict__ reps, const 
     o[12] = 0.5 * pw[6]; o[13] = 0.5 * pw[7]; o[14] = 0.5 * po[6]; o[15] = 0.5 * po[7]; o[16] = px[3];
 }
 
+// the half-list kernel for a block size (128, 256 or 512 waters) and virial flag
+using WaterHFn = decltype(&k_water_h<256, false>);
+WaterHFn water_h_fn(int hb, bool vir)
+{
+    switch (hb) {
+    case 128: return vir ? k_water_h<128, true> : k_water_h<128, false>;
+    case 512: return vir ? k_water_h<512, true> : k_water_h<512, false>;
+    default: return vir ? k_water_h<256, true> : k_water_h<256, false>;
+    }
+}
+
 template <typename T>
 void realspace_t(NbCtx *c)
 {
@@ -1170,8 +1182,7 @@ void realspace_t(NbCtx *c)
     if (sizeof(T) == 4 && c->nW > 0 && c->whalf) {
         // the water sites' gradients are sums of atomics: cleared first
         cudaMemsetAsync(c->d_grad_site, 0, sizeof(long long) * 9 * (size_t)c->nW, s);
-        (c->hb == 128 ? (c->virial ? k_water_h<128, true> : k_water_h<128, false>)
-                      : (c->virial ? k_water_h<256, true> : k_water_h<256, false>))<<<(int)c->hblocks.size(), c->hb, (size_t)36 * c->jcap, s>>>(
+        water_h_fn(c->hb, c->virial)<<<(int)c->hblocks.size(), c->hb, (size_t)36 * c->jcap, s>>>(
             c->d_hblocks, c->d_reps, (const float4 *)c->d_pos, (const float4 *)c->d_woff, c->d_site_lj,
             c->d_site_flags, c->d_hrow, c->caph, c->d_hcnt, c->d_jset, c->d_jn, c->jcap, c->d_wl2_off, c->d_wl2,
             cap_int(c->cap_wl2), c->d_grad_site, c->d_e_unit, c->water_excl_fast);
@@ -1239,7 +1250,7 @@ bool nb_half_two_blocks(NbCtx *c)
 {
     int smax = 0;
     cudaFuncAttributes fa;
-    const void *fn = c->hb == 128 ? (const void *)k_water_h<128, false> : (const void *)k_water_h<256, false>;
+    const void *fn = (const void *)water_h_fn(c->hb, false);
     if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device) != cudaSuccess ||
         cudaFuncGetAttributes(&fa, fn) != cudaSuccess)
         return false;
@@ -1251,8 +1262,7 @@ int nb_half_configure(NbCtx *c)
 {
     int optin = 0;
     NB_CUDA_OK(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-    const void *fns[2] = {c->hb == 128 ? (const void *)k_water_h<128, false> : (const void *)k_water_h<256, false>,
-                          c->hb == 128 ? (const void *)k_water_h<128, true> : (const void *)k_water_h<256, true>};
+    const void *fns[2] = {(const void *)water_h_fn(c->hb, false), (const void *)water_h_fn(c->hb, true)};
     const size_t dyn = (size_t)36 * c->jcap;
     for (const void *fn : fns) {
         cudaFuncAttributes fa;

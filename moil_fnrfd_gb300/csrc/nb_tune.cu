@@ -205,13 +205,14 @@ int moil_nb_autotune(moil_nb_ctx *h, int nrep, const moil_replica *reps, const d
         s.groups = P;
         rc = consider(s);
     }
-    // 2. water kernel: full lists, half lists in blocks of 128 and 256 waters
+    // 2. water kernel: full lists, half lists in blocks of 128, 256 and 512 waters
     if (rc == MOIL_NB_OK) {
         cur = best_s;
-        const moil_nb_shape cand[3] = {{MOIL_NB_WATER_FULL, 256, cur.tiled, cur.groups},
+        const moil_nb_shape cand[4] = {{MOIL_NB_WATER_FULL, 256, cur.tiled, cur.groups},
                                        {MOIL_NB_WATER_HALF, 128, cur.tiled, cur.groups},
-                                       {MOIL_NB_WATER_HALF, 256, cur.tiled, cur.groups}};
-        for (int k = 0; k < 3 && rc == MOIL_NB_OK; ++k) rc = consider(cand[k]);
+                                       {MOIL_NB_WATER_HALF, 256, cur.tiled, cur.groups},
+                                       {MOIL_NB_WATER_HALF, 512, cur.tiled, cur.groups}};
+        for (int k = 0; k < 4 && rc == MOIL_NB_OK; ++k) rc = consider(cand[k]);
     }
     // 3. how the water rows are built
     if (rc == MOIL_NB_OK) {

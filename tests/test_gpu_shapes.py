@@ -2,8 +2,8 @@
 
 Every shape evaluates MOIL's pair set: the full-list water kernel (one water per thread over
 both directions), the half-list kernel (each water pair once, the partner's share summed per
-block in int32 shared-memory accumulators at 2^17 or 2^16 units per kcal/mol/Å) with blocks of
-128 and 256 waters, and the water rows built by cell search or by all-pairs tiles.  Each is
+block in int32 shared-memory accumulators at 2^17, 2^16 or 2^15 units per kcal/mol/Å) with blocks
+of 128, 256 and 512 waters, and the water rows built by cell search or by all-pairs tiles.  Each is
 held to the mixed path's tolerances against the oracle in parity mode (relative RMS gradient
 error <= 1e-5, |dE_total|/|E_total| <= 1e-6, each term within 1e-6 of the energy-term scale),
 gives the oracle's site-pair count, and is bit-identical run to run.
@@ -20,7 +20,7 @@ from test_gpu_parity import check
 pytestmark = pytest.mark.gpu
 
 SHAPES = [dict(water_kernel=WATER_FULL), dict(water_kernel=WATER_HALF, half_block=128),
-          dict(water_kernel=WATER_HALF, half_block=256)]
+          dict(water_kernel=WATER_HALF, half_block=256), dict(water_kernel=WATER_HALF, half_block=512)]
 
 
 def _ids(shapes):

@@ -33,7 +33,7 @@ def test_autotune_picks_a_timed_shape_that_matches_the_oracle(batch, tmp_path):
     res = nb.autotune(dc.data_ptr(), dd.data_ptr(), evals=4)
     best, trials = res["best"], res["trials"]
     # groups 1..4, then the water kernels, then the row builds, duplicates timed once
-    assert 6 <= len(trials) <= 10
+    assert 6 <= len(trials) <= 11
     assert all(t["ms_per_eval"] > 0 for t in trials)
     assert best in [t["shape"] for t in trials]
     assert min(trials, key=lambda t: t["ms_per_eval"])["shape"] == best
