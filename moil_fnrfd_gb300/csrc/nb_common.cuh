@@ -132,7 +132,7 @@ struct EChunk { int rep, kind, begin, end; };
 
 // work descriptors for the PME plane / column kernels
 struct PlaneWork { int rep, z; };
-struct ColWork { int rep, kx, ky0; };   // z columns at fixed kx for ky in [ky0, ky0 + tile)
+struct ColWork { int rep, kx, ky0, nky; };   // z columns at fixed kx for ky in [ky0, ky0 + nky)
 
 // ---------------------------------------------------------------------------------
 // precision traits

@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(256, 6) k_zconv_f(const ColWork *__restrict__ 
     const ColWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
-    const int tk = min(NB_TKF, n2 - w.ky0);
+    const int tk = w.nky;
     const float *etab = etab_all + R.bsp0;
     float2 *A = (float2 *)smem, *B = A + zconv_buf_elems(n3);
     FftCtx c3;
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(256) k_press_zvir_f(const ColWork *__restrict_
     const ColWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
-    const int tk = min(NB_TKF, n2 - w.ky0);
+    const int tk = w.nky;
     const float *bsp = bsp_all + R.bsp0;
     float2 *A = (float2 *)smem, *B = A + zconv_buf_elems(n3);
     FftCtx c3;
@@ -834,7 +834,7 @@ __global__ void __launch_bounds__(256) k_zconv(const ColWork *__restrict__ work,
     ColWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
-    const int tk = min(NB_TK, n2 - w.ky0);
+    const int tk = w.nky;
     const int n3p = n3 | 1;
     const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
     const C *tw = (const C *)tw_v;
@@ -901,7 +901,7 @@ __global__ void __launch_bounds__(256) k_press_zvir(const ColWork *__restrict__ 
     const ColWork w = work[blockIdx.x];
     const RepDev &R = reps[w.rep];
     const int n1 = R.n1, n2 = R.n2, n3 = R.n3, n1h = R.n1h;
-    const int tk = min(NB_TK, n2 - w.ky0);
+    const int tk = w.nky;
     const int n3p = n3 | 1;
     const FftPlanDev p3 = plans[rep_plan[3 * w.rep + 2]];
     const C *tw = (const C *)tw_v;
@@ -1137,6 +1137,21 @@ size_t zconv_smem(int n3)
 }
 template <typename T> int col_tile() { return sizeof(T) == 4 ? NB_TKF : NB_TK; }
 
+// the z-column work items of one kx: the n2 columns in ceil(n2 / tile) runs of equal length
+// (within one), so no block of the column kernels works on a short remainder alone (n2 = 36
+// gives two runs of 18, not 32 and 4: every Stockham pass of a run then fits one sweep of the
+// block's threads)
+void push_col_runs(std::vector<ColWork> &cols, int rep, int kx, int n2, int tile)
+{
+    const int nrun = (n2 + tile - 1) / tile, base = n2 / nrun, extra = n2 % nrun;
+    int ky0 = 0;
+    for (int k = 0; k < nrun; ++k) {
+        const int len = base + (k < extra ? 1 : 0);
+        cols.push_back(ColWork{rep, kx, ky0, len});
+        ky0 += len;
+    }
+}
+
 // raise a kernel's dynamic shared-memory limit to at least `bytes` (never lower it)
 template <typename K>
 cudaError_t raise_smem_limit(K *kernel, size_t bytes)
@@ -1232,7 +1247,7 @@ int configure_t(NbCtx *c)
         for (int z = 0; z < R.n3; ++z) c->planes.push_back(PlaneWork{r, z});
         c->col_begin[r] = (int)c->cols.size();
         for (int kx = 0; kx < R.n1h; ++kx)
-            for (int ky0 = 0; ky0 < R.n2; ky0 += tk) c->cols.push_back(ColWork{r, kx, ky0});
+            push_col_runs(c->cols, r, kx, R.n2, tk);
         sf = std::max(sf, plane_fwd_smem<T>(R.n1, R.n2));
         si = std::max(si, plane_inv_smem<T>(R.n1, R.n2));
         sz = std::max(sz, zconv_smem<T>(R.n3));
@@ -1555,7 +1570,7 @@ extern "C" int moil_nb_pme_noalloc(const double *d_coor, const double *d_q, int 
     tmp.nzbin = n3;
     for (int z = 0; z < n3; ++z) tmp.planes.push_back(PlaneWork{0, z});
     for (int kx = 0; kx < R.n1h; ++kx)
-        for (int ky0 = 0; ky0 < n2; ky0 += NB_TKF) tmp.cols.push_back(ColWork{0, kx, ky0});
+        push_col_runs(tmp.cols, 0, kx, n2, NB_TKF);
     int col_begin[2] = {0, (int)tmp.cols.size()};
     tmp.smem_plane_fwd = plane_fwd_smem<float>(n1, n2);
     tmp.smem_plane_inv = plane_inv_smem<float>(n1, n2);
