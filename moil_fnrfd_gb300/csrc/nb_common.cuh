@@ -128,7 +128,7 @@ __device__ __forceinline__ void pme_fr_split(double v, int &i, double &w)
 // a chunk of one replica's per-unit, per-atom or per-column energy partials (the energy
 // reduction): kind 0 water units, 1 other units, 2 atoms, 3 PME column items; [begin, end)
 struct EChunk { int rep, kind, begin, end; };
-#define NB_FE_SEG 4096
+#define NB_FE_SEG 1024
 
 // work descriptors for the PME plane / column kernels
 struct PlaneWork { int rep, z; };

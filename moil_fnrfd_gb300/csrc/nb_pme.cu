@@ -702,7 +702,8 @@ __global__ void __launch_bounds__(256, 4) k_pme_gather_f(int nsite, const int *_
 #pragma unroll
     for (int t = 0; t < 4; ++t) xs[t] = pme_wrap(i1 - 3 + t, n1);
     // without an x wrap the four stencil points of a row are contiguous: two aligned float4
-    // loads hold them (the grid allocation ends 16 bytes past its last plane for the second).
+    // loads hold them, one when they start 16-byte aligned (the grid allocation ends 16 bytes
+    // past its last plane for the second).
     // fr1 can round to n1 itself (index n1 wraps to 0), which takes the wrapped path.
     const bool contig = i1 >= 3 && i1 < n1;
     float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -717,8 +718,9 @@ __global__ void __launch_bounds__(256, 4) k_pme_gather_f(int nsite, const int *_
             if (contig) {
                 const uintptr_t a = (uintptr_t)(row + i1 - 3);
                 const float4 *p4 = (const float4 *)(a & ~(uintptr_t)15);
-                const float4 c0 = __ldg(p4), c1 = __ldg(p4 + 1);
                 const int sh = (int)((a >> 2) & 3);
+                const float4 c0 = __ldg(p4);
+                const float4 c1 = sh != 0 ? __ldg(p4 + 1) : c0;     // an aligned row needs one load
                 q4[0] = sh == 0 ? c0.x : (sh == 1 ? c0.y : (sh == 2 ? c0.z : c0.w));
                 q4[1] = sh == 0 ? c0.y : (sh == 1 ? c0.z : (sh == 2 ? c0.w : c1.x));
                 q4[2] = sh == 0 ? c0.z : (sh == 1 ? c0.w : (sh == 2 ? c1.x : c1.y));
