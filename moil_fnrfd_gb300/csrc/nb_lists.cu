@@ -410,6 +410,7 @@ __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], float 
     const float2 iL[3] = {pf2(R.invL[0]), pf2(R.invL[1]), pf2(R.invL[2])};
     const float2 nL[3] = {pf2(-R.L[0]), pf2(-R.L[1]), pf2(-R.L[2])};
     const float2 mg = pf2(12582912.f), nmg = pf2(-12582912.f), m1 = pf2(-1.f);
+    const float2 nrl2 = pf2(-rl2), nrc2 = pf2(-rc2);
     E *row = (E *)l1 + (size_t)i * cap_row;
     int nn = 0, nf = 0;
     float ilo[3], ihi[3];
@@ -464,8 +465,10 @@ __device__ __forceinline__ void wlist_tile(int2 w, float (*sj)[NB_WTILE], float 
                     x = __ffma2_rn(n, nL[d], x);
                     r2 = __ffma2_rn(x, x, r2);
                 }
-                m |= ((unsigned)(r2.x < rl2) << b) | ((unsigned)(r2.y < rl2) << (b + 1));
-                mn |= ((unsigned)(r2.x <= rc2) << b) | ((unsigned)(r2.y <= rc2) << (b + 1));
+                // r2 < r as the sign bit of r2 - r, one packed subtraction for both molecules
+                const float2 dl = __fadd2_rn(r2, nrl2), dc = __fadd2_rn(r2, nrc2);
+                m |= ((__float_as_uint(dl.x) >> 31) | ((__float_as_uint(dl.y) >> 31) << 1)) << b;
+                mn |= ((__float_as_uint(dc.x) >> 31) | ((__float_as_uint(dc.y) >> 31) << 1)) << b;
             }
             unsigned keep = nv < 32 ? (1u << nv) - 1u : 0xffffffffu;   // past the last molecule
             const int self = il - t0 - 32 * q;
