@@ -722,8 +722,9 @@ __global__ void __launch_bounds__(HB, 512 / HB) k_water_h(const int2 *__restrict
             const int j0 = wat0 + (int)(e0 & 0xffffu), j1 = wat0 + (int)(e1 & 0xffffu);
             const int l0 = (int)(e0 >> 16), l1 = (int)(e1 >> 16);
             const float4 o0 = oa, o1 = ob;
-            // the warp's row lines (one 128-byte line per entry) eight iterations ahead
-            nb_prefetch_l1(hr + (size_t)min(k + 16, k1 - 1) * HB);
+            // the warp's row lines (one 128-byte line per entry) four iterations ahead (further
+            // ahead, the prefetched lines take L1 from the partner records)
+            nb_prefetch_l1(hr + (size_t)min(k + 8, k1 - 1) * HB);
             if (k + 2 < k1) {
                 ea = hr[(size_t)(k + 2) * HB];
                 eb = k + 3 < k1 ? hr[(size_t)(k + 3) * HB] : ea;
